@@ -1,0 +1,138 @@
+"""Seeded synthetic scenes with the shapes of the benchmark workloads.
+
+The particle lattice follows the reference add-on's recipe
+(latest_prebuilt/addons/newton_vulkan_plugin.py:363-374: meshgrid lattice,
+centred, uniform jitter); Z is up as in the reference (plane z = altitude,
+gravity (0, 0, -9.81)). No dataset is involved: every array is generated from
+a fixed numpy seed so both the CUDA path and the CPU oracle see the same input.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED_JITTER = 42
+SEED_VELOCITY = 43
+SEED_HEIGHTFIELD = 44
+SEED_BOXES = 45
+SEED_BATCH = 46
+SEED_TARGET = 47
+
+
+def lattice(dims, spacing, bottom_z, jitter, seed=SEED_JITTER, center_xy=(0.0, 0.0)):
+    """dims=(nx, ny, nz) lattice, centred in x/y, lowest layer at bottom_z,
+    jitter uniform in [-jitter, +jitter] per component."""
+    nx, ny, nz = dims
+    px = np.arange(nx) * spacing
+    py = np.arange(ny) * spacing
+    pz = np.arange(nz) * spacing
+    pts = np.stack(np.meshgrid(px, py, pz)).reshape(3, -1).T
+    ext = np.array([nx - 1, ny - 1, nz - 1], dtype=np.float64) * spacing
+    pts = pts - np.array([ext[0] * 0.5, ext[1] * 0.5, 0.0])
+    pts = pts + np.array([center_xy[0], center_xy[1], bottom_z])
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        pts = pts + (rng.random(pts.shape) - 0.5) * 2.0 * jitter
+    return np.ascontiguousarray(pts, dtype=np.float32)
+
+
+def heightfield(nv=256, extent=1.0, amplitude=0.025, waves=4, seed=SEED_HEIGHTFIELD):
+    """nv x nv vertex grid over [-extent/2, extent/2]^2 with
+    z = sum_k amplitude*sin(2*pi*k*(x cos t_k + y sin t_k) + p_k), k=1..waves;
+    2*(nv-1)^2 triangles (130,050 for nv=256). Returns (verts[nv*nv,3], tris[T,3])."""
+    rng = np.random.default_rng(seed)
+    theta = rng.random(waves) * 2.0 * math.pi
+    phase = rng.random(waves) * 2.0 * math.pi
+    xs = np.linspace(-extent * 0.5, extent * 0.5, nv)
+    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    Z = np.zeros_like(X)
+    for k in range(waves):
+        Z += amplitude * np.sin(2.0 * math.pi * (k + 1) * (X * math.cos(theta[k]) + Y * math.sin(theta[k])) + phase[k])
+    verts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1).astype(np.float32)
+    i = np.arange(nv - 1)
+    I, J = np.meshgrid(i, i, indexing="xy")
+    v00 = (J * nv + I).ravel()
+    v10 = v00 + 1
+    v01 = v00 + nv
+    v11 = v01 + 1
+    tris = np.empty((v00.size * 2, 3), np.uint32)
+    tris[0::2] = np.stack([v00, v10, v11], axis=1)
+    tris[1::2] = np.stack([v00, v11, v01], axis=1)
+    return verts, tris
+
+
+def box_mesh(half_extents, center=(0.0, 0.0, 0.0), quat_xyzw=(0.0, 0.0, 0.0, 1.0)):
+    """Closed 12-triangle box (outward winding), transformed to world space."""
+    hx, hy, hz = half_extents
+    c = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                  [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], np.float64)
+    v = c * np.array([hx, hy, hz])
+    x, y, z, w = quat_xyzw
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    v = v @ R.T + np.asarray(center, np.float64)
+    t = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4],
+                  [2, 3, 7], [2, 7, 6], [1, 2, 6], [1, 6, 5], [3, 0, 4], [3, 4, 7]], np.uint32)
+    return v.astype(np.float32), t
+
+
+@dataclass
+class Scene:
+    name: str
+    config: dict
+    positions: np.ndarray
+    velocities: np.ndarray
+    inv_mass: np.ndarray
+    radii: np.ndarray
+    flags: np.ndarray
+    meshes: list = field(default_factory=list)  # (verts, tris, margin, watertight or None)
+    dt: float = 1.0 / 60.0
+    substeps: int = 10
+    iterations: int = 1
+    frames: int = 1
+
+    @property
+    def n(self) -> int:
+        return int(self.positions.shape[0])
+
+    def apply_config(self, cfg) -> None:
+        for k, v in self.config.items():
+            setattr(cfg, k, v)
+
+
+def _base_config(radius, search_radius):
+    return dict(
+        soft_contact_mu=0.5, shape_material_mu=0.5, particle_mu=0.5,
+        soft_contact_relaxation=0.9, particle_adhesion=0.0, particle_cohesion=0.0,
+        particle_max_radius=radius, search_radius=search_radius, soft_contact_margin=0.01,
+        enable_restitution=True, soft_contact_restitution=0.2, has_ground_plane=True,
+        ground_plane_altitude=0.0, gravity=[0.0, 0.0, -9.81], particle_v_max=1e5,
+    )
+
+
+def pile(dims=(16, 16, 16), spacing=0.02, radius=0.01, jitter=0.002, bottom_z=0.02,
+         inv_mass=1000.0, seed=SEED_JITTER, frames=120, name="pile") -> Scene:
+    """Plain particle pile on the ground plane (4,096 particles for the default dims)."""
+    x = lattice(dims, spacing, bottom_z, jitter, seed)
+    n = x.shape[0]
+    return Scene(name=name, config=_base_config(radius, 2.0 * radius), positions=x,
+                 velocities=np.zeros_like(x), inv_mass=np.full(n, inv_mass, np.float32),
+                 radii=np.full(n, radius, np.float32), flags=np.ones(n, np.int32), frames=frames)
+
+
+def particles_on_mesh(dims=(64, 64, 64), spacing=0.01, radius=0.005, jitter=0.001, bottom_z=0.15,
+                      hf_vertices=256, inv_mass=1000.0, frames=300, name="particles_on_mesh") -> Scene:
+    """Lattice falling onto a sum-of-sines heightfield (262,144 particles, 130,050
+    triangles for the defaults) with plane, mesh and particle-particle contacts."""
+    sc = pile(dims, spacing, radius, jitter, bottom_z, inv_mass, frames=frames, name=name)
+    v, t = heightfield(hf_vertices)
+    sc.meshes.append((v, t, 0.0, None))
+    return sc
+
+
+def scaled(scene_fn, scale: int, **kw) -> Scene:
+    """Same recipe with every lattice dimension divided by `scale` (test sizes)."""
+    return scene_fn(**kw)
