@@ -1,0 +1,146 @@
+/*
+ * C ABI of libxpbd_gb300.so — a GB300 (sm_103a) XPBD particle substep that is
+ * a drop-in for the reference's `vkxpbd` module (src/bindings.cpp:8-300 over
+ * vkx::XpbdSolver, src/scene.h:74-135).
+ *
+ * Plain C types only: host pointers and sizes in, host buffers out. Every
+ * function returns 0 on success and a negative value on failure; the message
+ * of the last failure on the calling thread is returned by xpbd_last_error().
+ * The error strings of the reference are kept ("XpbdSolver not initialized",
+ * "Particle count mismatch", ...). A solver is not thread-safe (neither is the
+ * reference's, src/context.h:31); calls block until the GPU work they start
+ * has finished, like the reference's fence waits (src/scene.cpp:1003).
+ */
+#ifndef XPBD_GB300_H
+#define XPBD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XPBD_ABI_VERSION 1
+#define XPBD_NUM_CELLS (128 * 128 * 128) /* hash grid size, src/scene.cpp:17-18 */
+
+typedef struct xpbd_solver xpbd_solver;
+
+/* vkx::SolverConfig (src/scene.h:14-41), field for field; defaults from
+ * xpbd_config_default(). shader_dir, compat_mode and enable_validation are
+ * accepted and ignored (there are no shaders and no Vulkan layers). */
+typedef struct xpbd_config {
+    float dt;
+    int32_t substeps;
+    int32_t iterations;
+    float particle_v_max;
+    float soft_contact_mu;
+    float shape_material_mu;
+    float soft_contact_relaxation;
+    float particle_adhesion;
+    float particle_mu;
+    float particle_cohesion;
+    float particle_max_radius;
+    float search_radius;
+    float soft_contact_margin;
+    int32_t enable_restitution;
+    float soft_contact_restitution;
+    int32_t has_ground_plane;
+    float ground_plane_altitude;
+    float gravity[3];
+    char shader_dir[256];
+    int32_t device_index;
+    int32_t compat_mode;
+    int32_t enable_validation;
+    int32_t enable_diagnostics;
+    int32_t enable_profile;
+    uint32_t max_diag_pairs;
+    int32_t substep_batch_size;
+} xpbd_config;
+
+/* vkx::GPUPairRecord (src/scene.h:43-64). */
+typedef struct xpbd_pair_record {
+    uint32_t i, j;
+    float dist, err;
+    float normal[3];
+    float vrel[3];
+    float vn, vt_len, denom, lambda_n, lambda_f;
+    float delta_i[3];
+    uint32_t iter_index, pad0;
+} xpbd_pair_record;
+
+/* ---- library ------------------------------------------------------------ */
+const char* xpbd_last_error(void);
+int xpbd_abi_version(void);
+void xpbd_config_default(xpbd_config* cfg);                  /* SolverConfig() */
+int xpbd_device_count(int* count);                           /* enumerate_devices, bindings.cpp:48 */
+int xpbd_device_name(int index, char* buf, size_t cap);
+
+/* ---- scene build (src/scene.h:79-92) -------------------------------------- */
+int xpbd_create(xpbd_solver** out);                          /* XpbdSolver() */
+int xpbd_destroy(xpbd_solver* s);
+int xpbd_init(xpbd_solver* s, const xpbd_config* cfg, size_t num_particles,
+              size_t max_contacts);                          /* init, scene.cpp:65-152 */
+/* shape_rot_xyzw may be NULL (identity); watertight_override -1 = auto-detect,
+ * 0/1 = forced (scene.cpp:154-202). */
+int xpbd_add_mesh(xpbd_solver* s, const float* verts, size_t num_verts, const uint32_t* tris,
+                  size_t num_tris, float shape_margin, const float* shape_rot_xyzw,
+                  int watertight_override);
+int xpbd_finalize_meshes(xpbd_solver* s);                    /* scene.cpp:204-390 */
+/* q: n*3 floats; qd, inv_mass, radii, flags may be NULL (scene.cpp:592-615). */
+int xpbd_set_particles(xpbd_solver* s, const float* q, const float* qd, const float* inv_mass,
+                       const float* radii, const int32_t* flags, size_t n);
+/* vels may be NULL (zero velocity), scene.cpp:617-696. */
+int xpbd_update_mesh(xpbd_solver* s, size_t mesh_index, const float* verts, size_t num_verts,
+                     const float* vels);
+
+/* ---- stepping ------------------------------------------------------------- */
+int xpbd_step(xpbd_solver* s, float dt, int substeps, int iterations); /* scene.cpp:698-1092 */
+int xpbd_collide_only(xpbd_solver* s);                                  /* scene.cpp:1229-1245 */
+int xpbd_step_solve_only(xpbd_solver* s, float dt, int substeps, int iterations); /* :1094-1227 */
+
+/* ---- readback (scene.cpp:1247-1436) ---------------------------------------- */
+int xpbd_get_positions(xpbd_solver* s, float* out_xyz, size_t n);
+int xpbd_get_velocities(xpbd_solver* s, float* out_xyz, size_t n);
+size_t xpbd_particle_count(const xpbd_solver* s);
+size_t xpbd_mesh_count(const xpbd_solver* s);
+int xpbd_last_contact_count(const xpbd_solver* s);
+/* Contacts of the last collision pass in canonical order (plane contacts by
+ * particle, then mesh contacts by particle and mesh); each array holds at least
+ * xpbd_last_contact_count() entries (x3 floats for the vector arrays); any
+ * pointer may be NULL. */
+int xpbd_get_contacts(xpbd_solver* s, int32_t* particles, int32_t* shapes, float* normals,
+                      float* body_positions, float* body_velocities);
+int xpbd_set_contact_data(xpbd_solver* s, const int32_t* particles, const int32_t* shapes,
+                          const float* body_positions, const float* normals, int contact_count);
+int xpbd_get_sorted_cells(xpbd_solver* s, uint32_t* out, size_t n);
+int xpbd_get_sorted_point_ids(xpbd_solver* s, uint32_t* out, size_t n);
+int xpbd_get_cell_starts(xpbd_solver* s, int32_t* out, size_t n); /* n = XPBD_NUM_CELLS */
+int xpbd_get_cell_ends(xpbd_solver* s, int32_t* out, size_t n);
+/* Deltas of the last solver iteration (recorded while enable_diagnostics is set). */
+int xpbd_get_deltas(xpbd_solver* s, float* out_xyz, size_t n);
+/* Node halves of mesh `mesh_index` as built: 4 floats per node, .w = packed
+ * uint32 bits. Call with NULL buffers to get the node count. */
+int xpbd_get_mesh_bvh(xpbd_solver* s, size_t mesh_index, float* lowers, float* uppers,
+                      size_t cap_nodes, size_t* num_nodes);
+
+/* ---- diagnostics (bindings.cpp:239-287) ------------------------------------ */
+int xpbd_get_diag_pair_count(xpbd_solver* s, uint32_t* out);
+int xpbd_get_diag_overflow_count(xpbd_solver* s, uint32_t* out);
+int xpbd_reset_diag_buffers(xpbd_solver* s);
+int xpbd_get_diag_pairs(xpbd_solver* s, xpbd_pair_record* out, size_t cap, size_t* count);
+/* which: 0 = p11_diag (u32), 1 = p11_apply_diag (u32), 2 = shape_contact_diag (f32),
+ * 3 = mesh_candidate_diag (u32); 4-byte words. NULL out returns the length. */
+int xpbd_get_aux_diag(xpbd_solver* s, int which, void* out, size_t cap, size_t* count);
+int xpbd_print_profiler_summary(xpbd_solver* s);
+
+/* ---- extensions ------------------------------------------------------------ */
+/* Device status bits of the last step (1 = look-back timeout, 2 = BVH stack
+ * overflow, 4 = mesh contact slots full) and their counters. */
+int xpbd_get_status(xpbd_solver* s, uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XPBD_GB300_H */

@@ -1,0 +1,325 @@
+// Hash-grid construction: cell keys, onesweep radix sort, cell table + sorted
+// particle records. Replaces grid_cell_indices.comp, gpu_sort.h's
+// histogram/scan/scatter passes (sort_histogram.comp, sort_scan_{a,b,c}.comp,
+// sort_scatter.comp) and grid_offsets.comp with its 16 MiB of fills.
+#include <algorithm>
+#include <stdexcept>
+
+#include "kernels.h"
+#include "particle.cuh"
+#include "xmath.cuh"
+
+namespace xpbd {
+
+// ---------------------------------------------------------------------------
+// Keys + digit histograms of every sort pass (+ plane contacts when no mesh)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* __restrict__ x,
+                                                      const float4* __restrict__ v, const float* __restrict__ w,
+                                                      const float* __restrict__ r, const int* __restrict__ flags,
+                                                      PredictParams pp, PlaneParams pl, uint32_t* __restrict__ keys,
+                                                      int bits, int passes, uint32_t* __restrict__ hist,
+                                                      uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp) {
+    extern __shared__ uint32_t s_hist[];  // passes << bits
+    __shared__ uint32_t s_warp[8];
+    const int bins = 1 << bits;
+    for (int i = threadIdx.x; i < passes * bins; i += blockDim.x) s_hist[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) *stamp += 1u;  // new grid generation for this substep
+    __syncthreads();
+    uint32_t contacts = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // the trip count is uniform across the block so every lane takes part in match_any
+    const int64_t trips = (n + stride - 1) / stride;
+    for (int64_t t = 0; t < trips; t++) {
+        const int64_t i = t * stride + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0;
+        if (valid) {
+            const float4 xf = x[i];
+            const int fl = flags[i];
+            v3 xp, vp;
+            predict(xf, v[i], w[i], fl, pp, xp, vp);
+            key = hash_grid_index(xp, pp.inv);
+            keys[i] = key;
+            if (cinfo) {  // generate_plane_contacts.comp:32-38 on the pre-integration position
+                uint32_t info = 0;
+                if (pl.enabled && (fl & 1)) {
+                    float dist = xf.z - pl.altitude;
+                    if (dist < pl.margin + r[i]) info = kPlaneBit;
+                }
+                cinfo[i] = info;
+                contacts += info;
+            }
+        }
+        for (int p = 0; p < passes; p++) {
+            const uint32_t d = valid ? ((key >> (p * bits)) & (uint32_t)(bins - 1)) : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p * bins + d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * bins; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+    if (cinfo) {
+        uint32_t tot = block_sum(contacts, s_warp);
+        if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
+    }
+}
+
+void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
+                         const float* r, const int* flags, PredictParams pp, PlaneParams pl, uint32_t* keys,
+                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp) {
+    if (n <= 0) return;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
+    k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pp, pl, keys, sp.bits, sp.passes, hist, cinfo,
+                                            ccount, stamp);
+}
+
+// ---------------------------------------------------------------------------
+// Onesweep pass (stable LSD radix sort with decoupled look-back)
+//
+// Tiles take a ticket from an atomic counter so that a tile only waits on
+// tiles that started earlier. Inside a tile every warp ranks its keys in index
+// order with __match_any_sync (stable), warp-local digit counts are turned
+// into tile offsets with warp-shuffle scans, the tile publishes its per-digit
+// aggregate, looks back over its predecessors, and finally scatters through
+// shared memory so that global writes run in digit order (coalesced).
+// Every look-back wait is bounded by a 1 s timer; on expiry the kernel sets
+// kErrLookbackTimeout and continues (the host raises an error).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_scan, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_scan[warp] = incl;
+    __syncthreads();
+    uint32_t off = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; i++) {
+        uint32_t t = s_scan[i];
+        if (i < warp) off += t;
+        tot += t;
+    }
+    __syncthreads();
+    total = tot;
+    return off + incl - v;
+}
+
+template <int BITS, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, const uint32_t* __restrict__ keys_in,
+                                                      const uint32_t* __restrict__ vals_in,
+                                                      uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                      const uint32_t* __restrict__ hist, uint32_t* lookback,
+                                                      uint32_t* tile_counter, DeviceStatus* st) {
+    constexpr int BINS = 1 << BITS;
+    constexpr int WARPS = THREADS / 32;
+    constexpr int TILE = THREADS * ITEMS;
+    static_assert(BINS == THREADS, "one digit per thread");
+    extern __shared__ uint32_t smem[];
+    uint32_t* s_whist = smem;                 // WARPS * BINS
+    uint32_t* s_keys = s_whist + WARPS * BINS;  // TILE
+    uint32_t* s_vals = s_keys + TILE;          // TILE
+    uint32_t* s_gbase = s_vals + TILE;         // BINS
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_scan[WARPS];
+    __shared__ uint32_t s_texcl[BINS];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = tid; i < WARPS * BINS; i += THREADS) s_whist[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const int64_t base = (int64_t)tile * TILE;
+    const int valid_n = (n - base) < (int64_t)TILE ? (int)(n - base) : TILE;
+    const uint32_t lt = lanemask_lt();
+
+    uint32_t kreg[ITEMS], vreg[ITEMS], rreg[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+        const int local = warp * 32 * ITEMS + j * 32 + lane;
+        const bool valid = local < valid_n;
+        const int64_t gi = base + local;
+        uint32_t key = 0, val = 0;
+        if (valid) {
+            key = keys_in[gi];
+            val = vals_in ? vals_in[gi] : (uint32_t)gi;
+        }
+        const uint32_t d = valid ? ((key >> shift) & (BINS - 1)) : (uint32_t)BINS;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t old = 0;
+        if (valid) old = s_whist[warp * BINS + d];
+        __syncwarp();
+        if (valid && (peers & lt) == 0) s_whist[warp * BINS + d] = old + __popc(peers);
+        __syncwarp();
+        kreg[j] = key;
+        vreg[j] = val;
+        rreg[j] = old + __popc(peers & lt);
+    }
+    __syncthreads();
+
+    // thread `tid` owns digit `tid`: warp prefix (in place) and tile total
+    uint32_t tot = 0;
+#pragma unroll
+    for (int wv = 0; wv < WARPS; wv++) {
+        uint32_t c = s_whist[wv * BINS + tid];
+        s_whist[wv * BINS + tid] = tot;
+        tot += c;
+    }
+    uint32_t dummy;
+    const uint32_t tile_excl = block_excl_scan<THREADS>(tot, s_scan, dummy);
+    const uint32_t glob_excl = block_excl_scan<THREADS>(hist[tid], s_scan, dummy);
+
+    // decoupled look-back for digit `tid`
+    uint32_t* my = lookback + (size_t)tile * BINS + tid;
+    uint32_t prev = 0;
+    if (tile == 0) {
+        st_release(my, kFlagInc | tot);
+    } else {
+        st_release(my, kFlagAgg | tot);
+        int64_t p = (int64_t)tile - 1;
+        uint64_t t0 = 0;
+        while (p >= 0) {
+            const uint32_t sv = ld_acquire(lookback + (size_t)p * BINS + tid);
+            const uint32_t flag = sv & ~kCountMask;
+            if (flag == 0) {
+                const uint64_t now = globaltimer_ns();
+                if (t0 == 0) {
+                    t0 = now;
+                } else if (now - t0 > kWaitLimitNs) {
+                    atomicOr(&st->error_bits, kErrLookbackTimeout);
+                    atomicAdd(&st->lookback_timeouts, 1u);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            prev += sv & kCountMask;
+            if (flag == kFlagInc) break;
+            p--;
+            t0 = 0;
+        }
+        st_release(my, kFlagInc | ((prev + tot) & kCountMask));
+    }
+    // output slot = s_gbase[d] + position in the tile's digit-sorted order (modular arithmetic)
+    s_gbase[tid] = glob_excl + prev - tile_excl;
+    s_texcl[tid] = tile_excl;
+    __syncthreads();
+    // tile-sorted position = tile digit start + warp prefix + rank within the warp
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+        const int local = warp * 32 * ITEMS + j * 32 + lane;
+        if (local < valid_n) {
+            const uint32_t d = (kreg[j] >> shift) & (BINS - 1);
+            const uint32_t pos = s_texcl[d] + s_whist[warp * BINS + d] + rreg[j];
+            s_keys[pos] = kreg[j];
+            s_vals[pos] = vreg[j];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < valid_n; i += THREADS) {
+        const uint32_t key = s_keys[i];
+        const uint32_t g = s_gbase[(key >> shift) & (BINS - 1)] + (uint32_t)i;
+        keys_out[g] = key;
+        vals_out[g] = s_vals[i];
+    }
+}
+
+SortPlan make_sort_plan(int64_t n, int key_bits, int bits, int items) {
+    if (bits != 8 && bits != 7) throw std::runtime_error("unsupported radix digit width");
+    SortPlan p;
+    p.bits = bits;
+    p.passes = (key_bits + bits - 1) / bits;
+    p.threads = 1 << bits;
+    p.items = items;
+    p.tile = p.threads * items;
+    p.tiles = (int)((n + p.tile - 1) / p.tile);
+    if (p.tiles < 1) p.tiles = 1;
+    return p;
+}
+size_t sort_lookback_words(const SortPlan& p) { return (size_t)p.tiles << p.bits; }
+
+template <int BITS, int ITEMS>
+static void onesweep_variant(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* ki,
+                             const uint32_t* vi, uint32_t* ko, uint32_t* vo, const uint32_t* hist, uint32_t* lb,
+                             uint32_t* tc, DeviceStatus* st) {
+    constexpr int THREADS = 1 << BITS;
+    constexpr int TILE = THREADS * ITEMS;
+    size_t smem = sizeof(uint32_t) * ((size_t)(THREADS / 32) * (1 << BITS) + 2 * TILE + (1 << BITS));
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_onesweep<BITS, THREADS, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr_set = true;
+    }
+    k_onesweep<BITS, THREADS, ITEMS><<<sp.tiles, THREADS, smem, s>>>(n, pass * BITS, ki, vi, ko, vo, hist, lb, tc,
+                                                                     st);
+}
+
+void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
+                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                          const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
+                          DeviceStatus* st) {
+    if (n <= 0) return;
+#define XPBD_OS(B, I)                                                                                      \
+    if (sp.bits == B && sp.items == I)                                                                     \
+        return onesweep_variant<B, I>(s, n, sp, pass, keys_in, vals_in, keys_out, vals_out, hist_pass, \
+                                      lookback, tile_counter, st);
+    XPBD_OS(8, 8)
+    XPBD_OS(8, 16)
+    XPBD_OS(7, 16)
+    XPBD_OS(7, 32)
+#undef XPBD_OS
+    throw std::runtime_error("no onesweep variant for this sort plan");
+}
+
+// ---------------------------------------------------------------------------
+// Cell table (start, end, generation stamp) + sorted-order particle records
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t* __restrict__ skeys,
+                                                      const uint32_t* __restrict__ sids, const float4* __restrict__ x,
+                                                      const float4* __restrict__ v, const float* __restrict__ w,
+                                                      const float* __restrict__ r, const int* __restrict__ flags,
+                                                      PredictParams pp, int* __restrict__ table,
+                                                      const uint32_t* __restrict__ stamp, float4* __restrict__ rx,
+                                                      float4* __restrict__ rv, int* __restrict__ rf) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t key = skeys[k];
+    // grid_offsets.comp:20-34 without the table fills: a stale entry is
+    // recognised by its generation stamp instead of being zeroed
+    if (k == 0 || skeys[k - 1] != key) {
+        table[(size_t)key * 4 + 0] = (int)k;
+        table[(size_t)key * 4 + 2] = (int)*stamp;
+    }
+    if (k == n - 1 || skeys[k + 1] != key) table[(size_t)key * 4 + 1] = (int)(k + 1);
+    const uint32_t id = sids[k];
+    const int fl = flags[id];
+    const float wi = w[id];
+    v3 xp, vp;
+    predict(x[id], v[id], wi, fl, pp, xp, vp);
+    rx[k] = make_float4(xp.x, xp.y, xp.z, r[id]);
+    rv[k] = make_float4(vp.x, vp.y, vp.z, wi);
+    rf[k] = fl;
+}
+
+void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
+                         const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf) {
+    if (n <= 0) return;
+    int blocks = (int)((n + 255) / 256);
+    k_cells_gather<<<blocks, 256, 0, s>>>(n, skeys, sids, x, v, w, r, flags, pp, reinterpret_cast<int*>(table),
+                                          stamp, rx, rv, rf);
+}
+
+}  // namespace xpbd

@@ -1,0 +1,313 @@
+// Particle contact generation against the ground plane and triangle meshes
+// (generate_plane_contacts.comp, generate_mesh_contacts.comp). One thread per
+// particle writes its own contacts into per-particle slots, so the contact
+// order is fixed (plane, then meshes in index order) without a global atomic
+// slot counter.
+#include "kernels.h"
+#include "particle.cuh"
+#include "xmath.cuh"
+
+namespace xpbd {
+
+__device__ __forceinline__ float dist_sq_aabb(v3 p, v3 lo, v3 hi) {  // generate_mesh_contacts.comp:32-35
+    const v3 d = mk3(gmax(gmax(lo.x - p.x, 0.0f), p.x - hi.x), gmax(gmax(lo.y - p.y, 0.0f), p.y - hi.y),
+                     gmax(gmax(lo.z - p.z, 0.0f), p.z - hi.z));
+    return vdot(d, d);
+}
+
+__device__ __forceinline__ float comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// generate_mesh_contacts.comp:77-113
+__device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
+    const v3 adir = mk3(fabsf(dir.x), fabsf(dir.y), fabsf(dir.z));
+    int kz = 0;
+    if (adir.y > adir.x) kz = 1;
+    if (adir.z > (kz == 1 ? adir.y : adir.x)) kz = 2;
+    int kx = kz + 1;
+    if (kx == 3) kx = 0;
+    int ky = kx + 1;
+    if (ky == 3) ky = 0;
+    if (comp(dir, kz) < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    const float Sx = __fdiv_rn(comp(dir, kx), comp(dir, kz));
+    const float Sy = __fdiv_rn(comp(dir, ky), comp(dir, kz));
+    const float Sz = __fdiv_rn(1.0f, comp(dir, kz));
+    const v3 A = vsub(a, p), B = vsub(b, p), C = vsub(c, p);
+    const float Ax = comp(A, kx) - Sx * comp(A, kz), Ay = comp(A, ky) - Sy * comp(A, kz);
+    const float Bx = comp(B, kx) - Sx * comp(B, kz), By = comp(B, ky) - Sy * comp(B, kz);
+    const float Cx = comp(C, kx) - Sx * comp(C, kz), Cy = comp(C, ky) - Sy * comp(C, kz);
+    const float U = diff_product(Cx, By, Cy, Bx);
+    const float V = diff_product(Ax, Cy, Ay, Cx);
+    const float W = diff_product(Bx, Ay, By, Ax);
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float Az = Sz * comp(A, kz), Bz = Sz * comp(B, kz), Cz = Sz * comp(C, kz);
+    const float T = U * Az + V * Bz + W * Cz;
+    if ((T < 0.0f && det > 0.0f) || (T > 0.0f && det < 0.0f)) return false;
+    return true;
+}
+
+// generate_mesh_contacts.comp:115-179
+__device__ void closest_point_triangle(v3 p, v3 a, v3 b, v3 c, v3& cp, v3& tri_normal, v3& bary) {
+    const v3 ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
+    tri_normal = vnormalize(vcross(ab, ac));
+    float u, v;
+    const float d1 = exact_dot(ab, ap), d2 = exact_dot(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) {
+        v = 0.0f;
+        u = 1.0f;
+    } else {
+        const v3 bp = vsub(p, b);
+        const float d3 = exact_dot(ab, bp), d4 = exact_dot(ac, bp);
+        if (d3 >= 0.0f && d4 <= d3) {
+            v = 1.0f;
+            u = 0.0f;
+        } else {
+            const float vc = __fmaf_rn(d1, d4, -(d2 * d3));
+            if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+                v = exact_div1(d1, d1 - d3);
+                u = 1.0f - v;
+            } else {
+                const v3 cp_p = vsub(p, c);
+                const float d5 = exact_dot(ab, cp_p), d6 = exact_dot(ac, cp_p);
+                if (d6 >= 0.0f && d5 <= d6) {
+                    v = 0.0f;
+                    u = 0.0f;
+                } else {
+                    const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
+                    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+                        const float w_val = exact_div1(d2, d2 - d6);
+                        v = 0.0f;
+                        u = 1.0f - w_val;
+                    } else {
+                        const float va = __fmaf_rn(d3, d6, -(d5 * d4));
+                        if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+                            const float w_val = exact_div1(d4 - d3, (d4 - d3) + (d5 - d6));
+                            v = 1.0f - w_val;
+                            u = (1.0f - v) - w_val;
+                        } else {
+                            const float sum_vavb = va + vb;
+                            const float sum_all = vc + sum_vavb;
+                            const float r0 = __frcp_rn(sum_all);
+                            const float rem = __fmaf_rn(-sum_all, r0, 1.0f);
+                            const float denom = __fmaf_rn(rem, r0, r0);
+                            v = vb * denom;
+                            u = __fmaf_rn(-vc, denom, 1.0f - v);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const float w_out = (1.0f - u) - v;
+    bary = mk3(u, v, w_out);
+    cp = vadd(vadd(vmuls(a, u), vmuls(b, v)), vmuls(c, w_out));
+}
+
+__device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
+    return mk3(__ldg(p + i * 3), __ldg(p + i * 3 + 1), __ldg(p + i * 3 + 2));
+}
+
+// generate_mesh_contacts.comp:199-412 for mesh ci; returns true and the contact when one is emitted
+__device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, float eps_md, float eps2, v3& body_pos,
+                           v3& shape_v, v3& nrm, DeviceStatus* st) {
+    const float PI_ = 3.14159265359f;
+    const float max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
+    uint32_t stack[32];
+    uint32_t sp = 0;
+    stack[sp++] = __ldg(&mt.roots[ci]);
+    float min_dist = max_dist;
+    v3 acc_normal = mk3(0.0f, 0.0f, 0.0f);
+    uint32_t min_face = 0;
+    float sv_v = 0.0f, sv_w = 0.0f;
+    bool found = false;
+    const bool wt = __ldg(&mt.watertight[ci]) != 0;
+    float min_dist_sq = max_dist * max_dist;
+    bool overflow = false;
+    while (sp > 0) {
+        const uint32_t ni = stack[--sp];
+        const float4 lo4 = __ldg(&mt.nl[ni]), hi4 = __ldg(&mt.nu[ni]);
+        const float nds = dist_sq_aabb(p, xyz(lo4), xyz(hi4));
+        if (wt) {
+            if (nds > min_dist_sq) continue;
+        } else {
+            if (nds > (min_dist + eps_md) * (min_dist + eps_md)) continue;
+        }
+        const uint32_t lpk = __float_as_uint(lo4.w);
+        const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
+        const uint32_t right_i = __float_as_uint(hi4.w) & 0x3FFFFFFFu;
+        if (is_leaf) {
+            for (uint32_t pc = left_i; pc < right_i; pc++) {
+                const uint32_t t = __ldg(&mt.prim[pc]);
+                const v3 a = ldv(mt.verts, __ldg(&mt.tris[t * 3])), b = ldv(mt.verts, __ldg(&mt.tris[t * 3 + 1])),
+                         c = ldv(mt.verts, __ldg(&mt.tris[t * 3 + 2]));
+                const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+                const v3 normal = vcross(e0, e1);
+                const float e0n = vdot(e0, e0), e1n = vdot(e1, e1), e2n = vdot(e2, e2);
+                if (__fdiv_rn(vlength(normal), (e0n + e1n + e2n)) < 1.0e-6f) continue;
+                v3 cp, tn, tb;
+                closest_point_triangle(p, a, b, c, cp, tn, tb);
+                if (wt) {
+                    const v3 diff = vsub(cp, p);
+                    const float dist_sq = vdot(diff, diff);
+                    if (dist_sq < min_dist_sq) {
+                        min_dist_sq = dist_sq;
+                        min_face = t;
+                        sv_v = tb.y;
+                        sv_w = tb.z;
+                        found = true;
+                    }
+                } else {
+                    const float dist = exact_length(vsub(cp, p));
+                    if (dist < min_dist + eps_md) {
+                        float weight;
+                        const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
+                        const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
+                        if (lcp < eps2) {
+                            weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
+                        } else if (lcq < eps2) {
+                            weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
+                        } else if (lcr < eps2) {
+                            weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
+                        } else {
+                            const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
+                            if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
+                                (lcp * e1n - e1cp * e1cp < eps2 * e1n))
+                                weight = PI_;
+                            else
+                                weight = 2.0f * PI_;
+                        }
+                        if (dist > min_dist - eps_md) {
+                            acc_normal = vadd(acc_normal, vmuls(tn, weight));
+                            if (dist < min_dist) {
+                                min_dist = dist;
+                                min_face = t;
+                                sv_v = tb.y;
+                                sv_w = tb.z;
+                            }
+                        } else {
+                            min_dist = dist;
+                            min_face = t;
+                            sv_v = tb.y;
+                            sv_w = tb.z;
+                            acc_normal = vmuls(tn, weight);
+                        }
+                        found = true;
+                    }
+                }
+            }
+        } else {
+            const float4 llo = __ldg(&mt.nl[left_i]), lhi = __ldg(&mt.nu[left_i]);
+            const float4 rlo = __ldg(&mt.nl[right_i]), rhi = __ldg(&mt.nu[right_i]);
+            const float lds = dist_sq_aabb(p, xyz(llo), xyz(lhi)), rds = dist_sq_aabb(p, xyz(rlo), xyz(rhi));
+            const float thresh = wt ? min_dist_sq : ((min_dist + eps_md) * (min_dist + eps_md));
+            // the shader's 32-entry stack has no bound check; a push past it is
+            // dropped here and reported through the status word
+            if (lds < rds) {
+                if (rds < thresh) { if (sp < 32) stack[sp++] = right_i; else overflow = true; }
+                if (lds < thresh) { if (sp < 32) stack[sp++] = left_i; else overflow = true; }
+            } else {
+                if (lds < thresh) { if (sp < 32) stack[sp++] = left_i; else overflow = true; }
+                if (rds < thresh) { if (sp < 32) stack[sp++] = right_i; else overflow = true; }
+            }
+        }
+    }
+    if (overflow) {
+        atomicOr(&st->error_bits, kErrStackOverflow);
+        atomicAdd(&st->stack_overflows, 1u);
+    }
+    if (wt) min_dist = exact_sqrt(min_dist_sq);
+    if (!(found && min_dist < max_dist)) return false;
+    const float u_mesh = (1.0f - sv_v) - sv_w;
+    const float v_mesh = sv_v;
+    const uint32_t i0 = __ldg(&mt.tris[min_face * 3]), i1 = __ldg(&mt.tris[min_face * 3 + 1]),
+                   i2 = __ldg(&mt.tris[min_face * 3 + 2]);
+    const v3 v0 = ldv(mt.verts, i0), v1 = ldv(mt.verts, i1), v2 = ldv(mt.verts, i2);
+    const float w_eval = (1.0f - u_mesh) - v_mesh;
+    const v3 shape_p = vfma_vs(v2, w_eval, vfma_vs(v0, u_mesh, vmuls(v1, v_mesh)));
+    const v3 vel0 = ldv(mt.vels, i0), vel1 = ldv(mt.vels, i1), vel2 = ldv(mt.vels, i2);
+    shape_v = vfma_vs(vel2, w_eval, vfma_vs(vel0, u_mesh, vmuls(vel1, v_mesh)));
+    float sign;
+    if (wt) {
+        const v3 ray_dir = mk3(1.029700994f, 1.086472273f, 1.034694910f);
+        uint32_t hits = 0;
+        const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
+        for (uint32_t ti = 0; ti < pn; ti++) {
+            const uint32_t t = __ldg(&mt.prim[po + ti]);
+            if (intersect_ray_tri_woop(p, ray_dir, ldv(mt.verts, __ldg(&mt.tris[t * 3])),
+                                       ldv(mt.verts, __ldg(&mt.tris[t * 3 + 1])),
+                                       ldv(mt.verts, __ldg(&mt.tris[t * 3 + 2]))))
+                hits++;
+        }
+        sign = (hits & 1u) ? -1.0f : 1.0f;
+    } else {
+        sign = vdot(acc_normal, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
+    }
+    const v3 delta = vsub(p, shape_p);
+    const float delta_len = exact_length(delta);
+    nrm = delta_len > 0.0f ? vmuls(exact_div(delta, delta_len), sign) : mk3(0.0f, 0.0f, 1.0f);
+    const float d = delta_len * sign;
+    body_pos = vfma_vs(vneg(nrm), d, p);
+    return true;
+}
+
+__global__ void __launch_bounds__(128) k_collide(int64_t n, const float4* __restrict__ x, const float* __restrict__ r,
+                                                 const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
+                                                 int slot_cap, uint32_t* __restrict__ cinfo,
+                                                 float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+    __shared__ uint32_t s_warp[4];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t count = 0;
+    if (i < n) {
+        uint32_t info = 0;
+        const int fl = flags[i];
+        if (fl & 1) {
+            const v3 p = xyz(x[i]);
+            const float radius = r[i];
+            if (pl.enabled) {  // generate_plane_contacts.comp:37-38
+                const float dist = p.z - pl.altitude;
+                if (dist < pl.margin + radius) info |= kPlaneBit;
+            }
+            if (mt.n_meshes > 0) {
+                const float eps_md = mt.avg_edge * 1e-3f;
+                const float eps2 = eps_md * eps_md;
+                int used = 0;
+                float4* slots = cslot + (size_t)i * slot_cap * 3;
+                for (int ci = 0; ci < mt.n_meshes; ci++) {
+                    v3 bp, bv, nn;
+                    if (mesh_query(mt, ci, p, radius, eps_md, eps2, bp, bv, nn, st)) {
+                        if (used < slot_cap) {
+                            slots[used * 3 + 0] = make_float4(bp.x, bp.y, bp.z, __int_as_float(ci + 1));
+                            slots[used * 3 + 1] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+                            slots[used * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+                            used++;
+                        } else {
+                            atomicOr(&st->error_bits, kErrSlotOverflow);
+                            atomicAdd(&st->slot_overflows, 1u);
+                        }
+                    }
+                }
+                info |= (uint32_t)used << 1;
+            }
+        }
+        cinfo[i] = info;
+        count = (info & kPlaneBit) + (info >> 1);
+    }
+    const uint32_t tot = block_sum(count, s_warp);
+    if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
+}
+
+void launch_collide(cudaStream_t s, int64_t n, const float4* x, const float* r, const int* flags, PlaneParams pl,
+                    MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount,
+                    DeviceStatus* st) {
+    if (n <= 0) return;
+    const int threads = 128;
+    k_collide<<<(int)((n + threads - 1) / threads), threads, 0, s>>>(n, x, r, flags, pl, mt, slot_cap, cinfo, cslot,
+                                                                     ccount, st);
+}
+
+}  // namespace xpbd

@@ -1,0 +1,190 @@
+// Fused XPBD iteration: one thread per particle in hash-grid order computes
+// its shape-contact deltas (solve_particle_shape_contacts.comp), its
+// particle-particle delta (solve_particle_particle_contacts.comp), applies
+// them (apply_particle_deltas.comp) and, on the last iteration, the
+// restitution increments (apply_particle_shape_restitution.comp).
+//
+// The reference accumulates deltas and restitution with float atomicAdd from
+// one thread per contact, so its summation order varies run to run. Here each
+// particle owns its contacts and sums them in the canonical order (plane, then
+// mesh slots, then the particle-particle total), which makes the step
+// deterministic and needs no delta buffer, no fill and no atomics.
+#include "contact.cuh"
+#include "kernels.h"
+#include "xmath.cuh"
+
+namespace xpbd {
+
+template <bool LAST, bool ALL_ACTIVE, bool DIAG>
+__global__ void __launch_bounds__(128) k_solve(int64_t n, const uint32_t* __restrict__ sids,
+                                               const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                               const int* __restrict__ rf, const int4* __restrict__ table,
+                                               const uint32_t* __restrict__ stamp_p, const float4* __restrict__ x0a,
+                                               const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
+                                               const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt,
+                                               SolveParams sp, float4* __restrict__ rx_out,
+                                               float4* __restrict__ rv_out, float4* __restrict__ x_out,
+                                               float4* __restrict__ v_out, SolveDiag dg) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t stamp = *stamp_p;
+    const uint32_t id = sids[k];
+    const float4 ox = rx[k], ov = rv[k];
+    const int pflag = ALL_ACTIVE ? 1 : rf[k];
+    const v3 xp = xyz(ox), vp = xyz(ov);
+    const float radius = ox.w, w1 = ov.w;
+    v3 x_new = xp, v_new = vp;
+    v3 delta = mk3(0.0f, 0.0f, 0.0f);
+
+    if (pflag & 1) {
+        const uint32_t info = cinfo ? cinfo[id] : 0u;
+        const v3 x0 = xyz(x0a[id]);
+        const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
+        const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
+        // shape contacts, canonical order (scene.cpp:946-947)
+        for (int c = 0; c < ncon; c++) {
+            if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
+            const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
+            v3 fd;
+            if (shape_delta(ct, pflag, xp, vp, radius, w1, bt, sp, fd)) delta = vadd(delta, fd);
+        }
+        // particle-particle contacts (solve_particle_particle_contacts.comp:116-217)
+        const int is_proxy = pflag & 2;
+        const float R = radius + sp.max_radius + sp.k_coh;
+        const float inv = sp.inv;
+        const int32_t xs = f2i(floorf((xp.x - R) * inv)), ys = f2i(floorf((xp.y - R) * inv)),
+                      zs = f2i(floorf((xp.z - R) * inv));
+        const int32_t xe = min(f2i(floorf((xp.x + R) * inv)), xs + kGridDim - 1);
+        const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
+        const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
+        v3 acc = mk3(0.0f, 0.0f, 0.0f);
+        for (int32_t cz = zs; cz <= ze; cz++) {
+            for (int32_t cy = ys; cy <= ye; cy++) {
+                for (int32_t cx = xs; cx <= xe; cx++) {
+                    const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                    if ((uint32_t)e.z != stamp) continue;
+                    for (int kk = e.x; kk < e.y; kk++) {
+                        if (kk == k) continue;
+                        const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
+                        if ((nflag & 1) == 0) continue;
+                        if (!ALL_ACTIVE && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
+                            continue;
+                        const float4 nx = __ldg(&rx[kk]);
+                        const v3 raw = vsub(xp, xyz(nx));
+                        if (fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R) continue;
+                        const float d = exact_length(raw);
+                        const float err = d - radius - nx.w;
+                        if (err > sp.k_coh || d <= 0.0f) continue;
+                        const float4 nv = __ldg(&rv[kk]);
+                        const float denom = w1 + nv.w;
+                        if (denom <= 0.0f) continue;
+                        const v3 nn = exact_div(raw, d);
+                        const v3 vrel = vsub(vp, xyz(nv));
+                        const float vn = exact_dot(nn, vrel);
+                        const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y),
+                                          __fmaf_rn(vn, -nn.z, vrel.z));
+                        const float vt_len = exact_length(vt);
+                        const float lambda_f = gmax(sp.k_mu * err, -vt_len * sp.dt);
+                        const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+                        const v3 p2 = vmuls(nn, err);
+                        const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
+                                            __fmaf_rn(vt_dir.z, lambda_f, -p2.z));
+                        const v3 pair_d = exact_div(diff, denom);
+                        acc = vadd(acc, pair_d);
+                        if (DIAG && dg.pair_header) {  // solve_particle_particle_contacts.comp:180-207
+                            const uint32_t slot = atomicAdd(&dg.pair_header[0], 1u);
+                            if (slot < dg.max_pairs) {
+                                float* rec = dg.pairs + (size_t)slot * 20;
+                                const v3 t = mk3(__fmaf_rn(pair_d.x, w1, 0.0f), __fmaf_rn(pair_d.y, w1, 0.0f),
+                                                 __fmaf_rn(pair_d.z, w1, 0.0f));
+                                rec[0] = __uint_as_float(id);
+                                rec[1] = __uint_as_float(__ldg(&sids[kk]));
+                                rec[2] = d;
+                                rec[3] = err;
+                                rec[4] = nn.x;
+                                rec[5] = nn.y;
+                                rec[6] = nn.z;
+                                rec[7] = vrel.x;
+                                rec[8] = vrel.y;
+                                rec[9] = vrel.z;
+                                rec[10] = vn;
+                                rec[11] = vt_len;
+                                rec[12] = denom;
+                                rec[13] = err;
+                                rec[14] = lambda_f;
+                                rec[15] = __fmaf_rn(t.x, sp.relax, 0.0f);
+                                rec[16] = __fmaf_rn(t.y, sp.relax, 0.0f);
+                                rec[17] = __fmaf_rn(t.z, sp.relax, 0.0f);
+                                rec[18] = __uint_as_float((uint32_t)sp.iter_index);
+                                rec[19] = 0.0f;
+                            } else {
+                                atomicAdd(&dg.pair_header[1], 1u);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
+        const v3 total = mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f),
+                             __fmaf_rn(dw.z, sp.relax, 0.0f));
+        delta = vadd(delta, total);
+        // apply_particle_deltas.comp:43-54
+        x_new = vadd(xp, delta);
+        v_new = exact_div_apply(vsub(x_new, x0), sp.dt);
+        const float v_mag = vlength(v_new);
+        if (v_mag > sp.v_max) {
+            v_new = vmuls(v_new, __fdiv_rn(sp.v_max, v_mag));
+            x_new = vadd(x0, vmuls(v_new, sp.dt));
+        }
+        if (LAST && sp.enable_restitution && ncon) {
+            const v3 v_old = xyz(v0a[id]);
+            const v3 v_snap = v_new;
+            for (int c = 0; c < ncon; c++) {
+                if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
+                const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
+                v3 dv;
+                if (restitution_dv(ct, v_snap, x0, v_old, radius, bt, sp, dv)) v_new = vadd(v_new, dv);
+            }
+        }
+    }
+    if (dg.delta_out) {
+        dg.delta_out[(size_t)id * 3 + 0] = delta.x;
+        dg.delta_out[(size_t)id * 3 + 1] = delta.y;
+        dg.delta_out[(size_t)id * 3 + 2] = delta.z;
+    }
+    if (LAST) {
+        x_out[id] = make_float4(x_new.x, x_new.y, x_new.z, 0.0f);
+        v_out[id] = make_float4(v_new.x, v_new.y, v_new.z, 0.0f);
+    } else {
+        rx_out[k] = make_float4(x_new.x, x_new.y, x_new.z, radius);
+        rv_out[k] = make_float4(v_new.x, v_new.y, v_new.z, w1);
+    }
+}
+
+void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const float4* rx,
+                  const float4* rv, const int* rf, const int4* table, const uint32_t* stamp, const float4* x0,
+                  const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
+                  SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg) {
+    if (n <= 0) return;
+    const int threads = 128;
+    const int blocks = (int)((n + threads - 1) / threads);
+    const bool diag = dg.pair_header != nullptr;
+#define XPBD_SOLVE(L, A, D)                                                                                      \
+    if (last == L && all_active == A && diag == D) {                                                             \
+        k_solve<L, A, D><<<blocks, threads, 0, s>>>(n, sids, rx, rv, rf, table, stamp, x0, v0, cinfo, cslot, cr, \
+                                                    bt, sp, rx_out, rv_out, x_out, v_out, dg);                   \
+        return;                                                                                                  \
+    }
+    XPBD_SOLVE(true, true, false)
+    XPBD_SOLVE(true, false, false)
+    XPBD_SOLVE(false, true, false)
+    XPBD_SOLVE(false, false, false)
+    XPBD_SOLVE(true, true, true)
+    XPBD_SOLVE(true, false, true)
+    XPBD_SOLVE(false, true, true)
+    XPBD_SOLVE(false, false, true)
+#undef XPBD_SOLVE
+}
+
+}  // namespace xpbd

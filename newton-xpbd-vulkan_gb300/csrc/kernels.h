@@ -1,0 +1,148 @@
+// Launch interface between the host scene driver (solver.cpp) and the sm_103a
+// kernels (k_*.cu). Plain structs of device pointers and scalars; every launch
+// takes the solver's stream so that a frame can be captured into one graph.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace xpbd {
+
+constexpr int kGridDim = 128;                                   // hash grid, src/scene.cpp:17-18
+constexpr int kNumCells = kGridDim * kGridDim * kGridDim;
+constexpr int kGridOrigin = 1 << 20;                            // grid_cell_indices.comp:20
+
+// Device-side status word read back after every frame. A kernel that gives
+// up (bounded wait expired, fixed-size buffer full) sets a bit and continues;
+// the host turns a set bit into an error instead of hanging or faulting.
+struct DeviceStatus {
+    uint32_t error_bits;
+    uint32_t lookback_timeouts;
+    uint32_t stack_overflows;
+    uint32_t slot_overflows;
+    uint32_t pad[4];
+};
+enum : uint32_t {
+    kErrLookbackTimeout = 1u,  // a decoupled look-back wait expired
+    kErrStackOverflow = 2u,    // BVH traversal stack (32 entries) full
+    kErrSlotOverflow = 4u,     // more mesh contacts for one particle than slots
+};
+
+// Per-particle contact header (cinfo[i]): bit 0 = plane contact (shape 0),
+// bits 1..15 = number of generic contact slots used in cslot.
+// A generic slot is 3 float4: (body_pos.xyz, shape as int bits),
+// (normal.xyz, 0), (body_vel.xyz, 0).
+constexpr uint32_t kPlaneBit = 1u;
+
+struct PredictParams {
+    float dt, v_max, gx, gy, gz, inv;
+};
+struct PlaneParams {
+    int enabled;
+    float margin, altitude;
+};
+
+struct BodyTables {
+    const int* shape_body;   // [n_shapes]
+    const float* shape_mu;   // [n_shapes]
+    const float4* body_q;    // 2 per body: (pos, pad), (quat xyzw)
+    const float4* body_qd;   // 2 per body: (lin, pad), (ang, pad)
+    const float* body_com;   // 3 per body
+    const float* body_invI;  // 9 per body, row-major (solve_particle_shape_contacts.comp:46-48)
+    const float* body_invm;  // [n_bodies]
+    const int* body_flags;   // [n_bodies]
+};
+
+struct MeshTables {
+    const float4* nl;         // packed node lowers (xyz, packed word)
+    const float4* nu;         // packed node uppers
+    const float* verts;       // 3 per vertex
+    const float* vels;        // 3 per vertex
+    const uint32_t* tris;     // 3 per triangle, global vertex indices
+    const uint32_t* prim;     // global triangle index per leaf slot
+    const uint32_t* roots;    // [n_meshes]
+    const float* margins;     // [n_meshes]
+    const int* watertight;    // [n_meshes]
+    const uint32_t* prim_off; // [n_meshes]
+    const uint32_t* prim_cnt; // [n_meshes]
+    int n_meshes;
+    float avg_edge;           // mesh 0's average edge length (scene.cpp:325)
+    float soft_margin;
+};
+
+struct SolveParams {
+    float dt, relax, v_max, inv, max_radius;
+    float k_mu, k_coh;        // particle_mu, particle_cohesion
+    float soft_mu, ka;        // soft_contact_mu, particle_adhesion
+    float restitution;
+    int enable_restitution;
+    float altitude;
+    int slot_cap;             // generic contact slots per particle
+    int iter_index;
+    int64_t contact_max;
+};
+
+// Optional debugging outputs of the solve kernel.
+struct SolveDiag {
+    float* delta_out;         // [3n] last iteration's deltas in particle order, or null
+    uint32_t* pair_header;    // [2]: pair count, overflow count
+    float* pairs;             // 20 words per record (vkx::GPUPairRecord layout)
+    uint32_t max_pairs;
+};
+
+// Contact ranks for the contact_max cap and for compaction (canonical order:
+// plane block by particle, then generic block by particle and slot).
+struct ContactRanks {
+    const uint2* rank;        // per particle (exclusive plane count, exclusive slot count), or null
+    const uint32_t* totals;   // [2] total plane contacts, total slot contacts
+};
+
+// ---------------------------------------------------------------- sort ----
+struct SortPlan {
+    int bits;      // digit width
+    int passes;    // ceil(key_bits / bits)
+    int threads;   // CTA size (== 2^bits for the shipped variants)
+    int items;     // keys per thread
+    int tile;      // threads * items
+    int tiles;     // ceil(n / tile)
+};
+SortPlan make_sort_plan(int64_t n, int key_bits, int bits, int items);
+size_t sort_lookback_words(const SortPlan& p);  // per pass
+
+// keys[i] (+ optional plane contacts, + all-pass digit histograms)
+void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
+                         const float* r, const int* flags, PredictParams pp, PlaneParams pl,
+                         uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
+                         uint32_t* ccount, uint32_t* stamp);
+// one onesweep pass; vals_in == nullptr means vals are the element index
+void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
+                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                          const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
+                          DeviceStatus* st);
+// cell table + sorted-order particle records
+void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
+                         const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
+// plane + mesh contact generation (particle order)
+void launch_collide(cudaStream_t s, int64_t n, const float4* x, const float* r, const int* flags, PlaneParams pl,
+                    MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, DeviceStatus* st);
+// fused shape solve + particle-particle solve + apply (+ restitution on the last iteration)
+void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const float4* rx,
+                  const float4* rv, const int* rf, const int4* table, const uint32_t* stamp, const float4* x0,
+                  const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
+                  SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg);
+// exclusive scan of per-particle (plane bit, slot count) for the contact_max cap / compaction
+size_t contact_scan_words(int64_t n);
+void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2* rank, uint32_t* totals,
+                         uint32_t* lookback, uint32_t* tile_counter, DeviceStatus* st);
+// canonical SoA contact list (for the getters)
+void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, const float4* cslot, int slot_cap,
+                            const uint2* rank, const uint32_t* totals, int64_t contact_max, const float4* x_prev,
+                            float altitude, int32_t* part, int32_t* shape, float* bpos, float* bvel, float* nrm);
+// reference-layout cell tables from the stamped table
+void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends);
+// float4 state -> packed xyz
+void launch_unpack_xyz(cudaStream_t s, int64_t n, const float4* a, float* out);
+void launch_pack_xyz(cudaStream_t s, int64_t n, const float* in, float4* a);
+
+}  // namespace xpbd

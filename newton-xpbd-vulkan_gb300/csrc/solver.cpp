@@ -1,0 +1,835 @@
+// Host scene driver (see solver.h). Mirrors src/scene.cpp's public behaviour;
+// the Vulkan command-buffer recording, descriptor sets, staging buffers and
+// fences are replaced by device allocations, one stream and one CUDA graph per
+// frame.
+#include "solver.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+namespace xpbd {
+
+void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+    if (e == cudaSuccess) return;
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "CUDA error %d (%s) at %s:%d: %s", (int)e, cudaGetErrorString(e), file, line,
+                  what);
+    throw std::runtime_error(buf);
+}
+
+namespace {
+constexpr int kKeyBits = 21;  // 128^3 cells
+// profiler stage slots (names follow scene.cpp:1481-1505)
+enum ProfSlot {
+    P_CONTACT = 0, P_INTEGRATE_KEYS, P_SORT, P_CELLS, P_SOLVE, P_RANKS, P_COUNT
+};
+const char* kProfNames[P_COUNT] = {
+    "1. Contact Gen (plane + mesh)", "2b. Integrate + Cell Keys", "2e. Onesweep Sort (all passes)",
+    "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)", "1b. Contact Ranks (cap)"};
+uint32_t f2u(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+float u2f(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+bool env_on(const char* name) {
+    const char* e = std::getenv(name);
+    return e && (std::strcmp(e, "1") == 0 || std::strcmp(e, "true") == 0);
+}
+}  // namespace
+
+Solver::Solver() = default;
+
+Solver::~Solver() {
+    if (!initialized_) return;
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (profiling_) print_profiler_summary();
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    for (auto e : prof_events_) cudaEventDestroy(e);
+    if (pinned_) cudaFreeHost(pinned_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Solver::require_init() const {
+    if (!initialized_) throw std::runtime_error("XpbdSolver not initialized");
+}
+
+void Solver::clear_graphs() {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+}
+
+void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_contacts) {
+    if (initialized_) throw std::runtime_error("XpbdSolver::init called twice");
+    cfg_ = cfg;
+    n_ = num_particles;
+    contact_max_ = (int64_t)(max_contacts ? max_contacts : num_particles * 2);  // scene.cpp:68
+    int ndev = 0;
+    XPBD_CUDA(cudaGetDeviceCount(&ndev));
+    if (ndev == 0) throw std::runtime_error("no CUDA device");
+    device_ = cfg.device_index >= 0 ? cfg.device_index : 0;
+    if (device_ >= ndev) throw std::runtime_error("device_index out of range");
+    XPBD_CUDA(cudaSetDevice(device_));
+    XPBD_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+
+    for (int p = 0; p < 2; p++) {
+        x_[p].alloc(n_);
+        v_[p].alloc(n_);
+        rx_[p].alloc(n_);
+        rv_[p].alloc(n_);
+    }
+    w_.alloc(n_);
+    r_.alloc(n_);
+    flags_.alloc(n_);
+    rf_.alloc(n_);
+    keys_.alloc(n_);
+    for (int p = 0; p < 2; p++) {
+        pair_k_[p].alloc(n_);
+        pair_v_[p].alloc(n_);
+    }
+    // digit width 8, 16 keys per thread above 1M particles, 8 below (more tiles per SM)
+    plan_ = make_sort_plan((int64_t)n_, kKeyBits, 8, n_ >= (1u << 20) ? 16 : 8);
+    hist_off_ = 0;
+    lb_off_ = (size_t)plan_.passes << plan_.bits;
+    tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
+    sort_scratch_.alloc(tc_off_ + (size_t)plan_.passes);
+    table_.alloc(kNumCells);
+    stamp_.alloc(1);
+    cinfo_.alloc(n_);
+    slot_cap_ = 1;
+    cslot_.alloc(std::max<size_t>(n_, 1) * 3);
+    ensure_substep_capacity(16);
+    rank_.alloc(n_);
+    totals_.alloc(2);
+    scan_ws_.alloc(contact_scan_words((int64_t)n_));
+    status_.alloc(1);
+    diag_header_.alloc(2);
+    xyz_stage_.alloc(std::max<size_t>(n_, 1) * 3);
+    pinned_words_ = std::max<size_t>(n_ * 4, 64);
+    XPBD_CUDA(cudaMallocHost(&pinned_, pinned_words_ * sizeof(float)));
+    if (cfg_.enable_diagnostics) {
+        delta_.alloc(std::max<size_t>(n_, 1) * 3);
+        uint32_t mp = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
+        diag_pairs_.alloc((size_t)mp * 20);
+    }
+    profiling_ = cfg_.enable_profile || env_on("VKXPBD_PROFILE");
+    if (profiling_) std::printf("[Newton GB300] GPU profiler ENABLED (CUDA events)\n");
+    initialized_ = true;
+}
+
+void Solver::ensure_substep_capacity(int substeps) {
+    if (substeps <= ccount_cap_) return;
+    int cap = std::max(substeps, 16);
+    ccount_.alloc((size_t)cap);
+    ccount_cap_ = cap;
+    clear_graphs();
+}
+
+void Solver::add_mesh(const float* verts, size_t num_verts, const uint32_t* tris, size_t num_tris,
+                      float shape_margin, const float* rot, int wt_override) {
+    MeshData md;
+    md.vertices.assign(verts, verts + num_verts * 3);
+    md.indices.assign(tris, tris + num_tris * 3);
+    md.shape_margin = shape_margin;
+    if (rot) std::memcpy(md.shape_rot, rot, sizeof(float) * 4);
+    md.is_watertight = wt_override >= 0 ? (wt_override != 0) : tris_watertight(tris, num_tris, num_verts);
+    for (size_t i = 0; i < num_tris * 3; i++)
+        if (tris[i] >= num_verts) throw std::runtime_error("add_mesh: triangle index out of range");
+    meshes_.push_back(std::move(md));
+    finalized_ = false;
+}
+
+void Solver::finalize_meshes() {
+    if (!initialized_) throw std::runtime_error("XpbdSolver::init must be called before finalize_meshes");
+    XPBD_CUDA(cudaSetDevice(device_));
+    const size_t nm = meshes_.size(), nshapes = 1 + nm;
+    // shapes: 0 = plane (body -1), c+1 = mesh c (body c); all bodies static (scene.cpp:206-247)
+    std::vector<int> sb(nshapes);
+    std::vector<float> smu(nshapes, cfg_.shape_material_mu);
+    sb[0] = -1;
+    for (size_t c = 0; c < nm; c++) sb[1 + c] = (int)c;
+    shape_body_.alloc(nshapes);
+    shape_mu_.alloc(nshapes);
+    XPBD_CUDA(cudaMemcpy(shape_body_.p, sb.data(), nshapes * sizeof(int), cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(shape_mu_.p, smu.data(), nshapes * sizeof(float), cudaMemcpyHostToDevice));
+    const size_t nb = std::max<size_t>(nm, 1);
+    std::vector<float4> bq(nb * 2, make_float4(0, 0, 0, 0));
+    for (size_t b = 0; b < nb; b++) bq[b * 2 + 1] = make_float4(0, 0, 0, 1);
+    body_q_.alloc(nb * 2);
+    XPBD_CUDA(cudaMemcpy(body_q_.p, bq.data(), bq.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    body_qd_.alloc(nb * 2);
+    body_com_.alloc(nb * 3);
+    body_invI_.alloc(nb * 9);
+    body_invm_.alloc(nb);
+    body_flags_.alloc(nb);
+
+    // per-mesh LBVH on the host, then one packed node array for all meshes (scene.cpp:249-386)
+    all_verts_.clear();
+    std::vector<uint32_t> all_tris;
+    vert_offsets_.assign(nm, 0);
+    node_offsets_.assign(nm, 0);
+    prim_offsets_.assign(nm, 0);
+    size_t total_nodes = 0, total_prims = 0;
+    for (size_t c = 0; c < nm; c++) {
+        MeshData& m = meshes_[c];
+        const uint32_t vo = (uint32_t)(all_verts_.size() / 3);
+        vert_offsets_[c] = vo;
+        all_verts_.insert(all_verts_.end(), m.vertices.begin(), m.vertices.end());
+        const size_t to = all_tris.size() / 3;
+        for (uint32_t t : m.indices) all_tris.push_back(t + vo);
+        const size_t nt = m.indices.size() / 3;
+        if (nt == 0) throw std::runtime_error("add_mesh: mesh has no triangles");
+        m.bvh.build(all_verts_.data(), all_tris.data() + to * 3, nt);
+        double sum_len = 0.0;  // scene.cpp:274-281
+        for (size_t t = 0; t < nt; t++)
+            for (int e = 0; e < 3; e++) {
+                const uint32_t i0 = all_tris[(to + t) * 3 + e], i1 = all_tris[(to + t) * 3 + (e + 1) % 3];
+                const float dx = all_verts_[i1 * 3] - all_verts_[i0 * 3];
+                const float dy = all_verts_[i1 * 3 + 1] - all_verts_[i0 * 3 + 1];
+                const float dz = all_verts_[i1 * 3 + 2] - all_verts_[i0 * 3 + 2];
+                sum_len += std::sqrt(dx * dx + dy * dy + dz * dz);
+            }
+        m.avg_edge = (float)(sum_len / (double)(nt * 3));
+        node_offsets_[c] = total_nodes;
+        prim_offsets_[c] = total_prims;
+        total_nodes += 2 * nt;
+        total_prims += nt;
+    }
+    all_vels_.assign(all_verts_.size(), 0.0f);
+    slot_cap_ = (int)std::max<size_t>(1, std::min<size_t>(nm, 8));
+    cslot_.alloc(std::max<size_t>(n_, 1) * (size_t)slot_cap_ * 3, false);
+    if (nm > 0) {
+        std::vector<float4> nl(total_nodes), nu(total_nodes);
+        std::vector<uint32_t> prim(total_prims), roots(nm), poff(nm), pcnt(nm);
+        std::vector<float> margins(nm);
+        std::vector<int> wt(nm);
+        size_t tbase = 0;
+        for (size_t c = 0; c < nm; c++) {
+            const HostBvh& b = meshes_[c].bvh;
+            const size_t nb2 = node_offsets_[c], pb = prim_offsets_[c], nnodes = b.lowers.size() / 4;
+            roots[c] = (uint32_t)(nb2 + b.root);
+            for (size_t i = 0; i < nnodes; i++) {
+                const uint32_t lw = f2u(b.lowers[i * 4 + 3]), uw = f2u(b.uppers[i * 4 + 3]);
+                uint32_t nlw, nuw;
+                if ((lw >> 30) & 3u) {  // leaf: primitive range rebased to the global prim array
+                    nlw = ((lw & 0x3FFFFFFFu) + (uint32_t)pb) | (1u << 30);
+                    nuw = (uw & 0x3FFFFFFFu) + (uint32_t)pb;
+                } else {  // inner: child indices rebased to the global node array
+                    nlw = (lw & 0x3FFFFFFFu) + (uint32_t)nb2;
+                    nuw = (uw & 0x3FFFFFFFu) + (uint32_t)nb2;
+                }
+                nl[nb2 + i] = make_float4(b.lowers[i * 4], b.lowers[i * 4 + 1], b.lowers[i * 4 + 2], u2f(nlw));
+                nu[nb2 + i] = make_float4(b.uppers[i * 4], b.uppers[i * 4 + 1], b.uppers[i * 4 + 2], u2f(nuw));
+            }
+            const size_t nt = b.prims.size();
+            for (size_t i = 0; i < nt; i++) prim[pb + i] = b.prims[i] + (uint32_t)tbase;
+            poff[c] = (uint32_t)pb;
+            pcnt[c] = (uint32_t)nt;
+            margins[c] = meshes_[c].shape_margin;
+            wt[c] = meshes_[c].is_watertight ? 1 : 0;
+            tbase += nt;
+        }
+        auto up = [&](auto& dev, const auto& host) {
+            dev.alloc(host.size(), false);
+            XPBD_CUDA(cudaMemcpy(dev.p, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice));
+        };
+        up(nl_, nl);
+        up(nu_, nu);
+        up(prim_, prim);
+        up(roots_, roots);
+        up(prim_off_, poff);
+        up(prim_cnt_, pcnt);
+        up(margins_, margins);
+        up(watertight_, wt);
+        up(verts_, all_verts_);
+        up(vels_, all_vels_);
+        up(tris_, all_tris);
+        avg_edge0_ = meshes_[0].avg_edge;  // mesh 0's average edge for every mesh (scene.cpp:325)
+    }
+    const int64_t possible = (int64_t)n_ * ((cfg_.has_ground_plane ? 1 : 0) + (int64_t)nm);
+    need_ranks_ = possible > contact_max_;
+    clear_graphs();
+    finalized_ = true;
+}
+
+void Solver::set_particles(const float* q, const float* qd, const float* inv_mass, const float* radii,
+                           const int32_t* flags, size_t n) {
+    if (!initialized_) throw std::runtime_error("XpbdSolver not initialized");
+    if (n != n_) throw std::runtime_error("Particle count mismatch");
+    XPBD_CUDA(cudaSetDevice(device_));
+    if (n == 0) return;
+    std::memcpy(pinned_, q, n * 3 * sizeof(float));
+    XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
+    launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, x_[cur_].p);
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    if (qd) {
+        std::memcpy(pinned_, qd, n * 3 * sizeof(float));
+        XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
+        launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, v_[cur_].p);
+    } else {
+        XPBD_CUDA(cudaMemsetAsync(v_[cur_].p, 0, n * sizeof(float4), stream_));
+    }
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    auto up = [&](void* dst, const void* src) {
+        std::memcpy(pinned_, src, n * 4);
+        XPBD_CUDA(cudaMemcpyAsync(dst, pinned_, n * 4, cudaMemcpyHostToDevice, stream_));
+        XPBD_CUDA(cudaStreamSynchronize(stream_));
+    };
+    if (inv_mass) up(w_.p, inv_mass);
+    if (radii) up(r_.p, radii);
+    if (flags) {
+        up(flags_.p, flags);
+        bool all = true;
+        for (size_t i = 0; i < n && all; i++) all = (flags[i] & 3) == 1;
+        if (all != all_active_) clear_graphs();  // the graphs bake in the all-active kernel variant
+        all_active_ = all;
+    }
+}
+
+void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const float* vels) {
+    if (!finalized_) throw std::runtime_error("update_mesh: call finalize_meshes() first");
+    if (mi >= meshes_.size()) throw std::runtime_error("update_mesh: mesh_index out of range");
+    MeshData& m = meshes_[mi];
+    if (num_verts != m.vertices.size() / 3) throw std::runtime_error("update_mesh: vertex count mismatch");
+    XPBD_CUDA(cudaSetDevice(device_));
+    const size_t vs = vert_offsets_[mi];
+    std::memcpy(all_verts_.data() + vs * 3, verts, num_verts * 3 * sizeof(float));
+    if (vels)
+        std::memcpy(all_vels_.data() + vs * 3, vels, num_verts * 3 * sizeof(float));
+    else
+        std::fill(all_vels_.begin() + vs * 3, all_vels_.begin() + (vs + num_verts) * 3, 0.0f);
+    std::copy(verts, verts + num_verts * 3, m.vertices.begin());
+    // refit on the host (topology unchanged), then upload this mesh's slices
+    std::vector<uint32_t> tris(m.indices.size());
+    for (size_t k = 0; k < tris.size(); k++) tris[k] = m.indices[k] + (uint32_t)vs;
+    m.bvh.refit(all_verts_.data(), tris.data());
+    const size_t nnodes = m.bvh.lowers.size() / 4, nb = node_offsets_[mi], pb = prim_offsets_[mi];
+    std::vector<float4> nl(nnodes), nu(nnodes);
+    for (size_t i = 0; i < nnodes; i++) {
+        const uint32_t lw = f2u(m.bvh.lowers[i * 4 + 3]), uw = f2u(m.bvh.uppers[i * 4 + 3]);
+        uint32_t nlw, nuw;
+        if ((lw >> 30) & 3u) {
+            nlw = ((lw & 0x3FFFFFFFu) + (uint32_t)pb) | (1u << 30);
+            nuw = (uw & 0x3FFFFFFFu) + (uint32_t)pb;
+        } else {
+            nlw = (lw & 0x3FFFFFFFu) + (uint32_t)nb;
+            nuw = (uw & 0x3FFFFFFFu) + (uint32_t)nb;
+        }
+        nl[i] = make_float4(m.bvh.lowers[i * 4], m.bvh.lowers[i * 4 + 1], m.bvh.lowers[i * 4 + 2], u2f(nlw));
+        nu[i] = make_float4(m.bvh.uppers[i * 4], m.bvh.uppers[i * 4 + 1], m.bvh.uppers[i * 4 + 2], u2f(nuw));
+    }
+    XPBD_CUDA(cudaMemcpyAsync(nl_.p + nb, nl.data(), nnodes * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    XPBD_CUDA(cudaMemcpyAsync(nu_.p + nb, nu.data(), nnodes * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    XPBD_CUDA(cudaMemcpyAsync(verts_.p + vs * 3, verts, num_verts * 3 * sizeof(float), cudaMemcpyHostToDevice,
+                              stream_));
+    XPBD_CUDA(cudaMemcpyAsync(vels_.p + vs * 3, all_vels_.data() + vs * 3, num_verts * 3 * sizeof(float),
+                              cudaMemcpyHostToDevice, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
+PredictParams Solver::predict_params(float sdt) const {
+    PredictParams p;
+    p.dt = sdt;
+    p.v_max = cfg_.particle_v_max;
+    p.gx = cfg_.gravity[0];
+    p.gy = cfg_.gravity[1];
+    p.gz = cfg_.gravity[2];
+    p.inv = 1.0f / cfg_.search_radius;
+    return p;
+}
+
+SolveParams Solver::solve_params(float sdt, int it) const {
+    SolveParams s;
+    s.dt = sdt;
+    s.relax = cfg_.soft_contact_relaxation;
+    s.v_max = cfg_.particle_v_max;
+    s.inv = 1.0f / cfg_.search_radius;
+    s.max_radius = cfg_.particle_max_radius;
+    s.k_mu = cfg_.particle_mu;
+    s.k_coh = cfg_.particle_cohesion;
+    s.soft_mu = cfg_.soft_contact_mu;
+    s.ka = cfg_.particle_adhesion;
+    s.restitution = cfg_.soft_contact_restitution;
+    s.enable_restitution = cfg_.enable_restitution ? 1 : 0;
+    s.altitude = cfg_.ground_plane_altitude;
+    s.slot_cap = injected_ ? inj_cap_ : slot_cap_;
+    s.iter_index = it;
+    s.contact_max = contact_max_;
+    return s;
+}
+
+BodyTables Solver::body_tables() const {
+    BodyTables b;
+    b.shape_body = shape_body_.p;
+    b.shape_mu = shape_mu_.p;
+    b.body_q = body_q_.p;
+    b.body_qd = body_qd_.p;
+    b.body_com = body_com_.p;
+    b.body_invI = body_invI_.p;
+    b.body_invm = body_invm_.p;
+    b.body_flags = body_flags_.p;
+    return b;
+}
+
+MeshTables Solver::mesh_tables() const {
+    MeshTables m{};
+    m.nl = nl_.p;
+    m.nu = nu_.p;
+    m.verts = verts_.p;
+    m.vels = vels_.p;
+    m.tris = tris_.p;
+    m.prim = prim_.p;
+    m.roots = roots_.p;
+    m.margins = margins_.p;
+    m.watertight = watertight_.p;
+    m.prim_off = prim_off_.p;
+    m.prim_cnt = prim_cnt_.p;
+    m.n_meshes = (int)meshes_.size();
+    m.avg_edge = avg_edge0_;
+    m.soft_margin = cfg_.soft_contact_margin;
+    return m;
+}
+
+void Solver::prof_mark(int slot) {
+    cudaEvent_t e;
+    XPBD_CUDA(cudaEventCreate(&e));
+    XPBD_CUDA(cudaEventRecord(e, stream_));
+    prof_events_.push_back(e);
+    prof_slots_.push_back(slot);
+}
+
+// One substep reading state parity `src` and writing parity 1-src.
+void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int src, bool timed) {
+    const int64_t n = (int64_t)n_;
+    const int dst = 1 - src;
+    const PredictParams pp = predict_params(sdt);
+    PlaneParams pl;
+    pl.enabled = cfg_.has_ground_plane ? 1 : 0;
+    pl.margin = cfg_.soft_contact_margin;
+    pl.altitude = cfg_.ground_plane_altitude;
+    uint32_t* ccount = ccount_.p + sub;
+    const bool gen = mode == Mode::Step;
+    const bool mesh_pass = gen && !meshes_.empty();
+    DeviceStatus* st = status_.p;
+
+    if (timed) prof_mark(-1);
+    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
+    if (mesh_pass) launch_collide(stream_, n, x_[src].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p,
+                                  cslot_.p, ccount, st);
+    if (timed) prof_mark(P_CONTACT);
+    // plane contacts are fused into the key kernel when there is no mesh pass
+    uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
+    launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, pl, keys_.p, plan_,
+                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
+    if (timed) prof_mark(P_INTEGRATE_KEYS);
+    const uint32_t* kin = keys_.p;
+    const uint32_t* vin = nullptr;
+    const size_t lbw = sort_lookback_words(plan_);
+    for (int p = 0; p < plan_.passes; p++) {
+        uint32_t* ko = pair_k_[p & 1].p;
+        uint32_t* vo = pair_v_[p & 1].p;
+        launch_onesweep_pass(stream_, n, plan_, p, kin, vin, ko, vo,
+                             sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
+                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st);
+        kin = ko;
+        vin = vo;
+    }
+    if (timed) prof_mark(P_SORT);
+    const uint32_t* skeys = kin;
+    const uint32_t* sids = vin;
+    const uint32_t* info = injected_ && !gen ? inj_info_.p : cinfo_.p;
+    const float4* slots = injected_ && !gen ? inj_slot_.p : cslot_.p;
+    ContactRanks cr{nullptr, nullptr};
+    if (gen && need_ranks_) {
+        launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, nullptr, st);
+        cr.rank = rank_.p;
+        cr.totals = totals_.p;
+    }
+    if (timed) prof_mark(P_RANKS);
+    launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
+                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
+    if (timed) prof_mark(P_CELLS);
+    SolveDiag dg{nullptr, nullptr, nullptr, 0};
+    if (cfg_.enable_diagnostics) {
+        dg.delta_out = delta_.p;
+        dg.pair_header = diag_header_.p;
+        dg.pairs = diag_pairs_.p;
+        dg.max_pairs = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
+    }
+    const BodyTables bt = body_tables();
+    for (int it = 0; it < iterations; it++) {
+        const bool last = it == iterations - 1;
+        launch_solve(stream_, n, last, all_active_, sids, rx_[it & 1].p, rv_[it & 1].p, rf_.p, table_.p, stamp_.p,
+                     x_[src].p, v_[src].p, info, slots, cr, bt, solve_params(sdt, it), rx_[(it + 1) & 1].p,
+                     rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg);
+    }
+    if (iterations <= 0) {  // no solver iteration: the predicted state is the result
+        XPBD_CUDA(cudaMemcpyAsync(x_[dst].p, x_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        XPBD_CUDA(cudaMemcpyAsync(v_[dst].p, v_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+    }
+    if (timed) prof_mark(P_SOLVE);
+}
+
+void Solver::record_frame(Mode mode, float dt, int substeps, int iterations, int parity, bool timed) {
+    const float sdt = dt / (float)substeps;  // scene.cpp:701
+    XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, (size_t)substeps * sizeof(uint32_t), stream_));
+    int src = parity;
+    for (int sub = 0; sub < substeps; sub++) {
+        record_substep(mode, sub, iterations, sdt, src, timed);
+        src = 1 - src;
+    }
+}
+
+void Solver::run_frame(Mode mode, float dt, int substeps, int iterations) {
+    if (substeps <= 0) throw std::runtime_error("step: substeps must be positive");
+    ensure_substep_capacity(substeps);
+    XPBD_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(DeviceStatus), stream_));
+    if (n_ == 0) {
+        XPBD_CUDA(cudaStreamSynchronize(stream_));
+        return;
+    }
+    auto t0 = std::chrono::high_resolution_clock::now();
+    if (profiling_) {
+        record_frame(mode, dt, substeps, iterations, cur_, true);
+    } else {
+        GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode};
+        auto it = graphs_.find(key);
+        if (it == graphs_.end()) {
+            cudaGraph_t g;
+            XPBD_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            try {
+                record_frame(mode, dt, substeps, iterations, cur_, false);
+            } catch (...) {
+                cudaStreamEndCapture(stream_, &g);
+                throw;
+            }
+            XPBD_CUDA(cudaStreamEndCapture(stream_, &g));
+            cudaGraphExec_t ex;
+            XPBD_CUDA(cudaGraphInstantiate(&ex, g, 0));
+            cudaGraphDestroy(g);
+            it = graphs_.emplace(key, ex).first;
+        }
+        XPBD_CUDA(cudaGraphLaunch(it->second, stream_));
+    }
+    last_collide_src_ = cur_ ^ ((substeps - 1) & 1);
+    cur_ ^= (substeps & 1);
+    finish_frame(substeps);
+    if (profiling_) {
+        double wall = std::chrono::duration<double, std::milli>(std::chrono::high_resolution_clock::now() - t0).count();
+        prof_wall_ms_ += wall;
+        int last_slot = -1;
+        for (size_t k = 0; k < prof_events_.size(); k++) {
+            if (k > 0 && prof_slots_[k] >= 0) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, prof_events_[k - 1], prof_events_[k]);
+                prof_ms_[prof_slots_[k]] += ms;
+            }
+            last_slot = prof_slots_[k];
+        }
+        (void)last_slot;
+        for (auto e : prof_events_) cudaEventDestroy(e);
+        prof_events_.clear();
+        prof_slots_.clear();
+        prof_substeps_ += (uint64_t)substeps;
+    }
+}
+
+void Solver::finish_frame(int substeps) {
+    // one small readback per frame: the last substep's contact count + status (scene.cpp:1086-1091)
+    XPBD_CUDA(cudaMemcpyAsync(pinned_, ccount_.p + (substeps - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              stream_));
+    XPBD_CUDA(cudaMemcpyAsync(pinned_ + 1, status_.p, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    uint32_t raw;
+    std::memcpy(&raw, pinned_, 4);
+    std::memcpy(&host_status_, pinned_ + 1, sizeof(DeviceStatus));
+    if (host_status_.error_bits & kErrLookbackTimeout)
+        throw std::runtime_error("device wait timed out in the onesweep look-back (result discarded)");
+    if (host_status_.error_bits & kErrStackOverflow)
+        throw std::runtime_error("BVH traversal stack overflow (more than 32 pending nodes)");
+    if (host_status_.error_bits & kErrSlotOverflow)
+        throw std::runtime_error("more mesh contacts for one particle than contact slots");
+    contact_count_ = (int)std::min<int64_t>((int64_t)raw, contact_max_);
+    if (env_on("VKXPBD_CHECK_SORT_ORDER")) check_sort_order();
+}
+
+void Solver::step(float dt, int substeps, int iterations) {
+    if (!finalized_) finalize_meshes();  // scene.cpp:699
+    XPBD_CUDA(cudaSetDevice(device_));
+    injected_ = false;
+    run_frame(Mode::Step, dt, substeps, iterations);
+}
+
+void Solver::step_solve_only(float dt, int substeps, int iterations) {
+    if (!finalized_) finalize_meshes();
+    XPBD_CUDA(cudaSetDevice(device_));
+    if (!injected_) {  // no injected contacts: solve with none
+        inj_info_.alloc(n_);
+        inj_slot_.alloc(std::max<size_t>(n_, 1) * 3);
+        inj_cap_ = 1;
+        injected_ = true;
+        clear_graphs();
+    }
+    const int keep = contact_count_;
+    run_frame(Mode::SolveOnly, dt, substeps, iterations);
+    contact_count_ = keep;
+}
+
+void Solver::collide_only() {
+    require_init();
+    if (!finalized_) finalize_meshes();
+    XPBD_CUDA(cudaSetDevice(device_));
+    injected_ = false;
+    PlaneParams pl;
+    pl.enabled = cfg_.has_ground_plane ? 1 : 0;
+    pl.margin = cfg_.soft_contact_margin;
+    pl.altitude = cfg_.ground_plane_altitude;
+    ensure_substep_capacity(1);
+    XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
+    XPBD_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(DeviceStatus), stream_));
+    launch_collide(stream_, (int64_t)n_, x_[cur_].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p, cslot_.p,
+                   ccount_.p, status_.p);
+    last_collide_src_ = cur_;
+    finish_frame(1);
+}
+
+void Solver::set_contact_data(const int32_t* part, const int32_t* shape, const float* bpos, const float* nrm,
+                              int count) {
+    require_init();
+    if (!finalized_) finalize_meshes();
+    XPBD_CUDA(cudaSetDevice(device_));
+    contact_count_ = count;  // scene.cpp:1309
+    const size_t m = count > 0 ? std::min<size_t>((size_t)count, (size_t)contact_max_) : 0;
+    inj_part_.assign(part, part + m);
+    inj_shape_.assign(shape, shape + m);
+    inj_bpos_.assign(bpos, bpos + m * 3);
+    inj_nrm_.assign(nrm, nrm + m * 3);
+    // bucket by particle, keeping the given order inside a particle
+    std::vector<uint32_t> cnt(n_, 0);
+    for (size_t t = 0; t < m; t++) {
+        if (part[t] < 0 || (size_t)part[t] >= n_) throw std::runtime_error("set_contact_data: particle index out of range");
+        if (shape[t] < 0 || (size_t)shape[t] > meshes_.size())
+            throw std::runtime_error("set_contact_data: shape index out of range");
+        cnt[part[t]]++;
+    }
+    uint32_t cap = 1;
+    for (uint32_t c : cnt) cap = std::max(cap, c);
+    std::vector<float4> slots(n_ * cap * 3, make_float4(0, 0, 0, 0));
+    std::vector<uint32_t> info(n_, 0);
+    for (size_t t = 0; t < m; t++) {
+        const size_t i = (size_t)part[t];
+        const uint32_t k = info[i] >> 1;
+        float4* s = &slots[(i * cap + k) * 3];
+        s[0] = make_float4(bpos[t * 3], bpos[t * 3 + 1], bpos[t * 3 + 2], u2f((uint32_t)shape[t]));
+        s[1] = make_float4(nrm[t * 3], nrm[t * 3 + 1], nrm[t * 3 + 2], 0.0f);
+        s[2] = make_float4(0, 0, 0, 0);  // the reference uploads no body velocity here
+        info[i] = (k + 1) << 1;
+    }
+    if (!injected_ || (int)cap != inj_cap_) clear_graphs();
+    inj_cap_ = (int)cap;
+    inj_info_.alloc(n_, false);
+    inj_slot_.alloc(std::max<size_t>(n_ * cap * 3, 1), false);
+    if (n_) {
+        XPBD_CUDA(cudaMemcpy(inj_info_.p, info.data(), n_ * 4, cudaMemcpyHostToDevice));
+        XPBD_CUDA(cudaMemcpy(inj_slot_.p, slots.data(), slots.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    injected_ = true;
+}
+
+void Solver::get_positions(float* out, size_t n) {
+    if (!initialized_) return;
+    n = std::min(n, n_);
+    if (n == 0) return;
+    XPBD_CUDA(cudaSetDevice(device_));
+    launch_unpack_xyz(stream_, (int64_t)n, x_[cur_].p, xyz_stage_.p);
+    XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    std::memcpy(out, pinned_, n * 3 * sizeof(float));
+}
+
+void Solver::get_velocities(float* out, size_t n) {
+    if (!initialized_) return;
+    n = std::min(n, n_);
+    if (n == 0) return;
+    XPBD_CUDA(cudaSetDevice(device_));
+    launch_unpack_xyz(stream_, (int64_t)n, v_[cur_].p, xyz_stage_.p);
+    XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    std::memcpy(out, pinned_, n * 3 * sizeof(float));
+}
+
+void Solver::compact_contacts() {
+    const size_t cm = (size_t)std::max<int64_t>(contact_max_, 1);
+    if (c_part_.n < cm) {
+        c_part_.alloc(cm, false);
+        c_shape_.alloc(cm, false);
+        c_bpos_.alloc(cm * 3, false);
+        c_bvel_.alloc(cm * 3, false);
+        c_nrm_.alloc(cm * 3, false);
+    }
+    launch_contact_scan(stream_, (int64_t)n_, cinfo_.p, rank_.p, totals_.p, scan_ws_.p, nullptr, status_.p);
+    launch_contact_compact(stream_, (int64_t)n_, cinfo_.p, cslot_.p, slot_cap_, rank_.p, totals_.p, contact_max_,
+                           x_[last_collide_src_].p, cfg_.ground_plane_altitude, c_part_.p, c_shape_.p, c_bpos_.p,
+                           c_bvel_.p, c_nrm_.p);
+}
+
+void Solver::get_contacts(int32_t* part, int32_t* shape, float* nrm, float* bpos, float* bvel) {
+    if (!initialized_ || contact_count_ <= 0) return;
+    const size_t m = (size_t)contact_count_;
+    if (injected_) {  // the buffers hold the injected contacts (scene.cpp:1304-1315)
+        const size_t k = std::min(m, inj_part_.size());
+        if (part) std::memcpy(part, inj_part_.data(), k * 4);
+        if (shape) std::memcpy(shape, inj_shape_.data(), k * 4);
+        if (nrm) std::memcpy(nrm, inj_nrm_.data(), k * 12);
+        if (bpos) std::memcpy(bpos, inj_bpos_.data(), k * 12);
+        if (bvel) std::memset(bvel, 0, k * 12);
+        return;
+    }
+    XPBD_CUDA(cudaSetDevice(device_));
+    compact_contacts();
+    auto dl = [&](void* dst, const void* src, size_t bytes) {
+        if (dst) XPBD_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream_));
+    };
+    dl(part, c_part_.p, m * 4);
+    dl(shape, c_shape_.p, m * 4);
+    dl(nrm, c_nrm_.p, m * 12);
+    dl(bpos, c_bpos_.p, m * 12);
+    dl(bvel, c_bvel_.p, m * 12);
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Solver::get_sorted(uint32_t* cells, uint32_t* ids, size_t n) {
+    if (!initialized_) return;
+    n = std::min(n, n_);
+    XPBD_CUDA(cudaSetDevice(device_));
+    const int fin = (plan_.passes - 1) & 1;
+    if (cells) XPBD_CUDA(cudaMemcpyAsync(cells, pair_k_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
+    if (ids) XPBD_CUDA(cudaMemcpyAsync(ids, pair_v_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Solver::get_cell_tables(int32_t* starts, int32_t* ends) {
+    require_init();
+    XPBD_CUDA(cudaSetDevice(device_));
+    if (!cell_starts_.p) {
+        cell_starts_.alloc(kNumCells, false);
+        cell_ends_.alloc(kNumCells, false);
+    }
+    launch_cell_tables(stream_, table_.p, stamp_.p, cell_starts_.p, cell_ends_.p);
+    if (starts) XPBD_CUDA(cudaMemcpyAsync(starts, cell_starts_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
+    if (ends) XPBD_CUDA(cudaMemcpyAsync(ends, cell_ends_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Solver::get_deltas(float* out, size_t n) {
+    if (!initialized_) return;
+    n = std::min(n, n_);
+    if (!delta_.p) {
+        std::memset(out, 0, n * 12);
+        return;
+    }
+    XPBD_CUDA(cudaSetDevice(device_));
+    XPBD_CUDA(cudaMemcpy(out, delta_.p, n * 12, cudaMemcpyDeviceToHost));
+}
+
+size_t Solver::mesh_bvh(size_t mi, float* lowers, float* uppers, size_t cap) {
+    if (mi >= meshes_.size() || !finalized_) return 0;
+    const HostBvh& b = meshes_[mi].bvh;
+    const size_t nn = b.lowers.size() / 4;
+    if (lowers) std::memcpy(lowers, b.lowers.data(), std::min(cap, nn) * 16);
+    if (uppers) std::memcpy(uppers, b.uppers.data(), std::min(cap, nn) * 16);
+    return nn;
+}
+
+uint32_t Solver::diag_pair_count() {
+    if (!initialized_) return 0;
+    uint32_t h[2];
+    XPBD_CUDA(cudaSetDevice(device_));
+    XPBD_CUDA(cudaMemcpy(h, diag_header_.p, 8, cudaMemcpyDeviceToHost));
+    return h[0];
+}
+uint32_t Solver::diag_overflow_count() {
+    if (!initialized_) return 0;
+    uint32_t h[2];
+    XPBD_CUDA(cudaSetDevice(device_));
+    XPBD_CUDA(cudaMemcpy(h, diag_header_.p, 8, cudaMemcpyDeviceToHost));
+    return h[1];
+}
+void Solver::reset_diag_buffers() {
+    if (!initialized_) return;
+    XPBD_CUDA(cudaSetDevice(device_));
+    XPBD_CUDA(cudaMemset(diag_header_.p, 0, 8));
+}
+size_t Solver::diag_pairs(xpbd_pair_record* out, size_t cap) {
+    if (!diag_pairs_.p) return 0;
+    const uint32_t mp = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
+    const size_t avail = std::min<uint32_t>(diag_pair_count(), mp);  // bindings.cpp:364-372
+    const size_t k = std::min(avail, cap);
+    if (out && k) XPBD_CUDA(cudaMemcpy(out, diag_pairs_.p, k * sizeof(xpbd_pair_record), cudaMemcpyDeviceToHost));
+    return avail;
+}
+// The reference binds these buffers but no shader writes them (the shape,
+// apply and mesh shaders declare no binding for them), so they read back as
+// zeros of the sizes scene.cpp:117-128 allocates.
+size_t Solver::aux_diag(int which, void* out, size_t cap) {
+    size_t len = 32;
+    if (which == 2)
+        len = cfg_.enable_diagnostics ? (size_t)4 * (size_t)(contact_max_ > 0 ? contact_max_ : 100000) * 32 : 32;
+    if (!initialized_) len = 0;
+    if (out) std::memset(out, 0, std::min(cap, len) * 4);
+    return len;
+}
+
+void Solver::status(uint32_t out[4]) const {
+    out[0] = host_status_.error_bits;
+    out[1] = host_status_.lookback_timeouts;
+    out[2] = host_status_.stack_overflows;
+    out[3] = host_status_.slot_overflows;
+}
+
+void Solver::check_sort_order() {  // scene.cpp:1064-1084
+    std::vector<uint32_t> keys(n_);
+    get_sorted(keys.data(), nullptr, n_);
+    for (size_t i = 1; i < keys.size(); i++)
+        if (keys[i] < keys[i - 1]) {
+            std::fprintf(stderr, "[VKXPBD SORT CHECK ERROR] keys[%zu] = %u < keys[%zu] = %u!\n", i, keys[i], i - 1,
+                         keys[i - 1]);
+            return;
+        }
+    std::printf("[VKXPBD DEBUG] Sort check passed: %zu keys strictly non-decreasing.\n", keys.size());
+}
+
+void Solver::print_profiler_summary() {
+    if (!profiling_ || prof_substeps_ == 0) return;
+    double total = 0;
+    for (int i = 0; i < P_COUNT; i++) total += prof_ms_[i];
+    const double ns = (double)prof_substeps_;
+    const double gap = prof_wall_ms_ > total ? prof_wall_ms_ - total : 0.0;
+    std::printf("\n========================================================================================================\n");
+    std::printf("                               VKXPBD GPU TIMESTAMP PROFILER SUMMARY (CUDA events)                      \n");
+    std::printf("========================================================================================================\n");
+    std::printf("Total Substeps Recorded: %llu\n", (unsigned long long)prof_substeps_);
+    std::printf("Wall-Clock Step Time:    %10.2f ms (%8.4f ms/substep)\n", prof_wall_ms_, prof_wall_ms_ / ns);
+    std::printf("Summed GPU Active Time:  %10.2f ms (%8.4f ms/substep)\n", total, total / ns);
+    std::printf("Host / Sync Idle Gap:    %10.2f ms (%8.4f ms/substep, %5.1f%% of wall)\n", gap, gap / ns,
+                gap / (prof_wall_ms_ > 0 ? prof_wall_ms_ : 1.0) * 100.0);
+    std::printf("%-35s | %10s | %14s | %10s\n", "Kernel / Stage Group", "Total (ms)", "Per-Substep (ms)", "% GPU Time");
+    for (int i = 0; i < P_COUNT; i++)
+        std::printf("%-35s | %10.2f | %14.4f | %9.2f%%\n", kProfNames[i], prof_ms_[i], prof_ms_[i] / ns,
+                    prof_ms_[i] / (total > 0 ? total : 1.0) * 100.0);
+    std::printf("========================================================================================================\n\n");
+    std::fflush(stdout);
+}
+
+}  // namespace xpbd

@@ -1,0 +1,209 @@
+// Host scene driver: the GB300 counterpart of vkx::XpbdSolver
+// (src/scene.h:74-227, src/scene.cpp). Owns all device memory of one scene,
+// records one CUDA graph per (dt, substeps, iterations, state parity) and
+// replays it per frame.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/xpbd.h"
+#include "kernels.h"
+
+namespace xpbd {
+
+void cuda_check(cudaError_t e, const char* what, const char* file, int line);
+#define XPBD_CUDA(x) ::xpbd::cuda_check((x), #x, __FILE__, __LINE__)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void alloc(size_t count, bool zero = true) {
+        release();
+        n = count;
+        if (count) {
+            XPBD_CUDA(cudaMalloc(&p, count * sizeof(T)));
+            if (zero) XPBD_CUDA(cudaMemset(p, 0, count * sizeof(T)));
+        }
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// CPU LBVH over one triangle mesh, same topology as MeshLbvhBuilder::build
+// (src/mesh_lbvh.h:49-223). Node halves are 4 floats (xyz + packed word).
+struct HostBvh {
+    std::vector<float> lowers, uppers;  // 2*T nodes x 4
+    std::vector<uint32_t> prims;        // T
+    uint32_t root = 0;
+    void build(const float* pts, const uint32_t* tris, size_t num_tris);
+    void refit(const float* pts, const uint32_t* tris);
+};
+
+struct MeshData {  // src/scene.h:66-72
+    std::vector<float> vertices;
+    std::vector<uint32_t> indices;
+    float shape_margin = 0.0f;
+    float shape_rot[4] = {0.f, 0.f, 0.f, 1.f};
+    bool is_watertight = false;
+    HostBvh bvh;
+    float avg_edge = 0.0f;
+};
+
+bool tris_watertight(const uint32_t* tris, size_t num_tris, size_t num_verts);
+
+class Solver {
+   public:
+    Solver();
+    ~Solver();
+
+    void init(const xpbd_config& cfg, size_t num_particles, size_t max_contacts);
+    void add_mesh(const float* verts, size_t num_verts, const uint32_t* tris, size_t num_tris, float shape_margin,
+                  const float* rot_xyzw, int watertight_override);
+    void finalize_meshes();
+    void set_particles(const float* q, const float* qd, const float* inv_mass, const float* radii,
+                       const int32_t* flags, size_t n);
+    void update_mesh(size_t mesh_index, const float* verts, size_t num_verts, const float* vels);
+    void step(float dt, int substeps, int iterations);
+    void collide_only();
+    void step_solve_only(float dt, int substeps, int iterations);
+
+    void get_positions(float* out, size_t n);
+    void get_velocities(float* out, size_t n);
+    size_t particle_count() const { return n_; }
+    size_t mesh_count() const { return meshes_.size(); }
+    int last_contact_count() const { return contact_count_; }
+    void get_contacts(int32_t* part, int32_t* shape, float* nrm, float* bpos, float* bvel);
+    void set_contact_data(const int32_t* part, const int32_t* shape, const float* bpos, const float* nrm,
+                          int count);
+    void get_sorted(uint32_t* cells, uint32_t* ids, size_t n);
+    void get_cell_tables(int32_t* starts, int32_t* ends);
+    void get_deltas(float* out, size_t n);
+    size_t mesh_bvh(size_t mesh_index, float* lowers, float* uppers, size_t cap);
+    uint32_t diag_pair_count();
+    uint32_t diag_overflow_count();
+    void reset_diag_buffers();
+    size_t diag_pairs(xpbd_pair_record* out, size_t cap);
+    size_t aux_diag(int which, void* out, size_t cap);
+    void print_profiler_summary();
+    void status(uint32_t out[4]) const;
+
+   private:
+    enum class Mode { Step, SolveOnly };
+    struct GraphKey {
+        uint32_t dt_bits;
+        int substeps, iterations, parity, mode;
+        bool operator<(const GraphKey& o) const {
+            return std::tie(dt_bits, substeps, iterations, parity, mode) <
+                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode);
+        }
+    };
+    void require_init() const;
+    void clear_graphs();
+    void ensure_substep_capacity(int substeps);
+    void record_frame(Mode mode, float dt, int substeps, int iterations, int parity, bool timed);
+    void record_substep(Mode mode, int sub, int iterations, float sdt, int src, bool timed);
+    void run_frame(Mode mode, float dt, int substeps, int iterations);
+    void finish_frame(int substeps);
+    void compact_contacts();
+    void check_sort_order();
+    PredictParams predict_params(float sdt) const;
+    SolveParams solve_params(float sdt, int it) const;
+    BodyTables body_tables() const;
+    MeshTables mesh_tables() const;
+    void prof_mark(int slot);
+
+    xpbd_config cfg_{};
+    bool initialized_ = false, finalized_ = false;
+    int device_ = 0;
+    size_t n_ = 0;
+    int64_t contact_max_ = 0;
+    int contact_count_ = 0;
+    cudaStream_t stream_ = nullptr;
+
+    std::vector<MeshData> meshes_;
+    std::vector<size_t> vert_offsets_, node_offsets_, prim_offsets_;
+    std::vector<float> all_verts_, all_vels_;
+
+    // particle state, original order: [parity]
+    DevBuf<float4> x_[2], v_[2];
+    DevBuf<float> w_, r_;
+    DevBuf<int> flags_;
+    int cur_ = 0;
+    bool all_active_ = false;
+    // hash grid and sort
+    SortPlan plan_{};
+    DevBuf<uint32_t> keys_, pair_k_[2], pair_v_[2];
+    DevBuf<uint32_t> sort_scratch_;  // hist | lookback | tile counters (cleared per substep)
+    size_t hist_off_ = 0, lb_off_ = 0, tc_off_ = 0;
+    DevBuf<int4> table_;
+    DevBuf<uint32_t> stamp_;
+    DevBuf<float4> rx_[2], rv_[2];
+    DevBuf<int> rf_;
+    // contacts
+    int slot_cap_ = 1;
+    DevBuf<uint32_t> cinfo_;
+    DevBuf<float4> cslot_;
+    DevBuf<uint32_t> ccount_;  // one counter per substep of the frame
+    int ccount_cap_ = 0;
+    bool need_ranks_ = false;
+    DevBuf<uint2> rank_;
+    DevBuf<uint32_t> totals_, scan_ws_;
+    int last_collide_src_ = 0;  // parity of the positions the last collision pass read
+    // injected contacts (set_contact_data / step_solve_only)
+    bool injected_ = false;
+    int inj_cap_ = 1;
+    DevBuf<uint32_t> inj_info_;
+    DevBuf<float4> inj_slot_;
+    std::vector<int32_t> inj_part_, inj_shape_;
+    std::vector<float> inj_bpos_, inj_nrm_;
+    // shapes / bodies / meshes on device
+    DevBuf<int> shape_body_;
+    DevBuf<float> shape_mu_;
+    DevBuf<float4> body_q_, body_qd_;
+    DevBuf<float> body_com_, body_invI_, body_invm_;
+    DevBuf<int> body_flags_;
+    DevBuf<float4> nl_, nu_;
+    DevBuf<float> verts_, vels_;
+    DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
+    DevBuf<float> margins_;
+    DevBuf<int> watertight_;
+    float avg_edge0_ = 0.0f;
+    // diagnostics
+    DevBuf<float> delta_;
+    DevBuf<uint32_t> diag_header_;
+    DevBuf<float> diag_pairs_;
+    DevBuf<DeviceStatus> status_;
+    DeviceStatus host_status_{};
+    // staging
+    DevBuf<float> xyz_stage_;
+    float* pinned_ = nullptr;  // max(4n, ...) floats
+    size_t pinned_words_ = 0;
+    DevBuf<int32_t> c_part_, c_shape_;
+    DevBuf<float> c_bpos_, c_bvel_, c_nrm_;
+    DevBuf<int32_t> cell_starts_, cell_ends_;
+    // graphs
+    std::map<GraphKey, cudaGraphExec_t> graphs_;
+    // profiler (scene.cpp:1438-1515 stage names)
+    bool profiling_ = false;
+    std::vector<cudaEvent_t> prof_events_;
+    std::vector<int> prof_slots_;
+    double prof_ms_[16] = {0};
+    uint64_t prof_substeps_ = 0;
+    double prof_wall_ms_ = 0.0;
+};
+
+}  // namespace xpbd

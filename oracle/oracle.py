@@ -19,10 +19,10 @@ REFDIR = os.path.join(HERE, "_ref")
 NUM_CELLS = 128 ** 3
 
 
-def build(ref_checkout: str | None = None) -> None:
+def build() -> None:
+    """Oracle libraries, plus the reference's BVH shim where the checkout exists (Makefile REF)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "-j2", "all"])
-    if ref_checkout and os.path.isdir(os.path.join(ref_checkout, "src")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref_checkout}"])
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref-if-present"])
 
 
 class Config(C.Structure):
