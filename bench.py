@@ -1,0 +1,355 @@
+"""Benchmark: particle-substeps/s of the XPBD substep on one GB300.
+
+Workload (default): the particles-on-a-mesh scene — 262,144 particles
+(64^3 lattice, r = 0.005 m, seeded jitter) falling onto a 256x256-vertex
+sum-of-sines heightfield (130,050 triangles) with plane, mesh and
+particle-particle contacts, dt = 1/60 s, 10 substeps, 1 solver iteration,
+FP32. One step = one frame (10 substeps) of one continuous run: the scene is
+pre-rolled for --preroll frames (so the pile is in contact), then --warmup
+frames, then --steps timed frames. L2 is flushed (256 MiB write on the
+solver's stream) between timed frames; frame times come from CUDA events on
+the solver's stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--preroll P] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's shaders (the
+oracle, all host threads) on the same pre-rolled scene, one substep per step.
+Under torchrun every rank steps its own replica of the scene (the path does
+not shard); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "newton-xpbd-vulkan_gb300"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-substeps/s on 1 GB300, plain vs batched graph; fwd+bwd vs fwd time"
+UNIT = "particle-substeps/s"
+DT = 1.0 / 60.0
+SUBSTEPS = 10
+ITERATIONS = 1
+FLUSH_BYTES = 256 << 20
+
+# Algorithmic bytes per particle for one launch of each kernel (xyz vectors count
+# 12 B, scalars 4 B; neighbour gathers, contacts, BVH nodes and the cell table
+# count 0 — they can stay cache-resident). The whole substep's compulsory
+# traffic is 76 B per particle-substep at one iteration.
+ALG_BYTES = {
+    "1. Contact Gen (plane + mesh)": 24,       # x, r, flags in; contact header out
+    "2b. Integrate + Cell Keys": 40,           # x, v, w, flags, r in; key, header out
+    "2e. Onesweep Pass 0": 12,                 # key in; key, id out
+    "2e. Onesweep Pass 1": 16,                 # key, id in and out
+    "2e. Onesweep Pass 2": 16,
+    "2e. Onesweep Pass 3": 16,
+    "2g. Cell Table + Gather": 76,             # sorted key, id, x, v, w, r, flags in; records out
+    "3. Solve+Apply(+Restitution)": 96,        # records, id, x0, v0, header in; x, v out
+}
+STEP_ALG_BYTES = 76
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def reduce_max(value: float, world: int) -> float:
+    """Max over ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def build_scene(args):
+    from vkxpbd import scenes
+
+    return scenes.particles_on_mesh(frames=300)
+
+
+def make_solver(sc, device_index=-1):
+    import vkxpbd
+
+    cfg = vkxpbd.SolverConfig()
+    sc.apply_config(cfg)
+    cfg.device_index = device_index
+    s = vkxpbd.XpbdSolver()
+    s.init(cfg, sc.n)
+    for (v, t, margin, wt) in sc.meshes:
+        s.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
+    s.finalize_meshes()
+    s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+    return s, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dram_traffic(kernel_stage: str):
+    """Per-launch DRAM bytes of a kernel at this workload from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(kernel_stage)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_sample(sc, cfg, x, v, budget_s=15.0):
+    """Oracle (CPU restatement, all host threads) on the pre-rolled state: a bounded number of substeps."""
+    import oracle as O
+    from helpers import make_pair
+
+    O.load("f32").or_set_threads(os.cpu_count() or 1)
+    _, orc = make_pair(sc, cfg, gpu=False)
+    orc.set_particles(x, v)
+    t0 = time.perf_counter()
+    orc.step(DT, SUBSTEPS, ITERATIONS)  # one frame = SUBSTEPS substeps (dt/substeps each)
+    t1 = time.perf_counter() - t0
+    substeps = SUBSTEPS
+    frames = max(0, min(20, int(budget_s / max(t1, 1e-3)) - 1))
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        orc.step(DT, SUBSTEPS, ITERATIONS)
+    t2 = time.perf_counter() - t0
+    total_t, total_sub = t1 + t2, substeps * (1 + frames)
+    return {"value": sc.n * total_sub / total_t, "unit": UNIT, "cores": int(O.load("f32").or_get_threads()),
+            "kind": "port",
+            "sample": f"{total_sub} substeps of the pre-rolled {sc.n}-particle scene ({total_t:.1f} s)"}
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    sc = build_scene(args)
+    solver, cfg = make_solver(sc, device_index=local)
+    for _ in range(args.preroll):
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+    x_snap, v_snap = solver.get_positions(), solver.get_velocities()
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.ExternalStream(solver.cuda_stream, device=dev)
+    flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def flush():
+        with torch.cuda.stream(stream):
+            flush_buf.fill_(1.0)
+
+    for _ in range(args.warmup):
+        flush()
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    for k in range(args.steps):
+        flush()
+        starts[k].record(stream)
+        solver.step_async(DT, SUBSTEPS, ITERATIONS)
+        ends[k].record(stream)
+    solver.sync()
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    stats = solver.get_frame_stats()
+    dev_ms_max = reduce_max(dev_ms, world)
+    particle_substeps = sc.n * SUBSTEPS * args.steps * world
+    value = particle_substeps / (dev_ms_max * 1e-3)
+
+    # per-kernel device times (event-record nodes inside the frame graph), separate pass
+    solver.set_profiling(True)
+    solver.reset_stage_times()
+    prof_frames = min(args.steps, 30)
+    for _ in range(prof_frames):
+        flush()
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+    stage_ms, prof_substeps = solver.get_stage_times()
+    solver.set_profiling(False)
+    launches = {k: prof_substeps * (ITERATIONS if k.startswith("3.") else 1) for k in stage_ms}
+    ranked = sorted(((v, k) for k, v in stage_ms.items() if k in ALG_BYTES and v > 0), reverse=True)
+    dom_ms, dom = ranked[0]
+    avg_ms = dom_ms / launches[dom]
+    peak, peak_kind = measured_peak_hbm()
+    achieved = ALG_BYTES[dom] * sc.n / (avg_ms * 1e-3) / 1e9
+    step_gbs = STEP_ALG_BYTES * sc.n * SUBSTEPS * ITERATIONS / ((dev_ms / args.steps) * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "alg_bytes_per_launch": ALG_BYTES[dom] * sc.n, "avg_launch_us": round(avg_ms * 1e3, 2),
+                "traffic": dram_traffic(dom),
+                "share_of_step": round(dom_ms / sum(stage_ms.values()), 3)}
+
+    # end to end through the public API with host buffers: set_particles -> step -> readback
+    solver.set_particles(x_snap, v_snap)
+    x_h, v_h = x_snap.copy(), v_snap.copy()
+    e2e_s = 0.0
+    for k in range(args.steps):
+        flush()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        solver.set_particles(x_h, v_h)
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+        x_h = solver.get_positions()
+        v_h = solver.get_velocities()
+        e2e_s += time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s, world)
+    e2e = {"value": particle_substeps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(sc.n * 12 * 2),
+           "d2h_bytes_per_step": int(sc.n * 12 * 2)}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded lattice + sum-of-sines heightfield)",
+        "config": {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
+                   "substeps": SUBSTEPS, "iterations": ITERATIONS, "dt": DT, "step": "one frame (10 substeps)",
+                   "preroll_frames": args.preroll, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": roofline,
+        "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
+                          "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4)},
+        "stage_ms_per_substep": {k: round(v / max(prof_substeps, 1), 5) for k, v in stage_ms.items() if v > 0},
+        "e2e": e2e, "gpu_launches": int(stats["kernels_per_frame"] * args.steps), "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline_sample(sc, cfg, x_snap, v_snap, budget_s=args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path: the oracle port on all host threads."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    from helpers import config_for, make_pair
+
+    O.load("f32").or_set_threads(os.cpu_count() or 1)
+    sc = build_scene(args)
+    cfg = config_for(sc)
+    _, orc = make_pair(sc, cfg, gpu=False)
+    for _ in range(args.preroll):
+        orc.step(DT, SUBSTEPS, ITERATIONS)
+    sdt = DT / SUBSTEPS  # one step = one substep of the frame (dt/10)
+    for _ in range(args.warmup):
+        orc.step(sdt, 1, ITERATIONS)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.step(sdt, 1, ITERATIONS)
+    t = time.perf_counter() - t0
+    value = sc.n * args.steps / t
+    cores = int(O.load("f32").or_get_threads())
+    sample = f"{args.steps} substeps of the pre-rolled {sc.n}-particle scene after {args.preroll} pre-roll frames"
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + sum-of-sines heightfield)",
+           "config": {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
+                      "substeps": SUBSTEPS, "iterations": ITERATIONS, "dt": DT, "step": "one substep (dt/10)",
+                      "preroll_frames": args.preroll, "parallelism": "cpu threads"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--preroll", type=int, default=30)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

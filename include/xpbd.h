@@ -134,10 +134,27 @@ int xpbd_get_diag_pairs(xpbd_solver* s, xpbd_pair_record* out, size_t cap, size_
 int xpbd_get_aux_diag(xpbd_solver* s, int which, void* out, size_t cap, size_t* count);
 int xpbd_print_profiler_summary(xpbd_solver* s);
 
-/* ---- extensions ------------------------------------------------------------ */
+/* ---- extensions (no counterpart in the reference) -------------------------- */
 /* Device status bits of the last step (1 = look-back timeout, 2 = BVH stack
  * overflow, 4 = mesh contact slots full) and their counters. */
 int xpbd_get_status(xpbd_solver* s, uint32_t out[4]);
+/* xpbd_step without the wait: the frame's graph is queued on the solver's
+ * stream and the call returns. xpbd_sync (or any state call) waits, reads the
+ * contact count and checks the status word. */
+int xpbd_step_async(xpbd_solver* s, float dt, int substeps, int iterations);
+int xpbd_sync(xpbd_solver* s);
+/* The solver's cudaStream_t (as an opaque pointer) for event timing and for
+ * ordering work of other libraries against the solver. */
+void* xpbd_stream(xpbd_solver* s);
+/* Per-kernel timing: with profiling on, frame graphs carry event-record nodes
+ * around every kernel; synchronous steps accumulate device milliseconds per
+ * stage. Stage names come from xpbd_stage_name. */
+int xpbd_set_profiling(xpbd_solver* s, int on);
+int xpbd_get_stage_times(xpbd_solver* s, double* ms, size_t cap, size_t* num_stages, uint64_t* substeps);
+int xpbd_reset_stage_times(xpbd_solver* s);
+const char* xpbd_stage_name(int index);
+/* out = {kernel launches per frame, memset nodes per frame, frames run, cached graphs} */
+int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,7 @@
 // extern "C" boundary of libxpbd_gb300.so (declared in include/xpbd.h).
 // Each entry point catches C++ exceptions, stores the message in a
 // thread-local string and returns -1, so no exception crosses the ABI.
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <stdexcept>
@@ -228,6 +229,40 @@ int xpbd_print_profiler_summary(xpbd_solver* s) {
 
 int xpbd_get_status(xpbd_solver* s, uint32_t out[4]) {
     return guarded([&] { S(s).status(out); });
+}
+
+int xpbd_step_async(xpbd_solver* s, float dt, int substeps, int iterations) {
+    return guarded([&] { S(s).step_async(dt, substeps, iterations); });
+}
+
+int xpbd_sync(xpbd_solver* s) {
+    return guarded([&] { S(s).sync(); });
+}
+
+void* xpbd_stream(xpbd_solver* s) { return s ? (void*)s->impl.stream() : nullptr; }
+
+int xpbd_set_profiling(xpbd_solver* s, int on) {
+    return guarded([&] { S(s).set_profiling(on != 0); });
+}
+
+int xpbd_get_stage_times(xpbd_solver* s, double* ms, size_t cap, size_t* num_stages, uint64_t* substeps) {
+    return guarded([&] {
+        double tmp[32];
+        size_t k = S(s).stage_times(tmp, 32, substeps);
+        if (ms)
+            for (size_t i = 0; i < std::min(k, cap); i++) ms[i] = tmp[i];
+        if (num_stages) *num_stages = k;
+    });
+}
+
+int xpbd_reset_stage_times(xpbd_solver* s) {
+    return guarded([&] { S(s).reset_stage_times(); });
+}
+
+const char* xpbd_stage_name(int index) { return xpbd::Solver::stage_name(index); }
+
+int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]) {
+    return guarded([&] { S(s).frame_stats(out); });
 }
 
 }  // extern "C"

@@ -25,13 +25,15 @@ void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
 
 namespace {
 constexpr int kKeyBits = 21;  // 128^3 cells
-// profiler stage slots (names follow scene.cpp:1481-1505)
+// profiler stage slots, one per kernel (names follow scene.cpp:1481-1505 where they correspond)
 enum ProfSlot {
-    P_CONTACT = 0, P_INTEGRATE_KEYS, P_SORT, P_CELLS, P_SOLVE, P_RANKS, P_COUNT
+    P_CLEAR = 0, P_CONTACT, P_INTEGRATE_KEYS, P_SORT0, P_SORT1, P_SORT2, P_SORT3, P_RANKS, P_CELLS, P_SOLVE,
+    P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
-    "1. Contact Gen (plane + mesh)", "2b. Integrate + Cell Keys", "2e. Onesweep Sort (all passes)",
-    "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)", "1b. Contact Ranks (cap)"};
+    "0. Sort scratch clear (memset)", "1. Contact Gen (plane + mesh)", "2b. Integrate + Cell Keys",
+    "2e. Onesweep Pass 0", "2e. Onesweep Pass 1", "2e. Onesweep Pass 2", "2e. Onesweep Pass 3",
+    "1b. Contact Ranks (cap)", "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)"};
 uint32_t f2u(float f) {
     uint32_t u;
     std::memcpy(&u, &f, 4);
@@ -55,8 +57,7 @@ Solver::~Solver() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
     if (profiling_) print_profiler_summary();
-    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
-    for (auto e : prof_events_) cudaEventDestroy(e);
+    clear_graphs();
     if (pinned_) cudaFreeHost(pinned_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -66,7 +67,11 @@ void Solver::require_init() const {
 }
 
 void Solver::clear_graphs() {
-    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    if (pending_substeps_ && stream_) cudaStreamSynchronize(stream_);
+    for (auto& kv : graphs_) {
+        cudaGraphExecDestroy(kv.second.exec);
+        for (auto& m : kv.second.marks) cudaEventDestroy(m.first);
+    }
     graphs_.clear();
 }
 
@@ -268,6 +273,7 @@ void Solver::set_particles(const float* q, const float* qd, const float* inv_mas
     if (!initialized_) throw std::runtime_error("XpbdSolver not initialized");
     if (n != n_) throw std::runtime_error("Particle count mismatch");
     XPBD_CUDA(cudaSetDevice(device_));
+    sync();
     if (n == 0) return;
     std::memcpy(pinned_, q, n * 3 * sizeof(float));
     XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
@@ -303,6 +309,7 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
     MeshData& m = meshes_[mi];
     if (num_verts != m.vertices.size() / 3) throw std::runtime_error("update_mesh: vertex count mismatch");
     XPBD_CUDA(cudaSetDevice(device_));
+    sync();
     const size_t vs = vert_offsets_[mi];
     std::memcpy(all_verts_.data() + vs * 3, verts, num_verts * 3 * sizeof(float));
     if (vels)
@@ -402,15 +409,21 @@ MeshTables Solver::mesh_tables() const {
 }
 
 void Solver::prof_mark(int slot) {
+    if (!recording_ || !profiling_) return;
     cudaEvent_t e;
     XPBD_CUDA(cudaEventCreate(&e));
-    XPBD_CUDA(cudaEventRecord(e, stream_));
-    prof_events_.push_back(e);
-    prof_slots_.push_back(slot);
+    XPBD_CUDA(cudaEventRecord(e, stream_));  // becomes an event-record node of the frame graph
+    recording_->marks.emplace_back(e, slot);
+}
+void Solver::count_kernel(int k) {
+    if (recording_) recording_->kernels += (uint64_t)k;
+}
+void Solver::count_memset() {
+    if (recording_) recording_->memsets += 1;
 }
 
 // One substep reading state parity `src` and writing parity 1-src.
-void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int src, bool timed) {
+void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int src) {
     const int64_t n = (int64_t)n_;
     const int dst = 1 - src;
     const PredictParams pp = predict_params(sdt);
@@ -423,16 +436,22 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const bool mesh_pass = gen && !meshes_.empty();
     DeviceStatus* st = status_.p;
 
-    if (timed) prof_mark(-1);
+    prof_mark(-1);
     XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
-    if (mesh_pass) launch_collide(stream_, n, x_[src].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p,
-                                  cslot_.p, ccount, st);
-    if (timed) prof_mark(P_CONTACT);
+    count_memset();
+    prof_mark(P_CLEAR);
+    if (mesh_pass) {
+        launch_collide(stream_, n, x_[src].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount,
+                       st);
+        count_kernel();
+        prof_mark(P_CONTACT);
+    }
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, pl, keys_.p, plan_,
                         sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
-    if (timed) prof_mark(P_INTEGRATE_KEYS);
+    count_kernel();
+    prof_mark(P_INTEGRATE_KEYS);
     const uint32_t* kin = keys_.p;
     const uint32_t* vin = nullptr;
     const size_t lbw = sort_lookback_words(plan_);
@@ -442,10 +461,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         launch_onesweep_pass(stream_, n, plan_, p, kin, vin, ko, vo,
                              sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
                              sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st);
+        count_kernel();
+        prof_mark(P_SORT0 + std::min(p, 3));
         kin = ko;
         vin = vo;
     }
-    if (timed) prof_mark(P_SORT);
     const uint32_t* skeys = kin;
     const uint32_t* sids = vin;
     const uint32_t* info = injected_ && !gen ? inj_info_.p : cinfo_.p;
@@ -453,13 +473,15 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     ContactRanks cr{nullptr, nullptr};
     if (gen && need_ranks_) {
         launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, nullptr, st);
+        count_kernel(3);
+        prof_mark(P_RANKS);
         cr.rank = rank_.p;
         cr.totals = totals_.p;
     }
-    if (timed) prof_mark(P_RANKS);
     launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
                         stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
-    if (timed) prof_mark(P_CELLS);
+    count_kernel();
+    prof_mark(P_CELLS);
     SolveDiag dg{nullptr, nullptr, nullptr, 0};
     if (cfg_.enable_diagnostics) {
         dg.delta_out = delta_.p;
@@ -473,76 +495,83 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         launch_solve(stream_, n, last, all_active_, sids, rx_[it & 1].p, rv_[it & 1].p, rf_.p, table_.p, stamp_.p,
                      x_[src].p, v_[src].p, info, slots, cr, bt, solve_params(sdt, it), rx_[(it + 1) & 1].p,
                      rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg);
+        count_kernel();
+        prof_mark(P_SOLVE);
     }
     if (iterations <= 0) {  // no solver iteration: the predicted state is the result
         XPBD_CUDA(cudaMemcpyAsync(x_[dst].p, x_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
         XPBD_CUDA(cudaMemcpyAsync(v_[dst].p, v_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
     }
-    if (timed) prof_mark(P_SOLVE);
 }
 
-void Solver::record_frame(Mode mode, float dt, int substeps, int iterations, int parity, bool timed) {
+void Solver::record_frame(Mode mode, float dt, int substeps, int iterations, int parity) {
     const float sdt = dt / (float)substeps;  // scene.cpp:701
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, (size_t)substeps * sizeof(uint32_t), stream_));
+    count_memset();
     int src = parity;
     for (int sub = 0; sub < substeps; sub++) {
-        record_substep(mode, sub, iterations, sdt, src, timed);
+        record_substep(mode, sub, iterations, sdt, src);
         src = 1 - src;
     }
 }
 
-void Solver::run_frame(Mode mode, float dt, int substeps, int iterations) {
+void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool sync_now) {
     if (substeps <= 0) throw std::runtime_error("step: substeps must be positive");
+    if (pending_substeps_) sync();
     ensure_substep_capacity(substeps);
-    XPBD_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(DeviceStatus), stream_));
-    if (n_ == 0) {
-        XPBD_CUDA(cudaStreamSynchronize(stream_));
-        return;
-    }
+    if (n_ == 0) return;
     auto t0 = std::chrono::high_resolution_clock::now();
-    if (profiling_) {
-        record_frame(mode, dt, substeps, iterations, cur_, true);
-    } else {
-        GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode};
-        auto it = graphs_.find(key);
-        if (it == graphs_.end()) {
-            cudaGraph_t g;
-            XPBD_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-            try {
-                record_frame(mode, dt, substeps, iterations, cur_, false);
-            } catch (...) {
-                cudaStreamEndCapture(stream_, &g);
-                throw;
-            }
-            XPBD_CUDA(cudaStreamEndCapture(stream_, &g));
-            cudaGraphExec_t ex;
-            XPBD_CUDA(cudaGraphInstantiate(&ex, g, 0));
-            cudaGraphDestroy(g);
-            it = graphs_.emplace(key, ex).first;
+    GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0};
+    auto it = graphs_.find(key);
+    if (it == graphs_.end()) {
+        FrameGraph fg;
+        cudaGraph_t g;
+        recording_ = &fg;
+        XPBD_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            record_frame(mode, dt, substeps, iterations, cur_);
+        } catch (...) {
+            recording_ = nullptr;
+            cudaStreamEndCapture(stream_, &g);
+            for (auto& m : fg.marks) cudaEventDestroy(m.first);
+            throw;
         }
-        XPBD_CUDA(cudaGraphLaunch(it->second, stream_));
+        recording_ = nullptr;
+        XPBD_CUDA(cudaStreamEndCapture(stream_, &g));
+        XPBD_CUDA(cudaGraphInstantiate(&fg.exec, g, 0));
+        cudaGraphDestroy(g);
+        it = graphs_.emplace(key, std::move(fg)).first;
     }
+    XPBD_CUDA(cudaGraphLaunch(it->second.exec, stream_));
+    last_kernels_ = it->second.kernels;
+    last_memsets_ = it->second.memsets;
+    frames_run_++;
     last_collide_src_ = cur_ ^ ((substeps - 1) & 1);
     cur_ ^= (substeps & 1);
-    finish_frame(substeps);
+    pending_substeps_ = substeps;
+    if (!sync_now) return;
+    sync();
     if (profiling_) {
-        double wall = std::chrono::duration<double, std::milli>(std::chrono::high_resolution_clock::now() - t0).count();
-        prof_wall_ms_ += wall;
-        int last_slot = -1;
-        for (size_t k = 0; k < prof_events_.size(); k++) {
-            if (k > 0 && prof_slots_[k] >= 0) {
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, prof_events_[k - 1], prof_events_[k]);
-                prof_ms_[prof_slots_[k]] += ms;
-            }
-            last_slot = prof_slots_[k];
-        }
-        (void)last_slot;
-        for (auto e : prof_events_) cudaEventDestroy(e);
-        prof_events_.clear();
-        prof_slots_.clear();
+        accumulate_stage_times(it->second);
+        prof_wall_ms_ += std::chrono::duration<double, std::milli>(std::chrono::high_resolution_clock::now() - t0).count();
         prof_substeps_ += (uint64_t)substeps;
     }
+}
+
+void Solver::accumulate_stage_times(const FrameGraph& fg) {
+    for (size_t k = 1; k < fg.marks.size(); k++) {
+        const int slot = fg.marks[k].second;
+        if (slot < 0) continue;
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, fg.marks[k - 1].first, fg.marks[k].first) == cudaSuccess) prof_ms_[slot] += ms;
+    }
+}
+
+void Solver::sync() {
+    if (!pending_substeps_) return;
+    const int s = pending_substeps_;
+    pending_substeps_ = 0;
+    finish_frame(s);
 }
 
 void Solver::finish_frame(int substeps) {
@@ -550,26 +579,65 @@ void Solver::finish_frame(int substeps) {
     XPBD_CUDA(cudaMemcpyAsync(pinned_, ccount_.p + (substeps - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost,
                               stream_));
     XPBD_CUDA(cudaMemcpyAsync(pinned_ + 1, status_.p, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(DeviceStatus), stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));
     uint32_t raw;
     std::memcpy(&raw, pinned_, 4);
     std::memcpy(&host_status_, pinned_ + 1, sizeof(DeviceStatus));
+    contact_count_ = (int)std::min<int64_t>((int64_t)raw, contact_max_);
     if (host_status_.error_bits & kErrLookbackTimeout)
         throw std::runtime_error("device wait timed out in the onesweep look-back (result discarded)");
     if (host_status_.error_bits & kErrStackOverflow)
         throw std::runtime_error("BVH traversal stack overflow (more than 32 pending nodes)");
     if (host_status_.error_bits & kErrSlotOverflow)
         throw std::runtime_error("more mesh contacts for one particle than contact slots");
-    contact_count_ = (int)std::min<int64_t>((int64_t)raw, contact_max_);
     if (env_on("VKXPBD_CHECK_SORT_ORDER")) check_sort_order();
 }
 
 void Solver::step(float dt, int substeps, int iterations) {
     if (!finalized_) finalize_meshes();  // scene.cpp:699
     XPBD_CUDA(cudaSetDevice(device_));
+    if (injected_) clear_graphs();
     injected_ = false;
-    run_frame(Mode::Step, dt, substeps, iterations);
+    run_frame(Mode::Step, dt, substeps, iterations, true);
 }
+
+void Solver::step_async(float dt, int substeps, int iterations) {
+    if (!finalized_) finalize_meshes();
+    XPBD_CUDA(cudaSetDevice(device_));
+    if (injected_) clear_graphs();
+    injected_ = false;
+    run_frame(Mode::Step, dt, substeps, iterations, false);
+}
+
+void Solver::set_profiling(bool on) {
+    require_init();
+    if (on == profiling_) return;
+    sync();
+    profiling_ = on;
+}
+
+size_t Solver::stage_times(double* ms, size_t cap, uint64_t* substeps) const {
+    for (size_t i = 0; i < std::min<size_t>(cap, P_COUNT); i++) ms[i] = prof_ms_[i];
+    if (substeps) *substeps = prof_substeps_;
+    return P_COUNT;
+}
+
+void Solver::reset_stage_times() {
+    for (double& v : prof_ms_) v = 0.0;
+    prof_substeps_ = 0;
+    prof_wall_ms_ = 0.0;
+}
+
+void Solver::frame_stats(uint64_t out[4]) const {
+    out[0] = last_kernels_;
+    out[1] = last_memsets_;
+    out[2] = frames_run_;
+    out[3] = graphs_.size();
+}
+
+const char* Solver::stage_name(int i) { return (i >= 0 && i < P_COUNT) ? kProfNames[i] : ""; }
+int Solver::stage_count() { return P_COUNT; }
 
 void Solver::step_solve_only(float dt, int substeps, int iterations) {
     if (!finalized_) finalize_meshes();
@@ -582,7 +650,7 @@ void Solver::step_solve_only(float dt, int substeps, int iterations) {
         clear_graphs();
     }
     const int keep = contact_count_;
-    run_frame(Mode::SolveOnly, dt, substeps, iterations);
+    run_frame(Mode::SolveOnly, dt, substeps, iterations, true);
     contact_count_ = keep;
 }
 
@@ -590,6 +658,8 @@ void Solver::collide_only() {
     require_init();
     if (!finalized_) finalize_meshes();
     XPBD_CUDA(cudaSetDevice(device_));
+    sync();
+    if (injected_) clear_graphs();
     injected_ = false;
     PlaneParams pl;
     pl.enabled = cfg_.has_ground_plane ? 1 : 0;
@@ -597,7 +667,6 @@ void Solver::collide_only() {
     pl.altitude = cfg_.ground_plane_altitude;
     ensure_substep_capacity(1);
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
-    XPBD_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(DeviceStatus), stream_));
     launch_collide(stream_, (int64_t)n_, x_[cur_].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p, cslot_.p,
                    ccount_.p, status_.p);
     last_collide_src_ = cur_;
@@ -652,6 +721,7 @@ void Solver::get_positions(float* out, size_t n) {
     n = std::min(n, n_);
     if (n == 0) return;
     XPBD_CUDA(cudaSetDevice(device_));
+    sync();
     launch_unpack_xyz(stream_, (int64_t)n, x_[cur_].p, xyz_stage_.p);
     XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));
@@ -663,6 +733,7 @@ void Solver::get_velocities(float* out, size_t n) {
     n = std::min(n, n_);
     if (n == 0) return;
     XPBD_CUDA(cudaSetDevice(device_));
+    sync();
     launch_unpack_xyz(stream_, (int64_t)n, v_[cur_].p, xyz_stage_.p);
     XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));

@@ -100,24 +100,40 @@ class Solver {
     size_t aux_diag(int which, void* out, size_t cap);
     void print_profiler_summary();
     void status(uint32_t out[4]) const;
+    // extensions used by the benchmark harness
+    void step_async(float dt, int substeps, int iterations);
+    void sync();
+    cudaStream_t stream() const { return stream_; }
+    void set_profiling(bool on);
+    size_t stage_times(double* ms, size_t cap, uint64_t* substeps) const;
+    void reset_stage_times();
+    void frame_stats(uint64_t out[4]) const;
+    static const char* stage_name(int i);
+    static int stage_count();
 
    private:
     enum class Mode { Step, SolveOnly };
     struct GraphKey {
         uint32_t dt_bits;
-        int substeps, iterations, parity, mode;
+        int substeps, iterations, parity, mode, timed;
         bool operator<(const GraphKey& o) const {
-            return std::tie(dt_bits, substeps, iterations, parity, mode) <
-                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode);
+            return std::tie(dt_bits, substeps, iterations, parity, mode, timed) <
+                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode, o.timed);
         }
+    };
+    struct FrameGraph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<std::pair<cudaEvent_t, int>> marks;  // stage events captured as graph nodes
+        uint64_t kernels = 0, memsets = 0;
     };
     void require_init() const;
     void clear_graphs();
     void ensure_substep_capacity(int substeps);
-    void record_frame(Mode mode, float dt, int substeps, int iterations, int parity, bool timed);
-    void record_substep(Mode mode, int sub, int iterations, float sdt, int src, bool timed);
-    void run_frame(Mode mode, float dt, int substeps, int iterations);
+    void record_frame(Mode mode, float dt, int substeps, int iterations, int parity);
+    void record_substep(Mode mode, int sub, int iterations, float sdt, int src);
+    void run_frame(Mode mode, float dt, int substeps, int iterations, bool sync);
     void finish_frame(int substeps);
+    void accumulate_stage_times(const FrameGraph& fg);
     void compact_contacts();
     void check_sort_order();
     PredictParams predict_params(float sdt) const;
@@ -125,6 +141,8 @@ class Solver {
     BodyTables body_tables() const;
     MeshTables mesh_tables() const;
     void prof_mark(int slot);
+    void count_kernel(int k = 1);
+    void count_memset();
 
     xpbd_config cfg_{};
     bool initialized_ = false, finalized_ = false;
@@ -196,11 +214,13 @@ class Solver {
     DevBuf<float> c_bpos_, c_bvel_, c_nrm_;
     DevBuf<int32_t> cell_starts_, cell_ends_;
     // graphs
-    std::map<GraphKey, cudaGraphExec_t> graphs_;
-    // profiler (scene.cpp:1438-1515 stage names)
+    std::map<GraphKey, FrameGraph> graphs_;
+    FrameGraph* recording_ = nullptr;  // graph being captured (marks and node counts go here)
+    int pending_substeps_ = 0;         // frame launched by step_async and not yet synced
+    uint64_t frames_run_ = 0;
+    uint64_t last_kernels_ = 0, last_memsets_ = 0;
+    // profiler (stage names follow scene.cpp:1481-1505 where the stages correspond)
     bool profiling_ = false;
-    std::vector<cudaEvent_t> prof_events_;
-    std::vector<int> prof_slots_;
     double prof_ms_[16] = {0};
     uint64_t prof_substeps_ = 0;
     double prof_wall_ms_ = 0.0;

@@ -365,9 +365,44 @@ class XpbdSolver:
     def print_profiler_summary(self):
         _check(_lib.xpbd_print_profiler_summary(self._h))
 
-    # ---- extension ---------------------------------------------------------------
+    # ---- extensions (no counterpart in the reference) ---------------------------
     def get_status(self):
         """(error_bits, lookback_timeouts, stack_overflows, slot_overflows) of the last step."""
         out = (C.c_uint32 * 4)()
         _check(_lib.xpbd_get_status(self._h, out))
         return tuple(int(x) for x in out)
+
+    def step_async(self, dt=1.0 / 60.0, substeps=1, iterations=2):
+        """Queue one frame on the solver's stream and return without waiting."""
+        _check(_lib.xpbd_step_async(self._h, float(dt), int(substeps), int(iterations)))
+
+    def sync(self):
+        """Wait for queued frames, update last_contact_count and raise on a device error."""
+        _check(_lib.xpbd_sync(self._h))
+
+    @property
+    def cuda_stream(self) -> int:
+        """The solver's cudaStream_t as an integer handle (e.g. for torch.cuda.ExternalStream)."""
+        return int(_lib.xpbd_stream(self._h) or 0)
+
+    def set_profiling(self, on: bool):
+        _check(_lib.xpbd_set_profiling(self._h, 1 if on else 0))
+
+    def get_stage_times(self):
+        """({stage name: accumulated device ms}, substeps) of synchronous profiled steps."""
+        ms = (C.c_double * 32)()
+        k = C.c_size_t(0)
+        subs = C.c_uint64(0)
+        _check(_lib.xpbd_get_stage_times(self._h, ms, 32, C.byref(k), C.byref(subs)))
+        names = [_lib.xpbd_stage_name(i).decode() for i in range(k.value)]
+        return {names[i]: float(ms[i]) for i in range(k.value)}, int(subs.value)
+
+    def reset_stage_times(self):
+        _check(_lib.xpbd_reset_stage_times(self._h))
+
+    def get_frame_stats(self):
+        """{kernels, memsets} per frame of the last launched graph, frames run, cached graphs."""
+        out = (C.c_uint64 * 4)()
+        _check(_lib.xpbd_get_frame_stats(self._h, out))
+        return {"kernels_per_frame": int(out[0]), "memsets_per_frame": int(out[1]), "frames": int(out[2]),
+                "graphs": int(out[3])}

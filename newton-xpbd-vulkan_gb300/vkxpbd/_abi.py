@@ -83,6 +83,14 @@ SIGNATURES = {
     "xpbd_get_aux_diag": (C.c_int, [_P, C.c_int, C.c_void_p, _Z, C.POINTER(_Z)]),
     "xpbd_print_profiler_summary": (C.c_int, [_P]),
     "xpbd_get_status": (C.c_int, [_P, _U]),
+    "xpbd_step_async": (C.c_int, [_P, C.c_float, C.c_int, C.c_int]),
+    "xpbd_sync": (C.c_int, [_P]),
+    "xpbd_stream": (C.c_void_p, [_P]),
+    "xpbd_set_profiling": (C.c_int, [_P, C.c_int]),
+    "xpbd_get_stage_times": (C.c_int, [_P, C.POINTER(C.c_double), _Z, C.POINTER(_Z), C.POINTER(C.c_uint64)]),
+    "xpbd_reset_stage_times": (C.c_int, [_P]),
+    "xpbd_stage_name": (C.c_char_p, [C.c_int]),
+    "xpbd_get_frame_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
 }
 
 _lib = None
