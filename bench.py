@@ -246,6 +246,8 @@ def run_gpu(args):
     solver.set_profiling(False)
     launches = {k: prof_substeps * (ITERATIONS if k.startswith("3.") else 1) for k in stage_ms}
     ranked = sorted(((v, k) for k, v in stage_ms.items() if k in ALG_BYTES and v > 0), reverse=True)
+    if not ranked:
+        raise RuntimeError(f"no per-kernel stage times were recorded: {stage_ms}")
     dom_ms, dom = ranked[0]
     avg_ms = dom_ms / launches[dom]
     peak, peak_kind = measured_peak_hbm()

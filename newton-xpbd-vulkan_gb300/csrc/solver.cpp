@@ -412,7 +412,8 @@ void Solver::prof_mark(int slot) {
     if (!recording_ || !profiling_) return;
     cudaEvent_t e;
     XPBD_CUDA(cudaEventCreate(&e));
-    XPBD_CUDA(cudaEventRecord(e, stream_));  // becomes an event-record node of the frame graph
+    // "external" so that capture turns it into an event-record node of the frame graph
+    XPBD_CUDA(cudaEventRecordWithFlags(e, stream_, cudaEventRecordExternal));
     recording_->marks.emplace_back(e, slot);
 }
 void Solver::count_kernel(int k) {
