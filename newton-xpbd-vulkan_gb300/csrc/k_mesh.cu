@@ -51,10 +51,10 @@ __device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
     return true;
 }
 
-// generate_mesh_contacts.comp:115-179
-__device__ void closest_point_triangle(v3 p, v3 a, v3 b, v3 c, v3& cp, v3& tri_normal, v3& bary) {
+// generate_mesh_contacts.comp:115-179; the triangle normal normalize(cross(b-a, c-a)) depends on
+// the triangle only and is read from the triangle cache instead of being recomputed per visit
+__device__ void closest_point_triangle(v3 p, v3 a, v3 b, v3 c, v3& cp, v3& bary) {
     const v3 ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
-    tri_normal = vnormalize(vcross(ab, ac));
     float u, v;
     const float d1 = exact_dot(ab, ap), d2 = exact_dot(ac, ap);
     if (d1 <= 0.0f && d2 <= 0.0f) {
@@ -142,15 +142,16 @@ __device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, flo
         const uint32_t right_i = __float_as_uint(hi4.w) & 0x3FFFFFFFu;
         if (is_leaf) {
             for (uint32_t pc = left_i; pc < right_i; pc++) {
-                const uint32_t t = __ldg(&mt.prim[pc]);
-                const v3 a = ldv(mt.verts, __ldg(&mt.tris[t * 3])), b = ldv(mt.verts, __ldg(&mt.tris[t * 3 + 1])),
-                         c = ldv(mt.verts, __ldg(&mt.tris[t * 3 + 2]));
+                const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
+                if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
+                const float4 qa = __ldg(&mt.tri_cache[pc * 4]), qb = __ldg(&mt.tri_cache[pc * 4 + 1]),
+                             qc = __ldg(&mt.tri_cache[pc * 4 + 2]);
+                const uint32_t t = __float_as_uint(qa.w);
+                const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
                 const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
-                const v3 normal = vcross(e0, e1);
-                const float e0n = vdot(e0, e0), e1n = vdot(e1, e1), e2n = vdot(e2, e2);
-                if (__fdiv_rn(vlength(normal), (e0n + e1n + e2n)) < 1.0e-6f) continue;
-                v3 cp, tn, tb;
-                closest_point_triangle(p, a, b, c, cp, tn, tb);
+                const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
+                v3 cp, tb;
+                closest_point_triangle(p, a, b, c, cp, tb);
                 if (wt) {
                     const v3 diff = vsub(cp, p);
                     const float dist_sq = vdot(diff, diff);
@@ -237,11 +238,8 @@ __device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, flo
         uint32_t hits = 0;
         const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
         for (uint32_t ti = 0; ti < pn; ti++) {
-            const uint32_t t = __ldg(&mt.prim[po + ti]);
-            if (intersect_ray_tri_woop(p, ray_dir, ldv(mt.verts, __ldg(&mt.tris[t * 3])),
-                                       ldv(mt.verts, __ldg(&mt.tris[t * 3 + 1])),
-                                       ldv(mt.verts, __ldg(&mt.tris[t * 3 + 2]))))
-                hits++;
+            const float4* q = mt.tri_cache + (size_t)(po + ti) * 4;
+            if (intersect_ray_tri_woop(p, ray_dir, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
         }
         sign = (hits & 1u) ? -1.0f : 1.0f;
     } else {
@@ -255,14 +253,19 @@ __device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, flo
     return true;
 }
 
-__global__ void __launch_bounds__(128) k_collide(int64_t n, const float4* __restrict__ x, const float* __restrict__ r,
+// Thread t takes particle order[t]; with the previous substep's hash-grid order a
+// warp holds spatially adjacent particles, so their traversals follow similar
+// paths. Each particle's output depends on that particle only.
+__global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __restrict__ order,
+                                                 const float4* __restrict__ x, const float* __restrict__ r,
                                                  const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
                                                  float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
     __shared__ uint32_t s_warp[4];
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t count = 0;
-    if (i < n) {
+    if (tid < n) {
+        const int64_t i = order ? (int64_t)__ldg(&order[tid]) : tid;
         uint32_t info = 0;
         const int fl = flags[i];
         if (fl & 1) {
@@ -301,13 +304,48 @@ __global__ void __launch_bounds__(128) k_collide(int64_t n, const float4* __rest
     if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
 }
 
-void launch_collide(cudaStream_t s, int64_t n, const float4* x, const float* r, const int* flags, PlaneParams pl,
-                    MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount,
-                    DeviceStatus* st) {
+void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                    const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
+                    uint32_t* ccount, DeviceStatus* st) {
     if (n <= 0) return;
     const int threads = 128;
-    k_collide<<<(int)((n + threads - 1) / threads), threads, 0, s>>>(n, x, r, flags, pl, mt, slot_cap, cinfo, cslot,
-                                                                     ccount, st);
+    k_collide<<<(int)((n + threads - 1) / threads), threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo,
+                                                                     cslot, ccount, st);
+}
+
+// Triangle data that generate_mesh_contacts.comp:239-251 and :117 recompute on
+// every visit, evaluated once per leaf slot with the same operations.
+__global__ void k_tri_cache(int64_t first, int64_t count, const uint32_t* __restrict__ prim,
+                            const uint32_t* __restrict__ tris, const float* __restrict__ verts,
+                            float4* __restrict__ cache) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t pc = first + k;
+    const uint32_t t = prim[pc];
+    const v3 a = ldv(verts, tris[t * 3]), b = ldv(verts, tris[t * 3 + 1]), c = ldv(verts, tris[t * 3 + 2]);
+    const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+    const v3 normal = vcross(e0, e1);
+    const float e0n = vdot(e0, e0), e1n = vdot(e1, e1), e2n = vdot(e2, e2);
+    const bool skip = __fdiv_rn(vlength(normal), (e0n + e1n + e2n)) < 1.0e-6f;
+    const v3 tn = vnormalize(normal);  // normalize(cross(ab, ac)), ab = e0, ac = e1
+    cache[pc * 4 + 0] = make_float4(a.x, a.y, a.z, __uint_as_float(t));
+    cache[pc * 4 + 1] = make_float4(b.x, b.y, b.z, e0n);
+    cache[pc * 4 + 2] = make_float4(c.x, c.y, c.z, e1n);
+    cache[pc * 4 + 3] = make_float4(tn.x, tn.y, tn.z, skip ? -1.0f : e2n);
+}
+
+void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
+                      const float* verts, float4* cache) {
+    if (count <= 0) return;
+    k_tri_cache<<<(int)((count + 255) / 256), 256, 0, s>>>(first, count, prim, tris, verts, cache);
+}
+
+__global__ void k_iota(int64_t n, uint32_t* out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint32_t)i;
+}
+void launch_iota(cudaStream_t s, int64_t n, uint32_t* out) {
+    if (n > 0) k_iota<<<(int)((n + 255) / 256), 256, 0, s>>>(n, out);
 }
 
 }  // namespace xpbd

@@ -58,12 +58,37 @@ __global__ void __launch_bounds__(128) k_solve(int64_t n, const uint32_t* __rest
         const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
         const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
         v3 acc = mk3(0.0f, 0.0f, 0.0f);
+        // Cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at
+        // 128 or is clamped at 0, so their particles form one contiguous run of the
+        // sorted order, in the reference's visit order (x ascending, then sorted order).
+        const int32_t xo = xs + kGridOrigin;
+        const bool row_contiguous = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
         for (int32_t cz = zs; cz <= ze; cz++) {
             for (int32_t cy = ys; cy <= ye; cy++) {
-                for (int32_t cx = xs; cx <= xe; cx++) {
-                    const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
-                    if ((uint32_t)e.z != stamp) continue;
-                    for (int kk = e.x; kk < e.y; kk++) {
+                int32_t cx_end = xe;
+                int run_lo = 0, run_hi = 0;
+                if (row_contiguous) {
+                    const int c0 = cell_index(xs, cy, cz);
+                    run_lo = 0x7fffffff;
+                    run_hi = -1;
+                    for (int j = 0; j <= xe - xs; j++) {
+                        const int4 e = __ldg(&table[c0 + j]);
+                        if ((uint32_t)e.z == stamp) {
+                            run_lo = min(run_lo, e.x);
+                            run_hi = max(run_hi, e.y);
+                        }
+                    }
+                    cx_end = xs;  // one pass over the whole run
+                }
+                for (int32_t cx = xs; cx <= cx_end; cx++) {
+                    int lo = run_lo, hi = run_hi;
+                    if (!row_contiguous) {
+                        const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                        if ((uint32_t)e.z != stamp) continue;
+                        lo = e.x;
+                        hi = e.y;
+                    }
+                    for (int kk = lo; kk < hi; kk++) {
                         if (kk == k) continue;
                         const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
                         if ((nflag & 1) == 0) continue;

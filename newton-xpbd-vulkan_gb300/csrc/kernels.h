@@ -65,6 +65,9 @@ struct MeshTables {
     const int* watertight;    // [n_meshes]
     const uint32_t* prim_off; // [n_meshes]
     const uint32_t* prim_cnt; // [n_meshes]
+    // per leaf slot: (a.xyz, triangle id bits), (b.xyz, |e0|^2), (c.xyz, |e1|^2),
+    // (unit normal.xyz, |e2|^2 or -1 when the triangle is skipped as degenerate)
+    const float4* tri_cache;
     int n_meshes;
     float avg_edge;           // mesh 0's average edge length (scene.cpp:325)
     float soft_margin;
@@ -123,9 +126,14 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
                          int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
-// plane + mesh contact generation (particle order)
-void launch_collide(cudaStream_t s, int64_t n, const float4* x, const float* r, const int* flags, PlaneParams pl,
-                    MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, DeviceStatus* st);
+// plane + mesh contact generation; thread t handles particle order[t] (any permutation)
+void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                    const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
+                    uint32_t* ccount, DeviceStatus* st);
+// per-leaf-slot triangle cache for the slots [first, first + count)
+void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
+                      const float* verts, float4* cache);
+void launch_iota(cudaStream_t s, int64_t n, uint32_t* out);
 // fused shape solve + particle-particle solve + apply (+ restitution on the last iteration)
 void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const float4* rx,
                   const float4* rv, const int* rf, const int4* table, const uint32_t* stamp, const float4* x0,

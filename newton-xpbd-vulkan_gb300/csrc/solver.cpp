@@ -109,6 +109,9 @@ void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_conta
     lb_off_ = (size_t)plan_.passes << plan_.bits;
     tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
     sort_scratch_.alloc(tc_off_ + (size_t)plan_.passes);
+    // the final sort buffer doubles as the collision pass's thread -> particle order
+    launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
     table_.alloc(kNumCells);
     stamp_.alloc(1);
     cinfo_.alloc(n_);
@@ -261,6 +264,9 @@ void Solver::finalize_meshes() {
         up(vels_, all_vels_);
         up(tris_, all_tris);
         avg_edge0_ = meshes_[0].avg_edge;  // mesh 0's average edge for every mesh (scene.cpp:325)
+        tri_cache_.alloc(total_prims * 4, false);
+        launch_tri_cache(stream_, 0, (int64_t)total_prims, prim_.p, tris_.p, verts_.p, tri_cache_.p);
+        XPBD_CUDA(cudaStreamSynchronize(stream_));
     }
     const int64_t possible = (int64_t)n_ * ((cfg_.has_ground_plane ? 1 : 0) + (int64_t)nm);
     need_ranks_ = possible > contact_max_;
@@ -342,6 +348,8 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
                               stream_));
     XPBD_CUDA(cudaMemcpyAsync(vels_.p + vs * 3, all_vels_.data() + vs * 3, num_verts * 3 * sizeof(float),
                               cudaMemcpyHostToDevice, stream_));
+    launch_tri_cache(stream_, (int64_t)pb, (int64_t)(m.indices.size() / 3), prim_.p, tris_.p, verts_.p,
+                     tri_cache_.p);
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -402,6 +410,7 @@ MeshTables Solver::mesh_tables() const {
     m.watertight = watertight_.p;
     m.prim_off = prim_off_.p;
     m.prim_cnt = prim_cnt_.p;
+    m.tri_cache = tri_cache_.p;
     m.n_meshes = (int)meshes_.size();
     m.avg_edge = avg_edge0_;
     m.soft_margin = cfg_.soft_contact_margin;
@@ -442,7 +451,8 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     count_memset();
     prof_mark(P_CLEAR);
     if (mesh_pass) {
-        launch_collide(stream_, n, x_[src].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount,
+        launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
+                       slot_cap_, cinfo_.p, cslot_.p, ccount,
                        st);
         count_kernel();
         prof_mark(P_CONTACT);
@@ -668,7 +678,8 @@ void Solver::collide_only() {
     pl.altitude = cfg_.ground_plane_altitude;
     ensure_substep_capacity(1);
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
-    launch_collide(stream_, (int64_t)n_, x_[cur_].p, r_.p, flags_.p, pl, mesh_tables(), slot_cap_, cinfo_.p, cslot_.p,
+    launch_collide(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p, x_[cur_].p, r_.p, flags_.p, pl,
+                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p,
                    ccount_.p, status_.p);
     last_collide_src_ = cur_;
     finish_frame(1);

@@ -197,6 +197,7 @@ class Solver {
     DevBuf<float4> nl_, nu_;
     DevBuf<float> verts_, vels_;
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
+    DevBuf<float4> tri_cache_;
     DevBuf<float> margins_;
     DevBuf<int> watertight_;
     float avg_edge0_ = 0.0f;
