@@ -16,7 +16,7 @@
 namespace xpbd {
 
 template <bool LAST, bool ALL_ACTIVE, bool DIAG>
-__global__ void __launch_bounds__(128) k_solve(int64_t n, const uint32_t* __restrict__ sids,
+__global__ void __launch_bounds__(128, 8) k_solve(int64_t n, const uint32_t* __restrict__ sids,
                                                const float4* __restrict__ rx, const float4* __restrict__ rv,
                                                const int* __restrict__ rf, const int4* __restrict__ table,
                                                const uint32_t* __restrict__ stamp_p, const float4* __restrict__ x0a,
