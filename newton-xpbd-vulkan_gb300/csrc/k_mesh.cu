@@ -3,6 +3,8 @@
 // particle writes its own contacts into per-particle slots, so the contact
 // order is fixed (plane, then meshes in index order) without a global atomic
 // slot counter.
+#include <algorithm>
+
 #include "kernels.h"
 #include "particle.cuh"
 #include "xmath.cuh"
@@ -112,128 +114,149 @@ __device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
     return mk3(__ldg(p + i * 3), __ldg(p + i * 3 + 1), __ldg(p + i * 3 + 2));
 }
 
-// generate_mesh_contacts.comp:199-412 for mesh ci; returns true and the contact when one is emitted
-__device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, float eps_md, float eps2, v3& body_pos,
-                           v3& shape_v, v3& nrm, DeviceStatus* st) {
-    const float PI_ = 3.14159265359f;
-    const float max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
+// Traversal state of one particle against one mesh (generate_mesh_contacts.comp:201-331).
+struct MeshWalk {
     uint32_t stack[32];
-    uint32_t sp = 0;
-    stack[sp++] = __ldg(&mt.roots[ci]);
-    float min_dist = max_dist;
-    v3 acc_normal = mk3(0.0f, 0.0f, 0.0f);
-    uint32_t min_face = 0;
-    float sv_v = 0.0f, sv_w = 0.0f;
-    bool found = false;
-    const bool wt = __ldg(&mt.watertight[ci]) != 0;
-    float min_dist_sq = max_dist * max_dist;
-    bool overflow = false;
-    while (sp > 0) {
-        const uint32_t ni = stack[--sp];
-        const float4 lo4 = __ldg(&mt.nl[ni]), hi4 = __ldg(&mt.nu[ni]);
-        const float nds = dist_sq_aabb(p, xyz(lo4), xyz(hi4));
-        if (wt) {
-            if (nds > min_dist_sq) continue;
+    uint32_t sp;
+    float min_dist, min_dist_sq, max_dist;
+    v3 acc;
+    uint32_t min_face;
+    float sv_v, sv_w;
+    bool found, wt, overflow;
+};
+
+__device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, int ci, float radius) {
+    w.max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
+    w.sp = 0;
+    w.stack[w.sp++] = __ldg(&mt.roots[ci]);
+    w.min_dist = w.max_dist;
+    w.acc = mk3(0.0f, 0.0f, 0.0f);
+    w.min_face = 0;
+    w.sv_v = 0.0f;
+    w.sv_w = 0.0f;
+    w.found = false;
+    w.wt = __ldg(&mt.watertight[ci]) != 0;
+    w.min_dist_sq = w.max_dist * w.max_dist;
+}
+
+// Pops one node (:221-235, :315-330). Returns true when it is a leaf that passed the
+// distance test; its primitive range is returned for evaluation before the next pop.
+__device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, uint32_t& lo,
+                                         uint32_t& hi) {
+    const uint32_t ni = w.stack[--w.sp];
+    const float4 lo4 = __ldg(&mt.nl[ni]), hi4 = __ldg(&mt.nu[ni]);
+    const float nds = dist_sq_aabb(p, xyz(lo4), xyz(hi4));
+    if (w.wt) {
+        if (nds > w.min_dist_sq) return false;
+    } else {
+        if (nds > (w.min_dist + eps_md) * (w.min_dist + eps_md)) return false;
+    }
+    const uint32_t lpk = __float_as_uint(lo4.w);
+    const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
+    const uint32_t right_i = __float_as_uint(hi4.w) & 0x3FFFFFFFu;
+    if (is_leaf) {
+        lo = left_i;
+        hi = right_i;
+        return true;
+    }
+    const float4 llo = __ldg(&mt.nl[left_i]), lhi = __ldg(&mt.nu[left_i]);
+    const float4 rlo = __ldg(&mt.nl[right_i]), rhi = __ldg(&mt.nu[right_i]);
+    const float lds = dist_sq_aabb(p, xyz(llo), xyz(lhi)), rds = dist_sq_aabb(p, xyz(rlo), xyz(rhi));
+    const float thresh = w.wt ? w.min_dist_sq : ((w.min_dist + eps_md) * (w.min_dist + eps_md));
+    // the shader's 32-entry stack has no bound check; a push past it is dropped here
+    // and reported through the status word
+    if (lds < rds) {
+        if (rds < thresh) { if (w.sp < 32) w.stack[w.sp++] = right_i; else w.overflow = true; }
+        if (lds < thresh) { if (w.sp < 32) w.stack[w.sp++] = left_i; else w.overflow = true; }
+    } else {
+        if (lds < thresh) { if (w.sp < 32) w.stack[w.sp++] = left_i; else w.overflow = true; }
+        if (rds < thresh) { if (w.sp < 32) w.stack[w.sp++] = right_i; else w.overflow = true; }
+    }
+    return false;
+}
+
+// Evaluates the triangles of one leaf (:237-314).
+__device__ __forceinline__ void walk_leaf(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, float eps2,
+                                          uint32_t lo, uint32_t hi) {
+    const float PI_ = 3.14159265359f;
+    for (uint32_t pc = lo; pc < hi; pc++) {
+        const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
+        if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
+        const float4 qa = __ldg(&mt.tri_cache[pc * 4]), qb = __ldg(&mt.tri_cache[pc * 4 + 1]),
+                     qc = __ldg(&mt.tri_cache[pc * 4 + 2]);
+        const uint32_t t = __float_as_uint(qa.w);
+        const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
+        const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+        const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
+        v3 cp, tb;
+        closest_point_triangle(p, a, b, c, cp, tb);
+        if (w.wt) {
+            const v3 diff = vsub(cp, p);
+            const float dist_sq = vdot(diff, diff);
+            if (dist_sq < w.min_dist_sq) {
+                w.min_dist_sq = dist_sq;
+                w.min_face = t;
+                w.sv_v = tb.y;
+                w.sv_w = tb.z;
+                w.found = true;
+            }
         } else {
-            if (nds > (min_dist + eps_md) * (min_dist + eps_md)) continue;
-        }
-        const uint32_t lpk = __float_as_uint(lo4.w);
-        const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
-        const uint32_t right_i = __float_as_uint(hi4.w) & 0x3FFFFFFFu;
-        if (is_leaf) {
-            for (uint32_t pc = left_i; pc < right_i; pc++) {
-                const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
-                if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
-                const float4 qa = __ldg(&mt.tri_cache[pc * 4]), qb = __ldg(&mt.tri_cache[pc * 4 + 1]),
-                             qc = __ldg(&mt.tri_cache[pc * 4 + 2]);
-                const uint32_t t = __float_as_uint(qa.w);
-                const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
-                const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
-                const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
-                v3 cp, tb;
-                closest_point_triangle(p, a, b, c, cp, tb);
-                if (wt) {
-                    const v3 diff = vsub(cp, p);
-                    const float dist_sq = vdot(diff, diff);
-                    if (dist_sq < min_dist_sq) {
-                        min_dist_sq = dist_sq;
-                        min_face = t;
-                        sv_v = tb.y;
-                        sv_w = tb.z;
-                        found = true;
+            const float dist = exact_length(vsub(cp, p));
+            if (dist < w.min_dist + eps_md) {
+                float weight;
+                const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
+                const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
+                if (lcp < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
+                } else if (lcq < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
+                } else if (lcr < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
+                } else {
+                    const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
+                    if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
+                        (lcp * e1n - e1cp * e1cp < eps2 * e1n))
+                        weight = PI_;
+                    else
+                        weight = 2.0f * PI_;
+                }
+                if (dist > w.min_dist - eps_md) {
+                    w.acc = vadd(w.acc, vmuls(tn, weight));
+                    if (dist < w.min_dist) {
+                        w.min_dist = dist;
+                        w.min_face = t;
+                        w.sv_v = tb.y;
+                        w.sv_w = tb.z;
                     }
                 } else {
-                    const float dist = exact_length(vsub(cp, p));
-                    if (dist < min_dist + eps_md) {
-                        float weight;
-                        const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
-                        const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
-                        if (lcp < eps2) {
-                            weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
-                        } else if (lcq < eps2) {
-                            weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
-                        } else if (lcr < eps2) {
-                            weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
-                        } else {
-                            const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
-                            if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
-                                (lcp * e1n - e1cp * e1cp < eps2 * e1n))
-                                weight = PI_;
-                            else
-                                weight = 2.0f * PI_;
-                        }
-                        if (dist > min_dist - eps_md) {
-                            acc_normal = vadd(acc_normal, vmuls(tn, weight));
-                            if (dist < min_dist) {
-                                min_dist = dist;
-                                min_face = t;
-                                sv_v = tb.y;
-                                sv_w = tb.z;
-                            }
-                        } else {
-                            min_dist = dist;
-                            min_face = t;
-                            sv_v = tb.y;
-                            sv_w = tb.z;
-                            acc_normal = vmuls(tn, weight);
-                        }
-                        found = true;
-                    }
+                    w.min_dist = dist;
+                    w.min_face = t;
+                    w.sv_v = tb.y;
+                    w.sv_w = tb.z;
+                    w.acc = vmuls(tn, weight);
                 }
-            }
-        } else {
-            const float4 llo = __ldg(&mt.nl[left_i]), lhi = __ldg(&mt.nu[left_i]);
-            const float4 rlo = __ldg(&mt.nl[right_i]), rhi = __ldg(&mt.nu[right_i]);
-            const float lds = dist_sq_aabb(p, xyz(llo), xyz(lhi)), rds = dist_sq_aabb(p, xyz(rlo), xyz(rhi));
-            const float thresh = wt ? min_dist_sq : ((min_dist + eps_md) * (min_dist + eps_md));
-            // the shader's 32-entry stack has no bound check; a push past it is
-            // dropped here and reported through the status word
-            if (lds < rds) {
-                if (rds < thresh) { if (sp < 32) stack[sp++] = right_i; else overflow = true; }
-                if (lds < thresh) { if (sp < 32) stack[sp++] = left_i; else overflow = true; }
-            } else {
-                if (lds < thresh) { if (sp < 32) stack[sp++] = left_i; else overflow = true; }
-                if (rds < thresh) { if (sp < 32) stack[sp++] = right_i; else overflow = true; }
+                w.found = true;
             }
         }
     }
-    if (overflow) {
-        atomicOr(&st->error_bits, kErrStackOverflow);
-        atomicAdd(&st->stack_overflows, 1u);
-    }
-    if (wt) min_dist = exact_sqrt(min_dist_sq);
-    if (!(found && min_dist < max_dist)) return false;
-    const float u_mesh = (1.0f - sv_v) - sv_w;
-    const float v_mesh = sv_v;
-    const uint32_t i0 = __ldg(&mt.tris[min_face * 3]), i1 = __ldg(&mt.tris[min_face * 3 + 1]),
-                   i2 = __ldg(&mt.tris[min_face * 3 + 2]);
+}
+
+// Contact emission after the traversal of mesh ci (:333-411).
+__device__ __forceinline__ bool walk_finish(MeshWalk& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
+                                            v3& shape_v, v3& nrm) {
+    if (w.wt) w.min_dist = exact_sqrt(w.min_dist_sq);
+    if (!(w.found && w.min_dist < w.max_dist)) return false;
+    const float u_mesh = (1.0f - w.sv_v) - w.sv_w;
+    const float v_mesh = w.sv_v;
+    const uint32_t i0 = __ldg(&mt.tris[w.min_face * 3]), i1 = __ldg(&mt.tris[w.min_face * 3 + 1]),
+                   i2 = __ldg(&mt.tris[w.min_face * 3 + 2]);
     const v3 v0 = ldv(mt.verts, i0), v1 = ldv(mt.verts, i1), v2 = ldv(mt.verts, i2);
     const float w_eval = (1.0f - u_mesh) - v_mesh;
     const v3 shape_p = vfma_vs(v2, w_eval, vfma_vs(v0, u_mesh, vmuls(v1, v_mesh)));
     const v3 vel0 = ldv(mt.vels, i0), vel1 = ldv(mt.vels, i1), vel2 = ldv(mt.vels, i2);
     shape_v = vfma_vs(vel2, w_eval, vfma_vs(vel0, u_mesh, vmuls(vel1, v_mesh)));
     float sign;
-    if (wt) {
+    if (w.wt) {
         const v3 ray_dir = mk3(1.029700994f, 1.086472273f, 1.034694910f);
         uint32_t hits = 0;
         const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
@@ -243,7 +266,7 @@ __device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, flo
         }
         sign = (hits & 1u) ? -1.0f : 1.0f;
     } else {
-        sign = vdot(acc_normal, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
+        sign = vdot(w.acc, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
     }
     const v3 delta = vsub(p, shape_p);
     const float delta_len = exact_length(delta);
@@ -253,52 +276,116 @@ __device__ bool mesh_query(const MeshTables& mt, int ci, v3 p, float radius, flo
     return true;
 }
 
-// Thread t takes particle order[t]; with the previous substep's hash-grid order a
-// warp holds spatially adjacent particles, so their traversals follow similar
-// paths. Each particle's output depends on that particle only.
+// Contact generation with persistent warps. Lanes take particles from a work
+// queue (in the previous substep's hash-grid order, so a warp's particles are
+// neighbours) and refill as soon as their particle is done; the traversal runs
+// "while-while": every lane pops inner nodes until it holds a leaf, then the
+// warp evaluates leaves together. Each particle's own sequence of node visits
+// and leaf evaluations is that of the shader, so its contacts are unchanged.
 __global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __restrict__ order,
                                                  const float4* __restrict__ x, const float* __restrict__ r,
                                                  const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
-                                                 float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+                                                 float4* __restrict__ cslot, uint32_t* ccount, uint32_t* queue,
+                                                 DeviceStatus* st) {
     __shared__ uint32_t s_warp[4];
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t count = 0;
-    if (tid < n) {
-        const int64_t i = order ? (int64_t)__ldg(&order[tid]) : tid;
-        uint32_t info = 0;
-        const int fl = flags[i];
-        if (fl & 1) {
-            const v3 p = xyz(x[i]);
-            const float radius = r[i];
-            if (pl.enabled) {  // generate_plane_contacts.comp:37-38
-                const float dist = p.z - pl.altitude;
-                if (dist < pl.margin + radius) info |= kPlaneBit;
-            }
-            if (mt.n_meshes > 0) {
-                const float eps_md = mt.avg_edge * 1e-3f;
-                const float eps2 = eps_md * eps_md;
-                int used = 0;
-                float4* slots = cslot + (size_t)i * slot_cap * 3;
-                for (int ci = 0; ci < mt.n_meshes; ci++) {
-                    v3 bp, bv, nn;
-                    if (mesh_query(mt, ci, p, radius, eps_md, eps2, bp, bv, nn, st)) {
-                        if (used < slot_cap) {
-                            slots[used * 3 + 0] = make_float4(bp.x, bp.y, bp.z, __int_as_float(ci + 1));
-                            slots[used * 3 + 1] = make_float4(nn.x, nn.y, nn.z, 0.0f);
-                            slots[used * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
-                            used++;
-                        } else {
-                            atomicOr(&st->error_bits, kErrSlotOverflow);
-                            atomicAdd(&st->slot_overflows, 1u);
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    const float eps_md = mt.avg_edge * 1e-3f;
+    const float eps2 = eps_md * eps_md;
+    int64_t i = -1;
+    bool done = false, stack_ovf = false, slot_ovf = false;
+    v3 p = mk3(0.0f, 0.0f, 0.0f);
+    float radius = 0.0f;
+    uint32_t info = 0, count = 0;
+    int used = 0, ci = 0;
+    MeshWalk w;
+    w.sp = 0;
+    w.overflow = false;
+    while (true) {
+        // refill: lanes without a particle take the next queue entries; particles with
+        // no mesh work (inactive, or no mesh) complete right here
+        while (true) {
+            const bool need = !done && i < 0;
+            const uint32_t m = __ballot_sync(FULL, need);
+            if (!m) break;
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(m));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint64_t t = (uint64_t)base + (uint64_t)__popc(m & lt);
+                if (t >= (uint64_t)n) {
+                    done = true;
+                } else {
+                    i = order ? (int64_t)__ldg(&order[t]) : (int64_t)t;
+                    info = 0;
+                    used = 0;
+                    bool traverse = false;
+                    if (flags[i] & 1) {
+                        p = xyz(x[i]);
+                        radius = r[i];
+                        if (pl.enabled) {  // generate_plane_contacts.comp:37-38
+                            const float dist = p.z - pl.altitude;
+                            if (dist < pl.margin + radius) info |= kPlaneBit;
+                        }
+                        if (mt.n_meshes > 0) {
+                            ci = 0;
+                            walk_begin(w, mt, 0, radius);
+                            traverse = true;
                         }
                     }
+                    if (!traverse) {
+                        cinfo[i] = info;
+                        count += info & kPlaneBit;
+                        i = -1;
+                    }
                 }
-                info |= (uint32_t)used << 1;
             }
         }
-        cinfo[i] = info;
-        count = (info & kPlaneBit) + (info >> 1);
+        if (__all_sync(FULL, done)) break;
+        const bool busy = i >= 0;
+        bool holds = false;
+        uint32_t llo = 0, lhi = 0;
+        while (true) {  // inner nodes until every busy lane holds a leaf or has an empty stack
+            const bool more = busy && !holds && w.sp > 0;
+            if (!__any_sync(FULL, more)) break;
+            if (more) holds = walk_pop(w, mt, p, eps_md, llo, lhi);
+        }
+        if (holds) walk_leaf(w, mt, p, eps_md, eps2, llo, lhi);
+        if (busy && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
+            v3 bp, bv, nn;
+            if (walk_finish(w, mt, ci, p, bp, bv, nn)) {
+                if (used < slot_cap) {
+                    float4* s = cslot + ((size_t)i * slot_cap + used) * 3;
+                    s[0] = make_float4(bp.x, bp.y, bp.z, __int_as_float(ci + 1));
+                    s[1] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+                    s[2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+                    used++;
+                } else {
+                    slot_ovf = true;
+                }
+            }
+            stack_ovf |= w.overflow;
+            w.overflow = false;
+            if (++ci < mt.n_meshes) {
+                walk_begin(w, mt, ci, radius);
+            } else {
+                info |= (uint32_t)used << 1;
+                cinfo[i] = info;
+                count += (info & kPlaneBit) + (uint32_t)used;
+                i = -1;
+            }
+        }
+    }
+    if (stack_ovf) {
+        atomicOr(&st->error_bits, kErrStackOverflow);
+        atomicAdd(&st->stack_overflows, 1u);
+    }
+    if (slot_ovf) {
+        atomicOr(&st->error_bits, kErrSlotOverflow);
+        atomicAdd(&st->slot_overflows, 1u);
     }
     const uint32_t tot = block_sum(count, s_warp);
     if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
@@ -306,11 +393,11 @@ __global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __re
 
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, DeviceStatus* st) {
+                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st) {
     if (n <= 0) return;
     const int threads = 128;
-    k_collide<<<(int)((n + threads - 1) / threads), threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo,
-                                                                     cslot, ccount, st);
+    const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 8);
+    k_collide<<<blocks, threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo, cslot, ccount, queue, st);
 }
 
 // Triangle data that generate_mesh_contacts.comp:239-251 and :117 recompute on

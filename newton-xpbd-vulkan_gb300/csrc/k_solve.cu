@@ -15,16 +15,79 @@
 
 namespace xpbd {
 
+constexpr int kSolveThreads = 128;
+constexpr int kPairCap = 16;  // accepted neighbours buffered per thread before the pair math runs
+
+// Pair math of solve_particle_particle_contacts.comp:159-207 for the neighbours
+// buffered in shared memory (slot kk, distance d), accumulated in buffer order.
+template <bool DIAG>
+__device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThreads], const float (*s_d)[kSolveThreads],
+                                           const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                           const uint32_t* __restrict__ sids, v3 xp, v3 vp, float radius, float w1,
+                                           uint32_t id, const SolveParams& sp, const SolveDiag& dg, v3& acc) {
+    for (int q = 0; q < np; q++) {
+        const int kk = s_kk[q][threadIdx.x];
+        const float d = s_d[q][threadIdx.x];
+        const float4 nx = __ldg(&rx[kk]);
+        const float4 nv = __ldg(&rv[kk]);
+        const v3 raw = vsub(xp, xyz(nx));
+        const float err = d - radius - nx.w;
+        const float denom = w1 + nv.w;
+        if (denom <= 0.0f) continue;
+        const v3 nn = exact_div(raw, d);
+        const v3 vrel = vsub(vp, xyz(nv));
+        const float vn = exact_dot(nn, vrel);
+        const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y), __fmaf_rn(vn, -nn.z, vrel.z));
+        const float vt_len = exact_length(vt);
+        const float lambda_f = gmax(sp.k_mu * err, -vt_len * sp.dt);
+        const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+        const v3 p2 = vmuls(nn, err);
+        const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
+                            __fmaf_rn(vt_dir.z, lambda_f, -p2.z));
+        const v3 pair_d = exact_div(diff, denom);
+        acc = vadd(acc, pair_d);
+        if (DIAG && dg.pair_header) {  // solve_particle_particle_contacts.comp:180-207
+            const uint32_t slot = atomicAdd(&dg.pair_header[0], 1u);
+            if (slot < dg.max_pairs) {
+                float* rec = dg.pairs + (size_t)slot * 20;
+                const v3 t = mk3(__fmaf_rn(pair_d.x, w1, 0.0f), __fmaf_rn(pair_d.y, w1, 0.0f),
+                                 __fmaf_rn(pair_d.z, w1, 0.0f));
+                rec[0] = __uint_as_float(id);
+                rec[1] = __uint_as_float(__ldg(&sids[kk]));
+                rec[2] = d;
+                rec[3] = err;
+                rec[4] = nn.x;
+                rec[5] = nn.y;
+                rec[6] = nn.z;
+                rec[7] = vrel.x;
+                rec[8] = vrel.y;
+                rec[9] = vrel.z;
+                rec[10] = vn;
+                rec[11] = vt_len;
+                rec[12] = denom;
+                rec[13] = err;
+                rec[14] = lambda_f;
+                rec[15] = __fmaf_rn(t.x, sp.relax, 0.0f);
+                rec[16] = __fmaf_rn(t.y, sp.relax, 0.0f);
+                rec[17] = __fmaf_rn(t.z, sp.relax, 0.0f);
+                rec[18] = __uint_as_float((uint32_t)sp.iter_index);
+                rec[19] = 0.0f;
+            } else {
+                atomicAdd(&dg.pair_header[1], 1u);
+            }
+        }
+    }
+}
+
 template <bool LAST, bool ALL_ACTIVE, bool DIAG>
-__global__ void __launch_bounds__(128, 8) k_solve(int64_t n, const uint32_t* __restrict__ sids,
-                                               const float4* __restrict__ rx, const float4* __restrict__ rv,
-                                               const int* __restrict__ rf, const int4* __restrict__ table,
-                                               const uint32_t* __restrict__ stamp_p, const float4* __restrict__ x0a,
-                                               const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
-                                               const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt,
-                                               SolveParams sp, float4* __restrict__ rx_out,
-                                               float4* __restrict__ rv_out, float4* __restrict__ x_out,
-                                               float4* __restrict__ v_out, SolveDiag dg) {
+__global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
+    int64_t n, const uint32_t* __restrict__ sids, const float4* __restrict__ rx, const float4* __restrict__ rv,
+    const int* __restrict__ rf, const int4* __restrict__ table, const uint32_t* __restrict__ stamp_p,
+    const float4* __restrict__ x0a, const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
+    const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ rx_out,
+    float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg) {
+    __shared__ int s_kk[kPairCap][kSolveThreads];
+    __shared__ float s_d[kPairCap][kSolveThreads];
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t stamp = *stamp_p;
@@ -48,7 +111,9 @@ __global__ void __launch_bounds__(128, 8) k_solve(int64_t n, const uint32_t* __r
             v3 fd;
             if (shape_delta(ct, pflag, xp, vp, radius, w1, bt, sp, fd)) delta = vadd(delta, fd);
         }
-        // particle-particle contacts (solve_particle_particle_contacts.comp:116-217)
+        // particle-particle contacts (solve_particle_particle_contacts.comp:116-217): the
+        // candidate filter (:145-157) runs first and buffers accepted neighbours; the pair
+        // math then runs over the buffer in candidate order, so lanes stay in step
         const int is_proxy = pflag & 2;
         const float R = radius + sp.max_radius + sp.k_coh;
         const float inv = sp.inv;
@@ -58,31 +123,29 @@ __global__ void __launch_bounds__(128, 8) k_solve(int64_t n, const uint32_t* __r
         const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
         const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
         v3 acc = mk3(0.0f, 0.0f, 0.0f);
-        // Cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at
-        // 128 or is clamped at 0, so their particles form one contiguous run of the
-        // sorted order, in the reference's visit order (x ascending, then sorted order).
+        int np = 0;
+        // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
+        // or is clamped at 0; their particles then form one run of the sorted order, in the
+        // reference's visit order (x ascending, then sorted order within a cell)
         const int32_t xo = xs + kGridOrigin;
-        const bool row_contiguous = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
+        const bool row_run = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
         for (int32_t cz = zs; cz <= ze; cz++) {
             for (int32_t cy = ys; cy <= ye; cy++) {
-                int32_t cx_end = xe;
-                int run_lo = 0, run_hi = 0;
-                if (row_contiguous) {
-                    const int c0 = cell_index(xs, cy, cz);
-                    run_lo = 0x7fffffff;
-                    run_hi = -1;
-                    for (int j = 0; j <= xe - xs; j++) {
-                        const int4 e = __ldg(&table[c0 + j]);
-                        if ((uint32_t)e.z == stamp) {
-                            run_lo = min(run_lo, e.x);
-                            run_hi = max(run_hi, e.y);
+                for (int32_t cx = xs; cx <= xe; cx++) {
+                    int lo, hi;
+                    if (row_run) {
+                        const int c0 = cell_index(xs, cy, cz);
+                        lo = 0x7fffffff;
+                        hi = -1;
+                        for (int j = 0; j <= xe - xs; j++) {
+                            const int4 e = __ldg(&table[c0 + j]);
+                            if ((uint32_t)e.z == stamp) {
+                                lo = min(lo, e.x);
+                                hi = max(hi, e.y);
+                            }
                         }
-                    }
-                    cx_end = xs;  // one pass over the whole run
-                }
-                for (int32_t cx = xs; cx <= cx_end; cx++) {
-                    int lo = run_lo, hi = run_hi;
-                    if (!row_contiguous) {
+                        cx = xe;  // the run covers the whole row
+                    } else {
                         const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
                         if ((uint32_t)e.z != stamp) continue;
                         lo = e.x;
@@ -100,56 +163,17 @@ __global__ void __launch_bounds__(128, 8) k_solve(int64_t n, const uint32_t* __r
                         const float d = exact_length(raw);
                         const float err = d - radius - nx.w;
                         if (err > sp.k_coh || d <= 0.0f) continue;
-                        const float4 nv = __ldg(&rv[kk]);
-                        const float denom = w1 + nv.w;
-                        if (denom <= 0.0f) continue;
-                        const v3 nn = exact_div(raw, d);
-                        const v3 vrel = vsub(vp, xyz(nv));
-                        const float vn = exact_dot(nn, vrel);
-                        const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y),
-                                          __fmaf_rn(vn, -nn.z, vrel.z));
-                        const float vt_len = exact_length(vt);
-                        const float lambda_f = gmax(sp.k_mu * err, -vt_len * sp.dt);
-                        const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
-                        const v3 p2 = vmuls(nn, err);
-                        const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
-                                            __fmaf_rn(vt_dir.z, lambda_f, -p2.z));
-                        const v3 pair_d = exact_div(diff, denom);
-                        acc = vadd(acc, pair_d);
-                        if (DIAG && dg.pair_header) {  // solve_particle_particle_contacts.comp:180-207
-                            const uint32_t slot = atomicAdd(&dg.pair_header[0], 1u);
-                            if (slot < dg.max_pairs) {
-                                float* rec = dg.pairs + (size_t)slot * 20;
-                                const v3 t = mk3(__fmaf_rn(pair_d.x, w1, 0.0f), __fmaf_rn(pair_d.y, w1, 0.0f),
-                                                 __fmaf_rn(pair_d.z, w1, 0.0f));
-                                rec[0] = __uint_as_float(id);
-                                rec[1] = __uint_as_float(__ldg(&sids[kk]));
-                                rec[2] = d;
-                                rec[3] = err;
-                                rec[4] = nn.x;
-                                rec[5] = nn.y;
-                                rec[6] = nn.z;
-                                rec[7] = vrel.x;
-                                rec[8] = vrel.y;
-                                rec[9] = vrel.z;
-                                rec[10] = vn;
-                                rec[11] = vt_len;
-                                rec[12] = denom;
-                                rec[13] = err;
-                                rec[14] = lambda_f;
-                                rec[15] = __fmaf_rn(t.x, sp.relax, 0.0f);
-                                rec[16] = __fmaf_rn(t.y, sp.relax, 0.0f);
-                                rec[17] = __fmaf_rn(t.z, sp.relax, 0.0f);
-                                rec[18] = __uint_as_float((uint32_t)sp.iter_index);
-                                rec[19] = 0.0f;
-                            } else {
-                                atomicAdd(&dg.pair_header[1], 1u);
-                            }
+                        s_kk[np][threadIdx.x] = kk;
+                        s_d[np][threadIdx.x] = d;
+                        if (++np == kPairCap) {
+                            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+                            np = 0;
                         }
                     }
                 }
             }
         }
+        pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
         const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
         const v3 total = mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f),
                              __fmaf_rn(dw.z, sp.relax, 0.0f));
@@ -192,7 +216,7 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
                   SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg) {
     if (n <= 0) return;
-    const int threads = 128;
+    const int threads = kSolveThreads;
     const int blocks = (int)((n + threads - 1) / threads);
     const bool diag = dg.pair_header != nullptr;
 #define XPBD_SOLVE(L, A, D)                                                                                      \

@@ -126,10 +126,11 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
                          int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
-// plane + mesh contact generation; thread t handles particle order[t] (any permutation)
+// plane + mesh contact generation over the particles order[0..n) (any permutation);
+// *queue is the work-queue counter and must be zero at launch
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, DeviceStatus* st);
+                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st);
 // per-leaf-slot triangle cache for the slots [first, first + count)
 void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
                       const float* verts, float4* cache);

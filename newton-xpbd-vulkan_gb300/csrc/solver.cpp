@@ -108,7 +108,8 @@ void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_conta
     hist_off_ = 0;
     lb_off_ = (size_t)plan_.passes << plan_.bits;
     tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
-    sort_scratch_.alloc(tc_off_ + (size_t)plan_.passes);
+    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter
+    sort_scratch_.alloc(cq_off_ + 1);
     // the final sort buffer doubles as the collision pass's thread -> particle order
     launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
     XPBD_CUDA(cudaStreamSynchronize(stream_));
@@ -452,8 +453,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     prof_mark(P_CLEAR);
     if (mesh_pass) {
         launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
-                       slot_cap_, cinfo_.p, cslot_.p, ccount,
-                       st);
+                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, st);
         count_kernel();
         prof_mark(P_CONTACT);
     }
@@ -678,9 +678,9 @@ void Solver::collide_only() {
     pl.altitude = cfg_.ground_plane_altitude;
     ensure_substep_capacity(1);
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
+    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p + cq_off_, 0, sizeof(uint32_t), stream_));
     launch_collide(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p, x_[cur_].p, r_.p, flags_.p, pl,
-                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p,
-                   ccount_.p, status_.p);
+                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount_.p, sort_scratch_.p + cq_off_, status_.p);
     last_collide_src_ = cur_;
     finish_frame(1);
 }

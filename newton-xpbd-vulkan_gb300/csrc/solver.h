@@ -166,7 +166,7 @@ class Solver {
     SortPlan plan_{};
     DevBuf<uint32_t> keys_, pair_k_[2], pair_v_[2];
     DevBuf<uint32_t> sort_scratch_;  // hist | lookback | tile counters (cleared per substep)
-    size_t hist_off_ = 0, lb_off_ = 0, tc_off_ = 0;
+    size_t hist_off_ = 0, lb_off_ = 0, tc_off_ = 0, cq_off_ = 0;
     DevBuf<int4> table_;
     DevBuf<uint32_t> stamp_;
     DevBuf<float4> rx_[2], rv_[2];
