@@ -115,8 +115,11 @@ __device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
 }
 
 // Traversal state of one particle against one mesh (generate_mesh_contacts.comp:201-331).
+// A stack entry keeps, besides the node, the squared box distance and the packed
+// child words read when its parent ordered its children, so a pop needs no load.
 struct MeshWalk {
-    uint32_t stack[32];
+    float snds[32];
+    uint32_t slw[32], suw[32];
     uint32_t sp;
     float min_dist, min_dist_sq, max_dist;
     v3 acc;
@@ -125,10 +128,23 @@ struct MeshWalk {
     bool found, wt, overflow;
 };
 
-__device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, int ci, float radius) {
+__device__ __forceinline__ void walk_push(MeshWalk& w, float nds, float4 lo4, float4 hi4) {
+    if (w.sp < 32) {
+        w.snds[w.sp] = nds;
+        w.slw[w.sp] = __float_as_uint(lo4.w);
+        w.suw[w.sp] = __float_as_uint(hi4.w);
+        w.sp++;
+    } else {
+        w.overflow = true;
+    }
+}
+
+__device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, int ci, float radius, v3 p) {
     w.max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
     w.sp = 0;
-    w.stack[w.sp++] = __ldg(&mt.roots[ci]);
+    const uint32_t root = __ldg(&mt.roots[ci]);
+    const float4 lo4 = __ldg(&mt.nl[root]), hi4 = __ldg(&mt.nu[root]);
+    walk_push(w, dist_sq_aabb(p, xyz(lo4), xyz(hi4)), lo4, hi4);
     w.min_dist = w.max_dist;
     w.acc = mk3(0.0f, 0.0f, 0.0f);
     w.min_face = 0;
@@ -143,17 +159,16 @@ __device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, in
 // distance test; its primitive range is returned for evaluation before the next pop.
 __device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, uint32_t& lo,
                                          uint32_t& hi) {
-    const uint32_t ni = w.stack[--w.sp];
-    const float4 lo4 = __ldg(&mt.nl[ni]), hi4 = __ldg(&mt.nu[ni]);
-    const float nds = dist_sq_aabb(p, xyz(lo4), xyz(hi4));
+    --w.sp;
+    const float nds = w.snds[w.sp];
     if (w.wt) {
         if (nds > w.min_dist_sq) return false;
     } else {
         if (nds > (w.min_dist + eps_md) * (w.min_dist + eps_md)) return false;
     }
-    const uint32_t lpk = __float_as_uint(lo4.w);
+    const uint32_t lpk = w.slw[w.sp];
     const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
-    const uint32_t right_i = __float_as_uint(hi4.w) & 0x3FFFFFFFu;
+    const uint32_t right_i = w.suw[w.sp] & 0x3FFFFFFFu;
     if (is_leaf) {
         lo = left_i;
         hi = right_i;
@@ -166,11 +181,11 @@ __device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p
     // the shader's 32-entry stack has no bound check; a push past it is dropped here
     // and reported through the status word
     if (lds < rds) {
-        if (rds < thresh) { if (w.sp < 32) w.stack[w.sp++] = right_i; else w.overflow = true; }
-        if (lds < thresh) { if (w.sp < 32) w.stack[w.sp++] = left_i; else w.overflow = true; }
+        if (rds < thresh) walk_push(w, rds, rlo, rhi);
+        if (lds < thresh) walk_push(w, lds, llo, lhi);
     } else {
-        if (lds < thresh) { if (w.sp < 32) w.stack[w.sp++] = left_i; else w.overflow = true; }
-        if (rds < thresh) { if (w.sp < 32) w.stack[w.sp++] = right_i; else w.overflow = true; }
+        if (lds < thresh) walk_push(w, lds, llo, lhi);
+        if (rds < thresh) walk_push(w, rds, rlo, rhi);
     }
     return false;
 }
@@ -282,7 +297,7 @@ __device__ __forceinline__ bool walk_finish(MeshWalk& w, const MeshTables& mt, i
 // "while-while": every lane pops inner nodes until it holds a leaf, then the
 // warp evaluates leaves together. Each particle's own sequence of node visits
 // and leaf evaluations is that of the shader, so its contacts are unchanged.
-__global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __restrict__ order,
+__global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* __restrict__ order,
                                                  const float4* __restrict__ x, const float* __restrict__ r,
                                                  const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
@@ -332,7 +347,7 @@ __global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __re
                         }
                         if (mt.n_meshes > 0) {
                             ci = 0;
-                            walk_begin(w, mt, 0, radius);
+                            walk_begin(w, mt, 0, radius, p);
                             traverse = true;
                         }
                     }
@@ -370,7 +385,7 @@ __global__ void __launch_bounds__(128) k_collide(int64_t n, const uint32_t* __re
             stack_ovf |= w.overflow;
             w.overflow = false;
             if (++ci < mt.n_meshes) {
-                walk_begin(w, mt, ci, radius);
+                walk_begin(w, mt, ci, radius, p);
             } else {
                 info |= (uint32_t)used << 1;
                 cinfo[i] = info;
