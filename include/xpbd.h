@@ -156,6 +156,22 @@ const char* xpbd_stage_name(int index);
 /* out = {kernel launches per frame, memset nodes per frame, frames run, cached graphs} */
 int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]);
 
+/* Allocation-free sort — no counterpart in the reference. For callers that
+ * cannot allocate device memory while they run (work captured into a CUDA
+ * graph owned by another framework, plugins inside an application with its own
+ * device memory pool, real-time loops that forbid allocator calls): the stable
+ * hash-grid radix sort of n keys of key_bits bits, values = input index, from
+ * device buffer d_keys into device buffers d_sorted_keys / d_sorted_ids, queued
+ * on `stream` (a cudaStream_t; NULL = legacy default stream). It calls no
+ * cudaMalloc/cudaFree: its scratch is a static device array of about 10.5 MiB
+ * that every GPU loading the library holds until exit, so n is limited to
+ * XPBD_NOALLOC_MAX_KEYS. The first call on a device resolves that array's
+ * device address (make it before any stream capture). All calls share the
+ * array: calls that overlap on the GPU race and give wrong results. */
+#define XPBD_NOALLOC_MAX_KEYS (1 << 20)
+int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint32_t* d_sorted_ids, size_t n,
+                           int key_bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -265,4 +265,12 @@ int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]) {
     return guarded([&] { S(s).frame_stats(out); });
 }
 
+int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint32_t* d_sorted_ids, size_t n,
+                           int key_bits, void* stream) {
+    return guarded([&] {
+        xpbd::sort_keys_noalloc(d_keys, d_sorted_keys, d_sorted_ids, (int64_t)n, key_bits,
+                                static_cast<cudaStream_t>(stream));
+    });
+}
+
 }  // extern "C"

@@ -151,6 +151,9 @@ void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, co
 // reference-layout cell tables from the stamped table
 void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends);
 // float4 state -> packed xyz
+// stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
+void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,
+                       cudaStream_t s);
 void launch_unpack_xyz(cudaStream_t s, int64_t n, const float4* a, float* out);
 void launch_pack_xyz(cudaStream_t s, int64_t n, const float* in, float4* a);
 

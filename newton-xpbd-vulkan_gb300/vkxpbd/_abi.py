@@ -91,6 +91,7 @@ SIGNATURES = {
     "xpbd_reset_stage_times": (C.c_int, [_P]),
     "xpbd_stage_name": (C.c_char_p, [C.c_int]),
     "xpbd_get_frame_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "xpbd_sort_keys_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _Z, C.c_int, C.c_void_p]),
 }
 
 _lib = None
