@@ -19,12 +19,17 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
                                                       const float* __restrict__ r, const int* __restrict__ flags,
                                                       PredictParams pp, PlaneParams pl, uint32_t* __restrict__ keys,
                                                       int bits, int passes, uint32_t* __restrict__ hist,
-                                                      uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp) {
+                                                      uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp,
+                                                      uint32_t* heavy_count) {
     extern __shared__ uint32_t s_hist[];  // passes << bits
     __shared__ uint32_t s_warp[8];
     const int bins = 1 << bits;
     for (int i = threadIdx.x; i < passes * bins; i += blockDim.x) s_hist[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) *stamp += 1u;  // new grid generation for this substep
+    if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) {  // new grid generation for this substep
+        const uint32_t g = *stamp;
+        if (heavy_count) heavy_count[g & 1u] = 0u;  // the contact pass has consumed this list
+        *stamp = g + 1u;
+    }
     __syncthreads();
     uint32_t contacts = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -68,12 +73,13 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
 
 void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
                          const float* r, const int* flags, PredictParams pp, PlaneParams pl, uint32_t* keys,
-                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp) {
+                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp,
+                         uint32_t* heavy_count) {
     if (n <= 0) return;
     int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
     size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
     k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pp, pl, keys, sp.bits, sp.passes, hist, cinfo,
-                                            ccount, stamp);
+                                            ccount, stamp, heavy_count);
 }
 
 // ---------------------------------------------------------------------------
