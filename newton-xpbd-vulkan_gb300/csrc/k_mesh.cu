@@ -310,9 +310,10 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
     const float eps2 = eps_md * eps_md;
     // heavy-first schedule: the particles whose traversal was expensive in the previous
     // substep are served first, then the rest in grid order (results do not depend on order)
-    const uint32_t gen = sch.heavy_list ? *sch.stamp : 0u;
+    const bool scheduled = sch.heavy_count != nullptr;  // an empty schedule: plain grid order
+    const uint32_t gen = scheduled ? *sch.stamp : 0u;
     const int cur = (int)(gen & 1u), nxt = cur ^ 1;
-    const uint64_t n_heavy = sch.heavy_list ? (uint64_t)sch.heavy_count[cur] : 0u;
+    const uint64_t n_heavy = scheduled ? (uint64_t)sch.heavy_count[cur] : 0u;
     const uint64_t qlen = n_heavy + (uint64_t)n;
     int64_t i = -1;
     bool done = false, stack_ovf = false, slot_ovf = false;
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
                 info |= (uint32_t)used << 1;
                 cinfo[i] = info;
                 count += (info & kPlaneBit) + (uint32_t)used;
-                if (sch.heavy_list && cost >= sch.threshold) {  // serve it early next substep
+                if (scheduled && cost >= sch.threshold) {  // serve it early next substep
                     const uint32_t slot = atomicAdd(&sch.heavy_count[nxt], 1u);
                     sch.heavy_list[nxt][slot] = (uint32_t)i;
                     sch.heavy_flag[nxt][i] = gen + 1u;
