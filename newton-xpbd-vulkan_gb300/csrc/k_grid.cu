@@ -27,7 +27,9 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
     for (int i = threadIdx.x; i < passes * bins; i += blockDim.x) s_hist[i] = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) {  // new grid generation for this substep
         const uint32_t g = *stamp;
-        if (heavy_count) heavy_count[g & 1u] = 0u;  // the contact pass has consumed this list
+        // the list of generation g+1 is built by this substep's cell/gather kernel; its
+        // previous contents were consumed by the contact pass one substep ago
+        if (heavy_count) heavy_count[(g + 1u) & 1u] = 0u;
         *stamp = g + 1u;
     }
     __syncthreads();
@@ -298,8 +300,33 @@ __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t*
                                                       const float* __restrict__ r, const int* __restrict__ flags,
                                                       PredictParams pp, int* __restrict__ table,
                                                       const uint32_t* __restrict__ stamp, float4* __restrict__ rx,
-                                                      float4* __restrict__ rv, int* __restrict__ rf) {
+                                                      float4* __restrict__ rv, int* __restrict__ rf,
+                                                      CollideSchedule sch) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sch.heavy_count) {
+        // particles the contact pass marked as expensive, appended in grid order (one
+        // atomic per block, block-local order kept) for early service next substep
+        __shared__ uint32_t s_cnt[8];
+        __shared__ uint32_t s_base;
+        const uint32_t g = *stamp;  // already advanced for this substep
+        const int par = (int)(g & 1u);
+        const bool heavy = k < n && sch.heavy_flag[par][sids[k]] == g;
+        const uint32_t m = __ballot_sync(0xffffffffu, heavy);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) s_cnt[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tot = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+                const uint32_t c = s_cnt[w];
+                s_cnt[w] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(&sch.heavy_count[par], tot) : 0u;
+        }
+        __syncthreads();
+        if (heavy) sch.heavy_list[par][s_base + s_cnt[warp] + __popc(m & lanemask_lt())] = sids[k];
+    }
     if (k >= n) return;
     const uint32_t key = skeys[k];
     // grid_offsets.comp:20-34 without the table fills: a stale entry is
@@ -321,11 +348,12 @@ __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t*
 
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
-                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf) {
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf,
+                         CollideSchedule sch) {
     if (n <= 0) return;
     int blocks = (int)((n + 255) / 256);
     k_cells_gather<<<blocks, 256, 0, s>>>(n, skeys, sids, x, v, w, r, flags, pp, reinterpret_cast<int*>(table),
-                                          stamp, rx, rv, rf);
+                                          stamp, rx, rv, rf, sch);
 }
 
 }  // namespace xpbd

@@ -411,11 +411,9 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
                 info |= (uint32_t)used << 1;
                 cinfo[i] = info;
                 count += (info & kPlaneBit) + (uint32_t)used;
-                if (scheduled && cost >= sch.threshold) {  // serve it early next substep
-                    const uint32_t slot = atomicAdd(&sch.heavy_count[nxt], 1u);
-                    sch.heavy_list[nxt][slot] = (uint32_t)i;
-                    sch.heavy_flag[nxt][i] = gen + 1u;
-                }
+                // mark it for early service next substep; the grid-order list is built by
+                // the cell/gather kernel of this substep
+                if (scheduled && cost >= sch.threshold) sch.heavy_flag[nxt][i] = gen + 1u;
                 i = -1;
             }
         }

@@ -122,10 +122,12 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
                           DeviceStatus* st);
-// cell table + sorted-order particle records
+// cell table + sorted-order particle records (+ the contact pass's heavy list, in grid order)
+struct CollideSchedule;
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
-                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf,
+                         CollideSchedule sch);
 // Heavy-first schedule of the contact pass: particles whose traversal cost reached
 // `threshold` in the previous substep are listed (parity = grid stamp & 1) and served
 // first. heavy_count[parity] is reset by the key kernel once the list is consumed.

@@ -456,8 +456,8 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
     count_memset();
     prof_mark(P_CLEAR);
+    CollideSchedule sch{{nullptr, nullptr}, {nullptr, nullptr}, nullptr, nullptr, 0};
     if (mesh_pass) {
-        CollideSchedule sch;
         sch.heavy_list[0] = heavy_list_[0].p;
         sch.heavy_list[1] = heavy_list_[1].p;
         sch.heavy_flag[0] = heavy_flag_[0].p;
@@ -473,7 +473,8 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, pl, keys_.p, plan_,
-                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p, heavy_count_.p);
+                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p,
+                        mesh_pass ? heavy_count_.p : nullptr);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
     const uint32_t* kin = keys_.p;
@@ -503,7 +504,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         cr.totals = totals_.p;
     }
     launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
-                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
+                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p, sch);
     count_kernel();
     prof_mark(P_CELLS);
     SolveDiag dg{nullptr, nullptr, nullptr, 0};
