@@ -19,19 +19,12 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
                                                       const float* __restrict__ r, const int* __restrict__ flags,
                                                       PredictParams pp, PlaneParams pl, uint32_t* __restrict__ keys,
                                                       int bits, int passes, uint32_t* __restrict__ hist,
-                                                      uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp,
-                                                      uint32_t* heavy_count) {
+                                                      uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp) {
     extern __shared__ uint32_t s_hist[];  // passes << bits
     __shared__ uint32_t s_warp[8];
     const int bins = 1 << bits;
     for (int i = threadIdx.x; i < passes * bins; i += blockDim.x) s_hist[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) {  // new grid generation for this substep
-        const uint32_t g = *stamp;
-        // the list of generation g+1 is built by this substep's cell/gather kernel; its
-        // previous contents were consumed by the contact pass one substep ago
-        if (heavy_count) heavy_count[(g + 1u) & 1u] = 0u;
-        *stamp = g + 1u;
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && stamp) *stamp += 1u;  // new grid generation for this substep
     __syncthreads();
     uint32_t contacts = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -75,13 +68,12 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
 
 void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
                          const float* r, const int* flags, PredictParams pp, PlaneParams pl, uint32_t* keys,
-                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp,
-                         uint32_t* heavy_count) {
+                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp) {
     if (n <= 0) return;
     int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
     size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
     k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pp, pl, keys, sp.bits, sp.passes, hist, cinfo,
-                                            ccount, stamp, heavy_count);
+                                            ccount, stamp);
 }
 
 // ---------------------------------------------------------------------------
@@ -300,33 +292,8 @@ __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t*
                                                       const float* __restrict__ r, const int* __restrict__ flags,
                                                       PredictParams pp, int* __restrict__ table,
                                                       const uint32_t* __restrict__ stamp, float4* __restrict__ rx,
-                                                      float4* __restrict__ rv, int* __restrict__ rf,
-                                                      CollideSchedule sch) {
+                                                      float4* __restrict__ rv, int* __restrict__ rf) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (sch.heavy_count) {
-        // particles the contact pass marked as expensive, appended in grid order (one
-        // atomic per block, block-local order kept) for early service next substep
-        __shared__ uint32_t s_cnt[8];
-        __shared__ uint32_t s_base;
-        const uint32_t g = *stamp;  // already advanced for this substep
-        const int par = (int)(g & 1u);
-        const bool heavy = k < n && sch.heavy_flag[par][sids[k]] == g;
-        const uint32_t m = __ballot_sync(0xffffffffu, heavy);
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (lane == 0) s_cnt[warp] = __popc(m);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t tot = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-                const uint32_t c = s_cnt[w];
-                s_cnt[w] = tot;
-                tot += c;
-            }
-            s_base = tot ? atomicAdd(&sch.heavy_count[par], tot) : 0u;
-        }
-        __syncthreads();
-        if (heavy) sch.heavy_list[par][s_base + s_cnt[warp] + __popc(m & lanemask_lt())] = sids[k];
-    }
     if (k >= n) return;
     const uint32_t key = skeys[k];
     // grid_offsets.comp:20-34 without the table fills: a stale entry is
@@ -348,12 +315,11 @@ __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t*
 
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
-                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf,
-                         CollideSchedule sch) {
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf) {
     if (n <= 0) return;
     int blocks = (int)((n + 255) / 256);
     k_cells_gather<<<blocks, 256, 0, s>>>(n, skeys, sids, x, v, w, r, flags, pp, reinterpret_cast<int*>(table),
-                                          stamp, rx, rv, rf, sch);
+                                          stamp, rx, rv, rf);
 }
 
 }  // namespace xpbd

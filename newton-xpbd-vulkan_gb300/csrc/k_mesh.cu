@@ -302,24 +302,18 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
                                                  const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
                                                  float4* __restrict__ cslot, uint32_t* ccount, uint32_t* queue,
-                                                 CollideSchedule sch, DeviceStatus* st) {
+                                                 DeviceStatus* st) {
+    __shared__ uint32_t s_warp[4];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const float eps_md = mt.avg_edge * 1e-3f;
     const float eps2 = eps_md * eps_md;
-    // heavy-first schedule: the particles whose traversal was expensive in the previous
-    // substep are served first, then the rest in grid order (results do not depend on order)
-    const bool scheduled = sch.heavy_count != nullptr;  // an empty schedule: plain grid order
-    const uint32_t gen = scheduled ? *sch.stamp : 0u;
-    const int cur = (int)(gen & 1u), nxt = cur ^ 1;
-    const uint64_t n_heavy = scheduled ? (uint64_t)sch.heavy_count[cur] : 0u;
-    const uint64_t qlen = n_heavy + (uint64_t)n;
     int64_t i = -1;
     bool done = false, stack_ovf = false, slot_ovf = false;
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
-    uint32_t info = 0, count = 0, cost = 0;
+    uint32_t info = 0, count = 0;
     int used = 0, ci = 0;
     MeshWalk w;
     w.sp = 0;
@@ -337,19 +331,10 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
             base = __shfl_sync(FULL, base, leader);
             if (need) {
                 const uint64_t t = (uint64_t)base + (uint64_t)__popc(m & lt);
-                int64_t pick = -1;
-                if (t >= qlen) {
+                if (t >= (uint64_t)n) {
                     done = true;
-                } else if (t < n_heavy) {
-                    pick = (int64_t)__ldg(&sch.heavy_list[cur][t]);
                 } else {
-                    const uint64_t u = t - n_heavy;
-                    const int64_t j = order ? (int64_t)__ldg(&order[u]) : (int64_t)u;
-                    if (!(n_heavy && sch.heavy_flag[cur][j] == gen)) pick = j;  // else: already served
-                }
-                if (pick >= 0) {
-                    i = pick;
-                    cost = 0;
+                    i = order ? (int64_t)__ldg(&order[t]) : (int64_t)t;
                     info = 0;
                     used = 0;
                     bool traverse = false;
@@ -381,15 +366,9 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
         while (true) {  // inner nodes until every busy lane holds a leaf or has an empty stack
             const bool more = busy && !holds && w.sp > 0;
             if (!__any_sync(FULL, more)) break;
-            if (more) {
-                holds = walk_pop(w, mt, p, eps_md, llo, lhi);
-                cost += 1;
-            }
+            if (more) holds = walk_pop(w, mt, p, eps_md, llo, lhi);
         }
-        if (holds) {
-            walk_leaf(w, mt, p, eps_md, eps2, llo, lhi);
-            cost += 4 * (lhi - llo);
-        }
+        if (holds) walk_leaf(w, mt, p, eps_md, eps2, llo, lhi);
         if (busy && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
             v3 bp, bv, nn;
             if (walk_finish(w, mt, ci, p, bp, bv, nn)) {
@@ -411,9 +390,6 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
                 info |= (uint32_t)used << 1;
                 cinfo[i] = info;
                 count += (info & kPlaneBit) + (uint32_t)used;
-                // mark it for early service next substep; the grid-order list is built by
-                // the cell/gather kernel of this substep
-                if (scheduled && cost >= sch.threshold) sch.heavy_flag[nxt][i] = gen + 1u;
                 i = -1;
             }
         }
@@ -426,19 +402,17 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
         atomicOr(&st->error_bits, kErrSlotOverflow);
         atomicAdd(&st->slot_overflows, 1u);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) count += __shfl_down_sync(FULL, count, o);
-    if (lane == 0 && count) atomicAdd(ccount, count);
+    const uint32_t tot = block_sum(count, s_warp);
+    if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
 }
 
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, uint32_t* queue, CollideSchedule sch, DeviceStatus* st) {
+                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st) {
     if (n <= 0) return;
     const int threads = 128;
     const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 8);
-    k_collide<<<blocks, threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo, cslot, ccount, queue, sch,
-                                         st);
+    k_collide<<<blocks, threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo, cslot, ccount, queue, st);
 }
 
 // Triangle data that generate_mesh_contacts.comp:239-251 and :117 recompute on

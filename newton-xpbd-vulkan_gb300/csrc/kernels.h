@@ -116,33 +116,21 @@ size_t sort_lookback_words(const SortPlan& p);  // per pass
 void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
                          const float* r, const int* flags, PredictParams pp, PlaneParams pl,
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
-                         uint32_t* ccount, uint32_t* stamp, uint32_t* heavy_count);
+                         uint32_t* ccount, uint32_t* stamp);
 // one onesweep pass; vals_in == nullptr means vals are the element index
 void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
                           DeviceStatus* st);
-// cell table + sorted-order particle records (+ the contact pass's heavy list, in grid order)
-struct CollideSchedule;
+// cell table + sorted-order particle records
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
-                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf,
-                         CollideSchedule sch);
-// Heavy-first schedule of the contact pass: particles whose traversal cost reached
-// `threshold` in the previous substep are listed (parity = grid stamp & 1) and served
-// first. heavy_count[parity] is reset by the key kernel once the list is consumed.
-struct CollideSchedule {
-    uint32_t* heavy_list[2];   // [n] each
-    uint32_t* heavy_flag[2];   // [n] each: stamp value of the list a particle is in
-    uint32_t* heavy_count;     // [2]
-    const uint32_t* stamp;     // grid generation counter
-    uint32_t threshold;        // node pops + 4 x triangle tests
-};
+                         int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
 // plane + mesh contact generation over the particles order[0..n) (any permutation);
 // *queue is the work-queue counter and must be zero at launch
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, uint32_t* queue, CollideSchedule sch, DeviceStatus* st);
+                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st);
 // per-leaf-slot triangle cache for the slots [first, first + count)
 void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
                       const float* verts, float4* cache);

@@ -115,11 +115,6 @@ void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_conta
     XPBD_CUDA(cudaStreamSynchronize(stream_));
     table_.alloc(kNumCells);
     stamp_.alloc(1);
-    for (int p = 0; p < 2; p++) {
-        heavy_list_[p].alloc(n_);
-        heavy_flag_[p].alloc(n_);
-    }
-    heavy_count_.alloc(2);
     cinfo_.alloc(n_);
     slot_cap_ = 1;
     cslot_.alloc(std::max<size_t>(n_, 1) * 3);
@@ -456,25 +451,16 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
     count_memset();
     prof_mark(P_CLEAR);
-    CollideSchedule sch{{nullptr, nullptr}, {nullptr, nullptr}, nullptr, nullptr, 0};
     if (mesh_pass) {
-        sch.heavy_list[0] = heavy_list_[0].p;
-        sch.heavy_list[1] = heavy_list_[1].p;
-        sch.heavy_flag[0] = heavy_flag_[0].p;
-        sch.heavy_flag[1] = heavy_flag_[1].p;
-        sch.heavy_count = heavy_count_.p;
-        sch.stamp = stamp_.p;
-        sch.threshold = 24;
         launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
-                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, sch, st);
+                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, st);
         count_kernel();
         prof_mark(P_CONTACT);
     }
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, pl, keys_.p, plan_,
-                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p,
-                        mesh_pass ? heavy_count_.p : nullptr);
+                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
     const uint32_t* kin = keys_.p;
@@ -504,7 +490,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         cr.totals = totals_.p;
     }
     launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
-                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p, sch);
+                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
     count_kernel();
     prof_mark(P_CELLS);
     SolveDiag dg{nullptr, nullptr, nullptr, 0};
@@ -694,8 +680,7 @@ void Solver::collide_only() {
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
     XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p + cq_off_, 0, sizeof(uint32_t), stream_));
     launch_collide(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p, x_[cur_].p, r_.p, flags_.p, pl,
-                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount_.p, sort_scratch_.p + cq_off_,
-                   CollideSchedule{{nullptr, nullptr}, {nullptr, nullptr}, nullptr, nullptr, 0}, status_.p);
+                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount_.p, sort_scratch_.p + cq_off_, status_.p);
     last_collide_src_ = cur_;
     finish_frame(1);
 }

@@ -198,7 +198,6 @@ class Solver {
     DevBuf<float> verts_, vels_;
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
     DevBuf<float4> tri_cache_;
-    DevBuf<uint32_t> heavy_list_[2], heavy_flag_[2], heavy_count_;  // contact-pass schedule
     DevBuf<float> margins_;
     DevBuf<int> watertight_;
     float avg_edge0_ = 0.0f;
