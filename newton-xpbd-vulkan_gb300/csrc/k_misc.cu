@@ -1,4 +1,4 @@
-// Contact ranking / compaction and state packing.
+// Contact ranking / compaction, reference-layout debug tables, state packing.
 #include "contact.cuh"
 #include "kernels.h"
 #include "particle.cuh"
@@ -197,6 +197,21 @@ void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, co
     if (n <= 0) return;
     k_contact_compact<<<(int)((n + 255) / 256), 256, 0, s>>>(n, cinfo, cslot, slot_cap, rank, totals, contact_max,
                                                              x_prev, altitude, part, shape, bpos, bvel, nrm);
+}
+
+__global__ void k_cell_tables(const int4* __restrict__ table, const uint32_t* __restrict__ stamp_p,
+                              int32_t* __restrict__ starts, int32_t* __restrict__ ends) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kNumCells) return;
+    const uint32_t stamp = *stamp_p;
+    const int4 e = table[c];
+    const bool live = (uint32_t)e.z == stamp;
+    starts[c] = live ? e.x : 0;
+    ends[c] = live ? e.y : 0;
+}
+
+void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends) {
+    k_cell_tables<<<(kNumCells + 255) / 256, 256, 0, s>>>(table, stamp, starts, ends);
 }
 
 __global__ void k_unpack_xyz(int64_t n, const float4* __restrict__ a, float* __restrict__ out) {

@@ -181,6 +181,8 @@ void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2
 void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, const float4* cslot, int slot_cap,
                             const uint2* rank, const uint32_t* totals, int64_t contact_max, const float4* x_prev,
                             float altitude, int32_t* part, int32_t* shape, float* bpos, float* bvel, float* nrm);
+// reference-layout cell tables from the stamped table
+void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends);
 // float4 state -> packed xyz
 // stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
 void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,

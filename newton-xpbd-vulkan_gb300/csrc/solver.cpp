@@ -819,25 +819,15 @@ void Solver::get_sorted(uint32_t* cells, uint32_t* ids, size_t n) {
 
 void Solver::get_cell_tables(int32_t* starts, int32_t* ends) {
     require_init();
-    // Offsets into the reference's linear-key order (grid_offsets.comp:16-34 over the
-    // linear-sorted keys after zero fills); the device table holds Morton-order offsets.
-    std::vector<int32_t> s0(kNumCells, 0), e0(kNumCells, 0);
-    if (n_ > 0) {
-        std::vector<uint32_t> cells(n_);
-        get_sorted(cells.data(), nullptr, n_);
-        for (size_t t = 0; t < n_; t++) {
-            const uint32_t c = cells[t];
-            if (t == 0) {
-                s0[c] = 0;
-            } else if (c != cells[t - 1]) {
-                s0[c] = (int32_t)t;
-                e0[cells[t - 1]] = (int32_t)t;
-            }
-            if (t == n_ - 1) e0[c] = (int32_t)t + 1;
-        }
+    XPBD_CUDA(cudaSetDevice(device_));
+    if (!cell_starts_.p) {
+        cell_starts_.alloc(kNumCells, false);
+        cell_ends_.alloc(kNumCells, false);
     }
-    if (starts) std::memcpy(starts, s0.data(), sizeof(int32_t) * kNumCells);
-    if (ends) std::memcpy(ends, e0.data(), sizeof(int32_t) * kNumCells);
+    launch_cell_tables(stream_, table_.p, stamp_.p, cell_starts_.p, cell_ends_.p);
+    if (starts) XPBD_CUDA(cudaMemcpyAsync(starts, cell_starts_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
+    if (ends) XPBD_CUDA(cudaMemcpyAsync(ends, cell_ends_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void Solver::get_deltas(float* out, size_t n) {

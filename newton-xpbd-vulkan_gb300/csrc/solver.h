@@ -213,6 +213,7 @@ class Solver {
     size_t pinned_words_ = 0;
     DevBuf<int32_t> c_part_, c_shape_;
     DevBuf<float> c_bpos_, c_bvel_, c_nrm_;
+    DevBuf<int32_t> cell_starts_, cell_ends_;
     // graphs
     std::map<GraphKey, FrameGraph> graphs_;
     FrameGraph* recording_ = nullptr;  // graph being captured (marks and node counts go here)
