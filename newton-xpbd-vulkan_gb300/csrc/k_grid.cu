@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
             const int fl = flags[i];
             v3 xp, vp;
             predict(xf, v[i], w[i], fl, pp, xp, vp);
-            key = morton_of_linear(hash_grid_index(xp, pp.inv));
+            key = hash_grid_index(xp, pp.inv);
             keys[i] = key;
             if (cinfo) {  // generate_plane_contacts.comp:32-38 on the pre-integration position
                 uint32_t info = 0;
@@ -297,14 +297,12 @@ __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t*
     if (k >= n) return;
     const uint32_t key = skeys[k];
     // grid_offsets.comp:20-34 without the table fills: a stale entry is
-    // recognised by its generation stamp instead of being zeroed; the table is
-    // indexed by the linear cell index, the sort runs on its Morton key
-    const size_t cell = linear_of_morton(key);
+    // recognised by its generation stamp instead of being zeroed
     if (k == 0 || skeys[k - 1] != key) {
-        table[cell * 4 + 0] = (int)k;
-        table[cell * 4 + 2] = (int)*stamp;
+        table[(size_t)key * 4 + 0] = (int)k;
+        table[(size_t)key * 4 + 2] = (int)*stamp;
     }
-    if (k == n - 1 || skeys[k + 1] != key) table[cell * 4 + 1] = (int)(k + 1);
+    if (k == n - 1 || skeys[k + 1] != key) table[(size_t)key * 4 + 1] = (int)(k + 1);
     const uint32_t id = sids[k];
     const int fl = flags[id];
     const float wi = w[id];

@@ -124,14 +124,34 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
         const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
         v3 acc = mk3(0.0f, 0.0f, 0.0f);
         int np = 0;
-        // cells in the reference's visit order (x fastest, then y, then z); inside a
-        // cell the sorted order is ascending particle id
+        // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
+        // or is clamped at 0; their particles then form one run of the sorted order, in the
+        // reference's visit order (x ascending, then sorted order within a cell)
+        const int32_t xo = xs + kGridOrigin;
+        const bool row_run = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
         for (int32_t cz = zs; cz <= ze; cz++) {
             for (int32_t cy = ys; cy <= ye; cy++) {
                 for (int32_t cx = xs; cx <= xe; cx++) {
-                    const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
-                    if ((uint32_t)e.z != stamp) continue;
-                    for (int kk = e.x; kk < e.y; kk++) {
+                    int lo, hi;
+                    if (row_run) {
+                        const int c0 = cell_index(xs, cy, cz);
+                        lo = 0x7fffffff;
+                        hi = -1;
+                        for (int j = 0; j <= xe - xs; j++) {
+                            const int4 e = __ldg(&table[c0 + j]);
+                            if ((uint32_t)e.z == stamp) {
+                                lo = min(lo, e.x);
+                                hi = max(hi, e.y);
+                            }
+                        }
+                        cx = xe;  // the run covers the whole row
+                    } else {
+                        const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                        if ((uint32_t)e.z != stamp) continue;
+                        lo = e.x;
+                        hi = e.y;
+                    }
+                    for (int kk = lo; kk < hi; kk++) {
                         if (kk == k) continue;
                         const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
                         if ((nflag & 1) == 0) continue;

@@ -12,39 +12,6 @@ constexpr int kGridDim = 128;                                   // hash grid, sr
 constexpr int kNumCells = kGridDim * kGridDim * kGridDim;
 constexpr int kGridOrigin = 1 << 20;                            // grid_cell_indices.comp:20
 
-#ifdef __CUDACC__
-#define XPBD_HD __host__ __device__ __forceinline__
-#else
-#define XPBD_HD inline
-#endif
-// Sort key of a cell: the Morton interleave of its wrapped (x, y, z) coordinates
-// (7 bits each). Any key that is a bijection of the cell keeps each cell's
-// particles contiguous and in ascending id after a stable sort, which is all the
-// reference's neighbour loops rely on; with the Morton key 32 consecutive
-// particles form a compact block of cells instead of a 32-cell line along x.
-XPBD_HD uint32_t spread7(uint32_t v) {
-    v &= 0x3ffu;
-    v = (v ^ (v << 16)) & 0xff0000ffu;
-    v = (v ^ (v << 8)) & 0x0300f00fu;
-    v = (v ^ (v << 4)) & 0x030c30c3u;
-    v = (v ^ (v << 2)) & 0x09249249u;
-    return v;
-}
-XPBD_HD uint32_t compact7(uint32_t v) {
-    v &= 0x09249249u;
-    v = (v ^ (v >> 2)) & 0x030c30c3u;
-    v = (v ^ (v >> 4)) & 0x0300f00fu;
-    v = (v ^ (v >> 8)) & 0xff0000ffu;
-    v = (v ^ (v >> 16)) & 0x000003ffu;
-    return v;
-}
-XPBD_HD uint32_t morton_of_linear(uint32_t cell) {
-    return (spread7(cell >> 14) << 2) | (spread7((cell >> 7) & 127u) << 1) | spread7(cell & 127u);
-}
-XPBD_HD uint32_t linear_of_morton(uint32_t key) {
-    return (compact7(key >> 2) << 14) | (compact7(key >> 1) << 7) | compact7(key);
-}
-
 // Device-side status word read back after every frame. A kernel that gives
 // up (bounded wait expired, fixed-size buffer full) sets a bit and continues;
 // the host turns a set bit into an error instead of hanging or faulting.

@@ -796,25 +796,10 @@ void Solver::get_sorted(uint32_t* cells, uint32_t* ids, size_t n) {
     if (!initialized_) return;
     n = std::min(n, n_);
     XPBD_CUDA(cudaSetDevice(device_));
-    sync();
-    // The grid is sorted by the Morton key of the cell; the reference's layout is the
-    // stable sort by linear cell index. Each cell is one contiguous run in ascending id
-    // in both, so a stable re-sort of the runs by linear index gives it exactly.
     const int fin = (plan_.passes - 1) & 1;
-    std::vector<uint32_t> mk(n_), id(n_);
-    XPBD_CUDA(cudaMemcpyAsync(mk.data(), pair_k_[fin].p, n_ * 4, cudaMemcpyDeviceToHost, stream_));
-    XPBD_CUDA(cudaMemcpyAsync(id.data(), pair_v_[fin].p, n_ * 4, cudaMemcpyDeviceToHost, stream_));
+    if (cells) XPBD_CUDA(cudaMemcpyAsync(cells, pair_k_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
+    if (ids) XPBD_CUDA(cudaMemcpyAsync(ids, pair_v_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));
-    std::vector<uint32_t> perm(n_);
-    for (size_t i = 0; i < n_; i++) {
-        mk[i] = linear_of_morton(mk[i]);
-        perm[i] = (uint32_t)i;
-    }
-    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return mk[a] < mk[b]; });
-    for (size_t i = 0; i < n; i++) {
-        if (cells) cells[i] = mk[perm[i]];
-        if (ids) ids[i] = id[perm[i]];
-    }
 }
 
 void Solver::get_cell_tables(int32_t* starts, int32_t* ends) {
