@@ -156,6 +156,23 @@ const char* xpbd_stage_name(int index);
 /* out = {kernel launches per frame, memset nodes per frame, frames run, cached graphs} */
 int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]);
 
+/* Batched scenes (the xpbd_batch_* family). One solver steps n_scenes
+ * independent scenes in one graph per frame, one launch per kernel for all of
+ * them. Each scene has its own 128^3 hash grid (the scene id is the high part of
+ * the sort key), so scene s steps exactly as a solver initialised with
+ * scene_counts[s] particles would. Particles are the concatenation of the
+ * scenes' particles in scene order: xpbd_set_particles, xpbd_get_positions and
+ * the other particle calls take all of them, scene s at offset
+ * offsets[s] = scene_counts[0] + ... + scene_counts[s-1]. Meshes, the plane and
+ * the configuration are shared by all scenes; max_contacts (0 = 2 x total
+ * particles) caps the whole batch. 1 <= n_scenes <= 2048. The cell-table getter
+ * reports scene 0. */
+int xpbd_batch_init(xpbd_solver* s, const xpbd_config* cfg, const size_t* scene_counts, size_t n_scenes,
+                    size_t max_contacts);
+size_t xpbd_batch_scene_count(xpbd_solver* s);
+/* offsets: n_scenes + 1 entries (the last is the total particle count) */
+int xpbd_batch_scene_offsets(xpbd_solver* s, size_t* offsets, size_t cap);
+
 /* Allocation-free sort — no counterpart in the reference. For callers that
  * cannot allocate device memory while they run (work captured into a CUDA
  * graph owned by another framework, plugins inside an application with its own

@@ -265,6 +265,28 @@ int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]) {
     return guarded([&] { S(s).frame_stats(out); });
 }
 
+int xpbd_batch_init(xpbd_solver* s, const xpbd_config* cfg, const size_t* scene_counts, size_t n_scenes,
+                    size_t max_contacts) {
+    return guarded([&] {
+        if (!scene_counts) throw std::runtime_error("xpbd_batch_init: scene_counts is NULL");
+        xpbd_config c;
+        if (cfg)
+            c = *cfg;
+        else
+            xpbd_config_default(&c);
+        S(s).init_batched(c, scene_counts, n_scenes, max_contacts);
+    });
+}
+
+size_t xpbd_batch_scene_count(xpbd_solver* s) { return s ? s->impl.scene_count() : 0; }
+
+int xpbd_batch_scene_offsets(xpbd_solver* s, size_t* offsets, size_t cap) {
+    return guarded([&] {
+        if (S(s).scene_count() + 1 > cap) throw std::runtime_error("xpbd_batch_scene_offsets: buffer too small");
+        S(s).scene_offsets(offsets);
+    });
+}
+
 int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint32_t* d_sorted_ids, size_t n,
                            int key_bits, void* stream) {
     return guarded([&] {

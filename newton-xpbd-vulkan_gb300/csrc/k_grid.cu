@@ -17,7 +17,8 @@ namespace xpbd {
 __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* __restrict__ x,
                                                       const float4* __restrict__ v, const float* __restrict__ w,
                                                       const float* __restrict__ r, const int* __restrict__ flags,
-                                                      PredictParams pp, PlaneParams pl, uint32_t* __restrict__ keys,
+                                                      const uint32_t* __restrict__ pscene, PredictParams pp,
+                                                      PlaneParams pl, uint32_t* __restrict__ keys,
                                                       int bits, int passes, uint32_t* __restrict__ hist,
                                                       uint32_t* __restrict__ cinfo, uint32_t* ccount, uint32_t* stamp) {
     extern __shared__ uint32_t s_hist[];  // passes << bits
@@ -40,6 +41,7 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
             v3 xp, vp;
             predict(xf, v[i], w[i], fl, pp, xp, vp);
             key = hash_grid_index(xp, pp.inv);
+            if (pscene) key |= pscene[i] << 21;  // scene-major key = entry of the scene's table
             keys[i] = key;
             if (cinfo) {  // generate_plane_contacts.comp:32-38 on the pre-integration position
                 uint32_t info = 0;
@@ -67,13 +69,14 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
 }
 
 void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
-                         const float* r, const int* flags, PredictParams pp, PlaneParams pl, uint32_t* keys,
-                         const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount, uint32_t* stamp) {
+                         const float* r, const int* flags, const uint32_t* pscene, PredictParams pp, PlaneParams pl,
+                         uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount,
+                         uint32_t* stamp) {
     if (n <= 0) return;
     int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
     size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
-    k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pp, pl, keys, sp.bits, sp.passes, hist, cinfo,
-                                            ccount, stamp);
+    k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pscene, pp, pl, keys, sp.bits, sp.passes, hist,
+                                            cinfo, ccount, stamp);
 }
 
 // ---------------------------------------------------------------------------

@@ -81,8 +81,9 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
 
 template <bool LAST, bool ALL_ACTIVE, bool DIAG>
 __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
-    int64_t n, const uint32_t* __restrict__ sids, const float4* __restrict__ rx, const float4* __restrict__ rv,
-    const int* __restrict__ rf, const int4* __restrict__ table, const uint32_t* __restrict__ stamp_p,
+    int64_t n, const uint32_t* __restrict__ sids, const uint32_t* __restrict__ skeys, const float4* __restrict__ rx,
+    const float4* __restrict__ rv, const int* __restrict__ rf, const int4* __restrict__ table_all,
+    const uint32_t* __restrict__ stamp_p,
     const float4* __restrict__ x0a, const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
     const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ rx_out,
     float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg) {
@@ -92,6 +93,8 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     if (k >= n) return;
     const uint32_t stamp = *stamp_p;
     const uint32_t id = sids[k];
+    // this particle's scene table (scene-major keys); one scene: the whole table
+    const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
     const float4 ox = rx[k], ov = rv[k];
     const int pflag = ALL_ACTIVE ? 1 : rf[k];
     const v3 xp = xyz(ox), vp = xyz(ov);
@@ -211,19 +214,20 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     }
 }
 
-void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const float4* rx,
-                  const float4* rv, const int* rf, const int4* table, const uint32_t* stamp, const float4* x0,
-                  const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
-                  SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg) {
+void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const uint32_t* skeys,
+                  const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
+                  const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr,
+                  BodyTables bt, SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out,
+                  SolveDiag dg) {
     if (n <= 0) return;
     const int threads = kSolveThreads;
     const int blocks = (int)((n + threads - 1) / threads);
     const bool diag = dg.pair_header != nullptr;
-#define XPBD_SOLVE(L, A, D)                                                                                      \
-    if (last == L && all_active == A && diag == D) {                                                             \
-        k_solve<L, A, D><<<blocks, threads, 0, s>>>(n, sids, rx, rv, rf, table, stamp, x0, v0, cinfo, cslot, cr, \
-                                                    bt, sp, rx_out, rv_out, x_out, v_out, dg);                   \
-        return;                                                                                                  \
+#define XPBD_SOLVE(L, A, D)                                                                                         \
+    if (last == L && all_active == A && diag == D) {                                                                \
+        k_solve<L, A, D><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo, cslot, \
+                                                    cr, bt, sp, rx_out, rv_out, x_out, v_out, dg);                  \
+        return;                                                                                                     \
     }
     XPBD_SOLVE(true, true, false)
     XPBD_SOLVE(true, false, false)

@@ -113,8 +113,11 @@ SortPlan make_sort_plan(int64_t n, int key_bits, int bits, int items);
 size_t sort_lookback_words(const SortPlan& p);  // per pass
 
 // keys[i] (+ optional plane contacts, + all-pass digit histograms)
+// Batched scenes: pscene[i] is particle i's scene and the key becomes (scene << 21) | cell,
+// which is also the entry of a scene-major table of 128^3 cells per scene (pscene == null:
+// one scene).
 void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float4* v, const float* w,
-                         const float* r, const int* flags, PredictParams pp, PlaneParams pl,
+                         const float* r, const int* flags, const uint32_t* pscene, PredictParams pp, PlaneParams pl,
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
                          uint32_t* ccount, uint32_t* stamp);
 // one onesweep pass; vals_in == nullptr means vals are the element index
@@ -136,8 +139,11 @@ void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32
                       const float* verts, float4* cache);
 void launch_iota(cudaStream_t s, int64_t n, uint32_t* out);
 // fused shape solve + particle-particle solve + apply (+ restitution on the last iteration)
-void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const float4* rx,
-                  const float4* rv, const int* rf, const int4* table, const uint32_t* stamp, const float4* x0,
+// skeys (sorted keys) is passed for batched scenes so that each particle looks up its own
+// scene's table; null for one scene
+void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const uint32_t* skeys,
+                  const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
+                  const float4* x0,
                   const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
                   SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg);
 // exclusive scan of per-particle (plane bit, slot count) for the contact_max cap / compaction
@@ -148,12 +154,12 @@ void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2
 void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, const float4* cslot, int slot_cap,
                             const uint2* rank, const uint32_t* totals, int64_t contact_max, const float4* x_prev,
                             float altitude, int32_t* part, int32_t* shape, float* bpos, float* bvel, float* nrm);
-// reference-layout cell tables from the stamped table
+// reference-layout cell tables from the stamped table (table of one scene)
 void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends);
-// float4 state -> packed xyz
 // stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
 void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,
                        cudaStream_t s);
+// float4 state <-> packed xyz
 void launch_unpack_xyz(cudaStream_t s, int64_t n, const float4* a, float* out);
 void launch_pack_xyz(cudaStream_t s, int64_t n, const float* in, float4* a);
 

@@ -24,7 +24,6 @@ void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
 }
 
 namespace {
-constexpr int kKeyBits = 21;  // 128^3 cells
 // profiler stage slots, one per kernel (names follow scene.cpp:1481-1505 where they correspond)
 enum ProfSlot {
     P_CLEAR = 0, P_CONTACT, P_INTEGRATE_KEYS, P_SORT0, P_SORT1, P_SORT2, P_SORT3, P_RANKS, P_CELLS, P_SOLVE,
@@ -76,10 +75,20 @@ void Solver::clear_graphs() {
 }
 
 void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_contacts) {
+    init_batched(cfg, &num_particles, 1, max_contacts);
+}
+
+void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, size_t n_scenes, size_t max_contacts) {
     if (initialized_) throw std::runtime_error("XpbdSolver::init called twice");
+    if (n_scenes < 1 || n_scenes > 2048) throw std::runtime_error("init: between 1 and 2048 scenes");
     cfg_ = cfg;
+    scene_off_.assign(n_scenes + 1, 0);
+    for (size_t s = 0; s < n_scenes; s++) scene_off_[s + 1] = scene_off_[s] + scene_counts[s];
+    const size_t num_particles = scene_off_[n_scenes];
     n_ = num_particles;
     contact_max_ = (int64_t)(max_contacts ? max_contacts : num_particles * 2);  // scene.cpp:68
+    key_bits_ = 21;
+    while (n_scenes > 1 && (size_t(1) << (key_bits_ - 21)) < n_scenes) key_bits_++;
     int ndev = 0;
     XPBD_CUDA(cudaGetDeviceCount(&ndev));
     if (ndev == 0) throw std::runtime_error("no CUDA device");
@@ -104,7 +113,14 @@ void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_conta
         pair_v_[p].alloc(n_);
     }
     // digit width 8, 16 keys per thread above 1M particles, 8 below (more tiles per SM)
-    plan_ = make_sort_plan((int64_t)n_, kKeyBits, 8, n_ >= (1u << 20) ? 16 : 8);
+    plan_ = make_sort_plan((int64_t)n_, key_bits_, 8, n_ >= (1u << 20) ? 16 : 8);
+    if (n_scenes > 1) {
+        std::vector<uint32_t> ps(n_);
+        for (size_t s = 0; s < n_scenes; s++)
+            for (size_t i = scene_off_[s]; i < scene_off_[s + 1]; i++) ps[i] = (uint32_t)s;
+        pscene_.alloc(n_, false);
+        if (n_) XPBD_CUDA(cudaMemcpy(pscene_.p, ps.data(), n_ * 4, cudaMemcpyHostToDevice));
+    }
     hist_off_ = 0;
     lb_off_ = (size_t)plan_.passes << plan_.bits;
     tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
@@ -113,7 +129,7 @@ void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_conta
     // the final sort buffer doubles as the collision pass's thread -> particle order
     launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
     XPBD_CUDA(cudaStreamSynchronize(stream_));
-    table_.alloc(kNumCells);
+    table_.alloc((size_t)n_scenes * kNumCells);
     stamp_.alloc(1);
     cinfo_.alloc(n_);
     slot_cap_ = 1;
@@ -459,7 +475,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     }
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
-    launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, pl, keys_.p, plan_,
+    launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pscene_.p, pp, pl, keys_.p, plan_,
                         sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
@@ -503,7 +519,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const BodyTables bt = body_tables();
     for (int it = 0; it < iterations; it++) {
         const bool last = it == iterations - 1;
-        launch_solve(stream_, n, last, all_active_, sids, rx_[it & 1].p, rv_[it & 1].p, rf_.p, table_.p, stamp_.p,
+        launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p, rv_[it & 1].p, rf_.p, table_.p, stamp_.p,
                      x_[src].p, v_[src].p, info, slots, cr, bt, solve_params(sdt, it), rx_[(it + 1) & 1].p,
                      rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg);
         count_kernel();

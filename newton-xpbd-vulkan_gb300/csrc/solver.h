@@ -71,6 +71,14 @@ class Solver {
     ~Solver();
 
     void init(const xpbd_config& cfg, size_t num_particles, size_t max_contacts);
+    // Independent scenes stepped together: particles are the concatenation of the
+    // scenes' particles; each scene has its own 128^3 hash grid, so each steps exactly
+    // as it would alone. At most 2048 scenes (the scene id rides in the sort key).
+    void init_batched(const xpbd_config& cfg, const size_t* scene_counts, size_t n_scenes, size_t max_contacts);
+    size_t scene_count() const { return scene_off_.empty() ? 0 : scene_off_.size() - 1; }
+    void scene_offsets(size_t* out) const {
+        for (size_t i = 0; i < scene_off_.size(); i++) out[i] = scene_off_[i];
+    }
     void add_mesh(const float* verts, size_t num_verts, const uint32_t* tris, size_t num_tris, float shape_margin,
                   const float* rot_xyzw, int watertight_override);
     void finalize_meshes();
@@ -162,6 +170,10 @@ class Solver {
     DevBuf<int> flags_;
     int cur_ = 0;
     bool all_active_ = false;
+    // batched scenes
+    std::vector<size_t> scene_off_;  // n_scenes + 1 prefix offsets
+    DevBuf<uint32_t> pscene_;        // scene of each particle (batched only)
+    int key_bits_ = 21;
     // hash grid and sort
     SortPlan plan_{};
     DevBuf<uint32_t> keys_, pair_k_[2], pair_v_[2];

@@ -148,6 +148,23 @@ class XpbdSolver:
     def init(self, config, num_particles, max_contacts=0):
         _check(_lib.xpbd_init(self._h, C.byref(config._c), int(num_particles), int(max_contacts)))
 
+    def init_batched(self, config, scene_counts, max_contacts=0):
+        """Independent scenes stepped together (xpbd_batch_init). Particle arrays passed to
+        set_particles and returned by the getters are the scenes' particles concatenated in
+        scene order; scene_offsets() gives where each scene starts."""
+        counts = [int(c) for c in scene_counts]
+        arr = (C.c_size_t * max(len(counts), 1))(*counts)
+        _check(_lib.xpbd_batch_init(self._h, C.byref(config._c), arr, len(counts), int(max_contacts)))
+
+    def scene_count(self):
+        return int(_lib.xpbd_batch_scene_count(self._h))
+
+    def scene_offsets(self):
+        k = self.scene_count()
+        out = (C.c_size_t * (k + 1))()
+        _check(_lib.xpbd_batch_scene_offsets(self._h, out, k + 1))
+        return np.array(out[:], dtype=np.int64)
+
     def add_mesh(self, vertices, indices, shape_margin=0.0, shape_rot=None, is_watertight=None):
         v = _f32(vertices).reshape(-1)
         t = _u32(indices).reshape(-1)

@@ -92,6 +92,9 @@ SIGNATURES = {
     "xpbd_stage_name": (C.c_char_p, [C.c_int]),
     "xpbd_get_frame_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "xpbd_sort_keys_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _Z, C.c_int, C.c_void_p]),
+    "xpbd_batch_init": (C.c_int, [_P, C.POINTER(Config), C.POINTER(C.c_size_t), _Z, _Z]),
+    "xpbd_batch_scene_count": (_Z, [_P]),
+    "xpbd_batch_scene_offsets": (C.c_int, [_P, C.POINTER(C.c_size_t), _Z]),
 }
 
 _lib = None

@@ -136,3 +136,57 @@ def particles_on_mesh(dims=(64, 64, 64), spacing=0.01, radius=0.005, jitter=0.00
 def scaled(scene_fn, scale: int, **kw) -> Scene:
     """Same recipe with every lattice dimension divided by `scale` (test sizes)."""
     return scene_fn(**kw)
+
+
+def pile_of(n, spacing=0.02, radius=0.01, jitter=0.002, bottom_z=0.02, inv_mass=1000.0,
+            seed=SEED_JITTER, frames=100, name="pile") -> Scene:
+    """Config-1-style pile of exactly n particles: a square-based lattice with side
+    ceil(cbrt(n)), filled layer by layer from the bottom, the top layer partial."""
+    side = max(1, int(math.ceil(round(n ** (1.0 / 3.0), 9))))
+    layers = max(1, -(-n // (side * side)))
+    x = lattice((side, side, layers), spacing, bottom_z, 0.0)
+    order = np.argsort(x[:, 2], kind="stable")[:n]
+    x = x[np.sort(order)]
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        x = (x + (rng.random(x.shape) - 0.5) * 2.0 * jitter).astype(np.float32)
+    return Scene(name=name, config=_base_config(radius, 2.0 * radius), positions=np.ascontiguousarray(x),
+                 velocities=np.zeros_like(x), inv_mass=np.full(n, inv_mass, np.float32),
+                 radii=np.full(n, radius, np.float32), flags=np.ones(n, np.int32), frames=frames)
+
+
+def batch_counts(n_scenes=512, lo=1024, hi=65536, seed=SEED_BATCH):
+    """Per-scene particle counts log-uniform in [lo, hi]: round(exp(U[ln lo, ln hi]))."""
+    rng = np.random.default_rng(seed)
+    return [int(round(math.exp(u))) for u in rng.uniform(math.log(lo), math.log(hi), n_scenes)]
+
+
+@dataclass
+class Batch:
+    """Independent scenes stepped by one batched solver (same configuration for all)."""
+    scenes: list
+
+    @property
+    def counts(self):
+        return [s.n for s in self.scenes]
+
+    @property
+    def n(self) -> int:
+        return int(sum(self.counts))
+
+    @property
+    def config(self) -> dict:
+        return self.scenes[0].config
+
+    def apply_config(self, cfg) -> None:
+        self.scenes[0].apply_config(cfg)
+
+    def concat(self, attr):
+        return np.ascontiguousarray(np.concatenate([getattr(s, attr) for s in self.scenes]))
+
+
+def batched_piles(n_scenes=512, lo=1024, hi=65536, seed=SEED_BATCH, frames=100) -> Batch:
+    """Batched uneven scenes: n_scenes piles with log-uniform particle counts, scene s
+    jittered with seed `seed + s`; plane only."""
+    counts = batch_counts(n_scenes, lo, hi, seed)
+    return Batch([pile_of(c, seed=seed + s, frames=frames, name=f"pile{s}") for s, c in enumerate(counts)])
