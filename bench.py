@@ -12,6 +12,11 @@ the solver's stream.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--preroll P] [--impl reference]
 
+The same line carries "batched": 512 independent piles (log-uniform 1,024-65,536
+particles, seed 46, plane + particle-particle contacts) stepped by one batched
+solver against the same scenes stepped one solver at a time (--batched-scenes 0
+skips it).
+
 --impl reference times the CPU restatement of the reference's shaders (the
 oracle, all host threads) on the same pre-rolled scene, one substep per step.
 Under torchrun every rank steps its own replica of the scene (the path does
@@ -290,6 +295,9 @@ def run_gpu(args):
         "stage_ms_per_substep": {k: round(v / max(prof_substeps, 1), 5) for k, v in stage_ms.items() if v > 0},
         "e2e": e2e, "gpu_launches": int(stats["kernels_per_frame"] * args.steps), "clocks": clk,
     }
+    if rank == 0 and args.batched_scenes > 0:
+        del solver
+        result["batched"] = measure_batched(args, dev, flush)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_sample(sc, cfg, x_snap, v_snap, budget_s=args.cpu_budget)
     if rank == 0:
@@ -298,6 +306,97 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def measure_batched(args, dev, flush):
+    """Batched uneven scenes: 512 piles with log-uniform counts in [1024, 65536] (seed 46),
+    plane + particle-particle contacts, 10 substeps x 1 iteration per frame. "batched" is one
+    solver stepping all scenes (one graph per frame, one launch per kernel for all scenes);
+    "plain" is one solver per scene, each frame stepped scene by scene with the blocking
+    step(), as a reference user drives several scenes. Aggregate particle-substeps/s."""
+    import torch
+    import vkxpbd
+    from vkxpbd import scenes
+
+    batch = scenes.batched_piles(args.batched_scenes)
+    cfg = vkxpbd.SolverConfig()
+    batch.apply_config(cfg)
+    cfg.device_index = dev.index
+    g = vkxpbd.XpbdSolver()
+    g.init_batched(cfg, batch.counts)
+    g.finalize_meshes()
+    g.set_particles(batch.concat("positions"), batch.concat("velocities"), batch.concat("inv_mass"),
+                    batch.concat("radii"), batch.concat("flags"))
+    frames = args.batched_frames
+    stream = torch.cuda.ExternalStream(g.cuda_stream, device=dev)
+    for _ in range(args.warmup):
+        g.step(DT, SUBSTEPS, ITERATIONS)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(frames):
+        ev[k][0].record(stream)
+        g.step_async(DT, SUBSTEPS, ITERATIONS)
+        ev[k][1].record(stream)
+    g.sync()
+    torch.cuda.synchronize(dev)
+    wall_b = time.perf_counter() - t0
+    dev_b = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
+    launches_b = g.get_frame_stats()["kernels_per_frame"]
+    work = batch.n * SUBSTEPS * frames
+    # per-kernel device times (separate pass with event-record nodes in the graph)
+    g.set_profiling(True)
+    g.reset_stage_times()
+    for _ in range(min(frames, 5)):
+        g.step(DT, SUBSTEPS, ITERATIONS)
+    stage_ms, prof_substeps = g.get_stage_times()
+    g.set_profiling(False)
+    peak, peak_kind = measured_peak_hbm()
+    stages = {}
+    for k, v in stage_ms.items():
+        if v <= 0:
+            continue
+        launches = prof_substeps * (ITERATIONS if k.startswith("3.") else 1)
+        us = v / launches * 1e3
+        st = {"us_per_launch": round(us, 2)}
+        if k in ALG_BYTES:
+            gbs = ALG_BYTES[k] * batch.n / (us * 1e-6) / 1e9
+            st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
+        stages[k] = st
+    step_gbs = STEP_ALG_BYTES * work / dev_b / 1e9
+    del g
+    torch.cuda.synchronize(dev)
+
+    plain = []
+    for sc in batch.scenes:
+        s = vkxpbd.XpbdSolver()
+        s.init(cfg, sc.n)
+        s.finalize_meshes()
+        s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+        plain.append(s)
+    for _ in range(args.warmup):
+        for s in plain:
+            s.step(DT, SUBSTEPS, ITERATIONS)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        for s in plain:
+            s.step(DT, SUBSTEPS, ITERATIONS)
+    torch.cuda.synchronize(dev)
+    wall_p = time.perf_counter() - t0
+    launches_p = sum(s.get_frame_stats()["kernels_per_frame"] for s in plain)
+    del plain
+    return {"workload": "batched_piles", "scenes": len(batch.scenes), "particles": batch.n,
+            "counts": "log-uniform 1024-65536, seed 46", "frames": frames, "warmup": args.warmup,
+            "batched_value": work / dev_b, "batched_wall_value": work / wall_b, "plain_value": work / wall_p,
+            "unit": UNIT, "batched_over_plain": (work / wall_b) / (work / wall_p),
+            "launches_per_frame": {"batched": int(launches_b), "plain": int(launches_p)},
+            "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
+                              "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
+                              "peak_source": peak_kind},
+            "stages": stages,
+            "note": "batched_value device-timed (CUDA events); *_wall_value and plain_value host wall clock "
+                    "around stepping; boxes (0-16 per scene) not included"}
 
 
 def run_reference(args):
@@ -344,6 +443,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-scenes", type=int, default=512, help="0 skips the batched-scenes measurement")
+    ap.add_argument("--batched-frames", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
