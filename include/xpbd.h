@@ -156,6 +156,32 @@ const char* xpbd_stage_name(int index);
 /* out = {kernel launches per frame, memset nodes per frame, frames run, cached graphs} */
 int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]);
 
+/* Rigid bodies — an extension: the reference's body table is static
+ * (src/scene.cpp:220-238) and its body shaders (integrate_bodies.comp,
+ * apply_body_deltas.comp, solve_body_contact_positions.comp) are never
+ * dispatched. Body b belongs to mesh b (shape b + 1, src/scene.cpp:213). A body
+ * with inv_mass > 0 is dynamic: its mesh's vertices are in the body frame, and
+ * every substep integrates it, applies the body deltas of its particle contacts
+ * and solves its rigid contacts (its mesh's vertices against the ground plane
+ * and the other meshes). Bodies with inv_mass == 0 keep the reference's static
+ * behaviour (world-space mesh, identity pose). Arrays hold one row per mesh:
+ * q (pos xyz, quat xyzw) x7, qd (linear, angular) x6, com x3, inertia and
+ * inv_inertia x9 (symmetric), inv_mass, flags (2 = kinematic). NULL keeps the
+ * current values. Call after xpbd_finalize_meshes. */
+typedef struct xpbd_body_params {
+    float angular_damping;             /* integrate_bodies.comp push constant */
+    float rigid_contact_margin;        /* vertex-to-shape distance that makes a rigid contact */
+    float rigid_contact_relaxation;    /* solve_body_contact_positions.comp push constant */
+    int32_t rigid_contact_con_weighting; /* apply_body_deltas.comp use_constraint_weights */
+    float rigid_mu_torsional;
+    float rigid_mu_rolling;
+} xpbd_body_params;
+void xpbd_body_params_default(xpbd_body_params* p);
+int xpbd_set_body_params(xpbd_solver* s, const xpbd_body_params* p);
+int xpbd_set_bodies(xpbd_solver* s, const float* q, const float* qd, const float* com, const float* inertia,
+                    const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t num_bodies);
+int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t num_bodies);
+
 /* Batched scenes (the xpbd_batch_* family). One solver steps n_scenes
  * independent scenes in one graph per frame, one launch per kernel for all of
  * them. Each scene has its own 128^3 hash grid (the scene id is the high part of

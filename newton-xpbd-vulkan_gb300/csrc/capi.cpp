@@ -265,6 +265,33 @@ int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]) {
     return guarded([&] { S(s).frame_stats(out); });
 }
 
+void xpbd_body_params_default(xpbd_body_params* p) {
+    if (!p) return;
+    p->angular_damping = 0.0f;
+    p->rigid_contact_margin = 0.01f;
+    p->rigid_contact_relaxation = 0.8f;
+    p->rigid_contact_con_weighting = 1;
+    p->rigid_mu_torsional = 0.0f;
+    p->rigid_mu_rolling = 0.0f;
+}
+
+int xpbd_set_body_params(xpbd_solver* s, const xpbd_body_params* p) {
+    return guarded([&] {
+        xpbd_body_params d;
+        xpbd_body_params_default(&d);
+        S(s).set_body_params(p ? *p : d);
+    });
+}
+
+int xpbd_set_bodies(xpbd_solver* s, const float* q, const float* qd, const float* com, const float* inertia,
+                    const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb) {
+    return guarded([&] { S(s).set_bodies(q, qd, com, inertia, inv_inertia, inv_mass, flags, nb); });
+}
+
+int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t nb) {
+    return guarded([&] { S(s).get_bodies(q, qd, nb); });
+}
+
 int xpbd_batch_init(xpbd_solver* s, const xpbd_config* cfg, const size_t* scene_counts, size_t n_scenes,
                     size_t max_contacts) {
     return guarded([&] {

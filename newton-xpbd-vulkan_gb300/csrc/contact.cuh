@@ -52,7 +52,8 @@ __device__ __forceinline__ void body_pose(const BodyTables& bt, int body, v3& po
 // solve_particle_shape_contacts.comp:109-191 for one contact of an active
 // particle. Returns false when the contact is skipped; fd is the particle delta.
 __device__ __forceinline__ bool shape_delta(const Contact& ct, int pflag, v3 px, v3 pv, float radius, float w1,
-                                            const BodyTables& bt, const SolveParams& sp, v3& fd) {
+                                            const BodyTables& bt, const SolveParams& sp, v3& fd, v3& delta_total_out,
+                                            v3& r_out) {
     const int body = bt.shape_body[ct.shape];
     if (pflag & 2) {
         if (body < 0) return false;
@@ -99,6 +100,8 @@ __device__ __forceinline__ bool shape_delta(const Contact& ct, int pflag, v3 px,
                         __fmaf_rn(vt_dir.z, lambda_f, -delta_n.z));
     const v3 delta_total = vmuls(exact_div(diff, denom), sp.relax);
     fd = mk3(w1 * delta_total.x, w1 * delta_total.y, w1 * delta_total.z);
+    delta_total_out = delta_total;
+    r_out = r;
     return true;
 }
 
@@ -115,15 +118,25 @@ __device__ __forceinline__ bool restitution_dv(const Contact& ct, v3 v_new, v3 p
     const v3 d_px = vsub(px_old, bx);
     const float c = __fmaf_rn(n.z, d_px.z, __fmaf_rn(n.x, d_px.x, n.y * d_px.y)) - radius;
     if (c > sp.ka) return false;
-    // body_q_prev / body_qd_prev are bound to body_q / body_qd (scene.cpp:577-580)
-    const v3 bx_prev = vadd(X_pos, quat_rotate(X_rot, ct.bpos));
-    const v3 r = vsub(bx_prev, vadd(X_pos, quat_rotate(X_rot, X_com)));
-    const v3 bv_contact = quat_rotate(X_rot, ct.bvel);
+    v3 X_pos_prev = X_pos;
+    q4 X_rot_prev = X_rot;
+    if (body >= 0) {
+        const float4 pp = bt.body_q_prev[body * 2], pq = bt.body_q_prev[body * 2 + 1];
+        X_pos_prev = xyz(pp);
+        X_rot_prev.x = pq.x;
+        X_rot_prev.y = pq.y;
+        X_rot_prev.z = pq.z;
+        X_rot_prev.w = pq.w;
+    }
+    const v3 bx_prev = vadd(X_pos_prev, quat_rotate(X_rot_prev, ct.bpos));
+    const v3 r = vsub(bx_prev, vadd(X_pos_prev, quat_rotate(X_rot_prev, X_com)));
+    const v3 bv_contact = quat_rotate(X_rot_prev, ct.bvel);
     v3 bv_old = bv_contact, bv_new = bv_contact;
     if (body >= 0) {
-        const v3 bvo = xyz(bt.body_qd[body * 2]), bwo = xyz(bt.body_qd[body * 2 + 1]);
+        const v3 bvo = xyz(bt.body_qd_prev[body * 2]), bwo = xyz(bt.body_qd_prev[body * 2 + 1]);
+        const v3 bvn = xyz(bt.body_qd[body * 2]), bwn = xyz(bt.body_qd[body * 2 + 1]);
         bv_old = vadd(vadd(bvo, vcross(bwo, r)), bv_contact);
-        bv_new = vadd(vadd(bvo, vcross(bwo, r)), bv_contact);
+        bv_new = vadd(vadd(bvn, vcross(bwn, r)), bv_contact);
     }
     const v3 vdo = vsub(v_old, bv_old);
     const float rel_old = __fmaf_rn(n.z, vdo.z, __fmaf_rn(n.y, vdo.y, n.x * vdo.x));

@@ -1,0 +1,757 @@
+// Rigid bodies: body integration (integrate_bodies.comp), body delta
+// application (apply_body_deltas.comp), rigid contact solve
+// (solve_body_contact_positions.comp), the rigid contact generator those
+// shaders lack, and particle contacts against the meshes of moving bodies.
+//
+// Body b belongs to mesh b (shape b + 1, scene.cpp:213). A body with inverse
+// mass > 0 is dynamic: its mesh vertices are in the body frame and its state
+// changes every substep. The reference dispatches none of these shaders (its
+// body table is static, scene.cpp:220-238), so their host order is the one of
+// an XPBD iteration: particle deltas, body deltas from particle contacts
+// (applied without constraint weights), then rigid contacts solved on that
+// state and applied with weights.
+//
+// Every per-body sum runs in a fixed order (entry order of the particle
+// contacts, then own vertices before partners' vertices for the rigid
+// contacts), replacing the shaders' float atomics.
+#include <algorithm>
+
+#include "contact.cuh"
+#include "kernels.h"
+#include "mesh.cuh"
+#include "particle.cuh"
+#include "xmath.cuh"
+
+namespace xpbd {
+
+// ---- Warp-convention quaternion helpers as written in integrate_bodies.comp:44-73,
+// apply_body_deltas.comp:43-58 and solve_body_contact_positions.comp:44-61 ----
+__device__ __forceinline__ v3 wq_rot(q4 q, v3 v) {  // v + 2*cross(q.xyz, cross(q.xyz, v) + v*q.w)
+    const v3 qv = mk3(q.x, q.y, q.z);
+    const v3 t = vadd(vcross(qv, v), vmuls(v, q.w));
+    return vadd(v, vmuls(vcross(qv, t), 2.0f));
+}
+__device__ __forceinline__ v3 wq_rot_inv(q4 q, v3 v) {
+    q4 c = q;
+    c.x = -q.x;
+    c.y = -q.y;
+    c.z = -q.z;
+    return wq_rot(c, v);
+}
+__device__ __forceinline__ q4 wq_mul(q4 p, q4 q) {
+    const v3 c = vcross(mk3(p.x, p.y, p.z), mk3(q.x, q.y, q.z));
+    q4 r;
+    r.w = p.w * q.w - vdot(mk3(p.x, p.y, p.z), mk3(q.x, q.y, q.z));
+    r.x = (p.w * q.x + q.w * p.x) + c.x;
+    r.y = (p.w * q.y + q.w * p.y) + c.y;
+    r.z = (p.w * q.z + q.w * p.z) + c.z;
+    return r;
+}
+__device__ __forceinline__ q4 q_axpy(q4 a, q4 b, float s) {
+    q4 r;
+    r.x = a.x + b.x * s;
+    r.y = a.y + b.y * s;
+    r.z = a.z + b.z * s;
+    r.w = a.w + b.w * s;
+    return r;
+}
+__device__ __forceinline__ q4 q_normalize(q4 a) {  // v / length(v), IEEE sqrt and division
+    const float l = __fsqrt_rn(((a.x * a.x + a.y * a.y) + a.z * a.z) + a.w * a.w);
+    q4 r;
+    r.x = __fdiv_rn(a.x, l);
+    r.y = __fdiv_rn(a.y, l);
+    r.z = __fdiv_rn(a.z, l);
+    r.w = __fdiv_rn(a.w, l);
+    return r;
+}
+// 3x3 (9 floats, column-major) times vector: col0*v.x + col1*v.y + col2*v.z
+__device__ __forceinline__ v3 colmul(const float* m, v3 v) {
+    return mk3((m[0] * v.x + m[3] * v.y) + m[6] * v.z, (m[1] * v.x + m[4] * v.y) + m[7] * v.z,
+               (m[2] * v.x + m[5] * v.y) + m[8] * v.z);
+}
+__device__ __forceinline__ q4 f4q(float4 a) {
+    q4 r;
+    r.x = a.x;
+    r.y = a.y;
+    r.z = a.z;
+    r.w = a.w;
+    return r;
+}
+__device__ __forceinline__ void st_state(float4* q, float4* qd, int b, v3 p, q4 r, v3 v, v3 w) {
+    q[b * 2] = make_float4(p.x, p.y, p.z, 0.0f);
+    q[b * 2 + 1] = make_float4(r.x, r.y, r.z, r.w);
+    qd[b * 2] = make_float4(v.x, v.y, v.z, 0.0f);
+    qd[b * 2 + 1] = make_float4(w.x, w.y, w.z, 0.0f);
+}
+
+// apply_body_deltas.comp:58-119 for body b with delta (dp, dq)
+__device__ void apply_body_delta(const BodyArrays& ba, int b, float dt, const float4* q, const float4* qd, v3 dp,
+                                 v3 dq, float inv_weight, int use_weights, float4* qo, float4* qdo) {
+    const float inv_m = ba.invm[b];
+    if (inv_m == 0.0f) {
+        qo[b * 2] = q[b * 2];
+        qo[b * 2 + 1] = q[b * 2 + 1];
+        qdo[b * 2] = qd[b * 2];
+        qdo[b * 2 + 1] = qd[b * 2 + 1];
+        return;
+    }
+    const v3 pos0 = xyz(q[b * 2]);
+    const q4 quat0 = f4q(q[b * 2 + 1]);
+    const v3 v0 = xyz(qd[b * 2]), w0 = xyz(qd[b * 2 + 1]);
+    const float* I9 = ba.I + b * 9;
+    const float* Iinv9 = ba.invI + b * 9;
+    const v3 com = mk3(ba.com[b * 3], ba.com[b * 3 + 1], ba.com[b * 3 + 2]);
+    float weight = 1.0f;
+    if (use_weights) {
+        if (inv_weight > 0.0f) weight = __fdiv_rn(1.0f, inv_weight);
+    }
+    dp = vmuls(dp, inv_m * weight);
+    const v3 dq_w = vmuls(dq, weight);
+    const v3 wb = wq_rot_inv(quat0, w0);
+    const v3 dwb = colmul(Iinv9, wq_rot_inv(quat0, dq_w));
+    const v3 tb = vadd(vcross(dwb, colmul(I9, vadd(wb, dwb))), vcross(wb, colmul(I9, dwb)));
+    const v3 dw1 = wq_rot(quat0, vsub(dwb, vmuls(colmul(Iinv9, tb), dt)));
+    q4 dq4;
+    dq4.x = dw1.x * dt;
+    dq4.y = dw1.y * dt;
+    dq4.z = dw1.z * dt;
+    dq4.w = 0.0f;
+    const q4 quat1 = q_normalize(q_axpy(quat0, wq_mul(dq4, quat0), 0.5f));
+    const v3 x_com = vadd(pos0, wq_rot(quat0, com));
+    v3 p1 = vadd(x_com, vmuls(dp, dt));
+    p1 = vsub(p1, wq_rot(quat1, com));
+    v3 v1 = vadd(v0, dp), w1 = vadd(w0, dw1);
+    if (vlength(v1) < 1e-4f) v1 = mk3(0.0f, 0.0f, 0.0f);
+    if (vlength(w1) < 1e-4f) w1 = mk3(0.0f, 0.0f, 0.0f);
+    st_state(qo, qdo, b, p1, quat1, v1, w1);
+}
+
+// integrate_bodies.comp:75-130 (body forces are zero); the pre-integration state
+// is kept as the substep's previous state
+__global__ void k_body_integrate(BodyArrays ba, float4* __restrict__ q_prev, float4* __restrict__ qd_prev,
+                                 RigidParams rp) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= ba.nb) return;
+    const float4 q0 = ba.q[b * 2], q1 = ba.q[b * 2 + 1], d0 = ba.qd[b * 2], d1 = ba.qd[b * 2 + 1];
+    q_prev[b * 2] = q0;
+    q_prev[b * 2 + 1] = q1;
+    qd_prev[b * 2] = d0;
+    qd_prev[b * 2 + 1] = d1;
+    if (ba.flags[b] & 2) return;  // KINEMATIC: unchanged
+    const float dt = rp.dt;
+    const v3 x0 = xyz(q0), v0 = xyz(d0), w0 = xyz(d1);
+    const q4 r0 = f4q(q1);
+    const v3 f0 = mk3(0.0f, 0.0f, 0.0f), t0 = f0;
+    const v3 com = mk3(ba.com[b * 3], ba.com[b * 3 + 1], ba.com[b * 3 + 2]);
+    const float inv_mass = ba.invm[b];
+    const v3 g = mk3(rp.gx, rp.gy, rp.gz);
+    const v3 x_com = vadd(x0, wq_rot(r0, com));
+    const float m_scale = inv_mass != 0.0f ? 1.0f : 0.0f;
+    const v3 v1 = vadd(v0, vmuls(vadd(vmuls(f0, inv_mass), vmuls(g, m_scale)), dt));
+    const v3 x1 = vadd(x_com, vmuls(v1, dt));
+    const v3 wb = wq_rot_inv(r0, w0);
+    const v3 Iwb = colmul(ba.I + b * 9, wb);
+    const v3 tb = vsub(wq_rot_inv(r0, t0), vcross(wb, Iwb));
+    const v3 dwb = vmuls(colmul(ba.invI + b * 9, tb), dt);
+    v3 w1 = wq_rot(r0, vadd(wb, dwb));
+    q4 wq;
+    wq.x = w1.x;
+    wq.y = w1.y;
+    wq.z = w1.z;
+    wq.w = 0.0f;
+    const q4 r1 = q_normalize(q_axpy(r0, wq_mul(wq, r0), 0.5f * dt));
+    w1 = vmuls(w1, 1.0f - rp.damping * dt);
+    st_state(ba.q, ba.qd, b, vsub(x1, wq_rot(r1, com)), r1, v1, w1);
+}
+
+void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp) {
+    if (ba.nb <= 0) return;
+    k_body_integrate<<<(ba.nb + 127) / 128, 128, 0, s>>>(ba, q_prev, qd_prev, rp);
+}
+
+// ---------------------------------------------------------------- broad phase ----
+// World box of each dynamic body's mesh: the body-frame root box of its BVH,
+// rotated and translated (quat_rotate of solve_particle_shape_contacts.comp:50-58).
+__global__ void k_body_bounds(BodyArrays ba, RigidTables rt, MeshTables mt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rt.n_dyn) return;
+    const int b = rt.dyn[i];
+    const uint32_t root = mt.roots[b];
+    const v3 lo = xyz(mt.nl[root]), hi = xyz(mt.nu[root]);
+    const v3 pos = xyz(ba.q[b * 2]);
+    const q4 rot = f4q(ba.q[b * 2 + 1]);
+    v3 wl = mk3(3.0e38f, 3.0e38f, 3.0e38f), wh = mk3(-3.0e38f, -3.0e38f, -3.0e38f);
+    for (int c = 0; c < 8; c++) {
+        const v3 corner = mk3((c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z);
+        const v3 p = vadd(pos, quat_rotate(rot, corner));
+        wl = mk3(fminf(wl.x, p.x), fminf(wl.y, p.y), fminf(wl.z, p.z));
+        wh = mk3(fmaxf(wh.x, p.x), fmaxf(wh.y, p.y), fmaxf(wh.z, p.z));
+    }
+    rt.wbox[i * 2] = make_float4(wl.x, wl.y, wl.z, mt.margins[b]);
+    rt.wbox[i * 2 + 1] = make_float4(wh.x, wh.y, wh.z, 0.0f);
+}
+
+// Pairs of dynamic bodies whose boxes, widened by the rigid contact margin, their
+// shape margins and a rounding pad, overlap. One warp per body; partners ascending.
+__global__ void k_body_pairs(RigidTables rt, RigidParams rp, DeviceStatus* st) {
+    const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= rt.n_dyn) return;
+    const float4 il = rt.wbox[i * 2], ih = rt.wbox[i * 2 + 1];
+    const float ei = rp.margin + il.w + rt.pad;
+    int count = 0;
+    for (int j0 = 0; j0 < rt.n_dyn; j0 += 32) {
+        const int j = j0 + lane;
+        bool ov = false;
+        if (j < rt.n_dyn && j != i) {
+            const float4 jl = rt.wbox[j * 2], jh = rt.wbox[j * 2 + 1];
+            const float ej = rp.margin + jl.w + rt.pad;
+            ov = (il.x - ei <= jh.x + ej) && (jl.x - ej <= ih.x + ei) && (il.y - ei <= jh.y + ej) &&
+                 (jl.y - ej <= ih.y + ei) && (il.z - ei <= jh.z + ej) && (jl.z - ej <= ih.z + ei);
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, ov);
+        if (ov) {
+            const int pos = count + __popc(m & lanemask_lt());
+            if (pos < kPartnerCap) rt.partners[i * kPartnerCap + pos] = rt.dyn[j];
+        }
+        count += __popc(m);
+    }
+    if (lane == 0) {
+        rt.partner_count[i] = count < kPartnerCap ? count : kPartnerCap;
+        if (count > kPartnerCap) atomicOr(&st->error_bits, kErrBodyOverflow);
+    }
+}
+
+void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
+                       DeviceStatus* st) {
+    if (rt.n_dyn <= 0) return;
+    k_body_bounds<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(ba, rt, mt);
+    k_body_pairs<<<(rt.n_dyn * 32 + 127) / 128, 128, 0, s>>>(rt, rp, st);
+}
+
+// ---------------------------------------------------------------- rigid contacts ----
+// One thread per vertex of a dynamic body's mesh: the vertex against the ground plane,
+// then the closest-point query of generate_mesh_contacts.comp (radius 0, the rigid
+// margin in place of the soft contact margin) against the static meshes and the
+// overlapping dynamic bodies' meshes, in mesh index order. Slot record (5 float4):
+// (p0, shape1 bits), (p1, thickness0), (normal, thickness1), (offset0, 0), (offset1, 0).
+__global__ void k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp, int n_vert,
+                                 DeviceStatus* st) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n_vert) return;
+    const float4 lv = rt.dv_local[d];
+    const int a = __float_as_int(lv.w);
+    const v3 V = xyz(lv);
+    const v3 pos_a = xyz(ba.q[a * 2]);
+    const q4 rot_a = f4q(ba.q[a * 2 + 1]);
+    const v3 P = vadd(pos_a, quat_rotate(rot_a, V));
+    const float th0 = mt.margins[a];
+    float4* out = rt.rc + (size_t)d * kRigidSlots * 5;
+    int cnt = 0;
+    bool ovf = false, stack_ovf = false;
+    if (rp.plane) {
+        const float dist = P.z - rp.altitude;
+        if (dist < rp.margin) {
+            const v3 n = mk3(0.0f, 0.0f, -1.0f);
+            const float th1 = 0.0f;
+            const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0)), o1 = vmuls(n, -th1);
+            out[0] = make_float4(V.x, V.y, V.z, __int_as_float(0));
+            out[1] = make_float4(P.x, P.y, rp.altitude, th0);
+            out[2] = make_float4(n.x, n.y, n.z, th1);
+            out[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+            out[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+            cnt = 1;
+        }
+    }
+    MeshTables rmt = mt;
+    rmt.soft_margin = rp.margin;
+    const int ia = rt.dyn_index[a];
+    const int pc = rt.partner_count[ia];
+    const int* partners = rt.partners + ia * kPartnerCap;
+    int si = 0, pi = 0;
+    while (si < mt.walk_count || pi < pc) {
+        const int ms = si < mt.walk_count ? mt.walk_list[si] : 0x7fffffff;
+        const int mp = pi < pc ? partners[pi] : 0x7fffffff;
+        int m;
+        bool pz;
+        if (ms < mp) {
+            m = ms;
+            si++;
+            pz = false;
+        } else {
+            m = mp;
+            pi++;
+            pz = true;
+        }
+        if (m == a) continue;
+        v3 Q = P, pos_m = mk3(0.0f, 0.0f, 0.0f);
+        q4 rot_m;
+        rot_m.x = rot_m.y = rot_m.z = 0.0f;
+        rot_m.w = 1.0f;
+        if (pz) {
+            pos_m = xyz(ba.q[m * 2]);
+            rot_m = f4q(ba.q[m * 2 + 1]);
+            Q = quat_rotate_inv(rot_m, vsub(P, pos_m));
+        }
+        v3 bpos, bvel, nrm;
+        if (!mesh_query(rmt, m, 0.0f, Q, bpos, bvel, nrm, stack_ovf)) continue;
+        if (cnt >= kRigidSlots) {
+            ovf = true;
+            continue;
+        }
+        const float th1 = mt.margins[m];
+        const v3 n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
+        const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0));
+        const v3 o1 = pz ? quat_rotate_inv(rot_m, vmuls(n, -th1)) : vmuls(n, -th1);
+        float4* o = out + cnt * 5;
+        o[0] = make_float4(V.x, V.y, V.z, __int_as_float(m + 1));
+        o[1] = make_float4(bpos.x, bpos.y, bpos.z, th0);
+        o[2] = make_float4(n.x, n.y, n.z, th1);
+        o[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+        o[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+        cnt++;
+    }
+    rt.rc_count[d] = cnt;
+    if (ovf) atomicOr(&st->error_bits, kErrBodyOverflow);
+    if (stack_ovf) {
+        atomicOr(&st->error_bits, kErrStackOverflow);
+        atomicAdd(&st->stack_overflows, 1u);
+    }
+}
+
+void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
+                           DeviceStatus* st) {
+    if (rt.n_vert <= 0) return;
+    k_rigid_contacts<<<(rt.n_vert + 127) / 128, 128, 0, s>>>(ba, rt, mt, rp, rt.n_vert, st);
+}
+
+// ---------------------------------------------------------------- particle contacts on moving meshes ----
+// One CTA of 128 particles (in hash-grid order, so they are neighbours) keeps the dynamic
+// bodies whose world boxes come near the CTA's particles, in ascending order; each
+// particle then queries those meshes in its body frame (generate_mesh_contacts.comp with
+// the pose inverted) and inserts the contacts into its slots in mesh order.
+__global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t* __restrict__ order,
+                                                      const float4* __restrict__ x, const float* __restrict__ r,
+                                                      const int* __restrict__ flags, MeshTables mt, RigidTables rt,
+                                                      int slot_cap, uint32_t* __restrict__ cinfo,
+                                                      float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+    __shared__ float s_red[4][7];
+    __shared__ int s_cand[128];
+    __shared__ int s_wcnt[4];
+    __shared__ uint32_t s_warp[4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i = -1;
+    bool active = false;
+    v3 p = mk3(0.0f, 0.0f, 0.0f);
+    float radius = 0.0f;
+    if (t < n) {
+        i = order ? (int64_t)order[t] : t;
+        active = (flags[i] & 1) != 0;
+        if (active) {
+            p = xyz(x[i]);
+            radius = r[i];
+        }
+    }
+    // CTA bounds of the active particles and their largest radius
+    float v[7] = {active ? p.x : 3.0e38f, active ? p.y : 3.0e38f, active ? p.z : 3.0e38f,
+                  active ? -p.x : 3.0e38f, active ? -p.y : 3.0e38f, active ? -p.z : 3.0e38f,
+                  active ? -radius : 3.0e38f};
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 7; k++) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if (lane == 0)
+        for (int k = 0; k < 7; k++) s_red[warp][k] = v[k];
+    __syncthreads();
+    for (int k = 0; k < 7; k++) v[k] = fminf(fminf(s_red[0][k], s_red[1][k]), fminf(s_red[2][k], s_red[3][k]));
+    if (v[0] > 1.0e38f) return;  // no active particle in this CTA (uniform)
+    const float E = mt.soft_margin - v[6] + 2.0f * rt.pad;
+    const v3 blo = mk3(v[0] - E, v[1] - E, v[2] - E), bhi = mk3(-v[3] + E, -v[4] + E, -v[5] + E);
+
+    uint32_t info = 0;
+    int used0 = 0, used = 0;
+    if (active) {
+        info = cinfo[i];
+        used0 = used = (int)(info >> 1);
+    }
+    bool slot_ovf = false, stack_ovf = false;
+    for (int c0 = 0; c0 < rt.n_dyn; c0 += 128) {
+        const int c = c0 + threadIdx.x;
+        bool near = false;
+        if (c < rt.n_dyn) {
+            const float4 l = rt.wbox[c * 2], h = rt.wbox[c * 2 + 1];
+            near = (blo.x <= h.x + l.w) && (l.x - l.w <= bhi.x) && (blo.y <= h.y + l.w) && (l.y - l.w <= bhi.y) &&
+                   (blo.z <= h.z + l.w) && (l.z - l.w <= bhi.z);
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, near);
+        __syncthreads();  // previous chunk's candidates consumed
+        if (lane == 0) s_wcnt[warp] = __popc(m);
+        __syncthreads();
+        int off = 0, total = 0;
+        for (int w = 0; w < 4; w++) {
+            if (w < warp) off += s_wcnt[w];
+            total += s_wcnt[w];
+        }
+        if (near) s_cand[off + __popc(m & lanemask_lt())] = c;
+        __syncthreads();
+        if (!active) continue;
+        for (int k = 0; k < total; k++) {
+            const int ci = s_cand[k];
+            const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
+            const float e = (mt.soft_margin + l.w) + radius + rt.pad;
+            if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
+                  p.z <= h.z + e))
+                continue;
+            const int mesh = rt.dyn[ci];
+            const v3 pos_m = xyz(mt.pose[mesh * 2]);
+            const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+            const v3 q = quat_rotate_inv(rot_m, vsub(p, pos_m));
+            v3 bp, bv, nn;
+            if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) continue;
+            const v3 nw = quat_rotate(rot_m, nn);
+            if (used >= slot_cap) {
+                slot_ovf = true;
+                continue;
+            }
+            float4* base = cslot + (size_t)i * slot_cap * 3;
+            int pos = used;
+            while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
+            for (int k2 = used; k2 > pos; k2--) {
+                base[k2 * 3] = base[(k2 - 1) * 3];
+                base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
+                base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
+            }
+            base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
+            base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
+            base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+            used++;
+        }
+    }
+    if (active && used != used0) cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1);
+    if (slot_ovf) {
+        atomicOr(&st->error_bits, kErrSlotOverflow);
+        atomicAdd(&st->slot_overflows, 1u);
+    }
+    if (stack_ovf) {
+        atomicOr(&st->error_bits, kErrStackOverflow);
+        atomicAdd(&st->stack_overflows, 1u);
+    }
+    const uint32_t tot = block_sum((uint32_t)(used - used0), s_warp);
+    if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
+}
+
+void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                          const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
+                          float4* cslot, uint32_t* ccount, DeviceStatus* st) {
+    if (n <= 0 || rt.n_dyn <= 0) return;
+    const int blocks = (int)((n + 127) / 128);
+    k_collide_posed<<<blocks, 128, 0, s>>>(n, order, x, r, flags, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+}
+
+// ---------------------------------------------------------------- body-delta entries ----
+__global__ void k_dyn_emit(int64_t n, const uint32_t* __restrict__ cinfo, DynSlots ds, const uint2* __restrict__ rank,
+                           uint32_t cap, int bits, int passes, uint32_t* __restrict__ keys, uint32_t* hist,
+                           DeviceStatus* st) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int used = (int)(cinfo[i] >> 1);
+    uint32_t e = rank[i].x;
+    bool ovf = false;
+    for (int j = 0; j < used; j++) {
+        const int shape = __float_as_int(ds.cslot[((size_t)i * ds.slot_cap + j) * 3].w);
+        const int body = ds.shape_body[shape];
+        if (body >= 0 && ds.body_invm[body] > 0.0f) {
+            if (e < cap) {
+                keys[e] = (uint32_t)body;
+                for (int p = 0; p < passes; p++)
+                    atomicAdd(&hist[(p << bits) + (((uint32_t)body >> (p * bits)) & ((1u << bits) - 1u))], 1u);
+            } else {
+                ovf = true;
+            }
+            e++;
+        }
+    }
+    if (ovf) atomicOr(&st->error_bits, kErrBodyOverflow);
+}
+
+void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank, uint32_t cap,
+                     const SortPlan& sp, uint32_t* keys, uint32_t* hist, DeviceStatus* st) {
+    if (n <= 0) return;
+    k_dyn_emit<<<(int)((n + 255) / 256), 256, 0, s>>>(n, cinfo, ds, rank, cap, sp.bits, sp.passes, keys, hist, st);
+}
+
+__global__ void k_body_segments(uint32_t cap, const uint32_t* __restrict__ count, const uint32_t* __restrict__ skeys,
+                                uint2* __restrict__ seg) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t e = *count < cap ? *count : cap;
+    if (t >= e) return;
+    const uint32_t key = skeys[t];
+    if (t == 0 || skeys[t - 1] != key) seg[key].x = t;
+    if (t == e - 1 || skeys[t + 1] != key) seg[key].y = t + 1;
+}
+
+void launch_body_segments(cudaStream_t s, uint32_t cap, const uint32_t* count, const uint32_t* skeys, uint2* seg) {
+    if (cap == 0) return;
+    k_body_segments<<<(cap + 255) / 256, 256, 0, s>>>(cap, count, skeys, seg);
+}
+
+// One warp per body: the body's particle-contact deltas summed in entry order (the
+// canonical contact order), then apply_body_deltas.comp without constraint weights.
+__global__ void k_body_particles(BodyArrays ba, const uint2* __restrict__ seg, const uint32_t* __restrict__ sorted,
+                                 const float4* __restrict__ bdel, const float4* __restrict__ q_in,
+                                 const float4* __restrict__ qd_in, float4* __restrict__ q_out,
+                                 float4* __restrict__ qd_out, RigidParams rp) {
+    const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= ba.nb) return;
+    v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
+    if (ba.invm[b] > 0.0f) {
+        const uint2 sg = seg[b];
+        for (uint32_t base = sg.x; base < sg.y; base += 32) {
+            float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = a;
+            if (base + lane < sg.y) {
+                const uint32_t e = sorted[base + lane];
+                a = bdel[(size_t)e * 2];
+                c = bdel[(size_t)e * 2 + 1];
+            }
+            const int m = (int)min(32u, sg.y - base);
+            for (int l = 0; l < m; l++) {
+                const float ax = __shfl_sync(0xffffffffu, a.x, l), ay = __shfl_sync(0xffffffffu, a.y, l),
+                            az = __shfl_sync(0xffffffffu, a.z, l), aw = __shfl_sync(0xffffffffu, a.w, l);
+                const float cx = __shfl_sync(0xffffffffu, c.x, l), cy = __shfl_sync(0xffffffffu, c.y, l),
+                            cz = __shfl_sync(0xffffffffu, c.z, l);
+                if (aw != 0.0f) {
+                    lin = vadd(lin, mk3(ax, ay, az));
+                    ang = vadd(ang, mk3(cx, cy, cz));
+                }
+            }
+        }
+    }
+    if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, 0.0f, 0, q_out, qd_out);
+}
+
+void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, const uint32_t* sorted_entries,
+                           const float4* bdel, const float4* q_in, const float4* qd_in, float4* q_out,
+                           float4* qd_out, RigidParams rp) {
+    if (ba.nb <= 0) return;
+    k_body_particles<<<(ba.nb * 32 + 127) / 128, 128, 0, s>>>(ba, seg, sorted_entries, bdel, q_in, qd_in, q_out,
+                                                             qd_out, rp);
+}
+
+// ---------------------------------------------------------------- rigid contact solve ----
+struct RigidContact {
+    int shape1;
+    v3 p0, p1, n, off0, off1;
+    float th0, th1;
+};
+__device__ __forceinline__ RigidContact load_rc(const float4* s) {
+    RigidContact c;
+    const float4 a = s[0], b = s[1], d = s[2], e = s[3], f = s[4];
+    c.p0 = xyz(a);
+    c.shape1 = __float_as_int(a.w);
+    c.p1 = xyz(b);
+    c.th0 = b.w;
+    c.n = xyz(d);
+    c.th1 = d.w;
+    c.off0 = xyz(e);
+    c.off1 = xyz(f);
+    return c;
+}
+
+// compute_contact_constraint_delta, solve_body_contact_positions.comp:63-83
+__device__ __forceinline__ float constraint_delta(float err, q4 qa, q4 qb, float m_inv_a, float m_inv_b,
+                                                  const float* ia, const float* ib, v3 lin_a, v3 lin_b, v3 ang_a,
+                                                  v3 ang_b, float relax, float dt) {
+    float denom = 0.0f;
+    denom += vdot(lin_a, lin_a) * m_inv_a;
+    denom += vdot(lin_b, lin_b) * m_inv_b;
+    const v3 ra = wq_rot_inv(qa, ang_a), rb = wq_rot_inv(qb, ang_b);
+    denom += vdot(ra, colmul(ia, ra));
+    denom += vdot(rb, colmul(ib, rb));
+    float dl = -err;
+    if (denom > 0.0f) dl = __fdiv_rn(dl, dt * denom);
+    return dl * relax;
+}
+
+// solve_body_contact_positions.comp:97-265 for one contact of shape_a (no impulse output)
+__device__ bool body_contact(const BodyArrays& ba, const float4* q, const float4* qd, int shape_a,
+                             const RigidContact& c, const RigidParams& rp, v3& lin_da, v3& ang_da, v3& lin_db,
+                             v3& ang_db) {
+    const float zero9[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int shape_b = c.shape1;
+    if (shape_a == shape_b) return false;
+    const int body_a = shape_a >= 0 ? ba.shape_body[shape_a] : -1;
+    const int body_b = shape_b >= 0 ? ba.shape_body[shape_b] : -1;
+    if (body_a == body_b) return false;
+    v3 pos_a = mk3(0.0f, 0.0f, 0.0f), pos_b = pos_a;
+    q4 quat_a;
+    quat_a.x = quat_a.y = quat_a.z = 0.0f;
+    quat_a.w = 1.0f;
+    q4 quat_b = quat_a;
+    if (body_a >= 0) {
+        pos_a = xyz(q[body_a * 2]);
+        quat_a = f4q(q[body_a * 2 + 1]);
+    }
+    if (body_b >= 0) {
+        pos_b = xyz(q[body_b * 2]);
+        quat_b = f4q(q[body_b * 2 + 1]);
+    }
+    const v3 bx_a = vadd(wq_rot(quat_a, c.p0), pos_a);
+    const v3 bx_b = vadd(wq_rot(quat_b, c.p1), pos_b);
+    const v3 n = c.n;
+    const float d = vdot(n, vsub(bx_b, bx_a)) - (c.th0 + c.th1);
+    if (d >= 0.0f) return false;
+    float m_inv_a = 0.0f, m_inv_b = 0.0f;
+    const float* ia = zero9;
+    const float* ib = zero9;
+    v3 com_a = mk3(0.0f, 0.0f, 0.0f), com_b = com_a, omega_a = com_a, omega_b = com_a;
+    if (body_a >= 0) {
+        m_inv_a = ba.invm[body_a];
+        ia = ba.invI + body_a * 9;
+        com_a = mk3(ba.com[body_a * 3], ba.com[body_a * 3 + 1], ba.com[body_a * 3 + 2]);
+        omega_a = xyz(qd[body_a * 2 + 1]);
+    }
+    if (body_b >= 0) {
+        m_inv_b = ba.invm[body_b];
+        ib = ba.invI + body_b * 9;
+        com_b = mk3(ba.com[body_b * 3], ba.com[body_b * 3 + 1], ba.com[body_b * 3 + 2]);
+        omega_b = xyz(qd[body_b * 2 + 1]);
+    }
+    int nz = 0;
+    float mu = 0.0f, mu_t = 0.0f, mu_r = 0.0f;
+    if (shape_a >= 0) {
+        nz += 1;
+        mu += ba.shape_mu[shape_a];
+        mu_t += rp.mu_t;
+        mu_r += rp.mu_r;
+    }
+    if (shape_b >= 0) {
+        nz += 1;
+        mu += ba.shape_mu[shape_b];
+        mu_t += rp.mu_t;
+        mu_r += rp.mu_r;
+    }
+    if (nz > 0) {
+        mu = __fdiv_rn(mu, (float)nz);
+        mu_t = __fdiv_rn(mu_t, (float)nz);
+        mu_r = __fdiv_rn(mu_r, (float)nz);
+    }
+    const v3 r_a = vsub(bx_a, vadd(wq_rot(quat_a, com_a), pos_a));
+    const v3 r_b = vsub(bx_b, vadd(wq_rot(quat_b, com_b), pos_b));
+    const v3 angular_a = vneg(vcross(r_a, n));
+    const v3 angular_b = vcross(r_b, n);
+    const float lambda_n = constraint_delta(d, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, vneg(n), n, angular_a,
+                                            angular_b, rp.relax, rp.dt);
+    lin_da = vmuls(vneg(n), lambda_n);
+    lin_db = vmuls(n, lambda_n);
+    ang_da = vmuls(angular_a, lambda_n);
+    ang_db = vmuls(angular_b, lambda_n);
+    if (mu > 0.0f) {
+        const v3 sbx_a = vadd(wq_rot(quat_a, vadd(c.p0, c.off0)), pos_a);
+        const v3 sbx_b = vadd(wq_rot(quat_b, vadd(c.p1, c.off1)), pos_b);
+        const v3 delta = vsub(sbx_b, sbx_a);
+        v3 fdel = vsub(delta, vmuls(n, vdot(n, delta)));
+        const v3 fr_a = vsub(sbx_a, vadd(wq_rot(quat_a, com_a), pos_a));
+        const v3 fr_b = vsub(sbx_b, vadd(wq_rot(quat_b, com_b), pos_b));
+        v3 rel = mk3(0.0f, 0.0f, 0.0f);
+        if (body_a >= 0 && (ba.flags[body_a] & 2)) {
+            const v3 va = vadd(xyz(qd[body_a * 2]), vcross(omega_a, fr_a));
+            rel = vsub(rel, vsub(va, vmuls(n, vdot(n, va))));
+        }
+        if (body_b >= 0 && (ba.flags[body_b] & 2)) {
+            const v3 vb = vadd(xyz(qd[body_b * 2]), vcross(omega_b, fr_b));
+            rel = vadd(rel, vsub(vb, vmuls(n, vdot(n, vb))));
+        }
+        fdel = vadd(fdel, vmuls(rel, rp.dt));
+        const float err = vlength(fdel);
+        if (err > 0.0f) {
+            const v3 perp = vnormalize(fdel);
+            const v3 angular_a_fr = vneg(vcross(fr_a, perp));
+            const v3 angular_b_fr = vcross(fr_b, perp);
+            float lambda_fr = constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, vneg(perp), perp,
+                                               angular_a_fr, angular_b_fr, rp.relax, rp.dt);
+            lambda_fr = gmax(lambda_fr, -lambda_n * mu);
+            lin_da = vsub(lin_da, vmuls(perp, lambda_fr));
+            lin_db = vadd(lin_db, vmuls(perp, lambda_fr));
+            ang_da = vadd(ang_da, vmuls(angular_a_fr, lambda_fr));
+            ang_db = vadd(ang_db, vmuls(angular_b_fr, lambda_fr));
+        }
+    }
+    v3 delta_omega = vsub(omega_b, omega_a);
+    const v3 zero = mk3(0.0f, 0.0f, 0.0f);
+    if (mu_t > 0.0f) {
+        const float err = vdot(delta_omega, n) * rp.dt;
+        if (fabsf(err) > 0.0f) {
+            float lt = constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, zero, zero, vneg(n), n,
+                                        rp.relax, rp.dt);
+            lt = gclamp(lt, -lambda_n * mu_t, lambda_n * mu_t);
+            ang_da = vsub(ang_da, vmuls(n, lt));
+            ang_db = vadd(ang_db, vmuls(n, lt));
+        }
+    }
+    if (mu_r > 0.0f) {
+        delta_omega = vsub(delta_omega, vmuls(n, vdot(n, delta_omega)));
+        const float err = vlength(delta_omega) * rp.dt;
+        if (err > 0.0f) {
+            const v3 roll_n = vnormalize(delta_omega);
+            float lr = constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, zero, zero, vneg(roll_n),
+                                        roll_n, rp.relax, rp.dt);
+            lr = gmax(lr, -lambda_n * mu_r);
+            ang_da = vsub(ang_da, vmuls(roll_n, lr));
+            ang_db = vadd(ang_db, vmuls(roll_n, lr));
+        }
+    }
+    return true;
+}
+
+// One thread per body: its rigid contacts as shape0 (own vertices), then as shape1
+// (the overlapping bodies' vertices on its mesh, partners ascending), summed in that
+// order; then apply_body_deltas.comp with the contact count as constraint weight.
+__global__ void k_body_rigid(BodyArrays ba, RigidTables rt, const float4* __restrict__ q_in,
+                             const float4* __restrict__ qd_in, float4* __restrict__ q_out,
+                             float4* __restrict__ qd_out, RigidParams rp) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= ba.nb) return;
+    v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
+    float cnt = 0.0f;
+    const int ib = rt.dyn_index[b];
+    if (ib >= 0) {
+        v3 la, aa, lb, ab;
+        for (uint32_t d = rt.dv_start[b]; d < rt.dv_start[b + 1]; d++) {
+            const int k = rt.rc_count[d];
+            for (int j = 0; j < k; j++) {
+                const RigidContact c = load_rc(rt.rc + ((size_t)d * kRigidSlots + j) * 5);
+                if (body_contact(ba, q_in, qd_in, b + 1, c, rp, la, aa, lb, ab)) {
+                    lin = vadd(lin, la);
+                    ang = vadd(ang, aa);
+                    cnt += 1.0f;
+                }
+            }
+        }
+        const int pc = rt.partner_count[ib];
+        for (int pi = 0; pi < pc; pi++) {
+            const int a = rt.partners[ib * kPartnerCap + pi];
+            for (uint32_t d = rt.dv_start[a]; d < rt.dv_start[a + 1]; d++) {
+                const int k = rt.rc_count[d];
+                for (int j = 0; j < k; j++) {
+                    const float4* sp = rt.rc + ((size_t)d * kRigidSlots + j) * 5;
+                    if (__float_as_int(sp[0].w) != b + 1) continue;
+                    const RigidContact c = load_rc(sp);
+                    if (body_contact(ba, q_in, qd_in, a + 1, c, rp, la, aa, lb, ab)) {
+                        lin = vadd(lin, lb);
+                        ang = vadd(ang, ab);
+                        cnt += 1.0f;
+                    }
+                }
+            }
+        }
+    }
+    apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.con_weighting, q_out, qd_out);
+}
+
+void launch_body_rigid(cudaStream_t s, BodyArrays ba, RigidTables rt, const float4* q_in, const float4* qd_in,
+                       float4* q_out, float4* qd_out, RigidParams rp) {
+    if (ba.nb <= 0) return;
+    k_body_rigid<<<(ba.nb + 63) / 64, 64, 0, s>>>(ba, rt, q_in, qd_in, q_out, qd_out, rp);
+}
+
+}  // namespace xpbd

@@ -124,7 +124,8 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
                                                       const uint32_t* __restrict__ vals_in,
                                                       uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                       const uint32_t* __restrict__ hist, uint32_t* lookback,
-                                                      uint32_t* tile_counter, DeviceStatus* st) {
+                                                      uint32_t* tile_counter, DeviceStatus* st,
+                                                      const uint32_t* __restrict__ n_dev) {
     constexpr int BINS = 1 << BITS;
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
@@ -144,6 +145,11 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
     __syncthreads();
     const uint32_t tile = s_tile;
     const int64_t base = (int64_t)tile * TILE;
+    if (n_dev) {  // device-side count: the tiles past it have nothing to sort and nobody waits on them
+        const int64_t nd = (int64_t)*n_dev;
+        if (nd < n) n = nd;
+        if (base >= n) return;
+    }
     const int valid_n = (n - base) < (int64_t)TILE ? (int)(n - base) : TILE;
     const uint32_t lt = lanemask_lt();
 
@@ -255,7 +261,7 @@ size_t sort_lookback_words(const SortPlan& p) { return (size_t)p.tiles << p.bits
 template <int BITS, int ITEMS>
 static void onesweep_variant(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* ki,
                              const uint32_t* vi, uint32_t* ko, uint32_t* vo, const uint32_t* hist, uint32_t* lb,
-                             uint32_t* tc, DeviceStatus* st) {
+                             uint32_t* tc, DeviceStatus* st, const uint32_t* n_dev) {
     constexpr int THREADS = 1 << BITS;
     constexpr int TILE = THREADS * ITEMS;
     size_t smem = sizeof(uint32_t) * ((size_t)(THREADS / 32) * (1 << BITS) + 2 * TILE + (1 << BITS));
@@ -266,18 +272,18 @@ static void onesweep_variant(cudaStream_t s, int64_t n, const SortPlan& sp, int 
         attr_set = true;
     }
     k_onesweep<BITS, THREADS, ITEMS><<<sp.tiles, THREADS, smem, s>>>(n, pass * BITS, ki, vi, ko, vo, hist, lb, tc,
-                                                                     st);
+                                                                     st, n_dev);
 }
 
 void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
-                          DeviceStatus* st) {
+                          DeviceStatus* st, const uint32_t* n_dev) {
     if (n <= 0) return;
 #define XPBD_OS(B, I)                                                                                      \
     if (sp.bits == B && sp.items == I)                                                                     \
         return onesweep_variant<B, I>(s, n, sp, pass, keys_in, vals_in, keys_out, vals_out, hist_pass, \
-                                      lookback, tile_counter, st);
+                                      lookback, tile_counter, st, n_dev);
     XPBD_OS(8, 8)
     XPBD_OS(8, 16)
     XPBD_OS(7, 16)

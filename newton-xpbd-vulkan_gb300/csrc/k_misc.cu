@@ -15,18 +15,31 @@ size_t contact_scan_words(int64_t n) {
     return (size_t)(tiles > 0 ? tiles : 1) * 2 + 2;
 }
 
-__device__ __forceinline__ uint2 info_counts(uint32_t info) { return make_uint2(info & kPlaneBit, info >> 1); }
+// (plane contacts, generic slots) of a particle; with ds.cslot set instead
+// (slots whose shape belongs to a dynamic body, 0)
+__device__ __forceinline__ uint2 particle_counts(const uint32_t* __restrict__ cinfo, int64_t i, const DynSlots& ds) {
+    const uint32_t info = cinfo[i];
+    if (!ds.cslot) return make_uint2(info & kPlaneBit, info >> 1);
+    const int used = (int)(info >> 1);
+    uint32_t d = 0;
+    for (int j = 0; j < used; j++) {
+        const int shape = __float_as_int(ds.cslot[((size_t)i * ds.slot_cap + j) * 3].w);
+        const int body = ds.shape_body[shape];
+        if (body >= 0 && ds.body_invm[body] > 0.0f) d++;
+    }
+    return make_uint2(d, 0u);
+}
 
 // phase 1: per-tile sums
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int64_t n, const uint32_t* __restrict__ cinfo,
-                                                             uint32_t* __restrict__ tile_sums) {
+                                                             DynSlots ds, uint32_t* __restrict__ tile_sums) {
     __shared__ uint32_t s_a[kScanThreads / 32], s_b[kScanThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     uint32_t a = 0, b = 0;
     for (int j = 0; j < kScanItems; j++) {
         const int64_t i = base + j * kScanThreads + threadIdx.x;
         if (i < n) {
-            const uint2 c = info_counts(cinfo[i]);
+            const uint2 c = particle_counts(cinfo, i, ds);
             a += c.x;
             b += c.y;
         }
@@ -104,7 +117,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(int tiles, uint32_t* __rest
 
 // phase 3: per-particle exclusive ranks
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(int64_t n, const uint32_t* __restrict__ cinfo,
-                                                           const uint32_t* __restrict__ tile_sums,
+                                                           DynSlots ds, const uint32_t* __restrict__ tile_sums,
                                                            uint2* __restrict__ rank) {
     __shared__ uint32_t s_a[kScanThreads / 32], s_b[kScanThreads / 32];
     // thread t owns kScanItems consecutive particles of the tile
@@ -113,7 +126,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(int64_t n, const uin
     uint2 c[kScanItems];
     for (int j = 0; j < kScanItems; j++) {
         const int64_t i = base + j;
-        c[j] = i < n ? info_counts(cinfo[i]) : make_uint2(0, 0);
+        c[j] = i < n ? particle_counts(cinfo, i, ds) : make_uint2(0, 0);
         a += c[j].x;
         b += c[j].y;
     }
@@ -153,9 +166,22 @@ void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2
         return;
     }
     const int tiles = (int)((n + kScanTile - 1) / kScanTile);
-    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, workspace);
+    const DynSlots none{nullptr, 0, nullptr, nullptr};
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace);
     k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals);
-    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, workspace, rank);
+    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace, rank);
+}
+
+void launch_dyn_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, uint2* rank, uint32_t* totals,
+                     uint32_t* workspace) {
+    if (n <= 0) {
+        cudaMemsetAsync(totals, 0, 2 * sizeof(uint32_t), s);
+        return;
+    }
+    const int tiles = (int)((n + kScanTile - 1) / kScanTile);
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace);
+    k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals);
+    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace, rank);
 }
 
 __global__ void k_contact_compact(int64_t n, const uint32_t* __restrict__ cinfo, const float4* __restrict__ cslot,

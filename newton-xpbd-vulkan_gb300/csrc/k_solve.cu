@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     const uint32_t* __restrict__ stamp_p,
     const float4* __restrict__ x0a, const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
     const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ rx_out,
-    float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg) {
+    float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg,
+    BodyDeltaOut bo) {
     __shared__ int s_kk[kPairCap][kSolveThreads];
     __shared__ float s_d[kPairCap][kSolveThreads];
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,11 +109,30 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
         const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
         const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
         // shape contacts, canonical order (scene.cpp:946-947)
+        uint32_t dyn_e = bo.bdel ? bo.dyn_rank[id].x : 0u;
         for (int c = 0; c < ncon; c++) {
-            if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
             const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
-            v3 fd;
-            if (shape_delta(ct, pflag, xp, vp, radius, w1, bt, sp, fd)) delta = vadd(delta, fd);
+            bool ok = false;
+            v3 fd, dtot, rr;
+            if (contact_kept(info, c, cr, id, sp.contact_max)) {
+                ok = shape_delta(ct, pflag, xp, vp, radius, w1, bt, sp, fd, dtot, rr);
+                if (ok) delta = vadd(delta, fd);
+            }
+            if (bo.bdel) {  // body delta of a dynamic-body contact (:193-199), summed per body later
+                const int body = bt.shape_body[ct.shape];
+                if (body >= 0 && bt.body_invm[body] > 0.0f) {
+                    float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+                    if (ok) {
+                        const v3 dv = mk3(__fdiv_rn(dtot.x, sp.dt), __fdiv_rn(dtot.y, sp.dt), __fdiv_rn(dtot.z, sp.dt));
+                        const v3 dw = vcross(rr, dv);
+                        a = make_float4(-dv.x, -dv.y, -dv.z, 1.0f);
+                        b = make_float4(-dw.x, -dw.y, -dw.z, 0.0f);
+                    }
+                    bo.bdel[(size_t)dyn_e * 2] = a;
+                    bo.bdel[(size_t)dyn_e * 2 + 1] = b;
+                    dyn_e++;
+                }
+            }
         }
         // particle-particle contacts (solve_particle_particle_contacts.comp:116-217): the
         // candidate filter (:145-157) runs first and buffers accepted neighbours; the pair
@@ -214,11 +234,51 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     }
 }
 
+// apply_particle_shape_restitution.comp:248-316 after the body passes: one thread per
+// particle in sorted order reads its final state, adds the restitution increments of its
+// contacts (canonical order, pre-restitution velocity) and writes particle order.
+__global__ void __launch_bounds__(kSolveThreads) k_restitute(
+    int64_t n, const uint32_t* __restrict__ sids, const float4* __restrict__ rx, const float4* __restrict__ rv,
+    const int* __restrict__ rf, const float4* __restrict__ x0a, const float4* __restrict__ v0a,
+    const uint32_t* __restrict__ cinfo, const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt,
+    SolveParams sp, float4* __restrict__ x_out, float4* __restrict__ v_out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t id = sids[k];
+    const float4 ox = rx[k], ov = rv[k];
+    v3 v_new = xyz(ov);
+    const uint32_t info = cinfo[id];
+    const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
+    // inactive particles keep their predicted state and take no restitution (:256)
+    if (sp.enable_restitution && ncon && (rf[k] & 1)) {
+        const v3 x0 = xyz(x0a[id]), v_old = xyz(v0a[id]);
+        const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
+        const v3 v_snap = v_new;
+        for (int c = 0; c < ncon; c++) {
+            if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
+            const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
+            v3 dv;
+            if (restitution_dv(ct, v_snap, x0, v_old, ox.w, bt, sp, dv)) v_new = vadd(v_new, dv);
+        }
+    }
+    x_out[id] = make_float4(ox.x, ox.y, ox.z, 0.0f);
+    v_out[id] = make_float4(v_new.x, v_new.y, v_new.z, 0.0f);
+}
+
+void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const float4* rx, const float4* rv,
+                      const int* rf, const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot,
+                      ContactRanks cr, BodyTables bt, SolveParams sp, float4* x_out, float4* v_out) {
+    if (n <= 0) return;
+    const int blocks = (int)((n + kSolveThreads - 1) / kSolveThreads);
+    k_restitute<<<blocks, kSolveThreads, 0, s>>>(n, sids, rx, rv, rf, x0, v0, cinfo, cslot, cr, bt, sp, x_out,
+                                                 v_out);
+}
+
 void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const uint32_t* skeys,
                   const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
                   const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr,
                   BodyTables bt, SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out,
-                  SolveDiag dg) {
+                  SolveDiag dg, BodyDeltaOut bo) {
     if (n <= 0) return;
     const int threads = kSolveThreads;
     const int blocks = (int)((n + threads - 1) / threads);
@@ -226,7 +286,7 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
 #define XPBD_SOLVE(L, A, D)                                                                                         \
     if (last == L && all_active == A && diag == D) {                                                                \
         k_solve<L, A, D><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo, cslot, \
-                                                    cr, bt, sp, rx_out, rv_out, x_out, v_out, dg);                  \
+                                                    cr, bt, sp, rx_out, rv_out, x_out, v_out, dg, bo);              \
         return;                                                                                                     \
     }
     XPBD_SOLVE(true, true, false)

@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/xpbd.h"
+
 namespace xpbd {
 
 constexpr int kGridDim = 128;                                   // hash grid, src/scene.cpp:17-18
@@ -26,6 +28,7 @@ enum : uint32_t {
     kErrLookbackTimeout = 1u,  // a decoupled look-back wait expired
     kErrStackOverflow = 2u,    // BVH traversal stack (32 entries) full
     kErrSlotOverflow = 4u,     // more mesh contacts for one particle than slots
+    kErrBodyOverflow = 8u,     // body partner list, rigid contact slots or body-delta entries full
 };
 
 // Per-particle contact header (cinfo[i]): bit 0 = plane contact (shape 0),
@@ -51,6 +54,10 @@ struct BodyTables {
     const float* body_invI;  // 9 per body, row-major (solve_particle_shape_contacts.comp:46-48)
     const float* body_invm;  // [n_bodies]
     const int* body_flags;   // [n_bodies]
+    // body state at the start of the substep (restitution); equal to body_q / body_qd
+    // while every body is static (scene.cpp:577-580)
+    const float4* body_q_prev;
+    const float4* body_qd_prev;
 };
 
 struct MeshTables {
@@ -68,6 +75,13 @@ struct MeshTables {
     // per leaf slot: (a.xyz, triangle id bits), (b.xyz, |e0|^2), (c.xyz, |e1|^2),
     // (unit normal.xyz, |e2|^2 or -1 when the triangle is skipped as degenerate)
     const float4* tri_cache;
+    // meshes whose body is dynamic hold body-frame vertices: pose = the bodies' state
+    // (2 float4 per mesh), posed[m] != 0 for those meshes, walk_list = the other meshes
+    // (null: every mesh is static)
+    const float4* pose;
+    const int* posed;
+    const int* walk_list;
+    int walk_count;
     int n_meshes;
     float avg_edge;           // mesh 0's average edge length (scene.cpp:325)
     float soft_margin;
@@ -83,6 +97,14 @@ struct SolveParams {
     int slot_cap;             // generic contact slots per particle
     int iter_index;
     int64_t contact_max;
+};
+
+// Per-slot body deltas written by the solve kernel for contacts with dynamic bodies
+// (solve_particle_shape_contacts.comp:193-199): entry dyn_rank[particle].x + j for the
+// particle's j-th dynamic slot, 2 float4 (-delta_v, valid), (-delta_w, 0).
+struct BodyDeltaOut {
+    float4* bdel;
+    const uint2* dyn_rank;  // .x
 };
 
 // Optional debugging outputs of the solve kernel.
@@ -120,11 +142,12 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          const float* r, const int* flags, const uint32_t* pscene, PredictParams pp, PlaneParams pl,
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
                          uint32_t* ccount, uint32_t* stamp);
-// one onesweep pass; vals_in == nullptr means vals are the element index
+// one onesweep pass; vals_in == nullptr means vals are the element index; n_dev (optional)
+// holds the element count on the device (at most n, the capacity the grid is sized for)
 void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
-                          DeviceStatus* st);
+                          DeviceStatus* st, const uint32_t* n_dev = nullptr);
 // cell table + sorted-order particle records
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,
@@ -145,11 +168,27 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
                   const float4* x0,
                   const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
-                  SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg);
+                  SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg,
+                  BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr});
+// restitution (apply_particle_shape_restitution.comp) after the body passes of the last
+// iteration, scattering the sorted final state to particle order
+void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const float4* rx, const float4* rv,
+                      const int* rf, const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot,
+                      ContactRanks cr, BodyTables bt, SolveParams sp, float4* x_out, float4* v_out);
 // exclusive scan of per-particle (plane bit, slot count) for the contact_max cap / compaction
 size_t contact_scan_words(int64_t n);
 void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2* rank, uint32_t* totals,
                          uint32_t* lookback, uint32_t* tile_counter, DeviceStatus* st);
+// exclusive scan of each particle's number of contact slots with a dynamic body
+// (rank[i].x; totals[0] = all of them)
+struct DynSlots {
+    const float4* cslot;
+    int slot_cap;
+    const int* shape_body;
+    const float* body_invm;
+};
+void launch_dyn_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, uint2* rank, uint32_t* totals,
+                     uint32_t* lookback);
 // canonical SoA contact list (for the getters)
 void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, const float4* cslot, int slot_cap,
                             const uint2* rank, const uint32_t* totals, int64_t contact_max, const float4* x_prev,
@@ -159,6 +198,71 @@ void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp
 // stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
 void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,
                        cudaStream_t s);
+// ---------------------------------------------------------------- bodies ----
+// Body b belongs to mesh b. Dynamic bodies (inv_m > 0) are listed in `dyn` (ascending);
+// their mesh vertices are dv_local[dv_start[b] .. dv_start[b + 1]) (body frame).
+struct BodyArrays {
+    float4* q;            // current state (2 float4 per body)
+    float4* qd;
+    const float* com;     // 3 per body
+    const float* I;       // 9 per body
+    const float* invI;    // 9 per body
+    const float* invm;
+    const int* flags;
+    const int* shape_body;
+    const float* shape_mu;
+    int nb;
+};
+struct RigidParams {
+    float dt, damping, margin, relax;
+    int con_weighting;
+    float mu_t, mu_r;
+    float gx, gy, gz;
+    int plane;
+    float altitude;
+};
+constexpr int kPartnerCap = 64;   // dynamic bodies whose boxes overlap one dynamic body
+constexpr int kRigidSlots = 4;    // rigid contacts per body vertex
+struct RigidTables {
+    int n_dyn;
+    const int* dyn;               // dynamic body ids, ascending
+    const int* dyn_index;         // body -> index in dyn, or -1
+    const uint32_t* dv_start;     // [nb + 1] vertex ranges per body (empty for static bodies)
+    const float4* dv_local;       // body-frame vertex, w = body id bits
+    float4* wbox;                 // 2 per dynamic body: world box lower, upper (w = shape margin)
+    int* partners;                // kPartnerCap per dynamic body
+    int* partner_count;
+    float4* rc;                   // kRigidSlots * 5 float4 per vertex
+    int* rc_count;
+    float pad;                    // conservative widening of the world boxes
+    int n_vert;                   // dv_start[nb]
+};
+// integrate_bodies.comp for every body; saves the pre-integration state to q_prev
+void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp);
+// world boxes of the dynamic bodies and their overlapping pairs
+void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp, DeviceStatus* st);
+// rigid contacts of every dynamic-body vertex against the plane and the other meshes
+void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
+                           DeviceStatus* st);
+// particle contacts against the meshes of dynamic bodies, merged into the slots in mesh order
+void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                          const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
+                          float4* cslot, uint32_t* ccount, DeviceStatus* st);
+// body-delta entries: key = body of each dynamic slot at position rank[i].x + j, digit histograms
+void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank,
+                     uint32_t cap, const SortPlan& sp, uint32_t* keys, uint32_t* hist, DeviceStatus* st);
+// [start, end) of every body in the sorted entry keys (seg zeroed beforehand)
+void launch_body_segments(cudaStream_t s, uint32_t cap, const uint32_t* count, const uint32_t* skeys, uint2* seg);
+// per body: sum of its particle-contact deltas in entry order, then apply_body_deltas.comp
+// without constraint weights (q_in -> q_out)
+void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, const uint32_t* sorted_entries,
+                           const float4* bdel, const float4* q_in, const float4* qd_in, float4* q_out,
+                           float4* qd_out, RigidParams rp);
+// per body: solve_body_contact_positions.comp over its rigid contacts, then apply_body_deltas.comp
+// with constraint weights (q_in -> q_out)
+void launch_body_rigid(cudaStream_t s, BodyArrays ba, RigidTables rt, const float4* q_in, const float4* qd_in,
+                       float4* q_out, float4* qd_out, RigidParams rp);
+
 // float4 state <-> packed xyz
 void launch_unpack_xyz(cudaStream_t s, int64_t n, const float4* a, float* out);
 void launch_pack_xyz(cudaStream_t s, int64_t n, const float* in, float4* a);

@@ -1,0 +1,306 @@
+// Closest-point query of one point against one triangle mesh's BVH
+// (generate_mesh_contacts.comp:197-411), shared by the particle contact
+// kernels and the rigid contact kernel.
+#pragma once
+#include "kernels.h"
+#include "xmath.cuh"
+
+namespace xpbd {
+
+__device__ __forceinline__ float dist_sq_aabb(v3 p, v3 lo, v3 hi) {  // generate_mesh_contacts.comp:32-35
+    const v3 d = mk3(gmax(gmax(lo.x - p.x, 0.0f), p.x - hi.x), gmax(gmax(lo.y - p.y, 0.0f), p.y - hi.y),
+                     gmax(gmax(lo.z - p.z, 0.0f), p.z - hi.z));
+    return vdot(d, d);
+}
+
+__device__ __forceinline__ float comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// generate_mesh_contacts.comp:77-113
+static __device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
+    const v3 adir = mk3(fabsf(dir.x), fabsf(dir.y), fabsf(dir.z));
+    int kz = 0;
+    if (adir.y > adir.x) kz = 1;
+    if (adir.z > (kz == 1 ? adir.y : adir.x)) kz = 2;
+    int kx = kz + 1;
+    if (kx == 3) kx = 0;
+    int ky = kx + 1;
+    if (ky == 3) ky = 0;
+    if (comp(dir, kz) < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    const float Sx = __fdiv_rn(comp(dir, kx), comp(dir, kz));
+    const float Sy = __fdiv_rn(comp(dir, ky), comp(dir, kz));
+    const float Sz = __fdiv_rn(1.0f, comp(dir, kz));
+    const v3 A = vsub(a, p), B = vsub(b, p), C = vsub(c, p);
+    const float Ax = comp(A, kx) - Sx * comp(A, kz), Ay = comp(A, ky) - Sy * comp(A, kz);
+    const float Bx = comp(B, kx) - Sx * comp(B, kz), By = comp(B, ky) - Sy * comp(B, kz);
+    const float Cx = comp(C, kx) - Sx * comp(C, kz), Cy = comp(C, ky) - Sy * comp(C, kz);
+    const float U = diff_product(Cx, By, Cy, Bx);
+    const float V = diff_product(Ax, Cy, Ay, Cx);
+    const float W = diff_product(Bx, Ay, By, Ax);
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float Az = Sz * comp(A, kz), Bz = Sz * comp(B, kz), Cz = Sz * comp(C, kz);
+    const float T = U * Az + V * Bz + W * Cz;
+    if ((T < 0.0f && det > 0.0f) || (T > 0.0f && det < 0.0f)) return false;
+    return true;
+}
+
+// generate_mesh_contacts.comp:115-179; the triangle normal normalize(cross(b-a, c-a)) depends on
+// the triangle only and is read from the triangle cache instead of being recomputed per visit
+static __device__ void closest_point_triangle(v3 p, v3 a, v3 b, v3 c, v3& cp, v3& bary) {
+    const v3 ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
+    float u, v;
+    const float d1 = exact_dot(ab, ap), d2 = exact_dot(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f) {
+        v = 0.0f;
+        u = 1.0f;
+    } else {
+        const v3 bp = vsub(p, b);
+        const float d3 = exact_dot(ab, bp), d4 = exact_dot(ac, bp);
+        if (d3 >= 0.0f && d4 <= d3) {
+            v = 1.0f;
+            u = 0.0f;
+        } else {
+            const float vc = __fmaf_rn(d1, d4, -(d2 * d3));
+            if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+                v = exact_div1(d1, d1 - d3);
+                u = 1.0f - v;
+            } else {
+                const v3 cp_p = vsub(p, c);
+                const float d5 = exact_dot(ab, cp_p), d6 = exact_dot(ac, cp_p);
+                if (d6 >= 0.0f && d5 <= d6) {
+                    v = 0.0f;
+                    u = 0.0f;
+                } else {
+                    const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
+                    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+                        const float w_val = exact_div1(d2, d2 - d6);
+                        v = 0.0f;
+                        u = 1.0f - w_val;
+                    } else {
+                        const float va = __fmaf_rn(d3, d6, -(d5 * d4));
+                        if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+                            const float w_val = exact_div1(d4 - d3, (d4 - d3) + (d5 - d6));
+                            v = 1.0f - w_val;
+                            u = (1.0f - v) - w_val;
+                        } else {
+                            const float sum_vavb = va + vb;
+                            const float sum_all = vc + sum_vavb;
+                            const float r0 = __frcp_rn(sum_all);
+                            const float rem = __fmaf_rn(-sum_all, r0, 1.0f);
+                            const float denom = __fmaf_rn(rem, r0, r0);
+                            v = vb * denom;
+                            u = __fmaf_rn(-vc, denom, 1.0f - v);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const float w_out = (1.0f - u) - v;
+    bary = mk3(u, v, w_out);
+    cp = vadd(vadd(vmuls(a, u), vmuls(b, v)), vmuls(c, w_out));
+}
+
+__device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
+    return mk3(__ldg(p + i * 3), __ldg(p + i * 3 + 1), __ldg(p + i * 3 + 2));
+}
+
+// Traversal state of one particle against one mesh (generate_mesh_contacts.comp:201-331).
+// A stack entry keeps, besides the node, the squared box distance and the packed
+// child words read when its parent ordered its children, so a pop needs no load.
+struct MeshWalk {
+    float snds[32];
+    uint32_t slw[32], suw[32];
+    uint32_t sp;
+    float min_dist, min_dist_sq, max_dist;
+    v3 acc;
+    uint32_t min_face;
+    float sv_v, sv_w;
+    bool found, wt, overflow;
+};
+
+__device__ __forceinline__ void walk_push(MeshWalk& w, float nds, float4 lo4, float4 hi4) {
+    if (w.sp < 32) {
+        w.snds[w.sp] = nds;
+        w.slw[w.sp] = __float_as_uint(lo4.w);
+        w.suw[w.sp] = __float_as_uint(hi4.w);
+        w.sp++;
+    } else {
+        w.overflow = true;
+    }
+}
+
+__device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, int ci, float radius, v3 p) {
+    w.max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
+    w.sp = 0;
+    const uint32_t root = __ldg(&mt.roots[ci]);
+    const float4 lo4 = __ldg(&mt.nl[root]), hi4 = __ldg(&mt.nu[root]);
+    walk_push(w, dist_sq_aabb(p, xyz(lo4), xyz(hi4)), lo4, hi4);
+    w.min_dist = w.max_dist;
+    w.acc = mk3(0.0f, 0.0f, 0.0f);
+    w.min_face = 0;
+    w.sv_v = 0.0f;
+    w.sv_w = 0.0f;
+    w.found = false;
+    w.wt = __ldg(&mt.watertight[ci]) != 0;
+    w.min_dist_sq = w.max_dist * w.max_dist;
+}
+
+// Pops one node (:221-235, :315-330). Returns true when it is a leaf that passed the
+// distance test; its primitive range is returned for evaluation before the next pop.
+__device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, uint32_t& lo,
+                                         uint32_t& hi) {
+    --w.sp;
+    const float nds = w.snds[w.sp];
+    if (w.wt) {
+        if (nds > w.min_dist_sq) return false;
+    } else {
+        if (nds > (w.min_dist + eps_md) * (w.min_dist + eps_md)) return false;
+    }
+    const uint32_t lpk = w.slw[w.sp];
+    const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
+    const uint32_t right_i = w.suw[w.sp] & 0x3FFFFFFFu;
+    if (is_leaf) {
+        lo = left_i;
+        hi = right_i;
+        return true;
+    }
+    const float4 llo = __ldg(&mt.nl[left_i]), lhi = __ldg(&mt.nu[left_i]);
+    const float4 rlo = __ldg(&mt.nl[right_i]), rhi = __ldg(&mt.nu[right_i]);
+    const float lds = dist_sq_aabb(p, xyz(llo), xyz(lhi)), rds = dist_sq_aabb(p, xyz(rlo), xyz(rhi));
+    const float thresh = w.wt ? w.min_dist_sq : ((w.min_dist + eps_md) * (w.min_dist + eps_md));
+    // the shader's 32-entry stack has no bound check; a push past it is dropped here
+    // and reported through the status word
+    if (lds < rds) {
+        if (rds < thresh) walk_push(w, rds, rlo, rhi);
+        if (lds < thresh) walk_push(w, lds, llo, lhi);
+    } else {
+        if (lds < thresh) walk_push(w, lds, llo, lhi);
+        if (rds < thresh) walk_push(w, rds, rlo, rhi);
+    }
+    return false;
+}
+
+// Evaluates the triangles of one leaf (:237-314).
+__device__ __forceinline__ void walk_leaf(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, float eps2,
+                                          uint32_t lo, uint32_t hi) {
+    const float PI_ = 3.14159265359f;
+    for (uint32_t pc = lo; pc < hi; pc++) {
+        const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
+        if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
+        const float4 qa = __ldg(&mt.tri_cache[pc * 4]), qb = __ldg(&mt.tri_cache[pc * 4 + 1]),
+                     qc = __ldg(&mt.tri_cache[pc * 4 + 2]);
+        const uint32_t t = __float_as_uint(qa.w);
+        const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
+        const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+        const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
+        v3 cp, tb;
+        closest_point_triangle(p, a, b, c, cp, tb);
+        if (w.wt) {
+            const v3 diff = vsub(cp, p);
+            const float dist_sq = vdot(diff, diff);
+            if (dist_sq < w.min_dist_sq) {
+                w.min_dist_sq = dist_sq;
+                w.min_face = t;
+                w.sv_v = tb.y;
+                w.sv_w = tb.z;
+                w.found = true;
+            }
+        } else {
+            const float dist = exact_length(vsub(cp, p));
+            if (dist < w.min_dist + eps_md) {
+                float weight;
+                const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
+                const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
+                if (lcp < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
+                } else if (lcq < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
+                } else if (lcr < eps2) {
+                    weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
+                } else {
+                    const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
+                    if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
+                        (lcp * e1n - e1cp * e1cp < eps2 * e1n))
+                        weight = PI_;
+                    else
+                        weight = 2.0f * PI_;
+                }
+                if (dist > w.min_dist - eps_md) {
+                    w.acc = vadd(w.acc, vmuls(tn, weight));
+                    if (dist < w.min_dist) {
+                        w.min_dist = dist;
+                        w.min_face = t;
+                        w.sv_v = tb.y;
+                        w.sv_w = tb.z;
+                    }
+                } else {
+                    w.min_dist = dist;
+                    w.min_face = t;
+                    w.sv_v = tb.y;
+                    w.sv_w = tb.z;
+                    w.acc = vmuls(tn, weight);
+                }
+                w.found = true;
+            }
+        }
+    }
+}
+
+// Contact emission after the traversal of mesh ci (:333-411).
+__device__ __forceinline__ bool walk_finish(MeshWalk& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
+                                            v3& shape_v, v3& nrm) {
+    if (w.wt) w.min_dist = exact_sqrt(w.min_dist_sq);
+    if (!(w.found && w.min_dist < w.max_dist)) return false;
+    const float u_mesh = (1.0f - w.sv_v) - w.sv_w;
+    const float v_mesh = w.sv_v;
+    const uint32_t i0 = __ldg(&mt.tris[w.min_face * 3]), i1 = __ldg(&mt.tris[w.min_face * 3 + 1]),
+                   i2 = __ldg(&mt.tris[w.min_face * 3 + 2]);
+    const v3 v0 = ldv(mt.verts, i0), v1 = ldv(mt.verts, i1), v2 = ldv(mt.verts, i2);
+    const float w_eval = (1.0f - u_mesh) - v_mesh;
+    const v3 shape_p = vfma_vs(v2, w_eval, vfma_vs(v0, u_mesh, vmuls(v1, v_mesh)));
+    const v3 vel0 = ldv(mt.vels, i0), vel1 = ldv(mt.vels, i1), vel2 = ldv(mt.vels, i2);
+    shape_v = vfma_vs(vel2, w_eval, vfma_vs(vel0, u_mesh, vmuls(vel1, v_mesh)));
+    float sign;
+    if (w.wt) {
+        const v3 ray_dir = mk3(1.029700994f, 1.086472273f, 1.034694910f);
+        uint32_t hits = 0;
+        const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
+        for (uint32_t ti = 0; ti < pn; ti++) {
+            const float4* q = mt.tri_cache + (size_t)(po + ti) * 4;
+            if (intersect_ray_tri_woop(p, ray_dir, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
+        }
+        sign = (hits & 1u) ? -1.0f : 1.0f;
+    } else {
+        sign = vdot(w.acc, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
+    }
+    const v3 delta = vsub(p, shape_p);
+    const float delta_len = exact_length(delta);
+    nrm = delta_len > 0.0f ? vmuls(exact_div(delta, delta_len), sign) : mk3(0.0f, 0.0f, 1.0f);
+    const float d = delta_len * sign;
+    body_pos = vfma_vs(vneg(nrm), d, p);
+    return true;
+}
+
+// Whole query of point p (in the mesh's own frame) against mesh ci by one thread.
+__device__ __forceinline__ bool mesh_query(const MeshTables& mt, int ci, float radius, v3 p, v3& body_pos,
+                                           v3& shape_v, v3& nrm, bool& overflow) {
+    const float eps_md = mt.avg_edge * 1e-3f;
+    const float eps2 = eps_md * eps_md;
+    MeshWalk w;
+    w.overflow = false;
+    walk_begin(w, mt, ci, radius, p);
+    while (w.sp > 0) {
+        uint32_t lo, hi;
+        if (walk_pop(w, mt, p, eps_md, lo, hi)) walk_leaf(w, mt, p, eps_md, eps2, lo, hi);
+    }
+    overflow |= w.overflow;
+    return walk_finish(w, mt, ci, p, body_pos, shape_v, nrm);
+}
+
+}  // namespace xpbd

@@ -27,12 +27,14 @@ namespace {
 // profiler stage slots, one per kernel (names follow scene.cpp:1481-1505 where they correspond)
 enum ProfSlot {
     P_CLEAR = 0, P_CONTACT, P_INTEGRATE_KEYS, P_SORT0, P_SORT1, P_SORT2, P_SORT3, P_RANKS, P_CELLS, P_SOLVE,
-    P_COUNT
+    P_BODY_CONTACT, P_BODY_ENTRIES, P_BODY_INTEGRATE, P_BODY_ITER, P_RESTITUTION, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "0. Sort scratch clear (memset)", "1. Contact Gen (plane + mesh)", "2b. Integrate + Cell Keys",
     "2e. Onesweep Pass 0", "2e. Onesweep Pass 1", "2e. Onesweep Pass 2", "2e. Onesweep Pass 3",
-    "1b. Contact Ranks (cap)", "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)"};
+    "1b. Contact Ranks (cap)", "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)",
+    "1c. Body Contacts (pairs, moving meshes, rigid)", "1d. Body Delta Entries (scan, sort)",
+    "2c. Integrate Bodies", "3b. Body Deltas (particle + rigid)", "3c. Restitution (bodies)"};
 uint32_t f2u(float f) {
     uint32_t u;
     std::memcpy(&u, &f, 4);
@@ -198,6 +200,9 @@ void Solver::finalize_meshes() {
     body_invI_.alloc(nb * 9);
     body_invm_.alloc(nb);
     body_flags_.alloc(nb);
+    body_I_.alloc(nb * 9);
+    dyn_any_ = false;
+    dyn_list_.clear();
 
     // per-mesh LBVH on the host, then one packed node array for all meshes (scene.cpp:249-386)
     all_verts_.clear();
@@ -411,7 +416,198 @@ BodyTables Solver::body_tables() const {
     b.body_invI = body_invI_.p;
     b.body_invm = body_invm_.p;
     b.body_flags = body_flags_.p;
+    b.body_q_prev = dyn_any_ ? body_q_prev_.p : body_q_.p;
+    b.body_qd_prev = dyn_any_ ? body_qd_prev_.p : body_qd_.p;
     return b;
+}
+
+BodyArrays Solver::body_arrays() const {
+    BodyArrays a;
+    a.q = body_q_.p;
+    a.qd = body_qd_.p;
+    a.com = body_com_.p;
+    a.I = body_I_.p;
+    a.invI = body_invI_.p;
+    a.invm = body_invm_.p;
+    a.flags = body_flags_.p;
+    a.shape_body = shape_body_.p;
+    a.shape_mu = shape_mu_.p;
+    a.nb = (int)meshes_.size();
+    return a;
+}
+
+RigidTables Solver::rigid_tables() const {
+    RigidTables t;
+    t.n_dyn = (int)dyn_list_.size();
+    t.dyn = dyn_.p;
+    t.dyn_index = dyn_index_.p;
+    t.dv_start = dv_start_.p;
+    t.dv_local = dv_local_.p;
+    t.wbox = wbox_.p;
+    t.partners = partners_.p;
+    t.partner_count = partner_count_.p;
+    t.rc = rc_.p;
+    t.rc_count = rc_count_.p;
+    t.pad = 1e-3f;
+    t.n_vert = n_dyn_verts_;
+    return t;
+}
+
+RigidParams Solver::rigid_params(float sdt) const {
+    RigidParams r;
+    r.dt = sdt;
+    r.damping = body_params_.angular_damping;
+    r.margin = body_params_.rigid_contact_margin;
+    r.relax = body_params_.rigid_contact_relaxation;
+    r.con_weighting = body_params_.rigid_contact_con_weighting;
+    r.mu_t = body_params_.rigid_mu_torsional;
+    r.mu_r = body_params_.rigid_mu_rolling;
+    r.gx = cfg_.gravity[0];
+    r.gy = cfg_.gravity[1];
+    r.gz = cfg_.gravity[2];
+    r.plane = cfg_.has_ground_plane ? 1 : 0;
+    r.altitude = cfg_.ground_plane_altitude;
+    return r;
+}
+
+void Solver::set_body_params(const xpbd_body_params& p) {
+    body_params_ = p;
+    clear_graphs();
+}
+
+void Solver::set_bodies(const float* q, const float* qd, const float* com, const float* inertia,
+                        const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb) {
+    if (!finalized_) throw std::runtime_error("set_bodies: call finalize_meshes() first");
+    if (nb != meshes_.size()) throw std::runtime_error("set_bodies: one body per mesh");
+    XPBD_CUDA(cudaSetDevice(device_));
+    sync();
+    if (nb == 0) return;
+    std::vector<float4> hq(nb * 2), hqd(nb * 2);
+    std::vector<float> hcom(nb * 3), hI(nb * 9), hinvI(nb * 9), hinvm(nb);
+    std::vector<int> hfl(nb);
+    XPBD_CUDA(cudaMemcpy(hq.data(), body_q_.p, nb * 2 * sizeof(float4), cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hqd.data(), body_qd_.p, nb * 2 * sizeof(float4), cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hcom.data(), body_com_.p, nb * 3 * 4, cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hI.data(), body_I_.p, nb * 9 * 4, cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hinvI.data(), body_invI_.p, nb * 9 * 4, cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hinvm.data(), body_invm_.p, nb * 4, cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hfl.data(), body_flags_.p, nb * 4, cudaMemcpyDeviceToHost));
+    for (size_t b = 0; b < nb; b++) {
+        if (q) {  // (pos xyz, quat xyzw)
+            hq[b * 2] = make_float4(q[b * 7], q[b * 7 + 1], q[b * 7 + 2], 0.0f);
+            hq[b * 2 + 1] = make_float4(q[b * 7 + 3], q[b * 7 + 4], q[b * 7 + 5], q[b * 7 + 6]);
+        }
+        if (qd) {  // (linear, angular)
+            hqd[b * 2] = make_float4(qd[b * 6], qd[b * 6 + 1], qd[b * 6 + 2], 0.0f);
+            hqd[b * 2 + 1] = make_float4(qd[b * 6 + 3], qd[b * 6 + 4], qd[b * 6 + 5], 0.0f);
+        }
+        if (com) std::memcpy(&hcom[b * 3], com + b * 3, 12);
+        if (inertia) std::memcpy(&hI[b * 9], inertia + b * 9, 36);
+        if (inv_inertia) std::memcpy(&hinvI[b * 9], inv_inertia + b * 9, 36);
+        if (inv_mass) hinvm[b] = inv_mass[b];
+        if (flags) hfl[b] = flags[b];
+    }
+    XPBD_CUDA(cudaMemcpy(body_q_.p, hq.data(), nb * 2 * sizeof(float4), cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_qd_.p, hqd.data(), nb * 2 * sizeof(float4), cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_com_.p, hcom.data(), nb * 3 * 4, cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_I_.p, hI.data(), nb * 9 * 4, cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_invI_.p, hinvI.data(), nb * 9 * 4, cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_invm_.p, hinvm.data(), nb * 4, cudaMemcpyHostToDevice));
+    XPBD_CUDA(cudaMemcpy(body_flags_.p, hfl.data(), nb * 4, cudaMemcpyHostToDevice));
+
+    // dynamic bodies: inverse mass > 0; their meshes are in the body frame
+    dyn_list_.clear();
+    std::vector<int> dyn_index(nb, -1), posed(nb, 0), walk;
+    for (size_t b = 0; b < nb; b++) {
+        if (hinvm[b] > 0.0f) {
+            dyn_index[b] = (int)dyn_list_.size();
+            dyn_list_.push_back((int)b);
+            posed[b] = 1;
+        } else {
+            walk.push_back((int)b);
+        }
+    }
+    dyn_any_ = !dyn_list_.empty();
+    clear_graphs();
+    if (!dyn_any_) return;
+    auto up = [&](auto& dev, const auto& host) {
+        dev.alloc(std::max<size_t>(host.size(), 1), false);
+        if (!host.empty())
+            XPBD_CUDA(cudaMemcpy(dev.p, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice));
+    };
+    std::vector<uint32_t> dv_start(nb + 1, 0);
+    std::vector<float4> dv_local;
+    for (size_t b = 0; b < nb; b++) {
+        dv_start[b] = (uint32_t)dv_local.size();
+        if (!posed[b]) continue;
+        const std::vector<float>& v = meshes_[b].vertices;
+        for (size_t k = 0; k + 2 < v.size(); k += 3) {
+            int bi = (int)b;
+            float bw;
+            std::memcpy(&bw, &bi, 4);
+            dv_local.push_back(make_float4(v[k], v[k + 1], v[k + 2], bw));
+        }
+    }
+    dv_start[nb] = (uint32_t)dv_local.size();
+    n_dyn_verts_ = (int)dv_local.size();
+    up(dyn_, dyn_list_);
+    up(dyn_index_, dyn_index);
+    up(posed_, posed);
+    up(walk_list_, walk);
+    walk_count_ = (int)walk.size();
+    up(dv_start_, dv_start);
+    up(dv_local_, dv_local);
+    const size_t nd = dyn_list_.size();
+    wbox_.alloc(nd * 2, true);
+    partners_.alloc(nd * kPartnerCap, true);
+    partner_count_.alloc(nd, true);
+    rc_.alloc(std::max<size_t>((size_t)n_dyn_verts_, 1) * kRigidSlots * 5, true);
+    rc_count_.alloc(std::max<size_t>((size_t)n_dyn_verts_, 1), true);
+    body_q_mid_.alloc(nb * 2, true);
+    body_qd_mid_.alloc(nb * 2, true);
+    body_q_prev_.alloc(nb * 2, true);
+    body_qd_prev_.alloc(nb * 2, true);
+    // body-delta entries of the particle contacts: one per slot with a dynamic body
+    entry_cap_ = (uint32_t)std::min<size_t>(n_ + 4096, (size_t)0x7fffffff);
+    int kb = 1;
+    while ((size_t(1) << kb) < nb) kb++;
+    eplan_ = make_sort_plan((int64_t)entry_cap_, kb, 8, 8);
+    ehist_off_ = 0;
+    elb_off_ = (size_t)eplan_.passes << eplan_.bits;
+    etc_off_ = elb_off_ + (size_t)eplan_.passes * sort_lookback_words(eplan_);
+    esort_scratch_.alloc(etc_off_ + (size_t)eplan_.passes, true);
+    ekeys_.alloc(entry_cap_, false);
+    for (int p = 0; p < 2; p++) {
+        epk_[p].alloc(entry_cap_, false);
+        epv_[p].alloc(entry_cap_, false);
+    }
+    seg_.alloc(nb, true);
+    bdel_.alloc((size_t)entry_cap_ * 2, false);
+    dyn_rank_.alloc(std::max<size_t>(n_, 1), false);
+    dyn_totals_.alloc(2, true);
+    dyn_ws_.alloc(contact_scan_words((int64_t)n_), true);
+}
+
+void Solver::get_bodies(float* q, float* qd, size_t nb) {
+    require_init();
+    if (nb != meshes_.size()) throw std::runtime_error("get_bodies: one body per mesh");
+    sync();
+    if (nb == 0) return;
+    std::vector<float4> hq(nb * 2), hqd(nb * 2);
+    XPBD_CUDA(cudaMemcpy(hq.data(), body_q_.p, nb * 2 * sizeof(float4), cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(hqd.data(), body_qd_.p, nb * 2 * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t b = 0; b < nb; b++) {
+        if (q) {
+            const float4 a = hq[b * 2], c = hq[b * 2 + 1];
+            const float v[7] = {a.x, a.y, a.z, c.x, c.y, c.z, c.w};
+            std::memcpy(q + b * 7, v, sizeof(v));
+        }
+        if (qd) {
+            const float4 a = hqd[b * 2], c = hqd[b * 2 + 1];
+            const float v[6] = {a.x, a.y, a.z, c.x, c.y, c.z};
+            std::memcpy(qd + b * 6, v, sizeof(v));
+        }
+    }
 }
 
 MeshTables Solver::mesh_tables() const {
@@ -428,6 +624,10 @@ MeshTables Solver::mesh_tables() const {
     m.prim_off = prim_off_.p;
     m.prim_cnt = prim_cnt_.p;
     m.tri_cache = tri_cache_.p;
+    m.pose = body_q_.p;
+    m.posed = dyn_any_ ? posed_.p : nullptr;
+    m.walk_list = dyn_any_ ? walk_list_.p : nullptr;
+    m.walk_count = dyn_any_ ? walk_count_ : (int)meshes_.size();
     m.n_meshes = (int)meshes_.size();
     m.avg_edge = avg_edge0_;
     m.soft_margin = cfg_.soft_contact_margin;
@@ -463,15 +663,60 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const bool mesh_pass = gen && !meshes_.empty();
     DeviceStatus* st = status_.p;
 
+    const bool bodies = gen && dyn_any_;  // dynamic bodies step with the particles
+    const RigidParams rp = rigid_params(sdt);
+    const BodyArrays ba = body_arrays();
+    const RigidTables rt = rigid_tables();
+    const DynSlots ds{cslot_.p, slot_cap_, shape_body_.p, body_invm_.p};
+
     prof_mark(-1);
     XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
     count_memset();
+    if (bodies) {
+        XPBD_CUDA(cudaMemsetAsync(esort_scratch_.p, 0, esort_scratch_.bytes(), stream_));
+        XPBD_CUDA(cudaMemsetAsync(seg_.p, 0, seg_.bytes(), stream_));
+        count_memset();
+        count_memset();
+    }
     prof_mark(P_CLEAR);
+    if (bodies) {
+        launch_body_pairs(stream_, ba, rt, mesh_tables(), rp, st);
+        count_kernel(2);
+        prof_mark(P_BODY_CONTACT);
+    }
     if (mesh_pass) {
         launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
                        slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, st);
         count_kernel();
         prof_mark(P_CONTACT);
+    }
+    if (bodies) {
+        launch_collide_posed(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p,
+                             mesh_tables(), rt, slot_cap_, cinfo_.p, cslot_.p, ccount, st);
+        launch_rigid_contacts(stream_, ba, rt, mesh_tables(), rp, st);
+        count_kernel(2);
+        prof_mark(P_BODY_CONTACT);
+        // body-delta entries: dynamic slots in contact order, grouped by body (stable sort)
+        launch_dyn_scan(stream_, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
+        launch_dyn_emit(stream_, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
+                        esort_scratch_.p + ehist_off_, st);
+        count_kernel(4);
+        const uint32_t* ek = ekeys_.p;
+        const uint32_t* ev = nullptr;
+        const size_t elbw = sort_lookback_words(eplan_);
+        for (int p = 0; p < eplan_.passes; p++) {
+            launch_onesweep_pass(stream_, (int64_t)entry_cap_, eplan_, p, ek, ev, epk_[p & 1].p, epv_[p & 1].p,
+                                 esort_scratch_.p + ehist_off_ + ((size_t)p << eplan_.bits),
+                                 esort_scratch_.p + elb_off_ + (size_t)p * elbw, esort_scratch_.p + etc_off_ + p, st,
+                                 dyn_totals_.p);
+            count_kernel();
+            ek = epk_[p & 1].p;
+            ev = epv_[p & 1].p;
+        }
+        launch_body_segments(stream_, entry_cap_, dyn_totals_.p, ek, seg_.p);
+        count_kernel();
+        sorted_entries_ = ev;
+        prof_mark(P_BODY_ENTRIES);
     }
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
@@ -479,6 +724,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
                         sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
+    if (bodies) {
+        launch_body_integrate(stream_, ba, body_q_prev_.p, body_qd_prev_.p, rp);
+        count_kernel();
+        prof_mark(P_BODY_INTEGRATE);
+    }
     const uint32_t* kin = keys_.p;
     const uint32_t* vin = nullptr;
     const size_t lbw = sort_lookback_words(plan_);
@@ -517,13 +767,28 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         dg.max_pairs = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
     }
     const BodyTables bt = body_tables();
+    const BodyDeltaOut bo{bodies ? bdel_.p : nullptr, bodies ? dyn_rank_.p : nullptr};
     for (int it = 0; it < iterations; it++) {
-        const bool last = it == iterations - 1;
-        launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p, rv_[it & 1].p, rf_.p, table_.p, stamp_.p,
-                     x_[src].p, v_[src].p, info, slots, cr, bt, solve_params(sdt, it), rx_[(it + 1) & 1].p,
-                     rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg);
+        // with dynamic bodies the restitution waits for the last body pass
+        const bool last = it == iterations - 1 && !bodies;
+        launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p,
+                     rv_[it & 1].p, rf_.p, table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, cr, bt,
+                     solve_params(sdt, it), rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo);
         count_kernel();
         prof_mark(P_SOLVE);
+        if (bodies) {
+            launch_body_particles(stream_, ba, seg_.p, sorted_entries_, bdel_.p, body_q_.p, body_qd_.p,
+                                  body_q_mid_.p, body_qd_mid_.p, rp);
+            launch_body_rigid(stream_, ba, rt, body_q_mid_.p, body_qd_mid_.p, body_q_.p, body_qd_.p, rp);
+            count_kernel(2);
+            prof_mark(P_BODY_ITER);
+        }
+    }
+    if (bodies && iterations > 0) {
+        launch_restitute(stream_, n, sids, rx_[iterations & 1].p, rv_[iterations & 1].p, rf_.p, x_[src].p,
+                         v_[src].p, info, slots, cr, bt, solve_params(sdt, iterations - 1), x_[dst].p, v_[dst].p);
+        count_kernel();
+        prof_mark(P_RESTITUTION);
     }
     if (iterations <= 0) {  // no solver iteration: the predicted state is the result
         XPBD_CUDA(cudaMemcpyAsync(x_[dst].p, x_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
@@ -618,6 +883,9 @@ void Solver::finish_frame(int substeps) {
         throw std::runtime_error("BVH traversal stack overflow (more than 32 pending nodes)");
     if (host_status_.error_bits & kErrSlotOverflow)
         throw std::runtime_error("more mesh contacts for one particle than contact slots");
+    if (host_status_.error_bits & kErrBodyOverflow)
+        throw std::runtime_error("body tables full (overlapping bodies, rigid contacts per vertex or body-delta "
+                                 "entries)");
     if (env_on("VKXPBD_CHECK_SORT_ORDER")) check_sort_order();
 }
 

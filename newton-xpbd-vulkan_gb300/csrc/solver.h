@@ -85,6 +85,12 @@ class Solver {
     void set_particles(const float* q, const float* qd, const float* inv_mass, const float* radii,
                        const int32_t* flags, size_t n);
     void update_mesh(size_t mesh_index, const float* verts, size_t num_verts, const float* vels);
+    // rigid bodies (one per mesh): q (pos xyz, quat xyzw) x7, qd (lin, ang) x6, com x3,
+    // inertia and inv_inertia x9, inv_mass, flags; null pointers keep the current values
+    void set_bodies(const float* q, const float* qd, const float* com, const float* inertia,
+                    const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb);
+    void get_bodies(float* q, float* qd, size_t nb);
+    void set_body_params(const xpbd_body_params& p);
     void step(float dt, int substeps, int iterations);
     void collide_only();
     void step_solve_only(float dt, int substeps, int iterations);
@@ -148,6 +154,9 @@ class Solver {
     SolveParams solve_params(float sdt, int it) const;
     BodyTables body_tables() const;
     MeshTables mesh_tables() const;
+    BodyArrays body_arrays() const;
+    RigidTables rigid_tables() const;
+    RigidParams rigid_params(float sdt) const;
     void prof_mark(int slot);
     void count_kernel(int k = 1);
     void count_memset();
@@ -206,6 +215,24 @@ class Solver {
     DevBuf<float4> body_q_, body_qd_;
     DevBuf<float> body_com_, body_invI_, body_invm_;
     DevBuf<int> body_flags_;
+    // dynamic bodies
+    DevBuf<float> body_I_;
+    bool dyn_any_ = false;
+    std::vector<int> dyn_list_;
+    xpbd_body_params body_params_{0.0f, 0.01f, 0.8f, 1, 0.0f, 0.0f};
+    DevBuf<float4> body_q_mid_, body_qd_mid_, body_q_prev_, body_qd_prev_;
+    DevBuf<int> dyn_, dyn_index_, posed_, walk_list_, partners_, partner_count_, rc_count_;
+    int walk_count_ = 0, n_dyn_verts_ = 0;
+    DevBuf<uint32_t> dv_start_;
+    DevBuf<float4> dv_local_, wbox_, rc_;
+    uint32_t entry_cap_ = 0;
+    SortPlan eplan_{};
+    size_t ehist_off_ = 0, elb_off_ = 0, etc_off_ = 0;
+    DevBuf<uint32_t> esort_scratch_, ekeys_, epk_[2], epv_[2];
+    const uint32_t* sorted_entries_ = nullptr;
+    DevBuf<uint2> seg_, dyn_rank_;
+    DevBuf<uint32_t> dyn_totals_, dyn_ws_;
+    DevBuf<float4> bdel_;
     DevBuf<float4> nl_, nu_;
     DevBuf<float> verts_, vels_;
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;

@@ -148,6 +148,40 @@ class XpbdSolver:
     def init(self, config, num_particles, max_contacts=0):
         _check(_lib.xpbd_init(self._h, C.byref(config._c), int(num_particles), int(max_contacts)))
 
+    # ---- rigid bodies (extension; one body per mesh) ------------------------------
+    def set_bodies(self, q=None, qd=None, com=None, inertia=None, inv_inertia=None, inv_mass=None, flags=None):
+        """Body table, one row per mesh (xpbd_set_bodies): q (nb, 7) position + quaternion xyzw,
+        qd (nb, 6) linear + angular velocity, com (nb, 3), inertia / inv_inertia (nb, 3, 3),
+        inv_mass (nb,), flags (nb,). None keeps the current values. Bodies with inv_mass > 0
+        are dynamic and their meshes are in the body frame."""
+        nb = self.mesh_count
+        arrs = [None if a is None else _f32(a).reshape(-1) for a in (q, qd, com, inertia, inv_inertia, inv_mass)]
+        fl = None if flags is None else _i32(flags).reshape(-1)
+        _check(_lib.xpbd_set_bodies(self._h, *[_ptr(a, _FP) for a in arrs], _ptr(fl, _IP), nb))
+
+    def get_body_q(self):
+        nb = self.mesh_count
+        q = np.zeros((nb, 7), np.float32)
+        _check(_lib.xpbd_get_bodies(self._h, _ptr(q, _FP), None, nb))
+        return q
+
+    def get_body_qd(self):
+        nb = self.mesh_count
+        qd = np.zeros((nb, 6), np.float32)
+        _check(_lib.xpbd_get_bodies(self._h, None, _ptr(qd, _FP), nb))
+        return qd
+
+    def set_body_params(self, **kw):
+        """angular_damping, rigid_contact_margin, rigid_contact_relaxation,
+        rigid_contact_con_weighting, rigid_mu_torsional, rigid_mu_rolling."""
+        bp = _abi.BodyParams()
+        _lib.xpbd_body_params_default(C.byref(bp))
+        for k, v in kw.items():
+            if not hasattr(bp, k):
+                raise AttributeError(k)
+            setattr(bp, k, v)
+        _check(_lib.xpbd_set_body_params(self._h, C.byref(bp)))
+
     def init_batched(self, config, scene_counts, max_contacts=0):
         """Independent scenes stepped together (xpbd_batch_init). Particle arrays passed to
         set_particles and returned by the getters are the scenes' particles concatenated in

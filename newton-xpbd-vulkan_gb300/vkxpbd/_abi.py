@@ -40,6 +40,16 @@ class PairRecord(C.Structure):
     ]
 
 
+class BodyParams(C.Structure):
+    """struct xpbd_body_params (include/xpbd.h)."""
+
+    _fields_ = [
+        ("angular_damping", C.c_float), ("rigid_contact_margin", C.c_float),
+        ("rigid_contact_relaxation", C.c_float), ("rigid_contact_con_weighting", C.c_int32),
+        ("rigid_mu_torsional", C.c_float), ("rigid_mu_rolling", C.c_float),
+    ]
+
+
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int32)
@@ -92,6 +102,10 @@ SIGNATURES = {
     "xpbd_stage_name": (C.c_char_p, [C.c_int]),
     "xpbd_get_frame_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "xpbd_sort_keys_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _Z, C.c_int, C.c_void_p]),
+    "xpbd_body_params_default": (None, [C.POINTER(BodyParams)]),
+    "xpbd_set_body_params": (C.c_int, [_P, C.POINTER(BodyParams)]),
+    "xpbd_set_bodies": (C.c_int, [_P, _F, _F, _F, _F, _F, _F, _I, _Z]),
+    "xpbd_get_bodies": (C.c_int, [_P, _F, _F, _Z]),
     "xpbd_batch_init": (C.c_int, [_P, C.POINTER(Config), C.POINTER(C.c_size_t), _Z, _Z]),
     "xpbd_batch_scene_count": (_Z, [_P]),
     "xpbd_batch_scene_offsets": (C.c_int, [_P, C.POINTER(C.c_size_t), _Z]),

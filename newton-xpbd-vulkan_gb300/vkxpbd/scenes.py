@@ -79,6 +79,50 @@ def box_mesh(half_extents, center=(0.0, 0.0, 0.0), quat_xyzw=(0.0, 0.0, 0.0, 1.0
     return v.astype(np.float32), t
 
 
+def box_inertia(half_extents, density=1000.0):
+    """Mass and body-frame inertia tensor of a solid box."""
+    hx, hy, hz = (float(h) for h in half_extents)
+    m = density * 8.0 * hx * hy * hz
+    inertia = np.diag([m / 3.0 * (hy * hy + hz * hz), m / 3.0 * (hx * hx + hz * hz), m / 3.0 * (hx * hx + hy * hy)])
+    return m, inertia
+
+
+def random_quats(n, rng):
+    """Quaternions (xyzw) uniform on SO(3): normalised Gaussian 4-vectors."""
+    q = rng.normal(size=(n, 4))
+    return q / np.linalg.norm(q, axis=1, keepdims=True)
+
+
+@dataclass
+class Bodies:
+    """Rigid-body table, one body per mesh (body b belongs to mesh b)."""
+    q: np.ndarray            # (nb, 7) position xyz, quaternion xyzw
+    qd: np.ndarray           # (nb, 6) linear, angular velocity
+    com: np.ndarray          # (nb, 3)
+    inertia: np.ndarray      # (nb, 3, 3)
+    inv_inertia: np.ndarray  # (nb, 3, 3)
+    inv_mass: np.ndarray     # (nb,)
+    flags: np.ndarray        # (nb,)
+
+    @staticmethod
+    def static(nb):
+        q = np.zeros((nb, 7), np.float32)
+        q[:, 6] = 1.0
+        z3 = np.zeros((nb, 3, 3), np.float32)
+        return Bodies(q, np.zeros((nb, 6), np.float32), np.zeros((nb, 3), np.float32), z3.copy(), z3.copy(),
+                      np.zeros(nb, np.float32), np.zeros(nb, np.int32))
+
+    def set_box(self, b, half_extents, pos, quat_xyzw, density=1000.0, vel=(0, 0, 0), ang=(0, 0, 0)):
+        m, inertia = box_inertia(half_extents, density)
+        self.q[b, 0:3] = pos
+        self.q[b, 3:7] = quat_xyzw
+        self.qd[b, 0:3] = vel
+        self.qd[b, 3:6] = ang
+        self.inertia[b] = inertia
+        self.inv_inertia[b] = np.linalg.inv(inertia)
+        self.inv_mass[b] = 1.0 / m
+
+
 @dataclass
 class Scene:
     name: str
@@ -89,6 +133,7 @@ class Scene:
     radii: np.ndarray
     flags: np.ndarray
     meshes: list = field(default_factory=list)  # (verts, tris, margin, watertight or None)
+    bodies: object = None                        # Bodies for the meshes, or None (all static)
     dt: float = 1.0 / 60.0
     substeps: int = 10
     iterations: int = 1
@@ -190,3 +235,37 @@ def batched_piles(n_scenes=512, lo=1024, hi=65536, seed=SEED_BATCH, frames=100) 
     jittered with seed `seed + s`; plane only."""
     counts = batch_counts(n_scenes, lo, hi, seed)
     return Batch([pile_of(c, seed=seed + s, frames=frames, name=f"pile{s}") for s, c in enumerate(counts)])
+
+
+def add_boxes(sc: Scene, half_extents, positions, quats, density=1000.0) -> Scene:
+    """Appends one dynamic box body (a watertight 12-triangle mesh in its body frame) per row."""
+    nb0 = len(sc.meshes)
+    for he in half_extents:
+        v, t = box_mesh(he)
+        sc.meshes.append((v, t, 0.0, True))
+    old = sc.bodies if sc.bodies is not None else Bodies.static(nb0)
+    b = Bodies.static(len(sc.meshes))
+    for name in ("q", "qd", "com", "inertia", "inv_inertia", "inv_mass", "flags"):
+        getattr(b, name)[:nb0] = getattr(old, name)[:nb0]
+    for k, (he, p, q) in enumerate(zip(half_extents, positions, quats)):
+        b.set_box(nb0 + k, he, p, q, density)
+    sc.bodies = b
+    return sc
+
+
+def mixed(dims=(128, 128, 64), spacing=0.01, radius=0.005, jitter=0.001, bottom_z=0.15, n_boxes=1024,
+          hf_vertices=256, seed=SEED_BOXES, frames=200, name="mixed") -> Scene:
+    """Particles, the heightfield and dynamic boxes: a dims lattice (1,048,576 particles for the
+    defaults) on the plane and the sum-of-sines heightfield, plus n_boxes boxes with half-extents
+    uniform in [0.02, 0.08] per axis, density 1000, orientations uniform on SO(3) and positions
+    uniform over the lattice footprint, in a layer from 0.1 m to 1.1 m above its top."""
+    sc = particles_on_mesh(dims, spacing, radius, jitter, bottom_z, hf_vertices, frames=frames, name=name)
+    rng = np.random.default_rng(seed)
+    he = rng.uniform(0.02, 0.08, size=(n_boxes, 3))
+    quats = random_quats(n_boxes, rng)
+    half_w = np.array([(dims[0] - 1) * spacing * 0.5, (dims[1] - 1) * spacing * 0.5])
+    top = bottom_z + (dims[2] - 1) * spacing
+    pos = np.empty((n_boxes, 3))
+    pos[:, 0:2] = rng.uniform(-half_w, half_w, size=(n_boxes, 2))
+    pos[:, 2] = rng.uniform(top + 0.1, top + 1.1, size=n_boxes)
+    return add_boxes(sc, he, pos, quats)

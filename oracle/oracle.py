@@ -57,6 +57,15 @@ _F = C.POINTER(C.c_float)
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
 _U = C.POINTER(C.c_uint32)
+class BodyParams(C.Structure):
+    _fields_ = [("angular_damping", C.c_float), ("rigid_contact_margin", C.c_float),
+                ("rigid_contact_relaxation", C.c_float), ("rigid_contact_con_weighting", C.c_int32),
+                ("rigid_mu_torsional", C.c_float), ("rigid_mu_rolling", C.c_float)]
+
+
+BODY_PARAM_DEFAULTS = dict(angular_damping=0.0, rigid_contact_margin=0.01, rigid_contact_relaxation=0.8,
+                           rigid_contact_con_weighting=1, rigid_mu_torsional=0.0, rigid_mu_rolling=0.0)
+
 _libs: dict = {}
 
 
@@ -78,7 +87,11 @@ def load(precision: str = "f32") -> C.CDLL:
     lib.or_finalize_meshes.argtypes = [_P]
     lib.or_update_mesh.argtypes = [_P, C.c_int64, _F, C.c_int64, _F]
     lib.or_set_particles.argtypes = [_P, _F, _F, _F, _F, _I, C.c_int64]
-    lib.or_set_bodies.argtypes = [_P, _F, _F, _F, _F, _F, _I, C.c_int64]
+    lib.or_set_bodies.argtypes = [_P, _F, _F, _F, _F, _F, _F, _I, C.c_int64]
+    lib.or_get_bodies.argtypes = [_P, _F, _F]
+    lib.or_set_body_params.argtypes = [_P, C.POINTER(BodyParams)]
+    lib.or_rigid_contact_overflows.restype = C.c_int64
+    lib.or_rigid_contact_overflows.argtypes = [_P]
     lib.or_step.argtypes = [_P, C.c_float, C.c_int, C.c_int]
     lib.or_collide_only.argtypes = [_P]
     lib.or_step_solve_only.argtypes = [_P, C.c_float, C.c_int, C.c_int]
@@ -171,12 +184,45 @@ class OracleSolver:
         if rc != 0:
             raise RuntimeError("Particle count mismatch")
 
-    def set_bodies(self, q=None, qd=None, com=None, inv_inertia=None, inv_mass=None, flags=None):
-        arrs = [None if a is None else f32(a).reshape(-1) for a in (q, qd, com, inv_inertia, inv_mass)]
+    def set_bodies(self, q=None, qd=None, com=None, inertia=None, inv_inertia=None, inv_mass=None, flags=None):
+        """q: (nb, 7) position xyz + quaternion xyzw; qd: (nb, 6) linear, angular velocity;
+        com (nb, 3); inertia, inv_inertia (nb, 3, 3); inv_mass (nb,); flags (nb,)."""
+        nb = self.meshes
+        q8 = qd8 = None
+        if q is not None:
+            q = f32(q).reshape(nb, 7)
+            q8 = np.zeros((nb, 8), np.float32)
+            q8[:, 0:3] = q[:, 0:3]
+            q8[:, 4:8] = q[:, 3:7]
+        if qd is not None:
+            qd = f32(qd).reshape(nb, 6)
+            qd8 = np.zeros((nb, 8), np.float32)
+            qd8[:, 0:3] = qd[:, 0:3]
+            qd8[:, 4:7] = qd[:, 3:6]
+        arrs = [None if a is None else f32(a).reshape(-1) for a in (q8, qd8, com, inertia, inv_inertia, inv_mass)]
         fl = None if flags is None else i32(flags)
-        rc = self.lib.or_set_bodies(self.h, *[_fp(a, _F) for a in arrs], _fp(fl, _I), self.meshes)
+        rc = self.lib.or_set_bodies(self.h, *[_fp(a, _F) for a in arrs], _fp(fl, _I), nb)
         if rc != 0:
             raise RuntimeError("oracle set_bodies failed")
+
+    def get_body_q(self):
+        q8 = np.zeros((self.meshes, 8), np.float32)
+        self.lib.or_get_bodies(self.h, _fp(q8, _F), None)
+        return np.ascontiguousarray(np.concatenate([q8[:, 0:3], q8[:, 4:8]], axis=1))
+
+    def get_body_qd(self):
+        qd8 = np.zeros((self.meshes, 8), np.float32)
+        self.lib.or_get_bodies(self.h, None, _fp(qd8, _F))
+        return np.ascontiguousarray(np.concatenate([qd8[:, 0:3], qd8[:, 4:7]], axis=1))
+
+    def set_body_params(self, **kw):
+        bp = BodyParams()
+        for k, v in {**BODY_PARAM_DEFAULTS, **kw}.items():
+            setattr(bp, k, v)
+        self.lib.or_set_body_params(self.h, C.byref(bp))
+
+    def rigid_contact_overflows(self):
+        return int(self.lib.or_rigid_contact_overflows(self.h))
 
     def step(self, dt=1.0 / 60.0, substeps=1, iterations=2):
         self.lib.or_step(self.h, float(dt), int(substeps), int(iterations))

@@ -215,6 +215,17 @@ typedef struct {
     float avg_edge;
 } or_mesh;
 
+/* Rigid contact generated for one vertex of a dynamic body's mesh (shape0 = that
+ * body's mesh shape): the record solve_body_contact_positions.comp:8-18 reads. */
+#define RC_CAP 4 /* contacts per vertex */
+typedef struct {
+    int32_t shape1;   /* 0 = ground plane, m + 1 = mesh m */
+    v3 p0, p1;        /* contact points in the frames of shape0's and shape1's bodies */
+    v3 off0, off1;    /* surface offsets in the same frames */
+    v3 n;             /* world normal, pointing from shape0 to shape1 */
+    real th0, th1;    /* thicknesses (shape margins) */
+} or_rcontact;
+
 struct or_solver {
     or_config cfg;
     int64_t n, cmax;
@@ -248,6 +259,15 @@ struct or_solver {
     int64_t nbody;
     real *body_q, *body_qd, *body_com, *body_invI, *body_invm;
     int32_t* body_flags;
+    /* dynamic bodies (extension): inertia, substep-start and mid-iteration states */
+    real *body_I, *body_qp, *body_qdp, *body_qm, *body_qdm;
+    int dyn_any;
+    or_body_params bp;
+    real* bdel;       /* per contact slot: body delta (lin xyz, ang xyz) */
+    uint8_t* bvalid;  /* per contact slot: bdel holds a contribution */
+    int32_t* rc_cnt;  /* per vertex of the concatenated vertex array */
+    or_rcontact* rc;  /* RC_CAP per vertex */
+    int64_t rc_overflow, partner_dummy;
 };
 
 static void* xcalloc(size_t n, size_t sz) {
@@ -281,6 +301,14 @@ or_solver* or_create(const or_config* cfg, int64_t n, int64_t max_contacts) {
     s->cbpos = xcalloc((size_t)s->cmax * 3, sizeof(real));
     s->cbvel = xcalloc((size_t)s->cmax * 3, sizeof(real));
     s->cnorm = xcalloc((size_t)s->cmax * 3, sizeof(real));
+    s->bdel = xcalloc((size_t)s->cmax * 6, sizeof(real));
+    s->bvalid = xcalloc((size_t)s->cmax, sizeof(uint8_t));
+    s->bp.angular_damping = 0.0f;
+    s->bp.rigid_contact_margin = 0.01f;
+    s->bp.rigid_contact_relaxation = 0.8f;
+    s->bp.rigid_contact_con_weighting = 1;
+    s->bp.rigid_mu_torsional = 0.0f;
+    s->bp.rigid_mu_rolling = 0.0f;
     s->cells = xcalloc((size_t)n, sizeof(uint32_t));
     s->ids = xcalloc((size_t)n, sizeof(uint32_t));
     s->scells = xcalloc((size_t)n, sizeof(uint32_t));
@@ -298,6 +326,12 @@ static void free_finalized(or_solver* s) {
     free(s->shape_body); free(s->shape_mu);
     free(s->body_q); free(s->body_qd); free(s->body_com); free(s->body_invI); free(s->body_invm);
     free(s->body_flags);
+    free(s->body_I); free(s->body_qp); free(s->body_qdp); free(s->body_qm); free(s->body_qdm);
+    free(s->rc_cnt); free(s->rc);
+    s->body_I = s->body_qp = s->body_qdp = s->body_qm = s->body_qdm = NULL;
+    s->rc_cnt = NULL;
+    s->rc = NULL;
+    s->dyn_any = 0;
     s->all_verts = s->all_vels = NULL; s->all_tris = NULL; s->nl = s->nu = NULL; s->prim = NULL;
     s->roots = s->prim_off = s->prim_cnt = NULL; s->shape_body = NULL; s->shape_mu = NULL;
     s->body_q = s->body_qd = s->body_com = s->body_invI = s->body_invm = NULL; s->body_flags = NULL;
@@ -308,6 +342,7 @@ void or_destroy(or_solver* s) {
     free(s->x); free(s->v); free(s->x0); free(s->v0); free(s->xo); free(s->vo); free(s->delta);
     free(s->vsnap); free(s->w); free(s->r); free(s->flags);
     free(s->cpart); free(s->cshape); free(s->cbpos); free(s->cbvel); free(s->cnorm);
+    free(s->bdel); free(s->bvalid);
     free(s->cells); free(s->ids); free(s->scells); free(s->sids); free(s->cstart); free(s->cend);
     for (int64_t m = 0; m < s->nmesh; m++) {
         free(s->meshes[m].verts); free(s->meshes[m].tris); free(s->meshes[m].lowers);
@@ -594,12 +629,19 @@ int or_finalize_meshes(or_solver* s) { /* scene.cpp:204-390 */
     s->body_invI = xcalloc((size_t)(nm ? nm : 1) * 9, sizeof(real));
     s->body_invm = xcalloc((size_t)(nm ? nm : 1), sizeof(real));
     s->body_flags = xcalloc((size_t)(nm ? nm : 1), sizeof(int32_t));
+    s->body_I = xcalloc((size_t)(nm ? nm : 1) * 9, sizeof(real));
+    s->body_qp = xcalloc((size_t)(nm ? nm : 1) * 8, sizeof(real));
+    s->body_qdp = xcalloc((size_t)(nm ? nm : 1) * 8, sizeof(real));
+    s->body_qm = xcalloc((size_t)(nm ? nm : 1) * 8, sizeof(real));
+    s->body_qdm = xcalloc((size_t)(nm ? nm : 1) * 8, sizeof(real));
     for (int64_t b = 0; b < nm; b++) s->body_q[b * 8 + 7] = RF(1.0);
 
     int64_t tv = 0, tt = 0;
     for (int64_t c = 0; c < nm; c++) { tv += s->meshes[c].nv; tt += s->meshes[c].nt; }
     s->n_all_verts = tv;
     s->n_all_tris = tt;
+    s->rc_cnt = xcalloc((size_t)(tv ? tv : 1), sizeof(int32_t));
+    s->rc = xcalloc((size_t)(tv ? tv : 1) * RC_CAP, sizeof(or_rcontact));
     s->all_verts = xcalloc((size_t)tv * 3, sizeof(float));
     s->all_vels = xcalloc((size_t)tv * 3, sizeof(float));
     s->all_tris = xcalloc((size_t)tt * 3, sizeof(uint32_t));
@@ -709,19 +751,33 @@ int or_set_particles(or_solver* s, const float* q, const float* qd, const float*
     return 0;
 }
 
-int or_set_bodies(or_solver* s, const float* q, const float* qd, const float* com, const float* invI,
-                  const float* invm, const int32_t* flags, int64_t nb) {
+int or_set_bodies(or_solver* s, const float* q, const float* qd, const float* com, const float* I,
+                  const float* invI, const float* invm, const int32_t* flags, int64_t nb) {
     if (!s->finalized || nb != s->nbody) return -1;
     for (int64_t b = 0; b < nb; b++) {
         if (q) for (int k = 0; k < 8; k++) s->body_q[b * 8 + k] = (real)q[b * 8 + k];
         if (qd) for (int k = 0; k < 8; k++) s->body_qd[b * 8 + k] = (real)qd[b * 8 + k];
         if (com) for (int k = 0; k < 3; k++) s->body_com[b * 3 + k] = (real)com[b * 3 + k];
+        if (I) for (int k = 0; k < 9; k++) s->body_I[b * 9 + k] = (real)I[b * 9 + k];
         if (invI) for (int k = 0; k < 9; k++) s->body_invI[b * 9 + k] = (real)invI[b * 9 + k];
         if (invm) s->body_invm[b] = (real)invm[b];
         if (flags) s->body_flags[b] = flags[b];
     }
+    s->dyn_any = 0;
+    for (int64_t b = 0; b < nb; b++)
+        if (s->body_invm[b] > RF(0.0)) s->dyn_any = 1;
     return 0;
 }
+
+void or_get_bodies(const or_solver* s, float* q, float* qd) {
+    for (int64_t i = 0; i < s->nbody * 8; i++) {
+        if (q) q[i] = (float)s->body_q[i];
+        if (qd) qd[i] = (float)s->body_qd[i];
+    }
+}
+
+void or_set_body_params(or_solver* s, const or_body_params* p) { s->bp = *p; }
+int64_t or_rigid_contact_overflows(const or_solver* s) { return s->rc_overflow; }
 
 static inline v3 ld3(const real* a, int64_t i) { return mk(a[i * 3], a[i * 3 + 1], a[i * 3 + 2]); }
 static inline void st3(real* a, int64_t i, v3 v) { a[i * 3] = v.x; a[i * 3 + 1] = v.y; a[i * 3 + 2] = v.z; }
@@ -868,17 +924,17 @@ static inline v3 vert(const or_solver* s, uint32_t t, int k) {
 }
 
 /* generate_mesh_contacts.comp:181-414, one particle, appends up to nmesh contacts */
-static int mesh_contacts(const or_solver* s, int64_t tid, contact_t* out, int* stack_overflow) {
-    int nout = 0;
-    if ((s->flags[tid] & 1) == 0) return 0;
-    real margin = (real)s->cfg.soft_contact_margin;
+/* Closest-point query of point p (in the mesh's own frame) against mesh ci, the
+ * per-mesh body of generate_mesh_contacts.comp:197-411: returns 1 and the contact's
+ * surface point, surface velocity and normal when the mesh is within
+ * margin + shape margin + radius. */
+static int mesh_query(const or_solver* s, int64_t ci, v3 p, real radius, real margin, v3* o_bpos, v3* o_bvel,
+                      v3* o_nrm, int* stack_overflow) {
     real avg_edge = (real)s->meshes[0].avg_edge;
     real eps_md = avg_edge * RF(1e-3);
     real eps2 = eps_md * eps_md;
     const real PI_ = RF(3.14159265359);
-    v3 p = ld3(s->x, tid);
-    real radius = s->r[tid];
-    for (int64_t ci = 0; ci < s->nmesh; ci++) {
+    {
         real max_dist = margin + (real)s->meshes[ci].margin + radius;
         uint32_t stack[32];
         uint32_t sp = 0;
@@ -1012,14 +1068,53 @@ static int mesh_contacts(const or_solver* s, int64_t tid, contact_t* out, int* s
             real delta_len = exact_length(delta);
             v3 nrm = delta_len > RF(0.0) ? vmuls(exact_div(delta, delta_len), sign) : mk(RF(0.0), RF(0.0), RF(1.0));
             real d = delta_len * sign;
-            v3 body_pos = vfma_vs(vneg(nrm), d, p);
-            contact_t* c = &out[nout++];
-            c->part = (int32_t)tid;
-            c->shape = (int32_t)ci + 1;
-            c->bpos = body_pos;
-            c->bvel = shape_v;
-            c->nrm = nrm;
+            *o_bpos = vfma_vs(vneg(nrm), d, p);
+            *o_bvel = shape_v;
+            *o_nrm = nrm;
+            return 1;
         }
+    }
+    return 0;
+}
+
+static inline int posed(const or_solver* s, int64_t b) { return s->dyn_any && s->body_invm[b] > RF(0.0); }
+
+static void body_state(const real* q, int64_t b, v3* pos, q4* rot) {
+    *pos = mk(q[b * 8], q[b * 8 + 1], q[b * 8 + 2]);
+    rot->x = q[b * 8 + 4];
+    rot->y = q[b * 8 + 5];
+    rot->z = q[b * 8 + 6];
+    rot->w = q[b * 8 + 7];
+}
+
+/* generate_mesh_contacts.comp:197-411 for every mesh, in index order. A mesh whose
+ * body is dynamic holds its vertices in the body frame: the particle is taken into
+ * that frame with the inverse of the pose the solve applies
+ * (solve_particle_shape_contacts.comp:134), the contact point and surface velocity
+ * stay in the body frame (the solve transforms them, :134 and :155) and the normal
+ * is rotated to world space (the solve reads it as is, :138). */
+static int mesh_contacts(const or_solver* s, int64_t tid, contact_t* out, int* stack_overflow) {
+    int nout = 0;
+    if ((s->flags[tid] & 1) == 0) return 0;
+    v3 p = ld3(s->x, tid);
+    real radius = s->r[tid];
+    for (int64_t ci = 0; ci < s->nmesh; ci++) {
+        v3 q = p, bpos, bvel, nrm;
+        v3 pos;
+        q4 rot;
+        int pz = posed(s, ci);
+        if (pz) {
+            body_state(s->body_q, ci, &pos, &rot);
+            q = quat_rotate_inv(rot, vsub(p, pos));
+        }
+        if (!mesh_query(s, ci, q, radius, (real)s->cfg.soft_contact_margin, &bpos, &bvel, &nrm, stack_overflow))
+            continue;
+        contact_t* c = &out[nout++];
+        c->part = (int32_t)tid;
+        c->shape = (int32_t)ci + 1;
+        c->bpos = bpos;
+        c->bvel = bvel;
+        c->nrm = pz ? quat_rotate(rot, nrm) : nrm;
     }
     return nout;
 }
@@ -1231,8 +1326,14 @@ static void shape_contact(or_solver* s, int64_t tid, const real* X, const real* 
     s->delta[pi * 3 + 0] += fd.x;
     s->delta[pi * 3 + 1] += fd.y;
     s->delta[pi * 3 + 2] += fd.z;
-    /* body deltas (solve_particle_shape_contacts.comp:193-199) are only produced for
-     * dynamic bodies; the reference's bodies are static (scene.cpp:228-237) */
+    if (body >= 0 && s->body_invm[body] > RF(0.0)) { /* :193-199, kept per slot and summed per body later */
+        v3 delta_v = mk(delta_total.x / dt, delta_total.y / dt, delta_total.z / dt);
+        v3 delta_w = vcross(r, delta_v);
+        real* o = &s->bdel[tid * 6];
+        o[0] = -delta_v.x; o[1] = -delta_v.y; o[2] = -delta_v.z;
+        o[3] = -delta_w.x; o[4] = -delta_w.y; o[5] = -delta_w.z;
+        s->bvalid[tid] = 1;
+    }
 }
 
 static inline int32_t cell_index(int32_t x, int32_t y, int32_t z) { /* pp shader :67-79 */
@@ -1341,8 +1442,11 @@ static void restitution_contact(or_solver* s, int64_t tid) {
     v3 X_pos, X_com;
     q4 X_rot;
     body_pose(s, body, &X_pos, &X_rot, &X_com);
-    v3 X_pos_prev = X_pos; /* body_q_prev is bound to body_q (scene.cpp:577-580) */
+    /* body_q_prev is bound to body_q (scene.cpp:577-580) while every body is static;
+     * with dynamic bodies it is the state at the start of the substep */
+    v3 X_pos_prev = X_pos;
     q4 X_rot_prev = X_rot;
+    if (s->dyn_any && body >= 0) body_state(s->body_qp, body, &X_pos_prev, &X_rot_prev);
     v3 c_bpos = ld3(s->cbpos, tid);
     v3 bx = vadd(X_pos, quat_rotate(X_rot, c_bpos));
     v3 n = ld3(s->cnorm, tid);
@@ -1354,10 +1458,13 @@ static void restitution_contact(or_solver* s, int64_t tid) {
     v3 bv_contact = quat_rotate(X_rot_prev, ld3(s->cbvel, tid));
     v3 bv_old = bv_contact, bv_new = bv_contact;
     if (body >= 0) {
-        v3 bvo = mk(s->body_qd[body * 8], s->body_qd[body * 8 + 1], s->body_qd[body * 8 + 2]);
-        v3 bwo = mk(s->body_qd[body * 8 + 4], s->body_qd[body * 8 + 5], s->body_qd[body * 8 + 6]);
+        const real* qdo = s->dyn_any ? s->body_qdp : s->body_qd;
+        v3 bvo = mk(qdo[body * 8], qdo[body * 8 + 1], qdo[body * 8 + 2]);
+        v3 bwo = mk(qdo[body * 8 + 4], qdo[body * 8 + 5], qdo[body * 8 + 6]);
+        v3 bvn = mk(s->body_qd[body * 8], s->body_qd[body * 8 + 1], s->body_qd[body * 8 + 2]);
+        v3 bwn = mk(s->body_qd[body * 8 + 4], s->body_qd[body * 8 + 5], s->body_qd[body * 8 + 6]);
         bv_old = vadd(vadd(bvo, vcross(bwo, r)), bv_contact);
-        bv_new = vadd(vadd(bvo, vcross(bwo, r)), bv_contact);
+        bv_new = vadd(vadd(bvn, vcross(bwn, r)), bv_contact);
     }
     v3 vdo = vsub(v_old, bv_old);
     real rel_old = R_FMA(n.z, vdo.z, R_FMA(n.y, vdo.y, n.x * vdo.x));
@@ -1372,11 +1479,401 @@ static void restitution_contact(or_solver* s, int64_t tid) {
     }
 }
 
+/* ------------------------------------------------------------------------- */
+/* Rigid bodies (extension). Body math follows integrate_bodies.comp,          */
+/* apply_body_deltas.comp and solve_body_contact_positions.comp, which the     */
+/* reference compiles but never dispatches; their Warp-convention quaternion    */
+/* helpers are restated here as written there.                                 */
+/* ------------------------------------------------------------------------- */
+static inline v3 wq_rot(q4 q, v3 v) { /* v + 2*cross(q.xyz, cross(q.xyz, v) + v*q.w), integrate_bodies.comp:66-69 */
+    v3 qv = mk(q.x, q.y, q.z);
+    v3 t = vadd(vcross(qv, v), vmuls(v, q.w));
+    return vadd(v, vmuls(vcross(qv, t), RF(2.0)));
+}
+static inline v3 wq_rot_inv(q4 q, v3 v) { /* integrate_bodies.comp:71-73 */
+    q4 c = q;
+    c.x = -q.x;
+    c.y = -q.y;
+    c.z = -q.z;
+    return wq_rot(c, v);
+}
+static inline q4 wq_mul(q4 p, q4 q) { /* integrate_bodies.comp:57-63 */
+    q4 r;
+    v3 c = vcross(mk(p.x, p.y, p.z), mk(q.x, q.y, q.z));
+    r.w = p.w * q.w - vdot(mk(p.x, p.y, p.z), mk(q.x, q.y, q.z));
+    r.x = (p.w * q.x + q.w * p.x) + c.x;
+    r.y = (p.w * q.y + q.w * p.y) + c.y;
+    r.z = (p.w * q.z + q.w * p.z) + c.z;
+    return r;
+}
+static inline q4 q_axpy(q4 a, q4 b, real s) { /* a + b * s */
+    q4 r;
+    r.x = a.x + b.x * s;
+    r.y = a.y + b.y * s;
+    r.z = a.z + b.z * s;
+    r.w = a.w + b.w * s;
+    return r;
+}
+static inline q4 q_normalize(q4 a) { /* normalize(vec4) = v / length(v), IEEE sqrt and division */
+    real l = R_SQRT(((a.x * a.x + a.y * a.y) + a.z * a.z) + a.w * a.w);
+    q4 r;
+    r.x = a.x / l;
+    r.y = a.y / l;
+    r.z = a.z / l;
+    r.w = a.w / l;
+    return r;
+}
+/* 3x3 times vector, 9 floats column-major: col0*v.x + col1*v.y + col2*v.z (integrate_bodies.comp:51-54) */
+static inline v3 colmul(const real* m, v3 v) {
+    return mk((m[0] * v.x + m[3] * v.y) + m[6] * v.z, (m[1] * v.x + m[4] * v.y) + m[7] * v.z,
+              (m[2] * v.x + m[5] * v.y) + m[8] * v.z);
+}
+static inline void st_state(real* q, real* qd, int64_t b, v3 p, q4 r, v3 v, v3 w) {
+    q[b * 8 + 0] = p.x; q[b * 8 + 1] = p.y; q[b * 8 + 2] = p.z; q[b * 8 + 3] = RF(0.0);
+    q[b * 8 + 4] = r.x; q[b * 8 + 5] = r.y; q[b * 8 + 6] = r.z; q[b * 8 + 7] = r.w;
+    qd[b * 8 + 0] = v.x; qd[b * 8 + 1] = v.y; qd[b * 8 + 2] = v.z; qd[b * 8 + 3] = RF(0.0);
+    qd[b * 8 + 4] = w.x; qd[b * 8 + 5] = w.y; qd[b * 8 + 6] = w.z; qd[b * 8 + 7] = RF(0.0);
+}
+
+/* integrate_bodies.comp:75-130 for body b (body forces are zero) */
+static void integrate_body(const or_solver* s, int64_t b, real dt, const real* q, const real* qd, real* qo,
+                           real* qdo) {
+    if (s->body_flags[b] & 2) { /* KINEMATIC */
+        memcpy(qo + b * 8, q + b * 8, 8 * sizeof(real));
+        memcpy(qdo + b * 8, qd + b * 8, 8 * sizeof(real));
+        return;
+    }
+    v3 x0, w0, v0;
+    q4 r0;
+    body_state(q, b, &x0, &r0);
+    v0 = mk(qd[b * 8], qd[b * 8 + 1], qd[b * 8 + 2]);
+    w0 = mk(qd[b * 8 + 4], qd[b * 8 + 5], qd[b * 8 + 6]);
+    v3 f0 = mk(RF(0.0), RF(0.0), RF(0.0)), t0 = f0;
+    v3 com = ld3(s->body_com, b);
+    real inv_mass = s->body_invm[b];
+    v3 g = mk((real)s->cfg.gravity[0], (real)s->cfg.gravity[1], (real)s->cfg.gravity[2]);
+    v3 x_com = vadd(x0, wq_rot(r0, com));
+    real m_scale = inv_mass != RF(0.0) ? RF(1.0) : RF(0.0);
+    v3 v1 = vadd(v0, vmuls(vadd(vmuls(f0, inv_mass), vmuls(g, m_scale)), dt));
+    v3 x1 = vadd(x_com, vmuls(v1, dt));
+    v3 wb = wq_rot_inv(r0, w0);
+    v3 Iwb = colmul(&s->body_I[b * 9], wb);
+    v3 tb = vsub(wq_rot_inv(r0, t0), vcross(wb, Iwb));
+    v3 dwb = vmuls(colmul(&s->body_invI[b * 9], tb), dt);
+    v3 w1 = wq_rot(r0, vadd(wb, dwb));
+    q4 wq;
+    wq.x = w1.x; wq.y = w1.y; wq.z = w1.z; wq.w = RF(0.0);
+    q4 r1 = q_normalize(q_axpy(r0, wq_mul(wq, r0), RF(0.5) * dt));
+    w1 = vmuls(w1, RF(1.0) - (real)s->bp.angular_damping * dt);
+    st_state(qo, qdo, b, vsub(x1, wq_rot(r1, com)), r1, v1, w1);
+}
+
+/* apply_body_deltas.comp:58-119 for body b with the 6-float delta d (lin, ang) */
+static void apply_body_delta(const or_solver* s, int64_t b, real dt, const real* q, const real* qd, const real* d,
+                             real inv_weight, int use_weights, real* qo, real* qdo) {
+    real inv_m = s->body_invm[b];
+    if (inv_m == RF(0.0)) {
+        memcpy(qo + b * 8, q + b * 8, 8 * sizeof(real));
+        memcpy(qdo + b * 8, qd + b * 8, 8 * sizeof(real));
+        return;
+    }
+    v3 pos0, v0, w0;
+    q4 quat0;
+    body_state(q, b, &pos0, &quat0);
+    v0 = mk(qd[b * 8], qd[b * 8 + 1], qd[b * 8 + 2]);
+    w0 = mk(qd[b * 8 + 4], qd[b * 8 + 5], qd[b * 8 + 6]);
+    const real* I9 = &s->body_I[b * 9];
+    const real* Iinv9 = &s->body_invI[b * 9];
+    v3 com = ld3(s->body_com, b);
+    v3 dp = mk(d[0], d[1], d[2]), dq = mk(d[3], d[4], d[5]);
+    real weight = RF(1.0);
+    if (use_weights) {
+        if (inv_weight > RF(0.0)) weight = RF(1.0) / inv_weight;
+    }
+    dp = vmuls(dp, inv_m * weight);
+    v3 dq_w = vmuls(dq, weight);
+    v3 wb = wq_rot_inv(quat0, w0);
+    v3 dwb = colmul(Iinv9, wq_rot_inv(quat0, dq_w));
+    v3 tb = vadd(vcross(dwb, colmul(I9, vadd(wb, dwb))), vcross(wb, colmul(I9, dwb)));
+    v3 dw1 = wq_rot(quat0, vsub(dwb, vmuls(colmul(Iinv9, tb), dt)));
+    q4 dq4;
+    dq4.x = dw1.x * dt; dq4.y = dw1.y * dt; dq4.z = dw1.z * dt; dq4.w = RF(0.0);
+    q4 quat1 = q_normalize(q_axpy(quat0, wq_mul(dq4, quat0), RF(0.5)));
+    v3 x_com = vadd(pos0, wq_rot(quat0, com));
+    v3 p1 = vadd(x_com, vmuls(dp, dt));
+    p1 = vsub(p1, wq_rot(quat1, com));
+    v3 v1 = vadd(v0, dp), w1 = vadd(w0, dw1);
+    if (vlength(v1) < RF(1e-4)) v1 = mk(RF(0.0), RF(0.0), RF(0.0));
+    if (vlength(w1) < RF(1e-4)) w1 = mk(RF(0.0), RF(0.0), RF(0.0));
+    st_state(qo, qdo, b, p1, quat1, v1, w1);
+}
+
+/* compute_contact_constraint_delta, solve_body_contact_positions.comp:63-83 */
+static real contact_constraint_delta(real err, q4 qa, q4 qb, real m_inv_a, real m_inv_b, const real* ia,
+                                     const real* ib, v3 lin_a, v3 lin_b, v3 ang_a, v3 ang_b, real relax, real dt) {
+    real denom = RF(0.0);
+    denom += vdot(lin_a, lin_a) * m_inv_a;
+    denom += vdot(lin_b, lin_b) * m_inv_b;
+    v3 ra = wq_rot_inv(qa, ang_a), rb = wq_rot_inv(qb, ang_b);
+    denom += vdot(ra, colmul(ia, ra));
+    denom += vdot(rb, colmul(ib, rb));
+    real dl = -err;
+    if (denom > RF(0.0)) dl /= dt * denom;
+    return dl * relax;
+}
+
+typedef struct { v3 lin_a, ang_a, lin_b, ang_b; } rc_delta;
+
+/* solve_body_contact_positions.comp:97-265 for one contact of shape_a (the
+ * contact-impulse debug output is not kept). Returns 0 when it is skipped. */
+static int body_contact(const or_solver* s, const real* q, const real* qd, int32_t shape_a, const or_rcontact* c,
+                        real dt, rc_delta* o) {
+    static const real zero9[9] = {0};
+    int32_t shape_b = c->shape1;
+    if (shape_a == shape_b) return 0;
+    int32_t body_a = shape_a >= 0 ? s->shape_body[shape_a] : -1;
+    int32_t body_b = shape_b >= 0 ? s->shape_body[shape_b] : -1;
+    if (body_a == body_b) return 0;
+    v3 pos_a = mk(RF(0.0), RF(0.0), RF(0.0)), pos_b = pos_a;
+    q4 quat_a = {RF(0.0), RF(0.0), RF(0.0), RF(1.0)}, quat_b = quat_a;
+    if (body_a >= 0) body_state(q, body_a, &pos_a, &quat_a);
+    if (body_b >= 0) body_state(q, body_b, &pos_b, &quat_b);
+    v3 bx_a = vadd(wq_rot(quat_a, c->p0), pos_a);
+    v3 bx_b = vadd(wq_rot(quat_b, c->p1), pos_b);
+    v3 n = c->n;
+    real d = vdot(n, vsub(bx_b, bx_a)) - (c->th0 + c->th1);
+    if (d >= RF(0.0)) return 0;
+    real m_inv_a = RF(0.0), m_inv_b = RF(0.0);
+    const real *ia = zero9, *ib = zero9;
+    v3 com_a = mk(RF(0.0), RF(0.0), RF(0.0)), com_b = com_a, omega_a = com_a, omega_b = com_a;
+    if (body_a >= 0) {
+        m_inv_a = s->body_invm[body_a];
+        ia = &s->body_invI[body_a * 9];
+        com_a = ld3(s->body_com, body_a);
+        omega_a = mk(qd[body_a * 8 + 4], qd[body_a * 8 + 5], qd[body_a * 8 + 6]);
+    }
+    if (body_b >= 0) {
+        m_inv_b = s->body_invm[body_b];
+        ib = &s->body_invI[body_b * 9];
+        com_b = ld3(s->body_com, body_b);
+        omega_b = mk(qd[body_b * 8 + 4], qd[body_b * 8 + 5], qd[body_b * 8 + 6]);
+    }
+    /* material averages (:159-178): every shape carries shape_material_mu and the
+     * torsional / rolling coefficients of the body parameters */
+    int nz = 0;
+    real mu = RF(0.0), mu_t = RF(0.0), mu_r = RF(0.0);
+    if (shape_a >= 0) { nz += 1; mu += s->shape_mu[shape_a]; mu_t += (real)s->bp.rigid_mu_torsional; mu_r += (real)s->bp.rigid_mu_rolling; }
+    if (shape_b >= 0) { nz += 1; mu += s->shape_mu[shape_b]; mu_t += (real)s->bp.rigid_mu_torsional; mu_r += (real)s->bp.rigid_mu_rolling; }
+    if (nz > 0) {
+        mu /= (real)nz;
+        mu_t /= (real)nz;
+        mu_r /= (real)nz;
+    }
+    v3 r_a = vsub(bx_a, vadd(wq_rot(quat_a, com_a), pos_a));
+    v3 r_b = vsub(bx_b, vadd(wq_rot(quat_b, com_b), pos_b));
+    v3 angular_a = vneg(vcross(r_a, n));
+    v3 angular_b = vcross(r_b, n);
+    real relax = (real)s->bp.rigid_contact_relaxation;
+    real lambda_n = contact_constraint_delta(d, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, vneg(n), n, angular_a,
+                                             angular_b, relax, dt);
+    v3 lin_da = vmuls(vneg(n), lambda_n), lin_db = vmuls(n, lambda_n);
+    v3 ang_da = vmuls(angular_a, lambda_n), ang_db = vmuls(angular_b, lambda_n);
+    if (mu > RF(0.0)) {
+        v3 sbx_a = vadd(wq_rot(quat_a, vadd(c->p0, c->off0)), pos_a);
+        v3 sbx_b = vadd(wq_rot(quat_b, vadd(c->p1, c->off1)), pos_b);
+        v3 delta = vsub(sbx_b, sbx_a);
+        v3 fdel = vsub(delta, vmuls(n, vdot(n, delta)));
+        v3 fr_a = vsub(sbx_a, vadd(wq_rot(quat_a, com_a), pos_a));
+        v3 fr_b = vsub(sbx_b, vadd(wq_rot(quat_b, com_b), pos_b));
+        v3 rel = mk(RF(0.0), RF(0.0), RF(0.0));
+        if (body_a >= 0 && (s->body_flags[body_a] & 2)) {
+            v3 va = vadd(mk(qd[body_a * 8], qd[body_a * 8 + 1], qd[body_a * 8 + 2]), vcross(omega_a, fr_a));
+            rel = vsub(rel, vsub(va, vmuls(n, vdot(n, va))));
+        }
+        if (body_b >= 0 && (s->body_flags[body_b] & 2)) {
+            v3 vb = vadd(mk(qd[body_b * 8], qd[body_b * 8 + 1], qd[body_b * 8 + 2]), vcross(omega_b, fr_b));
+            rel = vadd(rel, vsub(vb, vmuls(n, vdot(n, vb))));
+        }
+        fdel = vadd(fdel, vmuls(rel, dt));
+        real err = vlength(fdel);
+        if (err > RF(0.0)) {
+            v3 perp = vnormalize(fdel);
+            v3 angular_a_fr = vneg(vcross(fr_a, perp));
+            v3 angular_b_fr = vcross(fr_b, perp);
+            real lambda_fr = contact_constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, vneg(perp), perp,
+                                                      angular_a_fr, angular_b_fr, relax, dt);
+            lambda_fr = gmax(lambda_fr, -lambda_n * mu);
+            lin_da = vsub(lin_da, vmuls(perp, lambda_fr));
+            lin_db = vadd(lin_db, vmuls(perp, lambda_fr));
+            ang_da = vadd(ang_da, vmuls(angular_a_fr, lambda_fr));
+            ang_db = vadd(ang_db, vmuls(angular_b_fr, lambda_fr));
+        }
+    }
+    v3 delta_omega = vsub(omega_b, omega_a);
+    v3 zero = mk(RF(0.0), RF(0.0), RF(0.0));
+    if (mu_t > RF(0.0)) {
+        real err = vdot(delta_omega, n) * dt;
+        if (R_FABS(err) > RF(0.0)) {
+            real lt = contact_constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, zero, zero, vneg(n), n,
+                                               relax, dt);
+            lt = gclamp(lt, -lambda_n * mu_t, lambda_n * mu_t);
+            ang_da = vsub(ang_da, vmuls(n, lt));
+            ang_db = vadd(ang_db, vmuls(n, lt));
+        }
+    }
+    if (mu_r > RF(0.0)) {
+        delta_omega = vsub(delta_omega, vmuls(n, vdot(n, delta_omega)));
+        real err = vlength(delta_omega) * dt;
+        if (err > RF(0.0)) {
+            v3 roll_n = vnormalize(delta_omega);
+            real lr = contact_constraint_delta(err, quat_a, quat_b, m_inv_a, m_inv_b, ia, ib, zero, zero,
+                                               vneg(roll_n), roll_n, relax, dt);
+            lr = gmax(lr, -lambda_n * mu_r);
+            ang_da = vsub(ang_da, vmuls(roll_n, lr));
+            ang_db = vadd(ang_db, vmuls(roll_n, lr));
+        }
+    }
+    o->lin_a = lin_da;
+    o->ang_a = ang_da;
+    o->lin_b = lin_db;
+    o->ang_b = ang_db;
+    return 1;
+}
+
+static int64_t mesh_vert_off(const or_solver* s, int64_t m) {
+    int64_t o = 0;
+    for (int64_t c = 0; c < m; c++) o += s->meshes[c].nv;
+    return o;
+}
+
+/* Rigid contact generation (no reference counterpart: nothing in the reference
+ * generates the contacts solve_body_contact_positions.comp reads). Every vertex of
+ * a dynamic body's mesh is tested against the ground plane and, with the particle
+ * closest-point query of generate_mesh_contacts.comp at radius 0, against every
+ * other mesh; up to RC_CAP contacts per vertex, plane first, then meshes in index
+ * order. Uses the body states at the start of the substep. */
+static void rigid_collide(or_solver* s) {
+    real margin = (real)s->bp.rigid_contact_margin;
+    real alt = (real)s->cfg.ground_plane_altitude;
+    int ovf = 0;
+    for (int64_t a = 0; a < s->nmesh; a++) {
+        if (!posed(s, a)) continue;
+        v3 pos_a;
+        q4 rot_a;
+        body_state(s->body_q, a, &pos_a, &rot_a);
+        real th0 = (real)s->meshes[a].margin;
+        int64_t vo = mesh_vert_off(s, a);
+        for (int64_t v = 0; v < s->meshes[a].nv; v++) {
+            int64_t gv = vo + v;
+            v3 V = ld3f(s->all_verts, gv);
+            v3 P = vadd(pos_a, quat_rotate(rot_a, V));
+            int cnt = 0;
+            or_rcontact* out = &s->rc[gv * RC_CAP];
+            if (s->cfg.has_ground_plane) {
+                real dist = P.z - alt;
+                if (dist < margin) {
+                    or_rcontact* c = &out[cnt++];
+                    c->shape1 = 0;
+                    c->n = mk(RF(0.0), RF(0.0), RF(-1.0));
+                    c->p0 = V;
+                    c->p1 = mk(P.x, P.y, alt);
+                    c->th0 = th0;
+                    c->th1 = RF(0.0);
+                    c->off0 = quat_rotate_inv(rot_a, vmuls(c->n, th0));
+                    c->off1 = vmuls(c->n, -c->th1);
+                }
+            }
+            for (int64_t m = 0; m < s->nmesh; m++) {
+                if (m == a) continue;
+                v3 Q = P, bpos, bvel, nrm, pos_m;
+                q4 rot_m;
+                int pz = posed(s, m);
+                if (pz) {
+                    body_state(s->body_q, m, &pos_m, &rot_m);
+                    Q = quat_rotate_inv(rot_m, vsub(P, pos_m));
+                }
+                if (!mesh_query(s, m, Q, RF(0.0), margin, &bpos, &bvel, &nrm, &ovf)) continue;
+                if (cnt >= RC_CAP) {
+                    s->rc_overflow++;
+                    continue;
+                }
+                or_rcontact* c = &out[cnt++];
+                real th1 = (real)s->meshes[m].margin;
+                c->shape1 = (int32_t)m + 1;
+                c->n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
+                c->p0 = V;
+                c->p1 = bpos;
+                c->th0 = th0;
+                c->th1 = th1;
+                c->off0 = quat_rotate_inv(rot_a, vmuls(c->n, th0));
+                c->off1 = pz ? quat_rotate_inv(rot_m, vmuls(c->n, -th1)) : vmuls(c->n, -th1);
+            }
+            s->rc_cnt[gv] = cnt;
+        }
+    }
+    if (ovf) fprintf(stderr, "oracle: BVH traversal stack overflow (push dropped)\n");
+}
+
+/* One body pass of an iteration: particle-contact body deltas (summed per body in
+ * contact-slot order) applied without constraint weights, then the rigid contacts
+ * solved on that state and applied with weights (the order of one XPBD iteration). */
+static void bodies_iterate(or_solver* s, real dt) {
+    int64_t nb = s->nbody;
+    real* d6 = xcalloc((size_t)nb * 6, sizeof(real));
+    real* wc = xcalloc((size_t)nb, sizeof(real));
+    int64_t count = s->ccount_raw < s->cmax ? s->ccount_raw : s->cmax;
+    for (int64_t t = 0; t < count; t++) {
+        if (!s->bvalid[t]) continue;
+        int32_t b = s->shape_body[s->cshape[t]];
+        for (int k = 0; k < 6; k++) d6[b * 6 + k] += s->bdel[t * 6 + k];
+    }
+    for (int64_t b = 0; b < nb; b++)
+        apply_body_delta(s, b, dt, s->body_q, s->body_qd, &d6[b * 6], RF(0.0), 0, s->body_qm, s->body_qdm);
+    memset(d6, 0, sizeof(real) * 6 * (size_t)nb);
+    for (int64_t x = 0; x < nb; x++) {
+        if (!posed(s, x)) continue;
+        v3 lin = mk(RF(0.0), RF(0.0), RF(0.0)), ang = lin;
+        real cnt = RF(0.0);
+        rc_delta o;
+        int64_t vo = mesh_vert_off(s, x);
+        for (int64_t v = 0; v < s->meshes[x].nv; v++) /* x as shape0: its own vertices */
+            for (int j = 0; j < s->rc_cnt[vo + v]; j++)
+                if (body_contact(s, s->body_qm, s->body_qdm, (int32_t)x + 1, &s->rc[(vo + v) * RC_CAP + j], dt, &o)) {
+                    lin = vadd(lin, o.lin_a);
+                    ang = vadd(ang, o.ang_a);
+                    cnt += RF(1.0);
+                }
+        for (int64_t a = 0; a < nb; a++) { /* x as shape1: other bodies' vertices on x's mesh */
+            if (a == x || !posed(s, a)) continue;
+            int64_t ao = mesh_vert_off(s, a);
+            for (int64_t v = 0; v < s->meshes[a].nv; v++)
+                for (int j = 0; j < s->rc_cnt[ao + v]; j++) {
+                    const or_rcontact* c = &s->rc[(ao + v) * RC_CAP + j];
+                    if (c->shape1 != (int32_t)x + 1) continue;
+                    if (body_contact(s, s->body_qm, s->body_qdm, (int32_t)a + 1, c, dt, &o)) {
+                        lin = vadd(lin, o.lin_b);
+                        ang = vadd(ang, o.ang_b);
+                        cnt += RF(1.0);
+                    }
+                }
+        }
+        d6[x * 6 + 0] = lin.x; d6[x * 6 + 1] = lin.y; d6[x * 6 + 2] = lin.z;
+        d6[x * 6 + 3] = ang.x; d6[x * 6 + 4] = ang.y; d6[x * 6 + 5] = ang.z;
+        wc[x] = cnt;
+    }
+    for (int64_t b = 0; b < nb; b++)
+        apply_body_delta(s, b, dt, s->body_qm, s->body_qdm, &d6[b * 6], wc[b], s->bp.rigid_contact_con_weighting,
+                         s->body_q, s->body_qd);
+    free(d6);
+    free(wc);
+}
+
 static void iterate(or_solver* s, real dt, int iterations, real inv) { /* scene.cpp:934-980 */
     int64_t n = s->n;
     int64_t count = s->ccount_raw < s->cmax ? s->ccount_raw : s->cmax;
     for (int it = 0; it < iterations; it++) {
         memset(s->delta, 0, sizeof(real) * 3 * (size_t)n);
+        if (s->dyn_any) memset(s->bvalid, 0, (size_t)s->cmax);
         for (int64_t t = 0; t < count; t++) shape_contact(s, t, s->x, s->v, dt);
 #ifdef _OPENMP
 #pragma omp parallel for OMP_THREADS schedule(static, 256)
@@ -1385,6 +1882,7 @@ static void iterate(or_solver* s, real dt, int iterations, real inv) { /* scene.
         apply_deltas(s, s->x, s->v, dt);
         real* t0 = s->x; s->x = s->xo; s->xo = t0;
         real* t1 = s->v; s->v = s->vo; s->vo = t1;
+        if (s->dyn_any) bodies_iterate(s, dt);
     }
 }
 
@@ -1402,7 +1900,14 @@ int or_step(or_solver* s, float dt, int substeps, int iterations) { /* scene.cpp
     real sdt = (real)sdt_f, inv = (real)inv_f;
     for (int sub = 0; sub < substeps; sub++) {
         collide(s);
+        if (s->dyn_any) rigid_collide(s);
         integrate(s, sdt);
+        if (s->dyn_any) {
+            memcpy(s->body_qp, s->body_q, sizeof(real) * 8 * (size_t)s->nbody);
+            memcpy(s->body_qdp, s->body_qd, sizeof(real) * 8 * (size_t)s->nbody);
+            for (int64_t b = 0; b < s->nbody; b++)
+                integrate_body(s, b, sdt, s->body_qp, s->body_qdp, s->body_q, s->body_qd);
+        }
         build_grid(s, inv);
         iterate(s, sdt, iterations, inv);
         restitution(s);

@@ -76,12 +76,28 @@ int or_update_mesh(or_solver* s, int64_t mesh_index, const float* verts, int64_t
                    const float* vels);
 int or_set_particles(or_solver* s, const float* q, const float* qd, const float* inv_mass,
                      const float* radii, const int32_t* flags, int64_t n);
-/* Rigid-body state of the static body table (one body per mesh, scene.cpp:220-238).
- * q: 8 floats/body (pos xyz, pad, quat xyzw); qd: 8 floats/body (lin xyz, pad, ang xyz, pad);
- * com: 3/body; inv_I: 9/body row-major as read by solve_particle_shape_contacts.comp:46-48;
- * inv_m, flags: 1/body. Any pointer may be NULL to keep the current values. */
-int or_set_bodies(or_solver* s, const float* q, const float* qd, const float* com,
-                  const float* inv_I, const float* inv_m, const int32_t* flags, int64_t n_bodies);
+/* Rigid bodies (an extension: the reference's body table is static,
+ * scene.cpp:220-238). Body b belongs to mesh b (shape b + 1). q: 8 floats/body
+ * (pos xyz, pad, quat xyzw); qd: 8 floats/body (lin xyz, pad, ang xyz, pad);
+ * com: 3/body; inertia and inv_inertia: 9/body (symmetric, so the row-major read
+ * of solve_particle_shape_contacts.comp:46-48 and the column-major reads of
+ * integrate_bodies.comp:51-54, apply_body_deltas.comp:53-55 agree); inv_m and
+ * flags: 1/body. Any pointer may be NULL to keep the current values. A body with
+ * inv_m > 0 is dynamic: its mesh's vertices are in the body frame, and every
+ * substep integrates it and applies particle and rigid contact deltas to it. */
+int or_set_bodies(or_solver* s, const float* q, const float* qd, const float* com, const float* inertia,
+                  const float* inv_inertia, const float* inv_m, const int32_t* flags, int64_t n_bodies);
+void or_get_bodies(const or_solver* s, float* q, float* qd);
+typedef struct or_body_params {
+    float angular_damping;            /* integrate_bodies.comp push constant */
+    float rigid_contact_margin;       /* vertex-vs-shape contact generation distance */
+    float rigid_contact_relaxation;   /* solve_body_contact_positions.comp push constant */
+    int32_t rigid_contact_con_weighting; /* apply_body_deltas.comp use_constraint_weights */
+    float rigid_mu_torsional;
+    float rigid_mu_rolling;
+} or_body_params;
+void or_set_body_params(or_solver* s, const or_body_params* p);
+int64_t or_rigid_contact_overflows(const or_solver* s);
 
 int or_step(or_solver* s, float dt, int substeps, int iterations);
 int or_collide_only(or_solver* s);

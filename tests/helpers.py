@@ -17,10 +17,11 @@ def config_for(scene, **overrides):
     return cfg
 
 
-def make_pair(scene, cfg, max_contacts=0, gpu=True, precision="f32"):
+def make_pair(scene, cfg, max_contacts=0, gpu=True, precision="f32", body_params=None):
     """(gpu solver or None, oracle solver) with identical inputs."""
     import vkxpbd
 
+    body_params = dict(body_params or {})
     orc = O.OracleSolver(cfg, scene.n, max_contacts, precision=precision)
     g = None
     if gpu:
@@ -33,6 +34,14 @@ def make_pair(scene, cfg, max_contacts=0, gpu=True, precision="f32"):
     orc.finalize_meshes()
     if g is not None:
         g.finalize_meshes()
+    if getattr(scene, "bodies", None) is not None:
+        b = scene.bodies
+        bargs = (b.q, b.qd, b.com, b.inertia, b.inv_inertia, b.inv_mass, b.flags)
+        orc.set_bodies(*bargs)
+        orc.set_body_params(**body_params)
+        if g is not None:
+            g.set_bodies(*bargs)
+            g.set_body_params(**body_params)
     args = (scene.positions, scene.velocities, scene.inv_mass, scene.radii, scene.flags)
     orc.set_particles(*args)
     if g is not None:
@@ -65,3 +74,13 @@ def mesh_pile(n_side=16, hf=32, **kw):
     v, t = scenes.heightfield(hf, extent=0.4, amplitude=0.02)
     sc.meshes.append((v, t, 0.0, None))
     return sc
+
+
+def box_scene(n_side=6, boxes=((0.05, 0.04, 0.03),), positions=((0.0, 0.0, 0.25),), seed=3, hf=None, **kw):
+    """A small particle pile plus dynamic boxes (random orientations) dropped from above."""
+    sc = scenes.pile(dims=(n_side, n_side, n_side), spacing=0.01, radius=0.005, jitter=0.001, bottom_z=0.02, **kw)
+    if hf:
+        v, t = scenes.heightfield(hf, extent=0.4, amplitude=0.02)
+        sc.meshes.append((v, t, 0.0, None))
+    rng = np.random.default_rng(seed)
+    return scenes.add_boxes(sc, list(boxes), list(positions), scenes.random_quats(len(boxes), rng))
