@@ -198,6 +198,15 @@ def run_gpu(args):
     import torch
 
     rank, world, local = dist_env()
+    if args.only and "main" not in args.only.split(","):  # sub-measurements alone (not the contract line)
+        dev = torch.device("cuda", local)
+        parts = {}
+        if "batched" in args.only:
+            parts["batched"] = measure_batched(args, dev, None)
+        if "mixed" in args.only:
+            parts["mixed"] = measure_mixed(args, dev)
+        print(json.dumps(parts), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
 
@@ -295,9 +304,14 @@ def run_gpu(args):
         "stage_ms_per_substep": {k: round(v / max(prof_substeps, 1), 5) for k, v in stage_ms.items() if v > 0},
         "e2e": e2e, "gpu_launches": int(stats["kernels_per_frame"] * args.steps), "clocks": clk,
     }
-    if rank == 0 and args.batched_scenes > 0:
-        del solver
-        result["batched"] = measure_batched(args, dev, flush)
+    del solver
+    for name, on, fn in (("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev, flush)),
+                         ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev))):
+        if rank == 0 and on:
+            try:
+                result[name] = fn()
+            except RuntimeError as e:  # a device-side table overflow is reported, not fatal to the line
+                result[name] = {"error": str(e)}
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_sample(sc, cfg, x_snap, v_snap, budget_s=args.cpu_budget)
     if rank == 0:
@@ -399,6 +413,80 @@ def measure_batched(args, dev, flush):
                     "around stepping; boxes (0-16 per scene) not included"}
 
 
+def stage_table(stage_ms, prof_substeps, n, peak):
+    out = {}
+    for k, v in stage_ms.items():
+        if v <= 0:
+            continue
+        launches = prof_substeps * (ITERATIONS if k.startswith("3.") else 1)
+        us = v / launches * 1e3
+        st = {"us_per_launch": round(us, 2)}
+        if k in ALG_BYTES:
+            gbs = ALG_BYTES[k] * n / (us * 1e-6) / 1e9
+            st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
+        out[k] = st
+    return out
+
+
+def measure_mixed(args, dev):
+    """Mixed particles and rigid bodies: 1,048,576 particles (128x128x64 lattice, r 0.005) on the
+    plane and the 256x256 heightfield plus 1,024 dynamic boxes (half-extents U[0.02, 0.08],
+    density 1000, orientations uniform on SO(3), seed 45), 10 substeps x 1 iteration per frame,
+    body contact solve and body delta apply on. Device-timed frames after a pre-roll."""
+    import torch
+    import vkxpbd
+    from vkxpbd import scenes
+
+    sc = scenes.mixed()
+    cfg = vkxpbd.SolverConfig()
+    sc.apply_config(cfg)
+    cfg.device_index = dev.index
+    s = vkxpbd.XpbdSolver()
+    s.init(cfg, sc.n)
+    for (v, t, margin, wt) in sc.meshes:
+        s.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
+    s.finalize_meshes()
+    b = sc.bodies
+    s.set_bodies(b.q, b.qd, b.com, b.inertia, b.inv_inertia, b.inv_mass, b.flags)
+    s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+    for _ in range(args.mixed_preroll):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    for _ in range(args.warmup):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
+    frames = args.mixed_frames
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    torch.cuda.synchronize(dev)
+    for k in range(frames):
+        ev[k][0].record(stream)
+        s.step_async(DT, SUBSTEPS, ITERATIONS)
+        ev[k][1].record(stream)
+    s.sync()
+    torch.cuda.synchronize(dev)
+    dev_s = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
+    launches = s.get_frame_stats()["kernels_per_frame"]
+    s.set_profiling(True)
+    s.reset_stage_times()
+    for _ in range(min(frames, 5)):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    stage_ms, prof_substeps = s.get_stage_times()
+    s.set_profiling(False)
+    peak, peak_kind = measured_peak_hbm()
+    work = sc.n * SUBSTEPS * frames
+    step_gbs = STEP_ALG_BYTES * work / dev_s / 1e9
+    bq, bqd = s.get_body_q()[1:], s.get_body_qd()[1:]
+    return {"workload": "mixed", "particles": sc.n, "boxes": len(sc.meshes) - 1,
+            "triangles": int(sum(m[1].shape[0] for m in sc.meshes)), "preroll_frames": args.mixed_preroll,
+            "frames": frames, "value": work / dev_s, "unit": UNIT, "ms_per_frame": dev_s / frames * 1e3,
+            "launches_per_frame": int(launches),
+            "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
+                              "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
+                              "peak_source": peak_kind},
+            "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
+            "boxes_finite": bool(np.isfinite(bq).all() and np.isfinite(bqd).all()),
+            "box_height_range": [round(float(np.nanmin(bq[:, 2])), 3), round(float(np.nanmax(bq[:, 2])), 3)]}
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path: the oracle port on all host threads."""
     rank, world, _ = dist_env()
@@ -445,6 +533,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-scenes", type=int, default=512, help="0 skips the batched-scenes measurement")
     ap.add_argument("--batched-frames", type=int, default=10)
+    ap.add_argument("--mixed-frames", type=int, default=10, help="0 skips the particles + boxes measurement")
+    ap.add_argument("--mixed-preroll", type=int, default=20)
+    ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed (default all)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -175,6 +175,7 @@ typedef struct xpbd_body_params {
     int32_t rigid_contact_con_weighting; /* apply_body_deltas.comp use_constraint_weights */
     float rigid_mu_torsional;
     float rigid_mu_rolling;
+    int32_t particle_contact_con_weighting; /* particle-contact body deltas averaged per body */
 } xpbd_body_params;
 void xpbd_body_params_default(xpbd_body_params* p);
 int xpbd_set_body_params(xpbd_solver* s, const xpbd_body_params* p);

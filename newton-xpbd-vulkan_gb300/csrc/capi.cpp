@@ -273,6 +273,7 @@ void xpbd_body_params_default(xpbd_body_params* p) {
     p->rigid_contact_con_weighting = 1;
     p->rigid_mu_torsional = 0.0f;
     p->rigid_mu_rolling = 0.0f;
+    p->particle_contact_con_weighting = 1;
 }
 
 int xpbd_set_body_params(xpbd_solver* s, const xpbd_body_params* p) {

@@ -230,15 +230,19 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
 }
 
 // ---------------------------------------------------------------- rigid contacts ----
-// One thread per vertex of a dynamic body's mesh: the vertex against the ground plane,
+// One warp per vertex of a dynamic body's mesh: the vertex against the ground plane,
 // then the closest-point query of generate_mesh_contacts.comp (radius 0, the rigid
 // margin in place of the soft contact margin) against the static meshes and the
-// overlapping dynamic bodies' meshes, in mesh index order. Slot record (5 float4):
-// (p0, shape1 bits), (p1, thickness0), (normal, thickness1), (offset0, 0), (offset1, 0).
-__global__ void k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp, int n_vert,
-                                 DeviceStatus* st) {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n_vert) return;
+// overlapping dynamic bodies' meshes, in mesh index order (lane 0 merges the two
+// ascending lists 32 candidates at a time, each lane queries one). The first
+// kRigidSlots contacts are kept. Slot record (5 float4): (p0, shape1 bits),
+// (p1, thickness0), (normal, thickness1), (offset0, 0), (offset1, 0).
+__global__ void __launch_bounds__(128) k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
+                                                       DeviceStatus* st) {
+    __shared__ int s_cand[4][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (d >= rt.n_vert) return;  // uniform per warp
     const float4 lv = rt.dv_local[d];
     const int a = __float_as_int(lv.w);
     const v3 V = xyz(lv);
@@ -252,14 +256,16 @@ __global__ void k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, R
     if (rp.plane) {
         const float dist = P.z - rp.altitude;
         if (dist < rp.margin) {
-            const v3 n = mk3(0.0f, 0.0f, -1.0f);
-            const float th1 = 0.0f;
-            const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0)), o1 = vmuls(n, -th1);
-            out[0] = make_float4(V.x, V.y, V.z, __int_as_float(0));
-            out[1] = make_float4(P.x, P.y, rp.altitude, th0);
-            out[2] = make_float4(n.x, n.y, n.z, th1);
-            out[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
-            out[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+            if (lane == 0) {
+                const v3 n = mk3(0.0f, 0.0f, -1.0f);
+                const float th1 = 0.0f;
+                const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0)), o1 = vmuls(n, -th1);
+                out[0] = make_float4(V.x, V.y, V.z, __int_as_float(0));
+                out[1] = make_float4(P.x, P.y, rp.altitude, th0);
+                out[2] = make_float4(n.x, n.y, n.z, th1);
+                out[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+                out[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+            }
             cnt = 1;
         }
     }
@@ -268,61 +274,93 @@ __global__ void k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, R
     const int ia = rt.dyn_index[a];
     const int pc = rt.partner_count[ia];
     const int* partners = rt.partners + ia * kPartnerCap;
-    int si = 0, pi = 0;
-    while (si < mt.walk_count || pi < pc) {
-        const int ms = si < mt.walk_count ? mt.walk_list[si] : 0x7fffffff;
-        const int mp = pi < pc ? partners[pi] : 0x7fffffff;
-        int m;
-        bool pz;
-        if (ms < mp) {
-            m = ms;
-            si++;
-            pz = false;
-        } else {
-            m = mp;
-            pi++;
-            pz = true;
+    const int total = mt.walk_count + pc;
+    int si = 0, pi = 0;  // merge cursors (lane 0)
+    for (int c0 = 0; c0 < total; c0 += 32) {
+        if (lane == 0) {
+            for (int k = 0; k < 32; k++) {
+                int m = -1;
+                if (si < mt.walk_count || pi < pc) {
+                    const int ms = si < mt.walk_count ? mt.walk_list[si] : 0x7fffffff;
+                    const int mp = pi < pc ? partners[pi] : 0x7fffffff;
+                    if (ms < mp) {
+                        m = ms;
+                        si++;
+                    } else {
+                        m = mp;
+                        pi++;
+                    }
+                }
+                s_cand[warp][k] = m;
+            }
         }
-        if (m == a) continue;
-        v3 Q = P, pos_m = mk3(0.0f, 0.0f, 0.0f);
+        __syncwarp();
+        const int m = s_cand[warp][lane];
+        __syncwarp();
+        bool found = false;
+        v3 bpos, nrm, pos_m = mk3(0.0f, 0.0f, 0.0f);
         q4 rot_m;
         rot_m.x = rot_m.y = rot_m.z = 0.0f;
         rot_m.w = 1.0f;
-        if (pz) {
-            pos_m = xyz(ba.q[m * 2]);
-            rot_m = f4q(ba.q[m * 2 + 1]);
-            Q = quat_rotate_inv(rot_m, vsub(P, pos_m));
+        bool pz = false;
+        if (m >= 0 && m != a) {
+            pz = rt.dyn_index[m] >= 0;
+            bool near = true;
+            if (pz) {  // the vertex is far outside the partner's world box: no contact within the margin
+                const int im = rt.dyn_index[m];
+                const float4 l = rt.wbox[im * 2], h = rt.wbox[im * 2 + 1];
+                const float e = rp.margin + l.w + rt.pad;
+                near = P.x >= l.x - e && P.x <= h.x + e && P.y >= l.y - e && P.y <= h.y + e && P.z >= l.z - e &&
+                       P.z <= h.z + e;
+            }
+            if (near) {
+                v3 Q = P;
+                if (pz) {
+                    pos_m = xyz(ba.q[m * 2]);
+                    rot_m = f4q(ba.q[m * 2 + 1]);
+                    Q = quat_rotate_inv(rot_m, vsub(P, pos_m));
+                }
+                v3 bvel;
+                found = mesh_query(rmt, m, 0.0f, Q, bpos, bvel, nrm, stack_ovf);
+            }
         }
-        v3 bpos, bvel, nrm;
-        if (!mesh_query(rmt, m, 0.0f, Q, bpos, bvel, nrm, stack_ovf)) continue;
-        if (cnt >= kRigidSlots) {
-            ovf = true;
-            continue;
+        const uint32_t fm = __ballot_sync(0xffffffffu, found);
+        if (found) {
+            const int slot = cnt + __popc(fm & lanemask_lt());
+            if (slot < kRigidSlots) {
+                const float th1 = mt.margins[m];
+                const v3 n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
+                const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0));
+                const v3 o1 = pz ? quat_rotate_inv(rot_m, vmuls(n, -th1)) : vmuls(n, -th1);
+                float4* o = out + slot * 5;
+                o[0] = make_float4(V.x, V.y, V.z, __int_as_float(m + 1));
+                o[1] = make_float4(bpos.x, bpos.y, bpos.z, th0);
+                o[2] = make_float4(n.x, n.y, n.z, th1);
+                o[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+                o[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+            }
         }
-        const float th1 = mt.margins[m];
-        const v3 n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
-        const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0));
-        const v3 o1 = pz ? quat_rotate_inv(rot_m, vmuls(n, -th1)) : vmuls(n, -th1);
-        float4* o = out + cnt * 5;
-        o[0] = make_float4(V.x, V.y, V.z, __int_as_float(m + 1));
-        o[1] = make_float4(bpos.x, bpos.y, bpos.z, th0);
-        o[2] = make_float4(n.x, n.y, n.z, th1);
-        o[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
-        o[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
-        cnt++;
+        cnt += __popc(fm);
     }
-    rt.rc_count[d] = cnt;
-    if (ovf) atomicOr(&st->error_bits, kErrBodyOverflow);
-    if (stack_ovf) {
-        atomicOr(&st->error_bits, kErrStackOverflow);
-        atomicAdd(&st->stack_overflows, 1u);
+    if (cnt > kRigidSlots) {
+        ovf = true;
+        cnt = kRigidSlots;
+    }
+    const bool any_stack = __any_sync(0xffffffffu, stack_ovf);
+    if (lane == 0) {
+        rt.rc_count[d] = cnt;
+        if (ovf) atomicAdd(&st->rigid_slot_overflows, 1u);  // extra contacts dropped, in order
+        if (any_stack) {
+            atomicOr(&st->error_bits, kErrStackOverflow);
+            atomicAdd(&st->stack_overflows, 1u);
+        }
     }
 }
 
 void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                            DeviceStatus* st) {
     if (rt.n_vert <= 0) return;
-    k_rigid_contacts<<<(rt.n_vert + 127) / 128, 128, 0, s>>>(ba, rt, mt, rp, rt.n_vert, st);
+    k_rigid_contacts<<<(rt.n_vert * 32 + 127) / 128, 128, 0, s>>>(ba, rt, mt, rp, st);
 }
 
 // ---------------------------------------------------------------- particle contacts on moving meshes ----
@@ -371,7 +409,7 @@ __global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t
     int used0 = 0, used = 0;
     if (active) {
         info = cinfo[i];
-        used0 = used = (int)(info >> 1);
+        used0 = used = info_slots(info);
     }
     bool slot_ovf = false, stack_ovf = false;
     for (int c0 = 0; c0 < rt.n_dyn; c0 += 128) {
@@ -426,7 +464,9 @@ __global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t
             used++;
         }
     }
-    if (active && used != used0) cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1);
+    // every slot added here belongs to a dynamic body
+    if (active && used != used0)
+        cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
     if (slot_ovf) {
         atomicOr(&st->error_bits, kErrSlotOverflow);
         atomicAdd(&st->slot_overflows, 1u);
@@ -453,7 +493,9 @@ __global__ void k_dyn_emit(int64_t n, const uint32_t* __restrict__ cinfo, DynSlo
                            DeviceStatus* st) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int used = (int)(cinfo[i] >> 1);
+    const uint32_t info = cinfo[i];
+    if (info_dyn(info) == 0) return;
+    const int used = info_slots(info);
     uint32_t e = rank[i].x;
     bool ovf = false;
     for (int j = 0; j < used; j++) {
@@ -495,7 +537,8 @@ void launch_body_segments(cudaStream_t s, uint32_t cap, const uint32_t* count, c
 }
 
 // One warp per body: the body's particle-contact deltas summed in entry order (the
-// canonical contact order), then apply_body_deltas.comp without constraint weights.
+// canonical contact order), then apply_body_deltas.comp with their count as the
+// constraint weight (or none when particle_weighting is off).
 __global__ void k_body_particles(BodyArrays ba, const uint2* __restrict__ seg, const uint32_t* __restrict__ sorted,
                                  const float4* __restrict__ bdel, const float4* __restrict__ q_in,
                                  const float4* __restrict__ qd_in, float4* __restrict__ q_out,
@@ -504,6 +547,7 @@ __global__ void k_body_particles(BodyArrays ba, const uint2* __restrict__ seg, c
     const int lane = threadIdx.x & 31;
     if (b >= ba.nb) return;
     v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
+    float cnt = 0.0f;
     if (ba.invm[b] > 0.0f) {
         const uint2 sg = seg[b];
         for (uint32_t base = sg.x; base < sg.y; base += 32) {
@@ -522,11 +566,12 @@ __global__ void k_body_particles(BodyArrays ba, const uint2* __restrict__ seg, c
                 if (aw != 0.0f) {
                     lin = vadd(lin, mk3(ax, ay, az));
                     ang = vadd(ang, mk3(cx, cy, cz));
+                    cnt += 1.0f;
                 }
             }
         }
     }
-    if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, 0.0f, 0, q_out, qd_out);
+    if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.particle_weighting, q_out, qd_out);
 }
 
 void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, const uint32_t* sorted_entries,
@@ -703,55 +748,83 @@ __device__ bool body_contact(const BodyArrays& ba, const float4* q, const float4
     return true;
 }
 
-// One thread per body: its rigid contacts as shape0 (own vertices), then as shape1
-// (the overlapping bodies' vertices on its mesh, partners ascending), summed in that
-// order; then apply_body_deltas.comp with the contact count as constraint weight.
-__global__ void k_body_rigid(BodyArrays ba, RigidTables rt, const float4* __restrict__ q_in,
-                             const float4* __restrict__ qd_in, float4* __restrict__ q_out,
-                             float4* __restrict__ qd_out, RigidParams rp) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= ba.nb) return;
+// Adds the lanes' contributions to (lin, ang, cnt) in lane order (every lane ends
+// with the same sums).
+__device__ __forceinline__ void warp_ordered_add(bool ok, v3 l, v3 g, v3& lin, v3& ang, float& cnt) {
+    const uint32_t m = __ballot_sync(0xffffffffu, ok);
+    for (uint32_t r = m; r; r &= r - 1) {
+        const int src = __ffs(r) - 1;
+        const v3 ls = mk3(__shfl_sync(0xffffffffu, l.x, src), __shfl_sync(0xffffffffu, l.y, src),
+                          __shfl_sync(0xffffffffu, l.z, src));
+        const v3 gs = mk3(__shfl_sync(0xffffffffu, g.x, src), __shfl_sync(0xffffffffu, g.y, src),
+                          __shfl_sync(0xffffffffu, g.z, src));
+        lin = vadd(lin, ls);
+        ang = vadd(ang, gs);
+        cnt += 1.0f;
+    }
+}
+
+// One warp per body: its rigid contacts as shape0 (own vertices), then as shape1 (the
+// overlapping bodies' vertices on its mesh, partners ascending), one slot per lane in
+// (vertex, slot) order and summed in that order; then apply_body_deltas.comp with the
+// contact count as constraint weight.
+__global__ void __launch_bounds__(128) k_body_rigid(BodyArrays ba, RigidTables rt, const float4* __restrict__ q_in,
+                                                   const float4* __restrict__ qd_in, float4* __restrict__ q_out,
+                                                   float4* __restrict__ qd_out, RigidParams rp) {
+    const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= ba.nb) return;  // uniform per warp
     v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
     float cnt = 0.0f;
     const int ib = rt.dyn_index[b];
     if (ib >= 0) {
-        v3 la, aa, lb, ab;
-        for (uint32_t d = rt.dv_start[b]; d < rt.dv_start[b + 1]; d++) {
-            const int k = rt.rc_count[d];
-            for (int j = 0; j < k; j++) {
-                const RigidContact c = load_rc(rt.rc + ((size_t)d * kRigidSlots + j) * 5);
-                if (body_contact(ba, q_in, qd_in, b + 1, c, rp, la, aa, lb, ab)) {
-                    lin = vadd(lin, la);
-                    ang = vadd(ang, aa);
-                    cnt += 1.0f;
+        const uint32_t v0 = rt.dv_start[b], v1 = rt.dv_start[b + 1];
+        const uint32_t ns = (v1 - v0) * kRigidSlots;
+        for (uint32_t c0 = 0; c0 < ns; c0 += 32) {
+            const uint32_t idx = c0 + lane;
+            bool ok = false;
+            v3 la = mk3(0.0f, 0.0f, 0.0f), aa = la, lb, ab;
+            if (idx < ns) {
+                const uint32_t d = v0 + idx / kRigidSlots;
+                const int j = (int)(idx % kRigidSlots);
+                if (j < rt.rc_count[d]) {
+                    const RigidContact c = load_rc(rt.rc + ((size_t)d * kRigidSlots + j) * 5);
+                    ok = body_contact(ba, q_in, qd_in, b + 1, c, rp, la, aa, lb, ab);
                 }
             }
+            warp_ordered_add(ok, la, aa, lin, ang, cnt);
         }
         const int pc = rt.partner_count[ib];
         for (int pi = 0; pi < pc; pi++) {
             const int a = rt.partners[ib * kPartnerCap + pi];
-            for (uint32_t d = rt.dv_start[a]; d < rt.dv_start[a + 1]; d++) {
-                const int k = rt.rc_count[d];
-                for (int j = 0; j < k; j++) {
-                    const float4* sp = rt.rc + ((size_t)d * kRigidSlots + j) * 5;
-                    if (__float_as_int(sp[0].w) != b + 1) continue;
-                    const RigidContact c = load_rc(sp);
-                    if (body_contact(ba, q_in, qd_in, a + 1, c, rp, la, aa, lb, ab)) {
-                        lin = vadd(lin, lb);
-                        ang = vadd(ang, ab);
-                        cnt += 1.0f;
+            const uint32_t w0 = rt.dv_start[a], w1 = rt.dv_start[a + 1];
+            const uint32_t na = (w1 - w0) * kRigidSlots;
+            for (uint32_t c0 = 0; c0 < na; c0 += 32) {
+                const uint32_t idx = c0 + lane;
+                bool ok = false;
+                v3 la, aa, lb = mk3(0.0f, 0.0f, 0.0f), ab = lb;
+                if (idx < na) {
+                    const uint32_t d = w0 + idx / kRigidSlots;
+                    const int j = (int)(idx % kRigidSlots);
+                    if (j < rt.rc_count[d]) {
+                        const float4* sp = rt.rc + ((size_t)d * kRigidSlots + j) * 5;
+                        if (__float_as_int(sp[0].w) == b + 1) {
+                            const RigidContact c = load_rc(sp);
+                            ok = body_contact(ba, q_in, qd_in, a + 1, c, rp, la, aa, lb, ab);
+                        }
                     }
                 }
+                warp_ordered_add(ok, lb, ab, lin, ang, cnt);
             }
         }
     }
-    apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.con_weighting, q_out, qd_out);
+    if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.con_weighting, q_out, qd_out);
 }
 
 void launch_body_rigid(cudaStream_t s, BodyArrays ba, RigidTables rt, const float4* q_in, const float4* qd_in,
                        float4* q_out, float4* qd_out, RigidParams rp) {
     if (ba.nb <= 0) return;
-    k_body_rigid<<<(ba.nb + 63) / 64, 64, 0, s>>>(ba, rt, q_in, qd_in, q_out, qd_out, rp);
+    k_body_rigid<<<(ba.nb * 32 + 127) / 128, 128, 0, s>>>(ba, rt, q_in, qd_in, q_out, qd_out, rp);
 }
 
 }  // namespace xpbd

@@ -19,15 +19,8 @@ size_t contact_scan_words(int64_t n) {
 // (slots whose shape belongs to a dynamic body, 0)
 __device__ __forceinline__ uint2 particle_counts(const uint32_t* __restrict__ cinfo, int64_t i, const DynSlots& ds) {
     const uint32_t info = cinfo[i];
-    if (!ds.cslot) return make_uint2(info & kPlaneBit, info >> 1);
-    const int used = (int)(info >> 1);
-    uint32_t d = 0;
-    for (int j = 0; j < used; j++) {
-        const int shape = __float_as_int(ds.cslot[((size_t)i * ds.slot_cap + j) * 3].w);
-        const int body = ds.shape_body[shape];
-        if (body >= 0 && ds.body_invm[body] > 0.0f) d++;
-    }
-    return make_uint2(d, 0u);
+    if (!ds.cslot) return make_uint2(info & kPlaneBit, (uint32_t)info_slots(info));
+    return make_uint2((uint32_t)info_dyn(info), 0u);
 }
 
 // phase 1: per-tile sums
@@ -193,7 +186,7 @@ __global__ void k_contact_compact(int64_t n, const uint32_t* __restrict__ cinfo,
     const uint32_t info = cinfo[i];
     if (!info) return;
     const uint2 rk = rank[i];
-    const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
+    const int ncon = (int)(info & kPlaneBit) + info_slots(info);
     const v3 xp = xyz(x_prev[i]);
     for (int c = 0; c < ncon; c++) {
         int64_t pos;

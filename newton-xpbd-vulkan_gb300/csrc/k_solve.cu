@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     if (pflag & 1) {
         const uint32_t info = cinfo ? cinfo[id] : 0u;
         const v3 x0 = xyz(x0a[id]);
-        const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
+        const int ncon = (int)(info & kPlaneBit) + info_slots(info);
         const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
         // shape contacts, canonical order (scene.cpp:946-947)
         uint32_t dyn_e = bo.bdel ? bo.dyn_rank[id].x : 0u;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_restitute(
     const float4 ox = rx[k], ov = rv[k];
     v3 v_new = xyz(ov);
     const uint32_t info = cinfo[id];
-    const int ncon = (int)(info & kPlaneBit) + (int)(info >> 1);
+    const int ncon = (int)(info & kPlaneBit) + info_slots(info);
     // inactive particles keep their predicted state and take no restitution (:256)
     if (sp.enable_restitution && ncon && (rf[k] & 1)) {
         const v3 x0 = xyz(x0a[id]), v_old = xyz(v0a[id]);

@@ -22,20 +22,24 @@ struct DeviceStatus {
     uint32_t lookback_timeouts;
     uint32_t stack_overflows;
     uint32_t slot_overflows;
-    uint32_t pad[4];
+    uint32_t rigid_slot_overflows;  // rigid contacts dropped past kRigidSlots per vertex (as the oracle)
+    uint32_t pad[3];
 };
 enum : uint32_t {
     kErrLookbackTimeout = 1u,  // a decoupled look-back wait expired
     kErrStackOverflow = 2u,    // BVH traversal stack (32 entries) full
     kErrSlotOverflow = 4u,     // more mesh contacts for one particle than slots
-    kErrBodyOverflow = 8u,     // body partner list, rigid contact slots or body-delta entries full
+    kErrBodyOverflow = 8u,     // body partner list or body-delta entries full
 };
 
 // Per-particle contact header (cinfo[i]): bit 0 = plane contact (shape 0),
-// bits 1..15 = number of generic contact slots used in cslot.
+// bits 1..15 = number of generic contact slots used in cslot, bits 16..31 = how many
+// of them belong to dynamic bodies.
 // A generic slot is 3 float4: (body_pos.xyz, shape as int bits),
 // (normal.xyz, 0), (body_vel.xyz, 0).
 constexpr uint32_t kPlaneBit = 1u;
+__host__ __device__ __forceinline__ int info_slots(uint32_t info) { return (int)((info >> 1) & 0x7fffu); }
+__host__ __device__ __forceinline__ int info_dyn(uint32_t info) { return (int)(info >> 16); }
 
 struct PredictParams {
     float dt, v_max, gx, gy, gz, inv;
@@ -217,11 +221,12 @@ struct RigidParams {
     float dt, damping, margin, relax;
     int con_weighting;
     float mu_t, mu_r;
+    int particle_weighting;
     float gx, gy, gz;
     int plane;
     float altitude;
 };
-constexpr int kPartnerCap = 64;   // dynamic bodies whose boxes overlap one dynamic body
+constexpr int kPartnerCap = 256;  // dynamic bodies whose boxes overlap one dynamic body
 constexpr int kRigidSlots = 4;    // rigid contacts per body vertex
 struct RigidTables {
     int n_dyn;

@@ -27,14 +27,17 @@ namespace {
 // profiler stage slots, one per kernel (names follow scene.cpp:1481-1505 where they correspond)
 enum ProfSlot {
     P_CLEAR = 0, P_CONTACT, P_INTEGRATE_KEYS, P_SORT0, P_SORT1, P_SORT2, P_SORT3, P_RANKS, P_CELLS, P_SOLVE,
-    P_BODY_CONTACT, P_BODY_ENTRIES, P_BODY_INTEGRATE, P_BODY_ITER, P_RESTITUTION, P_COUNT
+    P_BODY_CONTACT, P_BODY_ENTRIES, P_BODY_INTEGRATE, P_BODY_ITER, P_RESTITUTION, P_POSED, P_RIGID,
+    P_BODY_RIGID_ITER, P_COUNT
 };
+static_assert(P_COUNT <= Solver::kMaxStages, "profiler stage table too small");
 const char* kProfNames[P_COUNT] = {
     "0. Sort scratch clear (memset)", "1. Contact Gen (plane + mesh)", "2b. Integrate + Cell Keys",
     "2e. Onesweep Pass 0", "2e. Onesweep Pass 1", "2e. Onesweep Pass 2", "2e. Onesweep Pass 3",
     "1b. Contact Ranks (cap)", "2g. Cell Table + Gather", "3. Solve+Apply(+Restitution)",
-    "1c. Body Contacts (pairs, moving meshes, rigid)", "1d. Body Delta Entries (scan, sort)",
-    "2c. Integrate Bodies", "3b. Body Deltas (particle + rigid)", "3c. Restitution (bodies)"};
+    "1c. Body Pairs (world boxes)", "1f. Body Delta Entries (scan, sort)", "2c. Integrate Bodies",
+    "3b. Body Deltas (particle contacts)", "3c. Restitution (bodies)", "1d. Contacts on Moving Meshes",
+    "1e. Rigid Contacts", "3d. Body Deltas (rigid contacts)"};
 uint32_t f2u(float f) {
     uint32_t u;
     std::memcpy(&u, &f, 4);
@@ -237,7 +240,8 @@ void Solver::finalize_meshes() {
         total_prims += nt;
     }
     all_vels_.assign(all_verts_.size(), 0.0f);
-    slot_cap_ = (int)std::max<size_t>(1, std::min<size_t>(nm, 8));
+    // contact slots per particle: one per mesh up to 8; 16 when there are more meshes (bodies)
+    slot_cap_ = (int)std::max<size_t>(1, nm <= 8 ? nm : 16);
     cslot_.alloc(std::max<size_t>(n_, 1) * (size_t)slot_cap_ * 3, false);
     if (nm > 0) {
         std::vector<float4> nl(total_nodes), nu(total_nodes);
@@ -462,6 +466,7 @@ RigidParams Solver::rigid_params(float sdt) const {
     r.con_weighting = body_params_.rigid_contact_con_weighting;
     r.mu_t = body_params_.rigid_mu_torsional;
     r.mu_r = body_params_.rigid_mu_rolling;
+    r.particle_weighting = body_params_.particle_contact_con_weighting;
     r.gx = cfg_.gravity[0];
     r.gy = cfg_.gravity[1];
     r.gz = cfg_.gravity[2];
@@ -568,7 +573,7 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     body_q_prev_.alloc(nb * 2, true);
     body_qd_prev_.alloc(nb * 2, true);
     // body-delta entries of the particle contacts: one per slot with a dynamic body
-    entry_cap_ = (uint32_t)std::min<size_t>(n_ + 4096, (size_t)0x7fffffff);
+    entry_cap_ = (uint32_t)std::min<size_t>(2 * n_ + 4096, (size_t)0x7fffffff);
     int kb = 1;
     while ((size_t(1) << kb) < nb) kb++;
     eplan_ = make_sort_plan((int64_t)entry_cap_, kb, 8, 8);
@@ -693,9 +698,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     if (bodies) {
         launch_collide_posed(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p,
                              mesh_tables(), rt, slot_cap_, cinfo_.p, cslot_.p, ccount, st);
+        count_kernel();
+        prof_mark(P_POSED);
         launch_rigid_contacts(stream_, ba, rt, mesh_tables(), rp, st);
-        count_kernel(2);
-        prof_mark(P_BODY_CONTACT);
+        count_kernel();
+        prof_mark(P_RIGID);
         // body-delta entries: dynamic slots in contact order, grouped by body (stable sort)
         launch_dyn_scan(stream_, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
         launch_dyn_emit(stream_, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
@@ -779,9 +786,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         if (bodies) {
             launch_body_particles(stream_, ba, seg_.p, sorted_entries_, bdel_.p, body_q_.p, body_qd_.p,
                                   body_q_mid_.p, body_qd_mid_.p, rp);
-            launch_body_rigid(stream_, ba, rt, body_q_mid_.p, body_qd_mid_.p, body_q_.p, body_qd_.p, rp);
-            count_kernel(2);
+            count_kernel();
             prof_mark(P_BODY_ITER);
+            launch_body_rigid(stream_, ba, rt, body_q_mid_.p, body_qd_mid_.p, body_q_.p, body_qd_.p, rp);
+            count_kernel();
+            prof_mark(P_BODY_RIGID_ITER);
         }
     }
     if (bodies && iterations > 0) {
@@ -884,8 +893,8 @@ void Solver::finish_frame(int substeps) {
     if (host_status_.error_bits & kErrSlotOverflow)
         throw std::runtime_error("more mesh contacts for one particle than contact slots");
     if (host_status_.error_bits & kErrBodyOverflow)
-        throw std::runtime_error("body tables full (overlapping bodies, rigid contacts per vertex or body-delta "
-                                 "entries)");
+        throw std::runtime_error("body tables full (more than 256 overlapping bodies, or more body-delta entries "
+                                 "than 2 x particles + 4096)");
     if (env_on("VKXPBD_CHECK_SORT_ORDER")) check_sort_order();
 }
 

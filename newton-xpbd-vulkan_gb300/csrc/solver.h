@@ -67,6 +67,7 @@ bool tris_watertight(const uint32_t* tris, size_t num_tris, size_t num_verts);
 
 class Solver {
    public:
+    static constexpr int kMaxStages = 32;  // >= the number of profiler stages (solver.cpp)
     Solver();
     ~Solver();
 
@@ -219,7 +220,7 @@ class Solver {
     DevBuf<float> body_I_;
     bool dyn_any_ = false;
     std::vector<int> dyn_list_;
-    xpbd_body_params body_params_{0.0f, 0.01f, 0.8f, 1, 0.0f, 0.0f};
+    xpbd_body_params body_params_{0.0f, 0.01f, 0.8f, 1, 0.0f, 0.0f, 1};
     DevBuf<float4> body_q_mid_, body_qd_mid_, body_q_prev_, body_qd_prev_;
     DevBuf<int> dyn_, dyn_index_, posed_, walk_list_, partners_, partner_count_, rc_count_;
     int walk_count_ = 0, n_dyn_verts_ = 0;
@@ -261,7 +262,7 @@ class Solver {
     uint64_t last_kernels_ = 0, last_memsets_ = 0;
     // profiler (stage names follow scene.cpp:1481-1505 where the stages correspond)
     bool profiling_ = false;
-    double prof_ms_[16] = {0};
+    double prof_ms_[kMaxStages] = {0};
     uint64_t prof_substeps_ = 0;
     double prof_wall_ms_ = 0.0;
 };

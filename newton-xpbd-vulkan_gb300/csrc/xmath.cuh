@@ -49,7 +49,11 @@ __device__ __forceinline__ v3 vfma_vs(v3 a, float s, v3 c) {  // fma(a, vec3(s),
 // exact_sqrt / exact_length / exact_dot / exact_div of
 // solve_particle_particle_contacts.comp:81-105 (identical copies live in the
 // shape-contact and mesh-contact shaders).
+// At a == 0 the shader's refinement evaluates fma(0, 0.5 / 0, 0): NaN in IEEE arithmetic
+// and undefined under Vulkan's division rules (a particle lying exactly on a mesh surface
+// then gets a NaN contact point). The refinement is meant to equal sqrt(a), so 0 is kept.
 __device__ __forceinline__ float exact_sqrt(float a) {
+    if (a == 0.0f) return a;
     float d = __fsqrt_rn(a);
     float r = __fmaf_rn(-d, d, a);
     return __fmaf_rn(r, __fdiv_rn(0.5f, d), d);

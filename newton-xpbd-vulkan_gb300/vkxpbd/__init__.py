@@ -173,7 +173,8 @@ class XpbdSolver:
 
     def set_body_params(self, **kw):
         """angular_damping, rigid_contact_margin, rigid_contact_relaxation,
-        rigid_contact_con_weighting, rigid_mu_torsional, rigid_mu_rolling."""
+        rigid_contact_con_weighting, rigid_mu_torsional, rigid_mu_rolling,
+        particle_contact_con_weighting."""
         bp = _abi.BodyParams()
         _lib.xpbd_body_params_default(C.byref(bp))
         for k, v in kw.items():

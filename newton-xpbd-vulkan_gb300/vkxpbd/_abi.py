@@ -47,6 +47,7 @@ class BodyParams(C.Structure):
         ("angular_damping", C.c_float), ("rigid_contact_margin", C.c_float),
         ("rigid_contact_relaxation", C.c_float), ("rigid_contact_con_weighting", C.c_int32),
         ("rigid_mu_torsional", C.c_float), ("rigid_mu_rolling", C.c_float),
+        ("particle_contact_con_weighting", C.c_int32),
     ]
 
 

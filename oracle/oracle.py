@@ -60,11 +60,13 @@ _U = C.POINTER(C.c_uint32)
 class BodyParams(C.Structure):
     _fields_ = [("angular_damping", C.c_float), ("rigid_contact_margin", C.c_float),
                 ("rigid_contact_relaxation", C.c_float), ("rigid_contact_con_weighting", C.c_int32),
-                ("rigid_mu_torsional", C.c_float), ("rigid_mu_rolling", C.c_float)]
+                ("rigid_mu_torsional", C.c_float), ("rigid_mu_rolling", C.c_float),
+                ("particle_contact_con_weighting", C.c_int32)]
 
 
 BODY_PARAM_DEFAULTS = dict(angular_damping=0.0, rigid_contact_margin=0.01, rigid_contact_relaxation=0.8,
-                           rigid_contact_con_weighting=1, rigid_mu_torsional=0.0, rigid_mu_rolling=0.0)
+                           rigid_contact_con_weighting=1, rigid_mu_torsional=0.0, rigid_mu_rolling=0.0,
+                           particle_contact_con_weighting=1)
 
 _libs: dict = {}
 

@@ -82,8 +82,12 @@ static inline v3 vfma_vs(v3 a, real s, v3 c) { /* fma(a, vec3(s), c) */
     return mk(R_FMA(a.x, s, c.x), R_FMA(a.y, s, c.y), R_FMA(a.z, s, c.z));
 }
 
-/* exact_sqrt: solve_particle_particle_contacts.comp:81-85 (same in the shape/mesh shaders) */
+/* exact_sqrt: solve_particle_particle_contacts.comp:81-85 (same in the shape/mesh shaders).
+ * At a == 0 the refinement evaluates fma(0, 0.5 / 0, 0), NaN in IEEE arithmetic and
+ * undefined under Vulkan's division rules; the refinement is meant to equal sqrt(a),
+ * so a is returned (a particle lying exactly on a mesh surface keeps a finite contact). */
 static inline real exact_sqrt(real a) {
+    if (a == RF(0.0)) return a;
     real d = R_SQRT(a);
     real r = R_FMA(-d, d, a);
     return R_FMA(r, RF(0.5) / d, d);
@@ -309,6 +313,7 @@ or_solver* or_create(const or_config* cfg, int64_t n, int64_t max_contacts) {
     s->bp.rigid_contact_con_weighting = 1;
     s->bp.rigid_mu_torsional = 0.0f;
     s->bp.rigid_mu_rolling = 0.0f;
+    s->bp.particle_contact_con_weighting = 1;
     s->cells = xcalloc((size_t)n, sizeof(uint32_t));
     s->ids = xcalloc((size_t)n, sizeof(uint32_t));
     s->scells = xcalloc((size_t)n, sizeof(uint32_t));
@@ -1815,8 +1820,9 @@ static void rigid_collide(or_solver* s) {
 }
 
 /* One body pass of an iteration: particle-contact body deltas (summed per body in
- * contact-slot order) applied without constraint weights, then the rigid contacts
- * solved on that state and applied with weights (the order of one XPBD iteration). */
+ * contact-slot order) applied with the number of those contacts as constraint
+ * weight (apply_body_deltas.comp:85-89; a switch turns it off), then the rigid
+ * contacts solved on that state and applied with their own count as weight. */
 static void bodies_iterate(or_solver* s, real dt) {
     int64_t nb = s->nbody;
     real* d6 = xcalloc((size_t)nb * 6, sizeof(real));
@@ -1826,9 +1832,12 @@ static void bodies_iterate(or_solver* s, real dt) {
         if (!s->bvalid[t]) continue;
         int32_t b = s->shape_body[s->cshape[t]];
         for (int k = 0; k < 6; k++) d6[b * 6 + k] += s->bdel[t * 6 + k];
+        wc[b] += RF(1.0);
     }
     for (int64_t b = 0; b < nb; b++)
-        apply_body_delta(s, b, dt, s->body_q, s->body_qd, &d6[b * 6], RF(0.0), 0, s->body_qm, s->body_qdm);
+        apply_body_delta(s, b, dt, s->body_q, s->body_qd, &d6[b * 6], wc[b], s->bp.particle_contact_con_weighting,
+                         s->body_qm, s->body_qdm);
+    memset(wc, 0, sizeof(real) * (size_t)nb);
     memset(d6, 0, sizeof(real) * 6 * (size_t)nb);
     for (int64_t x = 0; x < nb; x++) {
         if (!posed(s, x)) continue;

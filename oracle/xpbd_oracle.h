@@ -95,6 +95,7 @@ typedef struct or_body_params {
     int32_t rigid_contact_con_weighting; /* apply_body_deltas.comp use_constraint_weights */
     float rigid_mu_torsional;
     float rigid_mu_rolling;
+    int32_t particle_contact_con_weighting; /* average the particle-contact body deltas per body */
 } or_body_params;
 void or_set_body_params(or_solver* s, const or_body_params* p);
 int64_t or_rigid_contact_overflows(const or_solver* s);

@@ -237,3 +237,24 @@ def test_enumerate_devices_is_a_list():
     import vkxpbd
 
     assert isinstance(vkxpbd.enumerate_devices(), list)
+
+
+def test_particle_exactly_on_mesh_surface_gives_finite_contact():
+    """exact_sqrt(0): a particle whose closest surface point equals its position (seen in the
+    mixed workload after boxes pressed particles into the heightfield) keeps a finite contact."""
+    from vkxpbd import scenes
+
+    sc = scenes.particles_on_mesh(dims=(1, 1, 1))
+    p = np.array([[0.23391318321228027, -0.32021233439445496, 0.045575764030218124]], np.float32)
+    cfg = config_for(sc)
+    o = O.OracleSolver(cfg, 1, 0)
+    v, t, m, wt = sc.meshes[0]
+    o.add_mesh(v, t, m, None, wt)
+    o.finalize_meshes()
+    o.set_particles(p, np.zeros((1, 3), np.float32), np.full(1, 1000, np.float32), np.full(1, 0.005, np.float32),
+                    np.ones(1, np.int32))
+    o.collide_only()
+    c = o.get_contacts()
+    assert c["shapes"].tolist() == [1]
+    assert np.isfinite(c["body_positions"]).all() and np.isfinite(c["normals"]).all()
+    assert np.array_equal(c["body_positions"][0], p[0])

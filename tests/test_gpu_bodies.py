@@ -45,3 +45,16 @@ def test_boxes_stack_and_heightfield_bitexact():
     sc = box_scene(n_side=4, boxes=((0.05, 0.05, 0.03), (0.04, 0.03, 0.03), (0.03, 0.03, 0.03)),
                    positions=((0.0, 0.0, 0.12), (0.01, 0.0, 0.25), (0.2, 0.1, 0.15)), hf=24)
     _run(sc, 25, substeps=5, iterations=2, body_params=dict(rigid_mu_torsional=0.01, rigid_mu_rolling=0.01))
+
+
+def test_mixed_small_bitexact():
+    """A scaled-down particles + heightfield + falling boxes scene (the mixed workload's recipe)."""
+    from vkxpbd import scenes
+
+    sc = scenes.mixed(dims=(24, 24, 12), n_boxes=24, hf_vertices=64)
+    _run(sc, 20)
+
+
+def test_particle_weighting_off_bitexact():
+    sc = box_scene(n_side=8, positions=((0.035, 0.035, 0.12),))
+    _run(sc, 10, body_params=dict(particle_contact_con_weighting=0, rigid_contact_con_weighting=0))

@@ -200,3 +200,18 @@ def test_tolerance_floor():
     orc.step(1.0 / 60.0, 1, 1)
     a, b = g.get_positions(), orc.get_positions()
     assert np.all(np.abs(a - b) <= 1e-5 * np.maximum(np.abs(b), 1e-3))
+
+
+def test_particle_exactly_on_mesh_surface_bitexact():
+    from vkxpbd import scenes
+
+    sc = scenes.particles_on_mesh(dims=(1, 1, 1))
+    sc.positions = np.array([[0.23391318321228027, -0.32021233439445496, 0.045575764030218124]], np.float32)
+    cfg = config_for(sc)
+    g, orc = make_pair(sc, cfg)
+    g.collide_only()
+    orc.collide_only()
+    c = orc.get_contacts()
+    assert_bitexact(g.get_contact_body_positions(), c["body_positions"], "contact point")
+    assert_bitexact(g.get_contact_normals(), c["normals"], "contact normal")
+    _step_compare(g, orc, 3, 1.0 / 60.0, 10, 1, "on-surface particle")
