@@ -183,6 +183,28 @@ int xpbd_set_bodies(xpbd_solver* s, const float* q, const float* qd, const float
                     const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t num_bodies);
 int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t num_bodies);
 
+/* Differentiable rollout — an extension with no reference counterpart: the
+ * hand-written adjoint of the substep (integration, ground-plane and
+ * particle-particle contact projection, delta apply, restitution).
+ * xpbd_rollout steps `frames` frames exactly like xpbd_step and stores the state
+ * every checkpoint_frames frames; xpbd_rollout_backward replays each checkpointed
+ * segment and runs the adjoint of its substeps in reverse, returning the gradient
+ * of a loss on the final state (grad_x_final, grad_v_final: n*3 floats;
+ * grad_v_final may be NULL) with respect to the initial positions and velocities
+ * (n*3 each), the inverse masses (n) and params[4] = {soft_contact_mu,
+ * shape_material_mu, particle_mu, soft_contact_restitution}. Output pointers may be
+ * NULL. Contact sets and friction branches are those of the forward pass. Covered:
+ * one scene, ground plane and particle contacts (no meshes or bodies), every
+ * particle active, particles of equal radius, one solver iteration. The solver is
+ * left at the rollout's final state. */
+/* New contact / material parameters after init (e.g. between rollouts of an
+ * optimisation): every numeric field of cfg except device_index and the
+ * diagnostics / profiling switches, which stay as at init. */
+int xpbd_update_config(xpbd_solver* s, const xpbd_config* cfg);
+int xpbd_rollout(xpbd_solver* s, float dt, int substeps, int iterations, int frames, int checkpoint_frames);
+int xpbd_rollout_backward(xpbd_solver* s, const float* grad_x_final, const float* grad_v_final, float* grad_x0,
+                          float* grad_v0, float* grad_inv_mass, double* grad_params);
+
 /* Batched scenes (the xpbd_batch_* family). One solver steps n_scenes
  * independent scenes in one graph per frame, one launch per kernel for all of
  * them. Each scene has its own 128^3 hash grid (the scene id is the high part of

@@ -293,6 +293,25 @@ int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t nb) {
     return guarded([&] { S(s).get_bodies(q, qd, nb); });
 }
 
+int xpbd_update_config(xpbd_solver* s, const xpbd_config* cfg) {
+    return guarded([&] {
+        if (!cfg) throw std::runtime_error("xpbd_update_config: cfg is NULL");
+        S(s).update_config(*cfg);
+    });
+}
+
+int xpbd_rollout(xpbd_solver* s, float dt, int substeps, int iterations, int frames, int checkpoint_frames) {
+    return guarded([&] { S(s).rollout(dt, substeps, iterations, frames, checkpoint_frames); });
+}
+
+int xpbd_rollout_backward(xpbd_solver* s, const float* grad_x_final, const float* grad_v_final, float* grad_x0,
+                          float* grad_v0, float* grad_inv_mass, double* grad_params) {
+    return guarded([&] {
+        if (!grad_x_final) throw std::runtime_error("xpbd_rollout_backward: grad_x_final is NULL");
+        S(s).rollout_backward(grad_x_final, grad_v_final, grad_x0, grad_v0, grad_inv_mass, grad_params);
+    });
+}
+
 int xpbd_batch_init(xpbd_solver* s, const xpbd_config* cfg, const size_t* scene_counts, size_t n_scenes,
                     size_t max_contacts) {
     return guarded([&] {

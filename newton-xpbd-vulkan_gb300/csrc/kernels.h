@@ -268,6 +268,39 @@ void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, cons
 void launch_body_rigid(cudaStream_t s, BodyArrays ba, RigidTables rt, const float4* q_in, const float4* qd_in,
                        float4* q_out, float4* qd_out, RigidParams rp);
 
+// -------------------------------------------------------------- adjoint ----
+// One substep's adjoint (k_adjoint.cu). Arrays rx/rv/sids/table are the forward's
+// sorted records of that substep; x0/v0/cinfo its start state and plane contacts;
+// gx/gv the gradient of the loss with respect to the substep's end state (in) and
+// start state (out; may alias the input); gw accumulates dL/d(inverse mass).
+struct AdjointArgs {
+    int64_t n;
+    const uint32_t* sids;
+    const float4* rx;
+    const float4* rv;
+    const int4* table;
+    const uint32_t* stamp;
+    const float4* x0;
+    const float4* v0;
+    const uint32_t* cinfo;
+    const float4* gx_in;
+    const float4* gv_in;
+    float4* gx_out;
+    float4* gv_out;
+    float* gw;
+    float4* gacc;      // scratch, sorted order: dL/d(sum_j pair_d) of each particle
+    float4* part_xp;   // scratch, sorted order: own-state partials (w = dL/dw part)
+    float4* part_vp;
+    float4* part_x0;
+    float4* part_v0;
+    float* block_params;  // 3 per block
+    double* param_acc;    // [3]: plane mu (effective), particle mu, restitution
+    float dt, inv, relax, ka, altitude, mu_plane, k_mu, k_coh, max_radius, restitution;
+    int restitution_on;
+};
+void launch_adjoint_substep(cudaStream_t s, const AdjointArgs& a);
+size_t adjoint_block_count(int64_t n);
+
 // float4 state <-> packed xyz
 void launch_unpack_xyz(cudaStream_t s, int64_t n, const float4* a, float* out);
 void launch_pack_xyz(cudaStream_t s, int64_t n, const float* in, float4* a);

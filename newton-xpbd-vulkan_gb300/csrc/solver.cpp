@@ -306,6 +306,7 @@ void Solver::set_particles(const float* q, const float* qd, const float* inv_mas
     if (n != n_) throw std::runtime_error("Particle count mismatch");
     XPBD_CUDA(cudaSetDevice(device_));
     sync();
+    rollout_valid_ = false;
     if (n == 0) return;
     std::memcpy(pinned_, q, n * 3 * sizeof(float));
     XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
@@ -819,6 +820,7 @@ void Solver::record_frame(Mode mode, float dt, int substeps, int iterations, int
 void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool sync_now) {
     if (substeps <= 0) throw std::runtime_error("step: substeps must be positive");
     if (pending_substeps_) sync();
+    rollout_valid_ = false;  // the stored rollout no longer ends at the current state
     ensure_substep_capacity(substeps);
     if (n_ == 0) return;
     auto t0 = std::chrono::high_resolution_clock::now();
@@ -1206,6 +1208,205 @@ void Solver::print_profiler_summary() {
                     prof_ms_[i] / (total > 0 ? total : 1.0) * 100.0);
     std::printf("========================================================================================================\n\n");
     std::fflush(stdout);
+}
+
+void Solver::update_config(const xpbd_config& c) {
+    require_init();
+    sync();
+    const xpbd_config old = cfg_;
+    cfg_ = c;
+    // fixed after init: the device, diagnostics buffers and profiling
+    cfg_.device_index = old.device_index;
+    cfg_.enable_diagnostics = old.enable_diagnostics;
+    cfg_.max_diag_pairs = old.max_diag_pairs;
+    cfg_.enable_profile = old.enable_profile;
+    if (finalized_ && shape_mu_.p) {
+        std::vector<float> smu(shape_mu_.n, cfg_.shape_material_mu);
+        XPBD_CUDA(cudaMemcpy(shape_mu_.p, smu.data(), smu.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    clear_graphs();  // the frame graphs carry the parameters
+    rollout_valid_ = false;
+}
+
+// ---------------------------------------------------------------- differentiable rollout ----
+void Solver::rollout(float dt, int substeps, int iterations, int frames, int checkpoint_frames) {
+    require_init();
+    if (!finalized_) finalize_meshes();
+    if (!meshes_.empty() || dyn_any_ || pscene_.p || injected_)
+        throw std::runtime_error("rollout: the adjoint covers the ground plane and particle contacts of one scene");
+    if (iterations != 1) throw std::runtime_error("rollout: the adjoint covers one solver iteration");
+    if (!all_active_) throw std::runtime_error("rollout: every particle must be active");
+    if (substeps <= 0 || frames <= 0 || checkpoint_frames <= 0) throw std::runtime_error("rollout: bad counts");
+    XPBD_CUDA(cudaSetDevice(device_));
+    sync();
+    const size_t n = n_;
+    const int n_ckpt = (frames + checkpoint_frames - 1) / checkpoint_frames + 1;
+    ckpt_.alloc((size_t)n_ckpt * 2 * std::max<size_t>(n, 1), false);
+    auto save = [&](int slot) {
+        float4* dst = ckpt_.p + (size_t)slot * 2 * n;
+        XPBD_CUDA(cudaMemcpyAsync(dst, x_[cur_].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        XPBD_CUDA(cudaMemcpyAsync(dst + n, v_[cur_].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+    };
+    for (int f = 0; f < frames; f++) {
+        if (f % checkpoint_frames == 0) save(f / checkpoint_frames);
+        run_frame(Mode::Step, dt, substeps, 1, false);
+    }
+    sync();
+    save(n_ckpt - 1);
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    ro_dt_ = dt;
+    ro_substeps_ = substeps;
+    ro_frames_ = frames;
+    ro_ckpt_ = checkpoint_frames;
+    rollout_valid_ = true;
+}
+
+// Sorted records, cell table and plane contacts of the substep starting at x_[src], v_[src]
+// (the first kernels of record_substep).
+void Solver::prepare_grid(float sdt, int src) {
+    const int64_t n = (int64_t)n_;
+    const PredictParams pp = predict_params(sdt);
+    PlaneParams pl;
+    pl.enabled = cfg_.has_ground_plane ? 1 : 0;
+    pl.margin = cfg_.soft_contact_margin;
+    pl.altitude = cfg_.ground_plane_altitude;
+    DeviceStatus* st = status_.p;
+    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
+    launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, nullptr, pp, pl, keys_.p, plan_,
+                        sort_scratch_.p + hist_off_, cinfo_.p, ccount_.p, stamp_.p);
+    const uint32_t* kin = keys_.p;
+    const uint32_t* vin = nullptr;
+    const size_t lbw = sort_lookback_words(plan_);
+    for (int p = 0; p < plan_.passes; p++) {
+        launch_onesweep_pass(stream_, n, plan_, p, kin, vin, pair_k_[p & 1].p, pair_v_[p & 1].p,
+                             sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
+                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st);
+        kin = pair_k_[p & 1].p;
+        vin = pair_v_[p & 1].p;
+    }
+    launch_cells_gather(stream_, n, kin, vin, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p, stamp_.p,
+                        rx_[0].p, rv_[0].p, rf_.p);
+}
+
+void Solver::rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
+                              double* params) {
+    if (!rollout_valid_) throw std::runtime_error("rollout_backward: no rollout to differentiate");
+    XPBD_CUDA(cudaSetDevice(device_));
+    sync();
+    const size_t n = n_;
+    const float sdt = ro_dt_ / (float)ro_substeps_;  // as record_frame computes it
+    const int n_seg = (ro_frames_ + ro_ckpt_ - 1) / ro_ckpt_;
+    const size_t nn = std::max<size_t>(n, 1);
+    gx_.alloc(nn, false);
+    gv_.alloc(nn, false);
+    gw_.alloc(nn, true);
+    gacc_.alloc(nn, false);
+    part_xp_.alloc(nn, false);
+    part_vp_.alloc(nn, false);
+    part_x0_.alloc(nn, false);
+    part_v0_.alloc(nn, false);
+    const size_t blocks = adjoint_block_count((int64_t)n);
+    block_params_.alloc(std::max<size_t>(blocks, 1) * 3, false);
+    param_acc_.alloc(3, true);
+    traj_.alloc((size_t)ro_ckpt_ * ro_substeps_ * 2 * nn, false);
+    // upstream gradients (host xyz -> device float4)
+    auto upload = [&](const float* h, float4* d) {
+        if (h) {
+            std::memcpy(pinned_, h, n * 3 * sizeof(float));
+            XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
+            launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, d);
+            XPBD_CUDA(cudaStreamSynchronize(stream_));
+        } else {
+            XPBD_CUDA(cudaMemsetAsync(d, 0, n * sizeof(float4), stream_));
+        }
+    };
+    upload(gx_final, gx_.p);
+    upload(gv_final, gv_.p);
+    AdjointArgs a{};
+    a.n = (int64_t)n;
+    a.table = table_.p;
+    a.stamp = stamp_.p;
+    a.cinfo = cinfo_.p;
+    a.gx_in = gx_.p;
+    a.gv_in = gv_.p;
+    a.gx_out = gx_.p;
+    a.gv_out = gv_.p;
+    a.gw = gw_.p;
+    a.gacc = gacc_.p;
+    a.part_xp = part_xp_.p;
+    a.part_vp = part_vp_.p;
+    a.part_x0 = part_x0_.p;
+    a.part_v0 = part_v0_.p;
+    a.block_params = block_params_.p;
+    a.param_acc = param_acc_.p;
+    a.dt = sdt;
+    a.inv = 1.0f / cfg_.search_radius;
+    a.relax = cfg_.soft_contact_relaxation;
+    a.ka = cfg_.particle_adhesion;
+    a.altitude = cfg_.ground_plane_altitude;
+    a.mu_plane = 0.5f * (cfg_.soft_contact_mu + cfg_.shape_material_mu);
+    a.k_mu = cfg_.particle_mu;
+    a.k_coh = cfg_.particle_cohesion;
+    a.max_radius = cfg_.particle_max_radius;
+    a.restitution = cfg_.soft_contact_restitution;
+    a.restitution_on = cfg_.enable_restitution ? 1 : 0;
+    a.rx = rx_[0].p;
+    a.rv = rv_[0].p;
+    a.x0 = x_[0].p;
+    a.v0 = v_[0].p;
+    for (int c = n_seg - 1; c >= 0; c--) {
+        const int nf = std::min(ro_ckpt_, ro_frames_ - c * ro_ckpt_);
+        const int S = nf * ro_substeps_;
+        // replay the segment from its checkpoint, keeping every substep's start state
+        const float4* ck = ckpt_.p + (size_t)c * 2 * n;
+        XPBD_CUDA(cudaMemcpyAsync(x_[0].p, ck, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        XPBD_CUDA(cudaMemcpyAsync(v_[0].p, ck + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        int src = 0;
+        for (int t = 0; t < S; t++) {
+            float4* tr = traj_.p + (size_t)t * 2 * n;
+            XPBD_CUDA(cudaMemcpyAsync(tr, x_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+            XPBD_CUDA(cudaMemcpyAsync(tr + n, v_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+            if (t + 1 < S) {
+                record_substep(Mode::Step, 0, 1, sdt, src);
+                src = 1 - src;
+            }
+        }
+        // adjoint of the segment's substeps, last first
+        for (int t = S - 1; t >= 0; t--) {
+            const float4* tr = traj_.p + (size_t)t * 2 * n;
+            XPBD_CUDA(cudaMemcpyAsync(x_[0].p, tr, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+            XPBD_CUDA(cudaMemcpyAsync(v_[0].p, tr + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+            prepare_grid(sdt, 0);
+            a.sids = pair_v_[(plan_.passes - 1) & 1].p;
+            launch_adjoint_substep(stream_, a);
+        }
+    }
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    auto download = [&](const float4* d, float* h) {
+        if (!h) return;
+        launch_unpack_xyz(stream_, (int64_t)n, d, xyz_stage_.p);
+        XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+        XPBD_CUDA(cudaStreamSynchronize(stream_));
+        std::memcpy(h, pinned_, n * 3 * sizeof(float));
+    };
+    download(gx_.p, gx0);
+    download(gv_.p, gv0);
+    if (gw) XPBD_CUDA(cudaMemcpy(gw, gw_.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    double acc[3];
+    XPBD_CUDA(cudaMemcpy(acc, param_acc_.p, sizeof(acc), cudaMemcpyDeviceToHost));
+    if (params) {  // soft_contact_mu, shape_material_mu (plane mu = their mean), particle_mu, restitution
+        params[0] = 0.5 * acc[0];
+        params[1] = 0.5 * acc[0];
+        params[2] = acc[1];
+        params[3] = acc[2];
+    }
+    // leave the solver at the rollout's final state
+    const float4* fin = ckpt_.p + (size_t)((ro_frames_ + ro_ckpt_ - 1) / ro_ckpt_) * 2 * n;
+    XPBD_CUDA(cudaMemcpyAsync(x_[cur_].p, fin, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+    XPBD_CUDA(cudaMemcpyAsync(v_[cur_].p, fin + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+    const int cc = contact_count_;
+    finish_frame(1);  // raises on a device-side error of the replay
+    contact_count_ = cc;
 }
 
 }  // namespace xpbd

@@ -92,6 +92,13 @@ class Solver {
                     const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb);
     void get_bodies(float* q, float* qd, size_t nb);
     void set_body_params(const xpbd_body_params& p);
+    // differentiable rollout: `frames` frames like step(), checkpointing the state every
+    // checkpoint_frames frames; rollout_backward runs the adjoint of the whole rollout
+    void rollout(float dt, int substeps, int iterations, int frames, int checkpoint_frames);
+    // new material / contact parameters (every field but the sizes, device and diagnostics)
+    void update_config(const xpbd_config& cfg);
+    void rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
+                          double* params);
     void step(float dt, int substeps, int iterations);
     void collide_only();
     void step_solve_only(float dt, int substeps, int iterations);
@@ -241,6 +248,14 @@ class Solver {
     DevBuf<float> margins_;
     DevBuf<int> watertight_;
     float avg_edge0_ = 0.0f;
+    // differentiable rollout
+    bool rollout_valid_ = false;
+    float ro_dt_ = 0.0f;
+    int ro_substeps_ = 0, ro_frames_ = 0, ro_ckpt_ = 0;
+    DevBuf<float4> ckpt_, traj_, gx_, gv_, gacc_, part_xp_, part_vp_, part_x0_, part_v0_;
+    DevBuf<float> gw_, block_params_;
+    DevBuf<double> param_acc_;
+    void prepare_grid(float sdt, int src);
     // diagnostics
     DevBuf<float> delta_;
     DevBuf<uint32_t> diag_header_;

@@ -183,6 +183,33 @@ class XpbdSolver:
             setattr(bp, k, v)
         _check(_lib.xpbd_set_body_params(self._h, C.byref(bp)))
 
+    def update_config(self, config):
+        """New contact / material parameters after init (xpbd_update_config)."""
+        _check(_lib.xpbd_update_config(self._h, C.byref(config._c)))
+
+    # ---- differentiable rollout (extension) -----------------------------------------
+    def rollout(self, dt, substeps, frames, iterations=1, checkpoint_frames=2):
+        """Step `frames` frames (like step) keeping checkpoints for rollout_backward."""
+        _check(_lib.xpbd_rollout(self._h, float(dt), int(substeps), int(iterations), int(frames),
+                                 int(checkpoint_frames)))
+
+    def rollout_backward(self, grad_x_final, grad_v_final=None):
+        """Adjoint of the last rollout: dict of float32 gradients w.r.t. the initial
+        positions 'x0' (n, 3), velocities 'v0' (n, 3), inverse masses 'inv_mass' (n,) and the
+        float64 scalars 'soft_contact_mu', 'shape_material_mu', 'particle_mu',
+        'soft_contact_restitution'."""
+        n = self.particle_count
+        gx = _f32(grad_x_final).reshape(-1)
+        gv = None if grad_v_final is None else _f32(grad_v_final).reshape(-1)
+        out_x = np.zeros((n, 3), np.float32)
+        out_v = np.zeros((n, 3), np.float32)
+        out_w = np.zeros(n, np.float32)
+        params = (C.c_double * 4)()
+        _check(_lib.xpbd_rollout_backward(self._h, _ptr(gx, _FP), _ptr(gv, _FP), _ptr(out_x, _FP),
+                                          _ptr(out_v, _FP), _ptr(out_w, _FP), params))
+        return {"x0": out_x, "v0": out_v, "inv_mass": out_w, "soft_contact_mu": params[0],
+                "shape_material_mu": params[1], "particle_mu": params[2], "soft_contact_restitution": params[3]}
+
     def init_batched(self, config, scene_counts, max_contacts=0):
         """Independent scenes stepped together (xpbd_batch_init). Particle arrays passed to
         set_particles and returned by the getters are the scenes' particles concatenated in

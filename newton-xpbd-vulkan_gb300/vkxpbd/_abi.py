@@ -107,6 +107,9 @@ SIGNATURES = {
     "xpbd_set_body_params": (C.c_int, [_P, C.POINTER(BodyParams)]),
     "xpbd_set_bodies": (C.c_int, [_P, _F, _F, _F, _F, _F, _F, _I, _Z]),
     "xpbd_get_bodies": (C.c_int, [_P, _F, _F, _Z]),
+    "xpbd_update_config": (C.c_int, [_P, C.POINTER(Config)]),
+    "xpbd_rollout": (C.c_int, [_P, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "xpbd_rollout_backward": (C.c_int, [_P, _F, _F, _F, _F, _F, C.POINTER(C.c_double)]),
     "xpbd_batch_init": (C.c_int, [_P, C.POINTER(Config), C.POINTER(C.c_size_t), _Z, _Z]),
     "xpbd_batch_scene_count": (_Z, [_P]),
     "xpbd_batch_scene_offsets": (C.c_int, [_P, C.POINTER(C.c_size_t), _Z]),

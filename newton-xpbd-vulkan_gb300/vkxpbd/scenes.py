@@ -269,3 +269,20 @@ def mixed(dims=(128, 128, 64), spacing=0.01, radius=0.005, jitter=0.001, bottom_
     pos[:, 0:2] = rng.uniform(-half_w, half_w, size=(n_boxes, 2))
     pos[:, 2] = rng.uniform(top + 0.1, top + 1.1, size=n_boxes)
     return add_boxes(sc, he, pos, quats)
+
+
+def throw(dims=(32, 32, 32), spacing=0.02, radius=0.01, jitter=0.002, bottom_z=0.1, v_mean=(2.0, 3.0, 0.0),
+          v_std=0.1, inv_mass=1000.0, seed=SEED_VELOCITY, frames=60, name="throw") -> Scene:
+    """Differentiable throw: a dims lattice (32,768 particles for the defaults) with per-particle
+    velocities ~ N(v_mean, v_std^2) per component (seed 43), falling from bottom_z onto the
+    plane; plane and particle-particle contacts, restitution on."""
+    sc = pile(dims, spacing, radius, jitter, bottom_z, inv_mass, frames=frames, name=name)
+    rng = np.random.default_rng(seed)
+    sc.velocities = (np.asarray(v_mean, np.float64) + v_std * rng.normal(size=(sc.n, 3))).astype(np.float32)
+    return sc
+
+
+def throw_target(seed=SEED_TARGET):
+    """Target centroid of the throw loss: uniform in [-1, 1]^2 x [0, 0.5] (seed 47)."""
+    rng = np.random.default_rng(seed)
+    return np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(0, 0.5)], np.float64)

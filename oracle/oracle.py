@@ -92,6 +92,9 @@ def load(precision: str = "f32") -> C.CDLL:
     lib.or_set_bodies.argtypes = [_P, _F, _F, _F, _F, _F, _F, _I, C.c_int64]
     lib.or_get_bodies.argtypes = [_P, _F, _F]
     lib.or_set_body_params.argtypes = [_P, C.POINTER(BodyParams)]
+    _DP = C.POINTER(C.c_double)
+    lib.or_rollout.argtypes = [_P, C.c_float, C.c_int, C.c_int, C.c_int]
+    lib.or_rollout_backward.argtypes = [_P, _F, _F, _DP, _DP, _DP, _DP]
     lib.or_rigid_contact_overflows.restype = C.c_int64
     lib.or_rigid_contact_overflows.argtypes = [_P]
     lib.or_step.argtypes = [_P, C.c_float, C.c_int, C.c_int]
@@ -222,6 +225,32 @@ class OracleSolver:
         for k, v in {**BODY_PARAM_DEFAULTS, **kw}.items():
             setattr(bp, k, v)
         self.lib.or_set_body_params(self.h, C.byref(bp))
+
+    def rollout(self, dt, substeps, frames, iterations=1):
+        rc = self.lib.or_rollout(self.h, float(dt), int(substeps), int(iterations), int(frames))
+        if rc != 0:
+            raise RuntimeError("oracle rollout: plane and particle contacts only, one iteration")
+
+    def rollout_backward(self, gx_final, gv_final=None):
+        """Adjoint of the last rollout: dict of gradients (float64) w.r.t. initial positions,
+        initial velocities, inverse masses and the contact parameters."""
+        n = self.n
+        gx = f32(gx_final).reshape(-1)
+        gv = None if gv_final is None else f32(gv_final).reshape(-1)
+        out = {k: np.zeros(sz, np.float64) for k, sz in (("x0", 3 * n), ("v0", 3 * n), ("inv_mass", n), ("params", 4))}
+        D = C.POINTER(C.c_double)
+        rc = self.lib.or_rollout_backward(self.h, _fp(gx, _F), _fp(gv, _F), out["x0"].ctypes.data_as(D),
+                                          out["v0"].ctypes.data_as(D), out["inv_mass"].ctypes.data_as(D),
+                                          out["params"].ctypes.data_as(D))
+        if rc == -2:
+            raise RuntimeError("oracle rollout_backward: the v_max clamp fired in the forward pass")
+        if rc != 0:
+            raise RuntimeError("oracle rollout_backward: no rollout")
+        out["x0"] = out["x0"].reshape(n, 3)
+        out["v0"] = out["v0"].reshape(n, 3)
+        p = out.pop("params")
+        out.update(soft_contact_mu=p[0], shape_material_mu=p[1], particle_mu=p[2], soft_contact_restitution=p[3])
+        return out
 
     def rigid_contact_overflows(self):
         return int(self.lib.or_rigid_contact_overflows(self.h))

@@ -219,6 +219,14 @@ typedef struct {
     float avg_edge;
 } or_mesh;
 
+/* Stored trajectory of a differentiable rollout. */
+typedef struct {
+    int64_t steps;      /* substeps stored */
+    real *x, *v;        /* (steps + 1) x 3n: state at the start of every substep, then the final */
+    real sdt, inv;
+    int clamped;
+} or_traj;
+
 /* Rigid contact generated for one vertex of a dynamic body's mesh (shape0 = that
  * body's mesh shape): the record solve_body_contact_positions.comp:8-18 reads. */
 #define RC_CAP 4 /* contacts per vertex */
@@ -272,6 +280,7 @@ struct or_solver {
     int32_t* rc_cnt;  /* per vertex of the concatenated vertex array */
     or_rcontact* rc;  /* RC_CAP per vertex */
     int64_t rc_overflow, partner_dummy;
+    or_traj traj;     /* differentiable rollout */
 };
 
 static void* xcalloc(size_t n, size_t sz) {
@@ -348,6 +357,7 @@ void or_destroy(or_solver* s) {
     free(s->vsnap); free(s->w); free(s->r); free(s->flags);
     free(s->cpart); free(s->cshape); free(s->cbpos); free(s->cbvel); free(s->cnorm);
     free(s->bdel); free(s->bvalid);
+    free(s->traj.x); free(s->traj.v);
     free(s->cells); free(s->ids); free(s->scells); free(s->sids); free(s->cstart); free(s->cend);
     for (int64_t m = 0; m < s->nmesh; m++) {
         free(s->meshes[m].verts); free(s->meshes[m].tris); free(s->meshes[m].lowers);
@@ -1900,6 +1910,271 @@ static void restitution(or_solver* s) { /* scene.cpp:983-989 */
     int64_t count = s->ccount_raw < s->cmax ? s->ccount_raw : s->cmax;
     memcpy(s->vsnap, s->v, sizeof(real) * 3 * (size_t)s->n);
     for (int64_t t = 0; t < count; t++) restitution_contact(s, t);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Differentiable rollout: forward trajectory and hand-written adjoint          */
+/* ------------------------------------------------------------------------- */
+
+/* pair_backward: exact derivative of one particle-particle term of
+ * solve_particle_particle_contacts.comp:159-177 (pair_d = diff / (w_i + w_j)) for the
+ * upstream gradient G of pair_d; the contact set and the max() branch are fixed. */
+static void pair_backward(v3 raw, v3 vrel, real ri, real rj, real wi, real wj, real k_mu, real dt, v3 G, v3* g_u,
+                          v3* g_vrel, real* g_w, real* g_kmu, v3* pair_d) {
+    /* forward values, computed as the forward computes them (branch decisions must agree) */
+    real d = exact_length(raw);
+    real err = d - ri - rj;
+    real denom = wi + wj;
+    v3 nn = exact_div(raw, d);
+    real vn = exact_dot(nn, vrel);
+    v3 vt = mk(R_FMA(vn, -nn.x, vrel.x), R_FMA(vn, -nn.y, vrel.y), R_FMA(vn, -nn.z, vrel.z));
+    real vt_len = exact_length(vt);
+    real a = k_mu * err, b = -vt_len * dt;
+    int branch_a = !(a < b);
+    real lf = branch_a ? a : b;
+    v3 vt_dir = vt_len > RF(0.0) ? exact_div(vt, vt_len) : mk(RF(0.0), RF(0.0), RF(0.0));
+    v3 p2 = vmuls(nn, err);
+    v3 diff = mk(R_FMA(vt_dir.x, lf, -p2.x), R_FMA(vt_dir.y, lf, -p2.y), R_FMA(vt_dir.z, lf, -p2.z));
+    *pair_d = exact_div(diff, denom);
+    /* reverse mode */
+    v3 g_diff = vmuls(G, RF(1.0) / denom);
+    *g_w = -vdot(G, diff) / (denom * denom);
+    v3 g_vt_dir = vmuls(g_diff, lf);
+    real g_lf = vdot(g_diff, vt_dir);
+    v3 g_nn = vmuls(g_diff, -err);
+    real g_err = -vdot(g_diff, nn);
+    real g_vt_len = RF(0.0);
+    if (branch_a) {
+        g_err += k_mu * g_lf;
+        *g_kmu += err * g_lf;
+    } else {
+        g_vt_len = -dt * g_lf;
+    }
+    v3 g_vt = mk(RF(0.0), RF(0.0), RF(0.0));
+    if (vt_len > RF(0.0))
+        g_vt = vadd(vmuls(vsub(g_vt_dir, vmuls(vt_dir, vdot(vt_dir, g_vt_dir))), RF(1.0) / vt_len),
+                    vmuls(vt_dir, g_vt_len));
+    v3 gv = g_vt;
+    real g_vn = -vdot(g_vt, nn);
+    g_nn = vadd(g_nn, vmuls(g_vt, -vn));
+    g_nn = vadd(g_nn, vmuls(vrel, g_vn));
+    gv = vadd(gv, vmuls(nn, g_vn));
+    *g_vrel = gv;
+    *g_u = vadd(vmuls(vsub(g_nn, vmuls(nn, vdot(nn, g_nn))), RF(1.0) / d), vmuls(nn, g_err));
+}
+
+/* The particle-particle term of pair (i, j) with the forward's filters
+ * (solve_particle_particle_contacts.comp:145-157); returns 0 when it is skipped. */
+static int pair_term(const or_solver* s, int32_t i, int32_t j, const real* X, real R, v3* raw_out) {
+    v3 raw = vsub(ld3(X, i), ld3(X, j));
+    if (R_FABS(raw.x) > R || R_FABS(raw.y) > R || R_FABS(raw.z) > R) return 0;
+    real d = exact_length(raw);
+    real err = d - s->r[i] - s->r[j];
+    if (err > (real)s->cfg.particle_cohesion || d <= RF(0.0)) return 0;
+    if (s->w[i] + s->w[j] <= RF(0.0)) return 0;
+    *raw_out = raw;
+    return 1;
+}
+
+static or_traj* traj_of(or_solver* s) { return &s->traj; }
+
+int or_rollout(or_solver* s, float dt, int substeps, int iterations, int frames) {
+    if (!s->finalized) or_finalize_meshes(s);
+    if (s->nmesh > 0 || iterations != 1) return -1;
+    or_traj* T = traj_of(s);
+    free(T->x);
+    free(T->v);
+    T->steps = (int64_t)substeps * frames;
+    size_t n3 = (size_t)s->n * 3;
+    T->x = xcalloc((size_t)(T->steps + 1) * n3, sizeof(real));
+    T->v = xcalloc((size_t)(T->steps + 1) * n3, sizeof(real));
+    float sdt_f = dt / (float)substeps;
+    float inv_f = 1.0f / s->cfg.search_radius;
+    T->sdt = (real)sdt_f;
+    T->inv = (real)inv_f;
+    T->clamped = 0;
+    int64_t t = 0;
+    for (int f = 0; f < frames; f++)
+        for (int sub = 0; sub < substeps; sub++, t++) {
+            memcpy(T->x + (size_t)t * n3, s->x, n3 * sizeof(real));
+            memcpy(T->v + (size_t)t * n3, s->v, n3 * sizeof(real));
+            collide(s);
+            integrate(s, T->sdt);
+            for (int64_t i = 0; i < s->n; i++)
+                if (vlength(ld3(s->v, i)) > (real)s->cfg.particle_v_max) T->clamped = 1;
+            build_grid(s, T->inv);
+            iterate(s, T->sdt, 1, T->inv);
+            restitution(s);
+            for (int64_t i = 0; i < s->n; i++)
+                if (vlength(ld3(s->v, i)) > RF(0.5) * (real)s->cfg.particle_v_max) T->clamped = 1;
+        }
+    memcpy(T->x + (size_t)t * n3, s->x, n3 * sizeof(real));
+    memcpy(T->v + (size_t)t * n3, s->v, n3 * sizeof(real));
+    return 0;
+}
+
+int or_rollout_backward(or_solver* s, const float* gx_final, const float* gv_final, double* gx0_out,
+                        double* gv0_out, double* gw_out, double* params) {
+    or_traj* T = traj_of(s);
+    if (!T->x) return -1;
+    if (T->clamped) return -2;
+    int64_t n = s->n;
+    size_t n3 = (size_t)n * 3;
+    real dt = T->sdt, inv = T->inv;
+    real relax = (real)s->cfg.soft_contact_relaxation;
+    real ka = (real)s->cfg.particle_adhesion;
+    real e = (real)s->cfg.soft_contact_restitution;
+    real mu_plane = RF(0.5) * ((real)s->cfg.soft_contact_mu + s->shape_mu[0]);
+    real k_mu = (real)s->cfg.particle_mu;
+    real* Gx = xcalloc(n3, sizeof(real));
+    real* Gv = xcalloc(n3, sizeof(real));
+    real* gxp = xcalloc(n3, sizeof(real));
+    real* gvp = xcalloc(n3, sizeof(real));
+    real* gx0 = xcalloc(n3, sizeof(real));
+    real* gv0 = xcalloc(n3, sizeof(real));
+    real* gw = xcalloc((size_t)n, sizeof(real));
+    real g_mu = RF(0.0), g_kmu = RF(0.0), g_e = RF(0.0);
+    for (size_t k = 0; k < n3; k++) {
+        Gx[k] = (real)gx_final[k];
+        Gv[k] = gv_final ? (real)gv_final[k] : RF(0.0);
+    }
+    for (int64_t t = T->steps - 1; t >= 0; t--) {
+        /* replay the forward's intermediates of substep t */
+        memcpy(s->x, T->x + (size_t)t * n3, n3 * sizeof(real));
+        memcpy(s->v, T->v + (size_t)t * n3, n3 * sizeof(real));
+        collide(s);
+        integrate(s, dt); /* s->x, s->v = predicted; s->x0, s->v0 = start of the substep */
+        build_grid(s, inv);
+        memset(gx0, 0, n3 * sizeof(real));
+        memset(gv0, 0, n3 * sizeof(real));
+        memset(gvp, 0, n3 * sizeof(real));
+        int64_t count = s->ccount_raw < s->cmax ? s->ccount_raw : s->cmax;
+        real* gv1 = Gv; /* restitution: v_final.z = v1.z + (-v1.z + max(-e v0.z, 0)) */
+        if (s->cfg.enable_restitution) {
+            for (int64_t c = 0; c < count; c++) {
+                int32_t i = s->cpart[c];
+                v3 x0 = ld3(s->x0, i), v0 = ld3(s->v0, i);
+                v3 bx = ld3(s->cbpos, c);
+                real cc = (x0.z - bx.z) - s->r[i];
+                if (cc > ka) continue;
+                real rel_old = v0.z;
+                if (!(rel_old < RF(0.0))) continue;
+                real g_rt = gv1[i * 3 + 2];
+                gv1[i * 3 + 2] = RF(0.0);
+                if ((-e) * rel_old > RF(0.0)) {
+                    gv0[i * 3 + 2] += g_rt * (-e);
+                    g_e += g_rt * (-rel_old);
+                }
+            }
+        }
+        /* apply: x1 = xp + delta, v1 = (x1 - x0) / dt */
+        for (size_t k = 0; k < n3; k++) {
+            real gx1 = Gx[k] + gv1[k] / dt;
+            gx0[k] -= gv1[k] / dt;
+            gxp[k] = gx1; /* also dL/d delta */
+        }
+        real* gdelta = xcalloc(n3, sizeof(real));
+        memcpy(gdelta, gxp, n3 * sizeof(real));
+        /* plane contacts (solve_particle_shape_contacts.comp with w2 = 0) */
+        for (int64_t c = 0; c < count; c++) {
+            int32_t i = s->cpart[c];
+            v3 xp = ld3(s->x, i), vp = ld3(s->v, i);
+            v3 bx = ld3(s->cbpos, c);
+            real cc = (xp.z - bx.z) - s->r[i];
+            if (cc > ka) continue;
+            v3 vt = mk(vp.x, vp.y, RF(0.0));
+            real vt_len = exact_length(vt);
+            real a = mu_plane * cc, b = -vt_len * dt;
+            int branch_a = !(a < b);
+            real lf = branch_a ? a : b;
+            v3 vt_dir = vt_len > RF(0.0) ? exact_div(vt, vt_len) : mk(RF(0.0), RF(0.0), RF(0.0));
+            v3 g_diff = vmuls(ld3(gdelta, i), relax);
+            v3 g_vt_dir = vmuls(g_diff, lf);
+            real g_lf = vdot(g_diff, vt_dir);
+            real g_c = -g_diff.z, g_vt_len = RF(0.0);
+            if (branch_a) {
+                g_c += mu_plane * g_lf;
+                g_mu += cc * g_lf;
+            } else {
+                g_vt_len = -dt * g_lf;
+            }
+            if (vt_len > RF(0.0)) {
+                v3 g_vt = vadd(vmuls(vsub(g_vt_dir, vmuls(vt_dir, vdot(vt_dir, g_vt_dir))), RF(1.0) / vt_len),
+                               vmuls(vt_dir, g_vt_len));
+                gvp[i * 3 + 0] += g_vt.x;
+                gvp[i * 3 + 1] += g_vt.y;
+            }
+            gxp[i * 3 + 2] += g_c;
+        }
+        /* particle-particle: total_i = w_i * relax * sum_j pair_d_ij */
+        real R_add = (real)s->cfg.particle_max_radius + (real)s->cfg.particle_cohesion;
+        for (int64_t tid = 0; tid < n; tid++) {
+            int32_t i = (int32_t)s->sids[tid];
+            v3 x = ld3(s->x, i);
+            real R = s->r[i] + R_add;
+            v3 Gi = ld3(gdelta, i);
+            v3 gacc = vmuls(Gi, s->w[i] * relax);
+            v3 acc = mk(RF(0.0), RF(0.0), RF(0.0));
+            int32_t xs = f2i(R_FLOOR((x.x - R) * inv)), ys = f2i(R_FLOOR((x.y - R) * inv)),
+                    zs = f2i(R_FLOOR((x.z - R) * inv));
+            int32_t xe = f2i(R_FLOOR((x.x + R) * inv)), ye = f2i(R_FLOOR((x.y + R) * inv)),
+                    ze = f2i(R_FLOOR((x.z + R) * inv));
+            if (xe > xs + GRID_DIM - 1) xe = xs + GRID_DIM - 1;
+            if (ye > ys + GRID_DIM - 1) ye = ys + GRID_DIM - 1;
+            if (ze > zs + GRID_DIM - 1) ze = zs + GRID_DIM - 1;
+            for (int32_t cz = zs; cz <= ze; cz++)
+                for (int32_t cy = ys; cy <= ye; cy++)
+                    for (int32_t cx = xs; cx <= xe; cx++) {
+                        int32_t cell = cell_index(cx, cy, cz);
+                        for (int32_t k = s->cstart[cell]; k < s->cend[cell]; k++) {
+                            int32_t j = (int32_t)s->sids[k];
+                            v3 raw;
+                            if (j == i || !pair_term(s, i, j, s->x, R, &raw)) continue;
+                            v3 vrel = vsub(ld3(s->v, i), ld3(s->v, j));
+                            v3 g_u, g_vrel, pd;
+                            real g_den;
+                            pair_backward(raw, vrel, s->r[i], s->r[j], s->w[i], s->w[j], k_mu, dt, gacc, &g_u, &g_vrel,
+                                          &g_den, &g_kmu, &pd);
+                            acc = vadd(acc, pd);
+                            for (int a = 0; a < 3; a++) {
+                                real gu = a == 0 ? g_u.x : (a == 1 ? g_u.y : g_u.z);
+                                real gvr = a == 0 ? g_vrel.x : (a == 1 ? g_vrel.y : g_vrel.z);
+                                gxp[i * 3 + a] += gu;
+                                gxp[j * 3 + a] -= gu;
+                                gvp[i * 3 + a] += gvr;
+                                gvp[j * 3 + a] -= gvr;
+                            }
+                            gw[i] += g_den;
+                            gw[j] += g_den;
+                        }
+                    }
+            gw[i] += vdot(Gi, acc) * relax;
+        }
+        free(gdelta);
+        /* integrate: xp = x0 + vp dt, vp = v0 + g dt [w > 0] */
+        for (size_t k = 0; k < n3; k++) {
+            gvp[k] += gxp[k] * dt;
+            Gx[k] = gx0[k] + gxp[k];
+            Gv[k] = gv0[k] + gvp[k];
+        }
+    }
+    for (size_t k = 0; k < n3; k++) {
+        if (gx0_out) gx0_out[k] = (double)Gx[k];
+        if (gv0_out) gv0_out[k] = (double)Gv[k];
+    }
+    for (int64_t i = 0; i < n; i++)
+        if (gw_out) gw_out[i] = (double)gw[i];
+    if (params) {
+        params[0] = (double)(RF(0.5) * g_mu);
+        params[1] = (double)(RF(0.5) * g_mu);
+        params[2] = (double)g_kmu;
+        params[3] = (double)g_e;
+    }
+    /* leave the solver at the final state of the rollout */
+    memcpy(s->x, T->x + (size_t)T->steps * n3, n3 * sizeof(real));
+    memcpy(s->v, T->v + (size_t)T->steps * n3, n3 * sizeof(real));
+    free(Gx); free(Gv); free(gxp); free(gvp); free(gx0); free(gv0); free(gw);
+    return 0;
 }
 
 int or_step(or_solver* s, float dt, int substeps, int iterations) { /* scene.cpp:698-1092 */

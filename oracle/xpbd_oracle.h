@@ -109,6 +109,21 @@ int or_set_contact_data(or_solver* s, const int32_t* particles, const int32_t* s
 void or_get_positions(const or_solver* s, float* out_xyz);
 void or_get_velocities(const or_solver* s, float* out_xyz);
 void or_get_state64(const or_solver* s, double* x_out, double* v_out);
+
+/* Differentiable rollout (extension; no reference counterpart). or_rollout steps
+ * `frames` frames like or_step and keeps the state at the start of every substep;
+ * or_rollout_backward runs the adjoint of those substeps for the gradient of a loss
+ * with respect to the final positions / velocities (gx_final, gv_final; 3n each,
+ * gv_final may be NULL) and returns, in double precision, the gradients with respect
+ * to the initial positions and velocities (3n each), the inverse masses (n) and
+ * params[4] = {soft_contact_mu, shape_material_mu, particle_mu,
+ * soft_contact_restitution}. Supported: ground plane and particle-particle contacts,
+ * no meshes, every particle active, equal radii, one solver iteration, the v_max
+ * clamp inactive (returns -2 when a clamp fired). Contact sets and the branches of the
+ * friction max() are taken as fixed at their forward values. */
+int or_rollout(or_solver* s, float dt, int substeps, int iterations, int frames);
+int or_rollout_backward(or_solver* s, const float* gx_final, const float* gv_final, double* gx0, double* gv0,
+                        double* gw, double* params);
 int64_t or_contact_count(const or_solver* s);      /* clamped to contact_max */
 int64_t or_contact_count_raw(const or_solver* s);  /* unclamped counter value */
 void or_get_contacts(const or_solver* s, int32_t* particles, int32_t* shapes, float* body_pos,
