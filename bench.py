@@ -205,6 +205,8 @@ def run_gpu(args):
             parts["batched"] = measure_batched(args, dev, None)
         if "mixed" in args.only:
             parts["mixed"] = measure_mixed(args, dev)
+        if "diff" in args.only:
+            parts["diff"] = measure_diff(args, dev)
         print(json.dumps(parts), flush=True)
         return
     if world > 1:
@@ -306,7 +308,8 @@ def run_gpu(args):
     }
     del solver
     for name, on, fn in (("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev, flush)),
-                         ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev))):
+                         ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev)),
+                         ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev))):
         if rank == 0 and on:
             try:
                 result[name] = fn()
@@ -487,6 +490,62 @@ def measure_mixed(args, dev):
             "box_height_range": [round(float(np.nanmin(bq[:, 2])), 3), round(float(np.nanmax(bq[:, 2])), 3)]}
 
 
+def measure_diff(args, dev):
+    """Differentiable throw: 32,768 particles (32^3, spacing 0.02, r 0.01) with velocities
+    N((2,3,0), 0.1^2) (seed 43), 600 substeps (60 frames x 10), plane + particle contacts,
+    checkpoint every 20 substeps; loss = |mean(x_final) - target|^2 (target seed 47).
+    Forward = the checkpointed rollout; backward = replay + adjoint of every substep."""
+    import torch
+    import vkxpbd
+    from vkxpbd import scenes
+
+    sc = scenes.throw()
+    target = scenes.throw_target()
+    cfg = vkxpbd.SolverConfig()
+    sc.apply_config(cfg)
+    cfg.device_index = dev.index
+    s = vkxpbd.XpbdSolver()
+    s.init(cfg, sc.n)
+    s.finalize_meshes()
+    frames, ckpt = args.diff_frames, 2
+    fwd, bwd = [], []
+    for rep in range(args.diff_reps + 1):  # first repetition warms up (graph capture, allocations)
+        s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        s.rollout(DT, SUBSTEPS, frames, 1, ckpt)
+        x = s.get_positions()
+        t1 = time.perf_counter()
+        m = x.astype(np.float64).mean(axis=0)
+        gx = np.tile((2.0 * (m - target) / sc.n).astype(np.float32), (sc.n, 1))
+        t2 = time.perf_counter()
+        g = s.rollout_backward(gx)
+        t3 = time.perf_counter()
+        if rep:
+            fwd.append(t1 - t0)
+            bwd.append(t3 - t2)
+    f, b = statistics.median(fwd), statistics.median(bwd)
+    # growth of the exact gradient with the horizon (the Jacobian of the contact projection
+    # in a dense pile has modes larger than 1 per substep)
+    growth = {}
+    for hf in (1, 3, 6, 12, 24):
+        s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+        s.rollout(DT, SUBSTEPS, hf, 1, ckpt)
+        mh = s.get_positions().astype(np.float64).mean(axis=0)
+        gh = s.rollout_backward(np.tile((2.0 * (mh - target) / sc.n).astype(np.float32), (sc.n, 1)))
+        growth[str(hf * SUBSTEPS)] = {"v0_norm": float(np.linalg.norm(gh["v0"])),
+                                      "soft_contact_mu": float(gh["soft_contact_mu"])}
+    return {"workload": "diff_throw", "particles": sc.n, "substeps": frames * SUBSTEPS,
+            "checkpoint_substeps": ckpt * SUBSTEPS, "reps": args.diff_reps, "forward_s": f, "backward_s": b,
+            "fwd_bwd_over_fwd": (f + b) / f, "forward_value": sc.n * frames * SUBSTEPS / f, "unit": UNIT,
+            "loss": float(((m - target) ** 2).sum()),
+            "grad": {"soft_contact_mu": g["soft_contact_mu"], "particle_mu": g["particle_mu"],
+                     "soft_contact_restitution": g["soft_contact_restitution"],
+                     "v0_norm": float(np.linalg.norm(g["v0"])), "inv_mass_norm": float(np.linalg.norm(g["inv_mass"]))},
+            "gradient_vs_horizon_substeps": growth,
+            "note": "host wall clock around xpbd_rollout / xpbd_rollout_backward (synchronous calls)"}
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path: the oracle port on all host threads."""
     rank, world, _ = dist_env()
@@ -535,6 +594,8 @@ def main():
     ap.add_argument("--batched-frames", type=int, default=10)
     ap.add_argument("--mixed-frames", type=int, default=10, help="0 skips the particles + boxes measurement")
     ap.add_argument("--mixed-preroll", type=int, default=20)
+    ap.add_argument("--diff-frames", type=int, default=60, help="0 skips the differentiable rollout measurement")
+    ap.add_argument("--diff-reps", type=int, default=3)
     ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed (default all)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -10,12 +10,10 @@
 // pass (recomputed from the substep's start state), so the adjoint is the exact
 // derivative of the piecewise-smooth map the forward evaluates.
 //
-// Two kernels per substep, both in hash-grid order. adj_own: particle i's
-// restitution, apply and plane terms and, for every neighbour j of its
-// particle-particle sum, the derivative with respect to i's own state;
-// writes dL/d(sum) for i. adj_neighbours: particle j gathers the derivative of
-// every neighbour i's sum with respect to j's state (no atomics: the neighbour
-// relation is symmetric), then steps the adjoint through the integration.
+// Two kernels per substep, both in hash-grid order: adj_local (restitution,
+// apply and plane terms of each particle, and dL/d(sum_j pair_d) of each
+// particle) and adj_pairs (one pass over the neighbours that gathers every
+// pair's derivative without atomics, then the adjoint of the integration).
 #include "kernels.h"
 #include "particle.cuh"
 #include "xmath.cuh"
@@ -100,19 +98,22 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 constexpr int kAdjThreads = 128;
 
-__global__ void __launch_bounds__(kAdjThreads) k_adj_own(AdjointArgs a) {
+// Per-particle part: restitution, apply and plane terms (no neighbour access).
+// Writes dL/d(sum_j pair_d) of the particle (gacc) for the pair kernel.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_local(AdjointArgs a) {
     __shared__ float s_red[3][kAdjThreads / 32];
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    float g_mu = 0.0f, g_kmu = 0.0f, g_e = 0.0f;
+    float g_mu = 0.0f, g_e = 0.0f;
     if (k < a.n) {
         const uint32_t id = a.sids[k];
         const float4 ox = a.rx[k], ov = a.rv[k];
         const v3 xp = xyz(ox), vp = xyz(ov);
         const float r = ox.w, w = ov.w;
         const v3 x0 = xyz(a.x0[id]), v0 = xyz(a.v0[id]);
-        const uint32_t info = a.cinfo[id];
-        const bool plane = (info & kPlaneBit) != 0;
-        v3 gx1 = xyz(a.gx_in[id]), gv1 = xyz(a.gv_in[id]);
+        // plane contact of the substep (generate_plane_contacts.comp:32-38 on the start position)
+        const bool plane = a.plane_on && (a.flags[id] & 1) && (x0.z - a.altitude < a.margin + r);
+        const v3 gx1 = xyz(a.gx_in[id]);
+        v3 gv1 = xyz(a.gv_in[id]);
         v3 gx0a = mk3(0.0f, 0.0f, 0.0f), gv0a = gx0a;
         // restitution (apply_particle_shape_restitution.comp:283-315): v.z <- max(-e v0.z, 0)
         if (a.restitution_on && plane) {
@@ -131,7 +132,6 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_own(AdjointArgs a) {
         const v3 gdelta = vadd(gx1, vmuls(gv1, inv_dt));
         gx0a = vsub(gx0a, vmuls(gv1, inv_dt));
         v3 gxp = gdelta, gvp = mk3(0.0f, 0.0f, 0.0f);
-        float gw = 0.0f;
         // plane (solve_particle_shape_contacts.comp with a static body: w2 = 0, fd = diff relax)
         if (plane) {
             const float c = (xp.z - a.altitude) - r;
@@ -162,8 +162,47 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_own(AdjointArgs a) {
                 gxp.z += g_c;
             }
         }
-        // particle-particle: total = sum_j pair_d * w * relax; own-state derivatives
-        const v3 gacc = vmuls(gdelta, w * a.relax);
+        const v3 gacc = vmuls(gdelta, w * a.relax);  // total = sum_j pair_d * w * relax
+        a.gacc[k] = make_float4(gacc.x, gacc.y, gacc.z, 0.0f);
+        a.part_xp[k] = make_float4(gxp.x, gxp.y, gxp.z, 0.0f);
+        a.part_vp[k] = make_float4(gvp.x, gvp.y, gvp.z, 0.0f);
+        a.part_x0[k] = make_float4(gx0a.x, gx0a.y, gx0a.z, 0.0f);
+        a.part_v0[k] = make_float4(gv0a.x, gv0a.y, gv0a.z, 0.0f);
+        a.part_gd[k] = make_float4(gdelta.x, gdelta.y, gdelta.z, 0.0f);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    g_mu = warp_sum(g_mu);
+    g_e = warp_sum(g_e);
+    if (lane == 0) {
+        s_red[0][warp] = g_mu;
+        s_red[1][warp] = 0.0f;
+        s_red[2][warp] = g_e;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        float t = 0.0f;
+        for (int wv = 0; wv < kAdjThreads / 32; wv++) t += s_red[threadIdx.x][wv];
+        a.block_params[(size_t)blockIdx.x * 3 + threadIdx.x] = t;
+    }
+}
+
+// Pair part, one neighbour pass. The pair term is odd in (x_i - x_j, v_i - v_j), so its
+// Jacobian J is the same for the ordered pairs (i, j) and (j, i), and i's state receives
+// J^T (G_i - G_j) from the two sums that hold the pair (G = dL/d sum, the neighbour
+// relation being symmetric); likewise both inverse masses of a pair appear in both
+// terms through 1 / (w_i + w_j). Then the adjoint of the integration.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(AdjointArgs a) {
+    __shared__ float s_red[kAdjThreads / 32];
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float g_kmu = 0.0f;
+    if (k < a.n) {
+        const uint32_t id = a.sids[k];
+        const float4 ox = a.rx[k], ov = a.rv[k];
+        const v3 xp = xyz(ox), vp = xyz(ov);
+        const float r = ox.w, w = ov.w;
+        v3 gxp = xyz(a.part_xp[k]), gvp = xyz(a.part_vp[k]);
+        const v3 Gi = xyz(a.gacc[k]);
+        float gw = 0.0f;
         v3 acc = mk3(0.0f, 0.0f, 0.0f);
         const float R = r + a.max_radius + a.k_coh;
         for_cells(xp, R, a.inv, a.table, *a.stamp, [&](int kk) {
@@ -176,80 +215,41 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_own(AdjointArgs a) {
             if (err > a.k_coh || d <= 0.0f) return;
             const float4 nv = __ldg(&a.rv[kk]);
             if (w + nv.w <= 0.0f) return;
+            const v3 Gj = xyz(__ldg(&a.gacc[kk]));
             v3 g_u, g_vrel;
-            float g_den;
-            const v3 pd = pair_backward(raw, vsub(vp, xyz(nv)), r, nx.w, w, nv.w, a.k_mu, a.dt, gacc, g_u, g_vrel,
-                                        g_den, g_kmu);
+            float g_den, unused = 0.0f;
+            const v3 vrel = vsub(vp, xyz(nv));
+            const v3 pd = pair_backward(raw, vrel, r, nx.w, w, nv.w, a.k_mu, a.dt, vsub(Gi, Gj), g_u, g_vrel, g_den,
+                                        unused);
             acc = vadd(acc, pd);
             gxp = vadd(gxp, g_u);
             gvp = vadd(gvp, g_vrel);
             gw += g_den;
+            // particle_mu: the ordered term (i, j) of i's own sum (branch of the friction max)
+            const float vn = exact_dot(exact_div(raw, d), vrel);
+            const v3 nn = exact_div(raw, d);
+            const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y), __fmaf_rn(vn, -nn.z, vrel.z));
+            const float vt_len = exact_length(vt);
+            if (!(a.k_mu * err < -vt_len * a.dt) && vt_len > 0.0f)
+                g_kmu += err * vdot(Gi, exact_div(vt, vt_len)) / (w + nv.w);
         });
-        gw += vdot(gdelta, acc) * a.relax;
-        a.gacc[k] = make_float4(gacc.x, gacc.y, gacc.z, 0.0f);
-        a.part_xp[k] = make_float4(gxp.x, gxp.y, gxp.z, gw);
-        a.part_vp[k] = make_float4(gvp.x, gvp.y, gvp.z, 0.0f);
-        a.part_x0[k] = make_float4(gx0a.x, gx0a.y, gx0a.z, 0.0f);
-        a.part_v0[k] = make_float4(gv0a.x, gv0a.y, gv0a.z, 0.0f);
+        gw += vdot(xyz(a.part_gd[k]), acc) * a.relax;
+        // integrate (integrate_particles.comp:45-52): x_p = x0 + v_p dt, v_p = v0 + g dt
+        gvp = vadd(gvp, vmuls(gxp, a.dt));
+        const v3 gx0 = vadd(xyz(a.part_x0[k]), gxp), gv0 = vadd(xyz(a.part_v0[k]), gvp);
+        a.gx_out[id] = make_float4(gx0.x, gx0.y, gx0.z, 0.0f);
+        a.gv_out[id] = make_float4(gv0.x, gv0.y, gv0.z, 0.0f);
+        a.gw[id] += gw;
     }
-    // per-block sums of the parameter gradients (reduced in a fixed order afterwards)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    g_mu = warp_sum(g_mu);
     g_kmu = warp_sum(g_kmu);
-    g_e = warp_sum(g_e);
-    if (lane == 0) {
-        s_red[0][warp] = g_mu;
-        s_red[1][warp] = g_kmu;
-        s_red[2][warp] = g_e;
-    }
+    if (lane == 0) s_red[warp] = g_kmu;
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x == 0) {
         float t = 0.0f;
-        for (int wv = 0; wv < kAdjThreads / 32; wv++) t += s_red[threadIdx.x][wv];
-        a.block_params[(size_t)blockIdx.x * 3 + threadIdx.x] = t;
+        for (int wv = 0; wv < kAdjThreads / 32; wv++) t += s_red[wv];
+        a.block_params[(size_t)blockIdx.x * 3 + 1] = t;
     }
-}
-
-__global__ void __launch_bounds__(kAdjThreads) k_adj_neighbours(AdjointArgs a) {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
-    const uint32_t id = a.sids[k];
-    const float4 ox = a.rx[k], ov = a.rv[k];
-    const v3 xp = xyz(ox), vp = xyz(ov);
-    const float r = ox.w, w = ov.w;
-    const float4 pxp = a.part_xp[k];
-    v3 gxp = xyz(pxp), gvp = xyz(a.part_vp[k]);
-    float gw = pxp.w;
-    float unused_kmu = 0.0f;
-    // every neighbour i whose forward sum contains this particle: i's search box is at most
-    // 2 max_radius + cohesion wide, and i's own filters decide
-    const float Rb = (2.0f * a.max_radius + a.k_coh) * 1.001f;
-    for_cells(xp, Rb, a.inv, a.table, *a.stamp, [&](int kk) {
-        if (kk == (int)k) return;
-        const float4 nx = __ldg(&a.rx[kk]);
-        const float Ri = nx.w + a.max_radius + a.k_coh;
-        const v3 raw = vsub(xyz(nx), xp);  // x_i - x_j, as in i's forward sum
-        if (fabsf(raw.x) > Ri || fabsf(raw.y) > Ri || fabsf(raw.z) > Ri) return;
-        const float d = exact_length(raw);
-        const float err = d - nx.w - r;
-        if (err > a.k_coh || d <= 0.0f) return;
-        const float4 nv = __ldg(&a.rv[kk]);
-        if (nv.w + w <= 0.0f) return;
-        const float4 G4 = __ldg(&a.gacc[kk]);
-        v3 g_u, g_vrel;
-        float g_den;
-        pair_backward(raw, vsub(xyz(nv), vp), nx.w, r, nv.w, w, a.k_mu, a.dt, xyz(G4), g_u, g_vrel, g_den,
-                      unused_kmu);
-        gxp = vsub(gxp, g_u);
-        gvp = vsub(gvp, g_vrel);
-        gw += g_den;
-    });
-    // integrate (integrate_particles.comp:45-52): x_p = x0 + v_p dt, v_p = v0 + g dt
-    gvp = vadd(gvp, vmuls(gxp, a.dt));
-    const v3 gx0 = vadd(xyz(a.part_x0[k]), gxp), gv0 = vadd(xyz(a.part_v0[k]), gvp);
-    a.gx_out[id] = make_float4(gx0.x, gx0.y, gx0.z, 0.0f);
-    a.gv_out[id] = make_float4(gv0.x, gv0.y, gv0.z, 0.0f);
-    a.gw[id] += gw;
 }
 
 // Adds the per-block parameter gradients to the double accumulators, in block order.
@@ -261,11 +261,15 @@ __global__ void k_adj_params(int blocks, const float* __restrict__ block_params,
     acc[lane] += t;
 }
 
+__global__ void k_bump_stamp(uint32_t* stamp) { *stamp += 1u; }
+
+void launch_bump_stamp(cudaStream_t s, uint32_t* stamp) { k_bump_stamp<<<1, 1, 0, s>>>(stamp); }
+
 void launch_adjoint_substep(cudaStream_t s, const AdjointArgs& a) {
     if (a.n <= 0) return;
     const int blocks = (int)((a.n + kAdjThreads - 1) / kAdjThreads);
-    k_adj_own<<<blocks, kAdjThreads, 0, s>>>(a);
-    k_adj_neighbours<<<blocks, kAdjThreads, 0, s>>>(a);
+    k_adj_local<<<blocks, kAdjThreads, 0, s>>>(a);
+    k_adj_pairs<<<blocks, kAdjThreads, 0, s>>>(a);
     k_adj_params<<<1, 32, 0, s>>>(blocks, a.block_params, a.param_acc);
 }
 

@@ -282,7 +282,7 @@ struct AdjointArgs {
     const uint32_t* stamp;
     const float4* x0;
     const float4* v0;
-    const uint32_t* cinfo;
+    const int* flags;
     const float4* gx_in;
     const float4* gv_in;
     float4* gx_out;
@@ -293,12 +293,15 @@ struct AdjointArgs {
     float4* part_vp;
     float4* part_x0;
     float4* part_v0;
+    float4* part_gd;      // scratch, sorted order: dL/d delta
     float* block_params;  // 3 per block
     double* param_acc;    // [3]: plane mu (effective), particle mu, restitution
-    float dt, inv, relax, ka, altitude, mu_plane, k_mu, k_coh, max_radius, restitution;
-    int restitution_on;
+    float dt, inv, relax, ka, altitude, margin, mu_plane, k_mu, k_coh, max_radius, restitution;
+    int restitution_on, plane_on;
 };
 void launch_adjoint_substep(cudaStream_t s, const AdjointArgs& a);
+// new generation for the stamped cell table (before a cell table is rebuilt without the key kernel)
+void launch_bump_stamp(cudaStream_t s, uint32_t* stamp);
 size_t adjoint_block_count(int64_t n);
 
 // float4 state <-> packed xyz

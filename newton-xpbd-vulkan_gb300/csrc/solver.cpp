@@ -1305,10 +1305,13 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     part_vp_.alloc(nn, false);
     part_x0_.alloc(nn, false);
     part_v0_.alloc(nn, false);
+    part_gd_.alloc(nn, false);
     const size_t blocks = adjoint_block_count((int64_t)n);
     block_params_.alloc(std::max<size_t>(blocks, 1) * 3, false);
     param_acc_.alloc(3, true);
+    // per replayed substep: start state (x, v) and the sorted (key, id) pairs
     traj_.alloc((size_t)ro_ckpt_ * ro_substeps_ * 2 * nn, false);
+    traj_keys_.alloc((size_t)ro_ckpt_ * ro_substeps_ * 2 * nn, false);
     // upstream gradients (host xyz -> device float4)
     auto upload = [&](const float* h, float4* d) {
         if (h) {
@@ -1326,7 +1329,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     a.n = (int64_t)n;
     a.table = table_.p;
     a.stamp = stamp_.p;
-    a.cinfo = cinfo_.p;
+    a.flags = flags_.p;
     a.gx_in = gx_.p;
     a.gv_in = gv_.p;
     a.gx_out = gx_.p;
@@ -1337,6 +1340,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     a.part_vp = part_vp_.p;
     a.part_x0 = part_x0_.p;
     a.part_v0 = part_v0_.p;
+    a.part_gd = part_gd_.p;
     a.block_params = block_params_.p;
     a.param_acc = param_acc_.p;
     a.dt = sdt;
@@ -1344,6 +1348,8 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     a.relax = cfg_.soft_contact_relaxation;
     a.ka = cfg_.particle_adhesion;
     a.altitude = cfg_.ground_plane_altitude;
+    a.margin = cfg_.soft_contact_margin;
+    a.plane_on = cfg_.has_ground_plane ? 1 : 0;
     a.mu_plane = 0.5f * (cfg_.soft_contact_mu + cfg_.shape_material_mu);
     a.k_mu = cfg_.particle_mu;
     a.k_coh = cfg_.particle_cohesion;
@@ -1362,22 +1368,33 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
         XPBD_CUDA(cudaMemcpyAsync(x_[0].p, ck, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
         XPBD_CUDA(cudaMemcpyAsync(v_[0].p, ck + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
         int src = 0;
+        const int fin = (plan_.passes - 1) & 1;
         for (int t = 0; t < S; t++) {
             float4* tr = traj_.p + (size_t)t * 2 * n;
+            uint32_t* tk = traj_keys_.p + (size_t)t * 2 * n;
             XPBD_CUDA(cudaMemcpyAsync(tr, x_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
             XPBD_CUDA(cudaMemcpyAsync(tr + n, v_[src].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
             if (t + 1 < S) {
                 record_substep(Mode::Step, 0, 1, sdt, src);
                 src = 1 - src;
+            } else {
+                prepare_grid(sdt, src);  // the segment's last substep: its sort only
             }
+            XPBD_CUDA(cudaMemcpyAsync(tk, pair_k_[fin].p, n * 4, cudaMemcpyDeviceToDevice, stream_));
+            XPBD_CUDA(cudaMemcpyAsync(tk + n, pair_v_[fin].p, n * 4, cudaMemcpyDeviceToDevice, stream_));
         }
-        // adjoint of the segment's substeps, last first
+        // adjoint of the segment's substeps, last first: cell table and sorted records
+        // rebuilt from the stored sort
+        const PredictParams pp = predict_params(sdt);
         for (int t = S - 1; t >= 0; t--) {
             const float4* tr = traj_.p + (size_t)t * 2 * n;
-            XPBD_CUDA(cudaMemcpyAsync(x_[0].p, tr, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
-            XPBD_CUDA(cudaMemcpyAsync(v_[0].p, tr + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
-            prepare_grid(sdt, 0);
-            a.sids = pair_v_[(plan_.passes - 1) & 1].p;
+            const uint32_t* tk = traj_keys_.p + (size_t)t * 2 * n;
+            launch_bump_stamp(stream_, stamp_.p);
+            launch_cells_gather(stream_, (int64_t)n, tk, tk + n, tr, tr + n, w_.p, r_.p, flags_.p, pp, table_.p,
+                                stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
+            a.sids = tk + n;
+            a.x0 = tr;
+            a.v0 = tr + n;
             launch_adjoint_substep(stream_, a);
         }
     }

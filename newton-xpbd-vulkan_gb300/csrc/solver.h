@@ -252,7 +252,8 @@ class Solver {
     bool rollout_valid_ = false;
     float ro_dt_ = 0.0f;
     int ro_substeps_ = 0, ro_frames_ = 0, ro_ckpt_ = 0;
-    DevBuf<float4> ckpt_, traj_, gx_, gv_, gacc_, part_xp_, part_vp_, part_x0_, part_v0_;
+    DevBuf<float4> ckpt_, traj_, gx_, gv_, gacc_, part_xp_, part_vp_, part_x0_, part_v0_, part_gd_;
+    DevBuf<uint32_t> traj_keys_;
     DevBuf<float> gw_, block_params_;
     DevBuf<double> param_acc_;
     void prepare_grid(float sdt, int src);
