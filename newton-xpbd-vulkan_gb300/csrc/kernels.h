@@ -268,6 +268,28 @@ void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, cons
 void launch_body_rigid(cudaStream_t s, BodyArrays ba, RigidTables rt, const float4* q_in, const float4* qd_in,
                        float4* q_out, float4* qd_out, RigidParams rp);
 
+// ----------------------------------------------------------------- LBVH ----
+// Per-mesh topology of the original binary tree (node slots 0 .. 2T-1, local
+// indices), kept for the GPU refit.
+struct LbvhTopology {
+    int* parent;
+    int* child_l;
+    int* child_r;
+    uint8_t* marked;       // node is a (collapsed) leaf
+    uint8_t* reachable;    // node is reachable from the root of the collapsed tree
+    uint32_t* prim_local;  // triangle of each leaf slot, mesh-local
+};
+size_t lbvh_scratch_words(int num_tris);
+// build of one mesh of num_tris triangles (tris: that mesh's triangles, global vertex
+// indices) into the global node arrays at node_base, the primitive array at prim_base
+// (triangle ids + tri_base) and *root_global
+void launch_lbvh_build(cudaStream_t s, int num_tris, const float* verts, const uint32_t* tris, uint32_t node_base,
+                       uint32_t prim_base, uint32_t tri_base, float4* nl, float4* nu, uint32_t* prim,
+                       uint32_t* root_global, LbvhTopology topo, uint32_t* scratch, DeviceStatus* st);
+// refit after the vertices moved; nl / nu point at the mesh's first node
+void launch_lbvh_refit(cudaStream_t s, int num_tris, const float* verts, const uint32_t* tris, LbvhTopology topo,
+                       float4* nl, float4* nu, uint32_t* scratch);
+
 // -------------------------------------------------------------- adjoint ----
 // One substep's adjoint (k_adjoint.cu). Arrays rx/rv/sids/table are the forward's
 // sorted records of that substep; x0/v0/cinfo its start state and plane contacts;

@@ -207,7 +207,8 @@ void Solver::finalize_meshes() {
     dyn_any_ = false;
     dyn_list_.clear();
 
-    // per-mesh LBVH on the host, then one packed node array for all meshes (scene.cpp:249-386)
+    // concatenated vertex / triangle arrays, then one LBVH per mesh built on the GPU
+    // straight into the packed global node arrays (scene.cpp:249-386)
     all_verts_.clear();
     std::vector<uint32_t> all_tris;
     vert_offsets_.assign(nm, 0);
@@ -223,7 +224,6 @@ void Solver::finalize_meshes() {
         for (uint32_t t : m.indices) all_tris.push_back(t + vo);
         const size_t nt = m.indices.size() / 3;
         if (nt == 0) throw std::runtime_error("add_mesh: mesh has no triangles");
-        m.bvh.build(all_verts_.data(), all_tris.data() + to * 3, nt);
         double sum_len = 0.0;  // scene.cpp:274-281
         for (size_t t = 0; t < nt; t++)
             for (int e = 0; e < 3; e++) {
@@ -244,44 +244,22 @@ void Solver::finalize_meshes() {
     slot_cap_ = (int)std::max<size_t>(1, nm <= 8 ? nm : 16);
     cslot_.alloc(std::max<size_t>(n_, 1) * (size_t)slot_cap_ * 3, false);
     if (nm > 0) {
-        std::vector<float4> nl(total_nodes), nu(total_nodes);
-        std::vector<uint32_t> prim(total_prims), roots(nm), poff(nm), pcnt(nm);
+        std::vector<uint32_t> poff(nm), pcnt(nm);
         std::vector<float> margins(nm);
         std::vector<int> wt(nm);
-        size_t tbase = 0;
+        size_t max_nt = 0;
         for (size_t c = 0; c < nm; c++) {
-            const HostBvh& b = meshes_[c].bvh;
-            const size_t nb2 = node_offsets_[c], pb = prim_offsets_[c], nnodes = b.lowers.size() / 4;
-            roots[c] = (uint32_t)(nb2 + b.root);
-            for (size_t i = 0; i < nnodes; i++) {
-                const uint32_t lw = f2u(b.lowers[i * 4 + 3]), uw = f2u(b.uppers[i * 4 + 3]);
-                uint32_t nlw, nuw;
-                if ((lw >> 30) & 3u) {  // leaf: primitive range rebased to the global prim array
-                    nlw = ((lw & 0x3FFFFFFFu) + (uint32_t)pb) | (1u << 30);
-                    nuw = (uw & 0x3FFFFFFFu) + (uint32_t)pb;
-                } else {  // inner: child indices rebased to the global node array
-                    nlw = (lw & 0x3FFFFFFFu) + (uint32_t)nb2;
-                    nuw = (uw & 0x3FFFFFFFu) + (uint32_t)nb2;
-                }
-                nl[nb2 + i] = make_float4(b.lowers[i * 4], b.lowers[i * 4 + 1], b.lowers[i * 4 + 2], u2f(nlw));
-                nu[nb2 + i] = make_float4(b.uppers[i * 4], b.uppers[i * 4 + 1], b.uppers[i * 4 + 2], u2f(nuw));
-            }
-            const size_t nt = b.prims.size();
-            for (size_t i = 0; i < nt; i++) prim[pb + i] = b.prims[i] + (uint32_t)tbase;
-            poff[c] = (uint32_t)pb;
+            const size_t nt = meshes_[c].indices.size() / 3;
+            poff[c] = (uint32_t)prim_offsets_[c];
             pcnt[c] = (uint32_t)nt;
             margins[c] = meshes_[c].shape_margin;
             wt[c] = meshes_[c].is_watertight ? 1 : 0;
-            tbase += nt;
+            max_nt = std::max(max_nt, nt);
         }
         auto up = [&](auto& dev, const auto& host) {
             dev.alloc(host.size(), false);
             XPBD_CUDA(cudaMemcpy(dev.p, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice));
         };
-        up(nl_, nl);
-        up(nu_, nu);
-        up(prim_, prim);
-        up(roots_, roots);
         up(prim_off_, poff);
         up(prim_cnt_, pcnt);
         up(margins_, margins);
@@ -289,6 +267,21 @@ void Solver::finalize_meshes() {
         up(verts_, all_verts_);
         up(vels_, all_vels_);
         up(tris_, all_tris);
+        nl_.alloc(total_nodes, false);
+        nu_.alloc(total_nodes, false);
+        prim_.alloc(total_prims, false);
+        roots_.alloc(nm, false);
+        topo_parent_.alloc(total_nodes, false);
+        topo_child_l_.alloc(total_nodes, true);
+        topo_child_r_.alloc(total_nodes, true);
+        topo_marked_.alloc(total_nodes, false);
+        topo_reachable_.alloc(total_nodes, false);
+        topo_prim_.alloc(total_prims, false);
+        bvh_scratch_.alloc(lbvh_scratch_words((int)max_nt), false);
+        for (size_t c = 0; c < nm; c++)
+            launch_lbvh_build(stream_, (int)pcnt[c], verts_.p, tris_.p + (size_t)prim_offsets_[c] * 3,
+                              (uint32_t)node_offsets_[c], (uint32_t)prim_offsets_[c], (uint32_t)prim_offsets_[c],
+                              nl_.p, nu_.p, prim_.p, roots_.p + c, topology(c), bvh_scratch_.p, status_.p);
         avg_edge0_ = meshes_[0].avg_edge;  // mesh 0's average edge for every mesh (scene.cpp:325)
         tri_cache_.alloc(total_prims * 4, false);
         launch_tri_cache(stream_, 0, (int64_t)total_prims, prim_.p, tris_.p, verts_.p, tri_cache_.p);
@@ -350,33 +343,16 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
     else
         std::fill(all_vels_.begin() + vs * 3, all_vels_.begin() + (vs + num_verts) * 3, 0.0f);
     std::copy(verts, verts + num_verts * 3, m.vertices.begin());
-    // refit on the host (topology unchanged), then upload this mesh's slices
-    std::vector<uint32_t> tris(m.indices.size());
-    for (size_t k = 0; k < tris.size(); k++) tris[k] = m.indices[k] + (uint32_t)vs;
-    m.bvh.refit(all_verts_.data(), tris.data());
-    const size_t nnodes = m.bvh.lowers.size() / 4, nb = node_offsets_[mi], pb = prim_offsets_[mi];
-    std::vector<float4> nl(nnodes), nu(nnodes);
-    for (size_t i = 0; i < nnodes; i++) {
-        const uint32_t lw = f2u(m.bvh.lowers[i * 4 + 3]), uw = f2u(m.bvh.uppers[i * 4 + 3]);
-        uint32_t nlw, nuw;
-        if ((lw >> 30) & 3u) {
-            nlw = ((lw & 0x3FFFFFFFu) + (uint32_t)pb) | (1u << 30);
-            nuw = (uw & 0x3FFFFFFFu) + (uint32_t)pb;
-        } else {
-            nlw = (lw & 0x3FFFFFFFu) + (uint32_t)nb;
-            nuw = (uw & 0x3FFFFFFFu) + (uint32_t)nb;
-        }
-        nl[i] = make_float4(m.bvh.lowers[i * 4], m.bvh.lowers[i * 4 + 1], m.bvh.lowers[i * 4 + 2], u2f(nlw));
-        nu[i] = make_float4(m.bvh.uppers[i * 4], m.bvh.uppers[i * 4 + 1], m.bvh.uppers[i * 4 + 2], u2f(nuw));
-    }
-    XPBD_CUDA(cudaMemcpyAsync(nl_.p + nb, nl.data(), nnodes * sizeof(float4), cudaMemcpyHostToDevice, stream_));
-    XPBD_CUDA(cudaMemcpyAsync(nu_.p + nb, nu.data(), nnodes * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    // upload this mesh's vertices, then refit its BVH on the GPU (topology unchanged,
+    // scene.cpp:657-695 refits on the host and re-uploads every node)
+    const size_t nb = node_offsets_[mi], pb = prim_offsets_[mi], nt = m.indices.size() / 3;
     XPBD_CUDA(cudaMemcpyAsync(verts_.p + vs * 3, verts, num_verts * 3 * sizeof(float), cudaMemcpyHostToDevice,
                               stream_));
     XPBD_CUDA(cudaMemcpyAsync(vels_.p + vs * 3, all_vels_.data() + vs * 3, num_verts * 3 * sizeof(float),
                               cudaMemcpyHostToDevice, stream_));
-    launch_tri_cache(stream_, (int64_t)pb, (int64_t)(m.indices.size() / 3), prim_.p, tris_.p, verts_.p,
-                     tri_cache_.p);
+    launch_lbvh_refit(stream_, (int)nt, verts_.p, tris_.p + pb * 3, topology(mi), nl_.p + nb, nu_.p + nb,
+                      bvh_scratch_.p);
+    launch_tri_cache(stream_, (int64_t)pb, (int64_t)nt, prim_.p, tris_.p, verts_.p, tri_cache_.p);
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -1121,12 +1097,37 @@ void Solver::get_deltas(float* out, size_t n) {
     XPBD_CUDA(cudaMemcpy(out, delta_.p, n * 12, cudaMemcpyDeviceToHost));
 }
 
+LbvhTopology Solver::topology(size_t c) const {
+    LbvhTopology t;
+    const size_t nb = node_offsets_[c], pb = prim_offsets_[c];
+    t.parent = topo_parent_.p + nb;
+    t.child_l = topo_child_l_.p + nb;
+    t.child_r = topo_child_r_.p + nb;
+    t.marked = topo_marked_.p + nb;
+    t.reachable = topo_reachable_.p + nb;
+    t.prim_local = topo_prim_.p + pb;
+    return t;
+}
+
+// The mesh's node halves as the builder made them (mesh-local packed words), read back
+// from the global arrays (the packing of scene.cpp:287-321 undone).
 size_t Solver::mesh_bvh(size_t mi, float* lowers, float* uppers, size_t cap) {
     if (mi >= meshes_.size() || !finalized_) return 0;
-    const HostBvh& b = meshes_[mi].bvh;
-    const size_t nn = b.lowers.size() / 4;
-    if (lowers) std::memcpy(lowers, b.lowers.data(), std::min(cap, nn) * 16);
-    if (uppers) std::memcpy(uppers, b.uppers.data(), std::min(cap, nn) * 16);
+    const size_t nn = 2 * (meshes_[mi].indices.size() / 3), nb = node_offsets_[mi], pb = prim_offsets_[mi];
+    if (!lowers && !uppers) return nn;
+    sync();
+    std::vector<float4> l(nn), u(nn);
+    XPBD_CUDA(cudaMemcpy(l.data(), nl_.p + nb, nn * sizeof(float4), cudaMemcpyDeviceToHost));
+    XPBD_CUDA(cudaMemcpy(u.data(), nu_.p + nb, nn * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nn && i < cap; i++) {
+        const uint32_t lw = f2u(l[i].w), uw = f2u(u[i].w);
+        const bool leaf = (lw >> 30) & 3u;
+        const uint32_t base = (uint32_t)(leaf ? pb : nb);
+        const float lo[4] = {l[i].x, l[i].y, l[i].z, u2f(((lw & 0x3FFFFFFFu) - base) | (leaf ? (1u << 30) : 0u))};
+        const float hi[4] = {u[i].x, u[i].y, u[i].z, u2f((uw & 0x3FFFFFFFu) - base)};
+        if (lowers) std::memcpy(lowers + i * 4, lo, 16);
+        if (uppers) std::memcpy(uppers + i * 4, hi, 16);
+    }
     return nn;
 }
 

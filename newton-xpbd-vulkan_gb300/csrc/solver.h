@@ -43,23 +43,12 @@ struct DevBuf {
     size_t bytes() const { return n * sizeof(T); }
 };
 
-// CPU LBVH over one triangle mesh, same topology as MeshLbvhBuilder::build
-// (src/mesh_lbvh.h:49-223). Node halves are 4 floats (xyz + packed word).
-struct HostBvh {
-    std::vector<float> lowers, uppers;  // 2*T nodes x 4
-    std::vector<uint32_t> prims;        // T
-    uint32_t root = 0;
-    void build(const float* pts, const uint32_t* tris, size_t num_tris);
-    void refit(const float* pts, const uint32_t* tris);
-};
-
 struct MeshData {  // src/scene.h:66-72
     std::vector<float> vertices;
     std::vector<uint32_t> indices;
     float shape_margin = 0.0f;
     float shape_rot[4] = {0.f, 0.f, 0.f, 1.f};
     bool is_watertight = false;
-    HostBvh bvh;
     float avg_edge = 0.0f;
 };
 
@@ -162,6 +151,7 @@ class Solver {
     SolveParams solve_params(float sdt, int it) const;
     BodyTables body_tables() const;
     MeshTables mesh_tables() const;
+    LbvhTopology topology(size_t mesh) const;
     BodyArrays body_arrays() const;
     RigidTables rigid_tables() const;
     RigidParams rigid_params(float sdt) const;
@@ -245,6 +235,9 @@ class Solver {
     DevBuf<float> verts_, vels_;
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
     DevBuf<float4> tri_cache_;
+    DevBuf<int> topo_parent_, topo_child_l_, topo_child_r_;
+    DevBuf<uint8_t> topo_marked_, topo_reachable_;
+    DevBuf<uint32_t> topo_prim_, bvh_scratch_;
     DevBuf<float> margins_;
     DevBuf<int> watertight_;
     float avg_edge0_ = 0.0f;
