@@ -306,6 +306,8 @@ def run_gpu(args):
         "stage_ms_per_substep": {k: round(v / max(prof_substeps, 1), 5) for k, v in stage_ms.items() if v > 0},
         "e2e": e2e, "gpu_launches": int(stats["kernels_per_frame"] * args.steps), "clocks": clk,
     }
+    if rank == 0 and args.cache_frames > 0:
+        result["frame_cache"] = measure_cache(args, solver, sc)
     del solver
     for name, on, fn in (("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev, flush)),
                          ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev)),
@@ -490,6 +492,31 @@ def measure_mixed(args, dev):
             "box_height_range": [round(float(np.nanmin(bq[:, 2])), 3), round(float(np.nanmax(bq[:, 2])), 3)]}
 
 
+def measure_cache(args, solver, sc):
+    """The add-on's per-frame cache (step, then np.save of the positions): done synchronously
+    as the add-on does, and with the frame recorder (copy + file write overlap the next frame)."""
+    import tempfile
+
+    frames = args.cache_frames
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        for f in range(frames):
+            solver.step(DT, SUBSTEPS, ITERATIONS)
+            np.save(os.path.join(d, f"frame_{f + 1:04d}.npy"), solver.get_positions())
+        sync_s = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        solver.record_start(d, 1)
+        for f in range(frames):
+            solver.step_async(DT, SUBSTEPS, ITERATIONS)
+        written = solver.record_stop()
+        rec_s = time.perf_counter() - t0
+    work = sc.n * SUBSTEPS * frames
+    return {"frames": frames, "bytes_per_frame": sc.n * 12, "files_written": written, "unit": UNIT,
+            "synchronous_value": work / sync_s, "recorder_value": work / rec_s,
+            "note": "host wall clock; synchronous = step + get_positions + np.save per frame"}
+
+
 def measure_diff(args, dev):
     """Differentiable throw: 32,768 particles (32^3, spacing 0.02, r 0.01) with velocities
     N((2,3,0), 0.1^2) (seed 43), 600 substeps (60 frames x 10), plane + particle contacts,
@@ -595,6 +622,7 @@ def main():
     ap.add_argument("--mixed-frames", type=int, default=10, help="0 skips the particles + boxes measurement")
     ap.add_argument("--mixed-preroll", type=int, default=20)
     ap.add_argument("--diff-frames", type=int, default=60, help="0 skips the differentiable rollout measurement")
+    ap.add_argument("--cache-frames", type=int, default=50, help="0 skips the frame-cache measurement")
     ap.add_argument("--diff-reps", type=int, default=3)
     ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed (default all)")
     args = ap.parse_args()

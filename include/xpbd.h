@@ -197,6 +197,16 @@ int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t num_bodies);
  * one scene, ground plane and particle contacts (no meshes or bodies), every
  * particle active, particles of equal radius, one solver iteration. The solver is
  * left at the rollout's final state. */
+/* Frame cache — the add-on's per-frame np.save of get_positions()
+ * (newton_vulkan_plugin.py:626-631) without the wait: after every later step the
+ * positions are copied to pinned host memory on the solver's stream and written
+ * as <directory>/frame_%04d.npy (float32, shape (n, 3); numbering from
+ * first_frame) by a writer thread while the GPU runs the next frame.
+ * xpbd_record_stop waits for the pending files and reports how many were written
+ * (an I/O error is reported by the next step or by xpbd_record_stop). */
+int xpbd_record_start(xpbd_solver* s, const char* directory, int first_frame);
+int xpbd_record_stop(xpbd_solver* s, int* frames_written);
+
 /* New contact / material parameters after init (e.g. between rollouts of an
  * optimisation): every numeric field of cfg except device_index and the
  * diagnostics / profiling switches, which stay as at init. */

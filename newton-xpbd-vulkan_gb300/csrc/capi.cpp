@@ -293,6 +293,20 @@ int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t nb) {
     return guarded([&] { S(s).get_bodies(q, qd, nb); });
 }
 
+int xpbd_record_start(xpbd_solver* s, const char* directory, int first_frame) {
+    return guarded([&] {
+        if (!directory) throw std::runtime_error("xpbd_record_start: directory is NULL");
+        S(s).record_start(directory, first_frame);
+    });
+}
+
+int xpbd_record_stop(xpbd_solver* s, int* frames_written) {
+    return guarded([&] {
+        const int k = S(s).record_stop();
+        if (frames_written) *frames_written = k;
+    });
+}
+
 int xpbd_update_config(xpbd_solver* s, const xpbd_config* cfg) {
     return guarded([&] {
         if (!cfg) throw std::runtime_error("xpbd_update_config: cfg is NULL");

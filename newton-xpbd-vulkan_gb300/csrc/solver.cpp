@@ -59,6 +59,10 @@ Solver::Solver() = default;
 Solver::~Solver() {
     if (!initialized_) return;
     cudaSetDevice(device_);
+    try {
+        recorder_.stop();
+    } catch (...) {
+    }
     if (stream_) cudaStreamSynchronize(stream_);
     if (profiling_) print_profiler_summary();
     clear_graphs();
@@ -822,6 +826,10 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
         it = graphs_.emplace(key, std::move(fg)).first;
     }
     XPBD_CUDA(cudaGraphLaunch(it->second.exec, stream_));
+    if (recorder_.active()) {  // this frame's positions to the writer thread (after the graph)
+        launch_unpack_xyz(stream_, (int64_t)n_, x_[cur_ ^ (substeps & 1)].p, rec_stage_.p);
+        recorder_.enqueue(stream_, rec_stage_.p);
+    }
     last_kernels_ = it->second.kernels;
     last_memsets_ = it->second.memsets;
     frames_run_++;
@@ -1209,6 +1217,18 @@ void Solver::print_profiler_summary() {
                     prof_ms_[i] / (total > 0 ? total : 1.0) * 100.0);
     std::printf("========================================================================================================\n\n");
     std::fflush(stdout);
+}
+
+void Solver::record_start(const std::string& dir, int first_frame) {
+    require_init();
+    sync();
+    rec_stage_.alloc(std::max<size_t>(n_, 1) * 3, false);
+    recorder_.start(device_, n_, dir, first_frame);
+}
+
+int Solver::record_stop() {
+    sync();
+    return recorder_.stop();
 }
 
 void Solver::update_config(const xpbd_config& c) {

@@ -3,9 +3,13 @@
 // records one CUDA graph per (dt, substeps, iterations, state parity) and
 // replays it per frame.
 #pragma once
+#include <condition_variable>
 #include <cstdint>
+#include <deque>
 #include <map>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -54,6 +58,36 @@ struct MeshData {  // src/scene.h:66-72
 
 bool tris_watertight(const uint32_t* tris, size_t num_tris, size_t num_verts);
 
+// Writes frame_%04d.npy files of the positions after every step from a worker thread,
+// overlapping the next frame (recorder.cpp).
+class FrameRecorder {
+   public:
+    ~FrameRecorder();
+    void start(int device, size_t n, const std::string& dir, int first_frame);
+    int stop();  // waits for pending writes; returns the number of files written
+    void enqueue(cudaStream_t stream, const float* d_xyz);
+    bool active() const { return active_; }
+
+   private:
+    static constexpr int kSlots = 3;
+    struct Slot {
+        float* host = nullptr;
+        cudaEvent_t done = nullptr;
+        bool busy = false;
+        int frame = 0;
+    };
+    void run();
+    Slot slots_[kSlots];
+    std::thread worker_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<int> queue_;
+    std::string dir_, header_, error_;
+    size_t n_ = 0;
+    int device_ = 0, next_frame_ = 1, written_ = 0;
+    bool active_ = false, stop_flag_ = false;
+};
+
 class Solver {
    public:
     static constexpr int kMaxStages = 32;  // >= the number of profiler stages (solver.cpp)
@@ -80,6 +114,9 @@ class Solver {
     void set_bodies(const float* q, const float* qd, const float* com, const float* inertia,
                     const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb);
     void get_bodies(float* q, float* qd, size_t nb);
+    // frame cache: positions of every later step written to dir/frame_%04d.npy
+    void record_start(const std::string& dir, int first_frame);
+    int record_stop();
     void set_body_params(const xpbd_body_params& p);
     // differentiable rollout: `frames` frames like step(), checkpointing the state every
     // checkpoint_frames frames; rollout_backward runs the adjoint of the whole rollout
@@ -241,6 +278,9 @@ class Solver {
     DevBuf<float> margins_;
     DevBuf<int> watertight_;
     float avg_edge0_ = 0.0f;
+    // frame recorder
+    FrameRecorder recorder_;
+    DevBuf<float> rec_stage_;
     // differentiable rollout
     bool rollout_valid_ = false;
     float ro_dt_ = 0.0f;

@@ -183,6 +183,17 @@ class XpbdSolver:
             setattr(bp, k, v)
         _check(_lib.xpbd_set_body_params(self._h, C.byref(bp)))
 
+    def record_start(self, directory, first_frame=1):
+        """Write the positions after every later step to directory/frame_%04d.npy from a
+        writer thread (the add-on's cache, overlapped with the next frame)."""
+        _check(_lib.xpbd_record_start(self._h, os.fsencode(directory), int(first_frame)))
+
+    def record_stop(self):
+        """Wait for pending files; returns how many were written."""
+        k = C.c_int(0)
+        _check(_lib.xpbd_record_stop(self._h, C.byref(k)))
+        return int(k.value)
+
     def update_config(self, config):
         """New contact / material parameters after init (xpbd_update_config)."""
         _check(_lib.xpbd_update_config(self._h, C.byref(config._c)))
