@@ -222,11 +222,76 @@ __global__ void k_body_pairs(RigidTables rt, RigidParams rp, DeviceStatus* st) {
     }
 }
 
+// ------------------------------------------------------------- box grid ----
+__device__ __forceinline__ uint32_t box_cell_hash(int ix, int iy, int iz, int size) {
+    return (((uint32_t)ix * 73856093u) ^ ((uint32_t)iy * 19349663u) ^ ((uint32_t)iz * 83492791u)) &
+           (uint32_t)(size - 1);
+}
+__device__ __forceinline__ int cell_of(float v, float cs) { return f2i(floorf(v / cs)); }
+
+// each dynamic body's widened world box counts itself into the buckets of the cells it covers
+__global__ void k_boxgrid_count(RigidTables rt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rt.n_dyn) return;
+    const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
+    const float e = rt.grid_reach + l.w;
+    for (int z = cell_of(l.z - e, rt.grid_cs); z <= cell_of(h.z + e, rt.grid_cs); z++)
+        for (int y = cell_of(l.y - e, rt.grid_cs); y <= cell_of(h.y + e, rt.grid_cs); y++)
+            for (int x = cell_of(l.x - e, rt.grid_cs); x <= cell_of(h.x + e, rt.grid_cs); x++)
+                atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.grid_size)], 1u);
+}
+
+// exclusive scan of the bucket counts (one block); the counts become fill cursors
+__global__ void __launch_bounds__(1024) k_boxgrid_scan(RigidTables rt) {
+    __shared__ uint32_t s_sum[1024];
+    const int per = (rt.grid_size + 1023) / 1024;
+    const int b0 = threadIdx.x * per;
+    uint32_t t = 0;
+    for (int k = 0; k < per; k++)
+        if (b0 + k < rt.grid_size) t += rt.grid_count[b0 + k];
+    s_sum[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = threadIdx.x >= o ? s_sum[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s_sum[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = s_sum[threadIdx.x] - t;
+    for (int k = 0; k < per; k++) {
+        const int b = b0 + k;
+        if (b < rt.grid_size) {
+            rt.grid_start[b] = run;
+            run += rt.grid_count[b];
+            rt.grid_count[b] = 0;
+        }
+    }
+    if (threadIdx.x == 1023) rt.grid_start[rt.grid_size] = s_sum[1023];
+}
+
+__global__ void k_boxgrid_fill(RigidTables rt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rt.n_dyn) return;
+    const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
+    const float e = rt.grid_reach + l.w;
+    for (int z = cell_of(l.z - e, rt.grid_cs); z <= cell_of(h.z + e, rt.grid_cs); z++)
+        for (int y = cell_of(l.y - e, rt.grid_cs); y <= cell_of(h.y + e, rt.grid_cs); y++)
+            for (int x = cell_of(l.x - e, rt.grid_cs); x <= cell_of(h.x + e, rt.grid_cs); x++) {
+                const uint32_t b = box_cell_hash(x, y, z, rt.grid_size);
+                const uint32_t at = rt.grid_start[b] + atomicAdd(&rt.grid_count[b], 1u);
+                if (at < (uint32_t)rt.n_dyn * 8u) rt.grid_list[at] = (uint32_t)i;  // 8 cells per box at most
+            }
+}
+
 void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                        DeviceStatus* st) {
     if (rt.n_dyn <= 0) return;
     k_body_bounds<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(ba, rt, mt);
     k_body_pairs<<<(rt.n_dyn * 32 + 127) / 128, 128, 0, s>>>(rt, rp, st);
+    cudaMemsetAsync(rt.grid_count, 0, sizeof(uint32_t) * (size_t)rt.grid_size, s);
+    k_boxgrid_count<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(rt);
+    k_boxgrid_scan<<<1, 1024, 0, s>>>(rt);
+    k_boxgrid_fill<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(rt);
 }
 
 // ---------------------------------------------------------------- rigid contacts ----
@@ -364,109 +429,70 @@ void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTa
 }
 
 // ---------------------------------------------------------------- particle contacts on moving meshes ----
-// One CTA of 128 particles (in hash-grid order, so they are neighbours) keeps the dynamic
-// bodies whose world boxes come near the CTA's particles, in ascending order; each
-// particle then queries those meshes in its body frame (generate_mesh_contacts.comp with
-// the pose inverted) and inserts the contacts into its slots in mesh order.
+// One thread per particle (hash-grid order): the bodies listed in the particle's cell
+// of the box grid whose widened world box holds the particle are queried in their body
+// frame (generate_mesh_contacts.comp with the pose inverted); each contact is inserted
+// into the particle's slots at its mesh's place, so the list order does not matter.
 __global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t* __restrict__ order,
                                                       const float4* __restrict__ x, const float* __restrict__ r,
                                                       const int* __restrict__ flags, MeshTables mt, RigidTables rt,
                                                       int slot_cap, uint32_t* __restrict__ cinfo,
                                                       float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
-    __shared__ float s_red[4][7];
-    __shared__ int s_cand[128];
-    __shared__ int s_wcnt[4];
     __shared__ uint32_t s_warp[4];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t i = -1;
-    bool active = false;
-    v3 p = mk3(0.0f, 0.0f, 0.0f);
-    float radius = 0.0f;
-    if (t < n) {
-        i = order ? (int64_t)order[t] : t;
-        active = (flags[i] & 1) != 0;
-        if (active) {
-            p = xyz(x[i]);
-            radius = r[i];
-        }
-    }
-    // CTA bounds of the active particles and their largest radius
-    float v[7] = {active ? p.x : 3.0e38f, active ? p.y : 3.0e38f, active ? p.z : 3.0e38f,
-                  active ? -p.x : 3.0e38f, active ? -p.y : 3.0e38f, active ? -p.z : 3.0e38f,
-                  active ? -radius : 3.0e38f};
-    for (int o = 16; o > 0; o >>= 1)
-        for (int k = 0; k < 7; k++) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
-    if (lane == 0)
-        for (int k = 0; k < 7; k++) s_red[warp][k] = v[k];
-    __syncthreads();
-    for (int k = 0; k < 7; k++) v[k] = fminf(fminf(s_red[0][k], s_red[1][k]), fminf(s_red[2][k], s_red[3][k]));
-    if (v[0] > 1.0e38f) return;  // no active particle in this CTA (uniform)
-    const float E = mt.soft_margin - v[6] + 2.0f * rt.pad;
-    const v3 blo = mk3(v[0] - E, v[1] - E, v[2] - E), bhi = mk3(-v[3] + E, -v[4] + E, -v[5] + E);
-
-    uint32_t info = 0;
     int used0 = 0, used = 0;
-    if (active) {
-        info = cinfo[i];
-        used0 = used = info_slots(info);
-    }
     bool slot_ovf = false, stack_ovf = false;
-    for (int c0 = 0; c0 < rt.n_dyn; c0 += 128) {
-        const int c = c0 + threadIdx.x;
-        bool near = false;
-        if (c < rt.n_dyn) {
-            const float4 l = rt.wbox[c * 2], h = rt.wbox[c * 2 + 1];
-            near = (blo.x <= h.x + l.w) && (l.x - l.w <= bhi.x) && (blo.y <= h.y + l.w) && (l.y - l.w <= bhi.y) &&
-                   (blo.z <= h.z + l.w) && (l.z - l.w <= bhi.z);
-        }
-        const uint32_t m = __ballot_sync(0xffffffffu, near);
-        __syncthreads();  // previous chunk's candidates consumed
-        if (lane == 0) s_wcnt[warp] = __popc(m);
-        __syncthreads();
-        int off = 0, total = 0;
-        for (int w = 0; w < 4; w++) {
-            if (w < warp) off += s_wcnt[w];
-            total += s_wcnt[w];
-        }
-        if (near) s_cand[off + __popc(m & lanemask_lt())] = c;
-        __syncthreads();
-        if (!active) continue;
-        for (int k = 0; k < total; k++) {
-            const int ci = s_cand[k];
-            const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
-            const float e = (mt.soft_margin + l.w) + radius + rt.pad;
-            if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
-                  p.z <= h.z + e))
-                continue;
-            const int mesh = rt.dyn[ci];
-            const v3 pos_m = xyz(mt.pose[mesh * 2]);
-            const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
-            const v3 q = quat_rotate_inv(rot_m, vsub(p, pos_m));
-            v3 bp, bv, nn;
-            if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) continue;
-            const v3 nw = quat_rotate(rot_m, nn);
-            if (used >= slot_cap) {
-                slot_ovf = true;
-                continue;
+    if (t < n) {
+        const int64_t i = order ? (int64_t)order[t] : t;
+        if (flags[i] & 1) {
+            const v3 p = xyz(x[i]);
+            const float radius = r[i];
+            const uint32_t info = cinfo[i];
+            used0 = used = info_slots(info);
+            const uint32_t b = box_cell_hash(cell_of(p.x, rt.grid_cs), cell_of(p.y, rt.grid_cs),
+                                             cell_of(p.z, rt.grid_cs), rt.grid_size);
+            const uint32_t k0 = rt.grid_start[b], k1 = rt.grid_start[b + 1];
+            for (uint32_t k = k0; k < k1; k++) {
+                const int ci = (int)rt.grid_list[k];
+                const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
+                const float e = (mt.soft_margin + l.w) + radius + rt.pad;
+                if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
+                      p.z <= h.z + e))
+                    continue;
+                const int mesh = rt.dyn[ci];
+                const v3 pos_m = xyz(mt.pose[mesh * 2]);
+                const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+                const v3 q = quat_rotate_inv(rot_m, vsub(p, pos_m));
+                {  // the traversal's first test (root box in the body frame) without starting a traversal
+                    const uint32_t root = __ldg(&mt.roots[mesh]);
+                    const float md = mt.soft_margin + l.w + radius;  // walk_begin's max_dist
+                    if (dist_sq_aabb(q, xyz(__ldg(&mt.nl[root])), xyz(__ldg(&mt.nu[root]))) > md * md) continue;
+                }
+                v3 bp, bv, nn;
+                if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) continue;
+                const v3 nw = quat_rotate(rot_m, nn);
+                if (used >= slot_cap) {
+                    slot_ovf = true;
+                    continue;
+                }
+                float4* base = cslot + (size_t)i * slot_cap * 3;
+                int pos = used;
+                while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
+                for (int k2 = used; k2 > pos; k2--) {
+                    base[k2 * 3] = base[(k2 - 1) * 3];
+                    base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
+                    base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
+                }
+                base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
+                base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
+                base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+                used++;
             }
-            float4* base = cslot + (size_t)i * slot_cap * 3;
-            int pos = used;
-            while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
-            for (int k2 = used; k2 > pos; k2--) {
-                base[k2 * 3] = base[(k2 - 1) * 3];
-                base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
-                base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
-            }
-            base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
-            base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
-            base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
-            used++;
+            // every slot added here belongs to a dynamic body
+            if (used != used0)
+                cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
         }
     }
-    // every slot added here belongs to a dynamic body
-    if (active && used != used0)
-        cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
     if (slot_ovf) {
         atomicOr(&st->error_bits, kErrSlotOverflow);
         atomicAdd(&st->slot_overflows, 1u);

@@ -241,6 +241,14 @@ struct RigidTables {
     int* rc_count;
     float pad;                    // conservative widening of the world boxes
     int n_vert;                   // dv_start[nb]
+    // coarse hashed grid of the dynamic bodies' world boxes (widened by grid_reach) for the
+    // particle queries: cell size grid_cs >= any widened box, so a box covers <= 8 cells;
+    // bucket h lists its bodies (dyn indices, any order) in grid_list[grid_start[h] ..)
+    int grid_size;                // buckets (power of two)
+    float grid_cs, grid_reach;
+    uint32_t* grid_count;         // [grid_size]
+    uint32_t* grid_start;         // [grid_size + 1]
+    uint32_t* grid_list;          // [8 * n_dyn]
 };
 // integrate_bodies.comp for every body; saves the pre-integration state to q_prev
 void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp);

@@ -435,6 +435,14 @@ RigidTables Solver::rigid_tables() const {
     t.rc_count = rc_count_.p;
     t.pad = 1e-3f;
     t.n_vert = n_dyn_verts_;
+    // box grid: a particle's side of the widening (soft margin + radius + pad, radii bounded
+    // by particle_max_radius as for the neighbour search); cells larger than any widened box
+    t.grid_size = grid_size_;
+    t.grid_reach = cfg_.soft_contact_margin + cfg_.particle_max_radius + 2.0f * t.pad;
+    t.grid_cs = (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f + 1e-4f;
+    t.grid_count = grid_count_.p;
+    t.grid_start = grid_start_.p;
+    t.grid_list = grid_list_.p;
     return t;
 }
 
@@ -536,6 +544,26 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     }
     dv_start[nb] = (uint32_t)dv_local.size();
     n_dyn_verts_ = (int)dv_local.size();
+    // largest half-diagonal of a dynamic mesh's body-frame box and largest shape margin
+    dyn_half_diag_ = 0.0f;
+    dyn_max_margin_ = 0.0f;
+    for (int b : dyn_list_) {
+        float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+        const std::vector<float>& v = meshes_[b].vertices;
+        for (size_t k = 0; k + 2 < v.size(); k += 3)
+            for (int a = 0; a < 3; a++) {
+                lo[a] = std::min(lo[a], v[k + a]);
+                hi[a] = std::max(hi[a], v[k + a]);
+            }
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        dyn_half_diag_ = std::max(dyn_half_diag_, 0.5f * std::sqrt(dx * dx + dy * dy + dz * dz));
+        dyn_max_margin_ = std::max(dyn_max_margin_, meshes_[b].shape_margin);
+    }
+    grid_size_ = 64;
+    while ((size_t)grid_size_ < 16 * dyn_list_.size()) grid_size_ *= 2;
+    grid_count_.alloc((size_t)grid_size_, true);
+    grid_start_.alloc((size_t)grid_size_ + 1, true);
+    grid_list_.alloc(std::max<size_t>(dyn_list_.size() * 8, 1), true);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);
     up(posed_, posed);
