@@ -307,6 +307,23 @@ int xpbd_record_stop(xpbd_solver* s, int* frames_written) {
     });
 }
 
+int xpbd_autotune(xpbd_solver* s, int best[2], double* times_us) {
+    return guarded([&] {
+        int b = 0, i = 0;
+        const std::vector<double> t = S(s).autotune_sort(&b, &i);
+        if (best) {
+            best[0] = b;
+            best[1] = i;
+        }
+        if (times_us)
+            for (size_t k = 0; k < t.size(); k++) times_us[k] = t[k];
+    });
+}
+
+int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread) {
+    return guarded([&] { S(s).set_sort_variant(bits, keys_per_thread); });
+}
+
 int xpbd_update_config(xpbd_solver* s, const xpbd_config* cfg) {
     return guarded([&] {
         if (!cfg) throw std::runtime_error("xpbd_update_config: cfg is NULL");

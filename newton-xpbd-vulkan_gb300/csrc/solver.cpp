@@ -121,8 +121,6 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
         pair_k_[p].alloc(n_);
         pair_v_[p].alloc(n_);
     }
-    // digit width 8, 16 keys per thread above 1M particles, 8 below (more tiles per SM)
-    plan_ = make_sort_plan((int64_t)n_, key_bits_, 8, n_ >= (1u << 20) ? 16 : 8);
     if (n_scenes > 1) {
         std::vector<uint32_t> ps(n_);
         for (size_t s = 0; s < n_scenes; s++)
@@ -130,14 +128,9 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
         pscene_.alloc(n_, false);
         if (n_) XPBD_CUDA(cudaMemcpy(pscene_.p, ps.data(), n_ * 4, cudaMemcpyHostToDevice));
     }
-    hist_off_ = 0;
-    lb_off_ = (size_t)plan_.passes << plan_.bits;
-    tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
-    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter
-    sort_scratch_.alloc(cq_off_ + 1);
-    // the final sort buffer doubles as the collision pass's thread -> particle order
-    launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
-    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    // digit width 8, 16 keys per thread above 1M particles, 8 below (more tiles per SM);
+    // scenes of 1M particles and more are re-tuned on their first step (autotune_sort)
+    apply_sort_plan(8, n_ >= (1u << 20) ? 16 : 8);
     table_.alloc((size_t)n_scenes * kNumCells);
     stamp_.alloc(1);
     cinfo_.alloc(n_);
@@ -160,6 +153,85 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     profiling_ = cfg_.enable_profile || env_on("VKXPBD_PROFILE");
     if (profiling_) std::printf("[Newton GB300] GPU profiler ENABLED (CUDA events)\n");
     initialized_ = true;
+}
+
+void Solver::apply_sort_plan(int bits, int items) {
+    plan_ = make_sort_plan((int64_t)n_, key_bits_, bits, items);
+    hist_off_ = 0;
+    lb_off_ = (size_t)plan_.passes << plan_.bits;
+    tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
+    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter
+    sort_scratch_.alloc(cq_off_ + 1);
+    // the final sort buffer doubles as the collision pass's thread -> particle order (any
+    // permutation gives the same contacts)
+    launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    clear_graphs();
+}
+
+// Times every onesweep variant (digit width, keys per thread) on this scene's own keys
+// and keeps the fastest; the sort is stable, so the choice never changes a result.
+std::vector<double> Solver::autotune_sort(int* best_bits, int* best_items) {
+    require_init();
+    sync();
+    static const int kCand[][2] = {{8, 8}, {8, 16}, {7, 16}, {7, 32}};
+    std::vector<double> us;
+    double best = 1e30;
+    int bb = plan_.bits, bi = plan_.items;
+    cudaEvent_t e0, e1;
+    XPBD_CUDA(cudaEventCreate(&e0));
+    XPBD_CUDA(cudaEventCreate(&e1));
+    const PredictParams pp = predict_params(cfg_.dt / (float)std::max(1, cfg_.substeps));
+    PlaneParams pl{0, 0.0f, 0.0f};
+    for (const auto& c : kCand) {
+        apply_sort_plan(c[0], c[1]);
+        double t_best = 1e30;
+        for (int rep = 0; rep < 3; rep++) {
+            XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
+            launch_predict_keys(stream_, (int64_t)n_, x_[cur_].p, v_[cur_].p, w_.p, r_.p, flags_.p, pscene_.p, pp,
+                                pl, keys_.p, plan_, sort_scratch_.p + hist_off_, nullptr, nullptr, stamp_.p);
+            XPBD_CUDA(cudaEventRecord(e0, stream_));
+            const uint32_t* kin = keys_.p;
+            const uint32_t* vin = nullptr;
+            const size_t lbw = sort_lookback_words(plan_);
+            for (int p = 0; p < plan_.passes; p++) {
+                launch_onesweep_pass(stream_, (int64_t)n_, plan_, p, kin, vin, pair_k_[p & 1].p, pair_v_[p & 1].p,
+                                     sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
+                                     sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p,
+                                     status_.p);
+                kin = pair_k_[p & 1].p;
+                vin = pair_v_[p & 1].p;
+            }
+            XPBD_CUDA(cudaEventRecord(e1, stream_));
+            XPBD_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            XPBD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            t_best = std::min(t_best, (double)ms * 1e3);
+        }
+        us.push_back(t_best);
+        if (t_best < best) {
+            best = t_best;
+            bb = c[0];
+            bi = c[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply_sort_plan(bb, bi);
+    finish_frame(1);  // a device error of the trial sorts is raised here
+    sort_tuned_ = true;
+    if (best_bits) *best_bits = bb;
+    if (best_items) *best_items = bi;
+    return us;
+}
+
+void Solver::set_sort_variant(int bits, int items) {
+    require_init();
+    sync();
+    if (!((bits == 8 && (items == 8 || items == 16)) || (bits == 7 && (items == 16 || items == 32))))
+        throw std::runtime_error("set_sort_variant: (8, 8), (8, 16), (7, 16) or (7, 32)");
+    apply_sort_plan(bits, items);
+    sort_tuned_ = true;  // an explicit choice is kept
 }
 
 void Solver::ensure_substep_capacity(int substeps) {
@@ -831,6 +903,11 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     rollout_valid_ = false;  // the stored rollout no longer ends at the current state
     ensure_substep_capacity(substeps);
     if (n_ == 0) return;
+    if (!sort_tuned_ && n_ >= (1u << 20)) {  // large scenes: pick the sort variant on the real keys
+        const int cc = contact_count_;
+        autotune_sort(nullptr, nullptr);
+        contact_count_ = cc;
+    }
     auto t0 = std::chrono::high_resolution_clock::now();
     GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0};
     auto it = graphs_.find(key);

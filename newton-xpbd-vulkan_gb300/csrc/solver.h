@@ -123,6 +123,10 @@ class Solver {
     void rollout(float dt, int substeps, int iterations, int frames, int checkpoint_frames);
     // new material / contact parameters (every field but the sizes, device and diagnostics)
     void update_config(const xpbd_config& cfg);
+    // sort autotuner: times the onesweep variants on the current keys, keeps the fastest;
+    // returns the times (us) of {8b x 8, 8b x 16, 7b x 16, 7b x 32}
+    std::vector<double> autotune_sort(int* best_bits, int* best_items);
+    void set_sort_variant(int bits, int items);
     void rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
                           double* params);
     void step(float dt, int substeps, int iterations);
@@ -193,6 +197,8 @@ class Solver {
     RigidTables rigid_tables() const;
     RigidParams rigid_params(float sdt) const;
     void prof_mark(int slot);
+    void apply_sort_plan(int bits, int items);
+    bool sort_tuned_ = false;
     void count_kernel(int k = 1);
     void count_memset();
 

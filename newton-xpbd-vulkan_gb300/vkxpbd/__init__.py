@@ -194,6 +194,18 @@ class XpbdSolver:
         _check(_lib.xpbd_record_stop(self._h, C.byref(k)))
         return int(k.value)
 
+    def autotune(self):
+        """Pick the fastest sort variant on the current keys (xpbd_autotune)."""
+        best = (C.c_int * 2)()
+        t = (C.c_double * 4)()
+        _check(_lib.xpbd_autotune(self._h, best, t))
+        names = ["8b x8", "8b x16", "7b x16", "7b x32"]
+        return {"bits": int(best[0]), "keys_per_thread": int(best[1]),
+                "sort_us": {names[k]: float(t[k]) for k in range(4)}}
+
+    def set_sort_variant(self, bits, keys_per_thread):
+        _check(_lib.xpbd_set_sort_variant(self._h, int(bits), int(keys_per_thread)))
+
     def update_config(self, config):
         """New contact / material parameters after init (xpbd_update_config)."""
         _check(_lib.xpbd_update_config(self._h, C.byref(config._c)))

@@ -91,6 +91,8 @@ def test_batched_many_scenes_4_passes():
     batch = scenes.Batch([scenes.pile_of(c, seed=46 + s) for s, c in enumerate(counts)])
     cfg = config_for(batch)
     g = _batched(batch, cfg)
+    tuned = g.autotune()  # any sort variant must give the same result (stable sort)
+    assert tuned["bits"] in (7, 8) and len(tuned["sort_us"]) == 4
     rng = np.random.default_rng(0)
     pick = sorted(rng.choice(len(counts), 6, replace=False).tolist())
     oracles = {s: make_pair(batch.scenes[s], cfg, gpu=False)[1] for s in pick}
@@ -101,3 +103,18 @@ def test_batched_many_scenes_4_passes():
         for s, orc in oracles.items():
             orc.step(1.0 / 60.0, 10, 1)
             assert_bitexact(x[off[s]:off[s + 1]], orc.get_positions(), f"scene {s} frame {f}")
+
+
+@pytest.mark.parametrize("bits,items", [(8, 8), (8, 16), (7, 16), (7, 32)])
+def test_every_sort_variant_bitexact(bits, items):
+    """Each onesweep variant the autotuner chooses from gives the same (stable) result."""
+    from helpers import small_pile
+
+    sc = small_pile(12)
+    cfg = config_for(sc)
+    g, orc = make_pair(sc, cfg)
+    g.set_sort_variant(bits, items)
+    for f in range(3):
+        g.step(1.0 / 60.0, 10, 1)
+        orc.step(1.0 / 60.0, 10, 1)
+        assert_bitexact(g.get_positions(), orc.get_positions(), f"frame {f}")
