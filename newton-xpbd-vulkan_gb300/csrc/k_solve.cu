@@ -183,7 +183,13 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
                         const float4 nx = __ldg(&rx[kk]);
                         const v3 raw = vsub(xp, xyz(nx));
                         if (fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R) continue;
-                        const float d = exact_length(raw);
+                        // exact_length's squared sum; a candidate whose distance provably exceeds
+                        // r_i + r_j + cohesion (1.5e-5 relative margin, far above the rounding of
+                        // the filter) is rejected before the refined square root
+                        const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
+                        const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
+                        if (sq > reach * reach) continue;
+                        const float d = exact_sqrt(sq);
                         const float err = d - radius - nx.w;
                         if (err > sp.k_coh || d <= 0.0f) continue;
                         s_kk[np][threadIdx.x] = kk;
