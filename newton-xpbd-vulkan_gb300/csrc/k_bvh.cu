@@ -289,6 +289,30 @@ __global__ void k_lbvh_refit_write(int n, const uint8_t* __restrict__ reachable,
     nu[j] = make_float4(h.x, h.y, h.z, nu[j].w);
 }
 
+// One thread per node slot of the mesh: a reachable inner node X with children (a, b)
+// writes the record of a. Leaves and unreachable slots write nothing.
+__global__ void k_node_pairs(int n, uint32_t node_base, const uint8_t* __restrict__ reachable,
+                             const float4* __restrict__ nl, const float4* __restrict__ nu, float4* pair) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= 2 * n || !reachable[j]) return;
+    const uint32_t x = node_base + (uint32_t)j;
+    const uint32_t lw = __float_as_uint(nl[x].w), uw = __float_as_uint(nu[x].w);
+    if ((lw >> 30) & 3u) return;
+    const uint32_t a = lw & 0x3FFFFFFFu, b = uw & 0x3FFFFFFFu;
+    float4* rec = pair + (size_t)a * 4;
+    rec[0] = nl[a];
+    rec[1] = nu[a];
+    rec[2] = nl[b];
+    rec[3] = nu[b];
+}
+
+void launch_node_pairs(cudaStream_t st, int n, uint32_t node_base, const uint8_t* reachable, const float4* nl,
+                       const float4* nu, float4* pair) {
+    if (n <= 0) return;
+    k_node_pairs<<<(2 * n + kBvhThreads - 1) / kBvhThreads, kBvhThreads, 0, st>>>(n, node_base, reachable, nl, nu,
+                                                                                  pair);
+}
+
 size_t lbvh_scratch_words(int n) {
     const size_t nn = (size_t)(n > 0 ? n : 1);
     const size_t blocks = (nn + kBvhThreads - 1) / kBvhThreads;

@@ -14,17 +14,24 @@ namespace xpbd {
 
 // Contact generation with persistent warps. Lanes take particles from a work
 // queue (in the previous substep's hash-grid order, so a warp's particles are
-// neighbours) and refill as soon as their particle is done; the traversal runs
-// "while-while": every lane pops inner nodes until it holds a leaf, then the
-// warp evaluates leaves together. Each particle's own sequence of node visits
-// and leaf evaluations is that of the shader, so its contacts are unchanged.
-__global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* __restrict__ order,
+// neighbours), a warp refilling its lanes once none of them is busy. Every
+// iteration each busy lane advances its own traversal by one step: it pops stack
+// entries until one needs a load (pruned entries cost no load), and then either
+// tests one triangle of the leaf it holds or orders the children of an inner node;
+// both read one 64-byte record (triangle cache entry, or the sibling record of the
+// children), issued together. A warp is therefore never held back by a lane with
+// a long run of inner nodes before its next leaf: its time is set by its longest
+// particle, not by the sum of its per-leaf maxima. Each particle's own sequence of
+// node visits and triangle tests is that of the shader, so its contacts are
+// unchanged.
+constexpr int kCollideThreads = 128;
+__global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const uint32_t* __restrict__ order,
                                                  const float4* __restrict__ x, const float* __restrict__ r,
                                                  const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
                                                  float4* __restrict__ cslot, uint32_t* ccount, uint32_t* queue,
                                                  DeviceStatus* st) {
-    __shared__ uint32_t s_warp[4];
+    __shared__ uint32_t s_warp[kCollideThreads / 32];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
@@ -35,65 +42,86 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
     uint32_t info = 0, count = 0;
+    uint32_t pc = 0, phi = 0;  // triangles [pc, phi) of the leaf being tested
     int used = 0, ci = 0, wi = 0;
     // meshes walked here: all of them, or the static ones when some belong to dynamic bodies
     const int nwalk = mt.walk_list ? mt.walk_count : mt.n_meshes;
-    MeshWalk w;
+    MeshWalk<LocalStack> w;
     w.sp = 0;
     w.overflow = false;
     while (true) {
-        // refill: lanes without a particle take the next queue entries; particles with
-        // no mesh work (inactive, or no mesh) complete right here
-        while (true) {
-            const bool need = !done && i < 0;
-            const uint32_t m = __ballot_sync(FULL, need);
-            if (!m) break;
-            const int leader = __ffs(m) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(m));
-            base = __shfl_sync(FULL, base, leader);
-            if (need) {
-                const uint64_t t = (uint64_t)base + (uint64_t)__popc(m & lt);
-                if (t >= (uint64_t)n) {
-                    done = true;
-                } else {
-                    i = order ? (int64_t)__ldg(&order[t]) : (int64_t)t;
-                    info = 0;
-                    used = 0;
-                    bool traverse = false;
-                    if (flags[i] & 1) {
-                        p = xyz(x[i]);
-                        radius = r[i];
-                        if (pl.enabled) {  // generate_plane_contacts.comp:37-38
-                            const float dist = p.z - pl.altitude;
-                            if (dist < pl.margin + radius) info |= kPlaneBit;
+        // refill once no lane is busy: lanes without a particle take the next queue
+        // entries; particles with no mesh work (inactive, or no mesh) complete here
+        if (__ballot_sync(FULL, i >= 0) == 0) {
+            while (true) {
+                const bool need = !done && i < 0;
+                const uint32_t m = __ballot_sync(FULL, need);
+                if (!m) break;
+                const int leader = __ffs(m) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(m));
+                base = __shfl_sync(FULL, base, leader);
+                if (need) {
+                    const uint64_t t = (uint64_t)base + (uint64_t)__popc(m & lt);
+                    if (t >= (uint64_t)n) {
+                        done = true;
+                    } else {
+                        i = order ? (int64_t)__ldg(&order[t]) : (int64_t)t;
+                        info = 0;
+                        used = 0;
+                        bool traverse = false;
+                        if (flags[i] & 1) {
+                            p = xyz(x[i]);
+                            radius = r[i];
+                            if (pl.enabled) {  // generate_plane_contacts.comp:37-38
+                                const float dist = p.z - pl.altitude;
+                                if (dist < pl.margin + radius) info |= kPlaneBit;
+                            }
+                            if (nwalk > 0) {
+                                wi = 0;
+                                ci = mt.walk_list ? __ldg(&mt.walk_list[0]) : 0;
+                                walk_begin(w, mt, ci, radius, p);
+                                pc = phi = 0;
+                                traverse = true;
+                            }
                         }
-                        if (nwalk > 0) {
-                            wi = 0;
-                            ci = mt.walk_list ? __ldg(&mt.walk_list[0]) : 0;
-                            walk_begin(w, mt, ci, radius, p);
-                            traverse = true;
+                        if (!traverse) {
+                            cinfo[i] = info;
+                            count += info & kPlaneBit;
+                            i = -1;
                         }
-                    }
-                    if (!traverse) {
-                        cinfo[i] = info;
-                        count += info & kPlaneBit;
-                        i = -1;
                     }
                 }
             }
         }
         if (__all_sync(FULL, done)) break;
-        const bool busy = i >= 0;
-        bool holds = false;
-        uint32_t llo = 0, lhi = 0;
-        while (true) {  // inner nodes until every busy lane holds a leaf or has an empty stack
-            const bool more = busy && !holds && w.sp > 0;
-            if (!__any_sync(FULL, more)) break;
-            if (more) holds = walk_pop(w, mt, p, eps_md, llo, lhi);
+        if (i < 0) continue;
+        // one step: pop until an entry needs a load, then one triangle or one inner node
+        int kind = 0;  // 1: triangle pc, 2: children (ca, cb) of an inner node
+        uint32_t ca = 0, cb = 0;
+        while (pc >= phi && w.sp > 0) {
+            const int e = walk_pop_entry(w, eps_md, ca, cb);
+            if (e == 1) {
+                pc = ca;
+                phi = cb;
+            } else if (e == 2) {
+                kind = 2;
+                break;
+            }
         }
-        if (holds) walk_leaf(w, mt, p, eps_md, eps2, llo, lhi);
-        if (busy && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
+        if (pc < phi) kind = 1;
+        if (kind) {
+            const float4* rec = kind == 1 ? mt.tri_cache + (size_t)pc * 4 : mt.pair + (size_t)ca * 4;
+            const float4 f0 = __ldg(rec), f1 = __ldg(rec + 1), f2 = __ldg(rec + 2), f3 = __ldg(rec + 3);
+            if (kind == 1) {
+                // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (generate_mesh_contacts.comp:250-251)
+                if (f3.w >= 0.0f) walk_tri(w, p, eps_md, eps2, f0, f1, f2, f3);
+                pc++;
+            } else {
+                walk_children(w, p, eps_md, f0, f1, f2, f3);
+            }
+        }
+        if (pc >= phi && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
             v3 bp, bv, nn;
             if (walk_finish(w, mt, ci, p, bp, bv, nn)) {
                 if (used < slot_cap) {
@@ -111,6 +139,7 @@ __global__ void __launch_bounds__(128, 8) k_collide(int64_t n, const uint32_t* _
             if (++wi < nwalk) {
                 ci = mt.walk_list ? __ldg(&mt.walk_list[wi]) : wi;
                 walk_begin(w, mt, ci, radius, p);
+                pc = phi = 0;
             } else {
                 info |= (uint32_t)used << 1;
                 cinfo[i] = info;
@@ -135,7 +164,7 @@ void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const floa
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
                     uint32_t* ccount, uint32_t* queue, DeviceStatus* st) {
     if (n <= 0) return;
-    const int threads = 128;
+    const int threads = kCollideThreads;
     const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 8);
     k_collide<<<blocks, threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo, cslot, ccount, queue, st);
 }

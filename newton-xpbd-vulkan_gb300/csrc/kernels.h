@@ -79,6 +79,9 @@ struct MeshTables {
     // per leaf slot: (a.xyz, triangle id bits), (b.xyz, |e0|^2), (c.xyz, |e1|^2),
     // (unit normal.xyz, |e2|^2 or -1 when the triangle is skipped as degenerate)
     const float4* tri_cache;
+    // sibling records keyed by left child: pair[a*4 .. a*4+3] = nl[a], nu[a], nl[b], nu[b]
+    // for every inner node with children (a, b), so one pop reads one 64-byte record
+    const float4* pair;
     // meshes whose body is dynamic hold body-frame vertices: pose = the bodies' state
     // (2 float4 per mesh), posed[m] != 0 for those meshes, walk_list = the other meshes
     // (null: every mesh is static)
@@ -288,6 +291,10 @@ struct LbvhTopology {
     uint32_t* prim_local;  // triangle of each leaf slot, mesh-local
 };
 size_t lbvh_scratch_words(int num_tris);
+// Sibling records of one mesh's reachable inner nodes (MeshTables::pair), after a
+// build or refit of its node slots [node_base, node_base + 2 num_tris).
+void launch_node_pairs(cudaStream_t s, int num_tris, uint32_t node_base, const uint8_t* reachable, const float4* nl,
+                       const float4* nu, float4* pair);
 // build of one mesh of num_tris triangles (tris: that mesh's triangles, global vertex
 // indices) into the global node arrays at node_base, the primitive array at prim_base
 // (triangle ids + tri_base) and *root_global

@@ -110,12 +110,28 @@ __device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
     return mk3(__ldg(p + i * 3), __ldg(p + i * 3 + 1), __ldg(p + i * 3 + 2));
 }
 
+// Traversal stack of one thread (32 entries, local memory). An entry keeps, besides
+// the node, the squared box distance and the packed child words read when its parent
+// ordered its children, so a pop needs no load.
+struct LocalStack {
+    float nds[32];
+    uint32_t lw[32], uw[32];
+    __device__ __forceinline__ void put(uint32_t k, float d, uint32_t l, uint32_t u) {
+        nds[k] = d;
+        lw[k] = l;
+        uw[k] = u;
+    }
+    __device__ __forceinline__ float dist(uint32_t k) const { return nds[k]; }
+    __device__ __forceinline__ void words(uint32_t k, uint32_t& l, uint32_t& u) const {
+        l = lw[k];
+        u = uw[k];
+    }
+};
+
 // Traversal state of one particle against one mesh (generate_mesh_contacts.comp:201-331).
-// A stack entry keeps, besides the node, the squared box distance and the packed
-// child words read when its parent ordered its children, so a pop needs no load.
+template <class Stack>
 struct MeshWalk {
-    float snds[32];
-    uint32_t slw[32], suw[32];
+    Stack stk;
     uint32_t sp;
     float min_dist, min_dist_sq, max_dist;
     v3 acc;
@@ -124,18 +140,18 @@ struct MeshWalk {
     bool found, wt, overflow;
 };
 
-__device__ __forceinline__ void walk_push(MeshWalk& w, float nds, float4 lo4, float4 hi4) {
+template <class W>
+__device__ __forceinline__ void walk_push(W& w, float nds, float4 lo4, float4 hi4) {
     if (w.sp < 32) {
-        w.snds[w.sp] = nds;
-        w.slw[w.sp] = __float_as_uint(lo4.w);
-        w.suw[w.sp] = __float_as_uint(hi4.w);
+        w.stk.put(w.sp, nds, __float_as_uint(lo4.w), __float_as_uint(hi4.w));
         w.sp++;
     } else {
         w.overflow = true;
     }
 }
 
-__device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, int ci, float radius, v3 p) {
+template <class W>
+__device__ __forceinline__ void walk_begin(W& w, const MeshTables& mt, int ci, float radius, v3 p) {
     w.max_dist = mt.soft_margin + __ldg(&mt.margins[ci]) + radius;
     w.sp = 0;
     const uint32_t root = __ldg(&mt.roots[ci]);
@@ -151,27 +167,29 @@ __device__ __forceinline__ void walk_begin(MeshWalk& w, const MeshTables& mt, in
     w.min_dist_sq = w.max_dist * w.max_dist;
 }
 
-// Pops one node (:221-235, :315-330). Returns true when it is a leaf that passed the
-// distance test; its primitive range is returned for evaluation before the next pop.
-__device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, uint32_t& lo,
-                                         uint32_t& hi) {
+// Pops one stack entry (:221-235, :315-330). Returns 0 when the entry is pruned by
+// the current distance bound, 1 for a leaf (its primitive range in a, b) and 2 for
+// an inner node (its children in a, b, whose boxes walk_children then takes).
+template <class W>
+__device__ __forceinline__ int walk_pop_entry(W& w, float eps_md, uint32_t& a, uint32_t& b) {
     --w.sp;
-    const float nds = w.snds[w.sp];
+    const float nds = w.stk.dist(w.sp);
     if (w.wt) {
-        if (nds > w.min_dist_sq) return false;
+        if (nds > w.min_dist_sq) return 0;
     } else {
-        if (nds > (w.min_dist + eps_md) * (w.min_dist + eps_md)) return false;
+        if (nds > (w.min_dist + eps_md) * (w.min_dist + eps_md)) return 0;
     }
-    const uint32_t lpk = w.slw[w.sp];
-    const uint32_t left_i = lpk & 0x3FFFFFFFu, is_leaf = (lpk >> 30) & 3u;
-    const uint32_t right_i = w.suw[w.sp] & 0x3FFFFFFFu;
-    if (is_leaf) {
-        lo = left_i;
-        hi = right_i;
-        return true;
-    }
-    const float4 llo = __ldg(&mt.nl[left_i]), lhi = __ldg(&mt.nu[left_i]);
-    const float4 rlo = __ldg(&mt.nl[right_i]), rhi = __ldg(&mt.nu[right_i]);
+    uint32_t lpk, upk;
+    w.stk.words(w.sp, lpk, upk);
+    a = lpk & 0x3FFFFFFFu;
+    b = upk & 0x3FFFFFFFu;
+    return ((lpk >> 30) & 3u) ? 1 : 2;
+}
+
+// Orders and pushes the children of the inner node just popped (:316-330).
+template <class W>
+__device__ __forceinline__ void walk_children(W& w, v3 p, float eps_md, float4 llo, float4 lhi, float4 rlo,
+                                              float4 rhi) {
     const float lds = dist_sq_aabb(p, xyz(llo), xyz(lhi)), rds = dist_sq_aabb(p, xyz(rlo), xyz(rhi));
     const float thresh = w.wt ? w.min_dist_sq : ((w.min_dist + eps_md) * (w.min_dist + eps_md));
     // the shader's 32-entry stack has no bound check; a push past it is dropped here
@@ -183,77 +201,105 @@ __device__ __forceinline__ bool walk_pop(MeshWalk& w, const MeshTables& mt, v3 p
         if (lds < thresh) walk_push(w, lds, llo, lhi);
         if (rds < thresh) walk_push(w, rds, rlo, rhi);
     }
+}
+
+// Pops one node. Returns true when it is a leaf that passed the distance test; its
+// primitive range is returned for evaluation before the next pop.
+template <class W>
+__device__ __forceinline__ bool walk_pop(W& w, const MeshTables& mt, v3 p, float eps_md, uint32_t& lo,
+                                         uint32_t& hi) {
+    uint32_t a, b;
+    const int r = walk_pop_entry(w, eps_md, a, b);
+    if (r == 1) {
+        lo = a;
+        hi = b;
+        return true;
+    }
+    if (r == 2) {
+        const float4* rec = mt.pair + (size_t)a * 4;  // nl[a], nu[a], nl[b], nu[b]
+        walk_children(w, p, eps_md, __ldg(rec), __ldg(rec + 1), __ldg(rec + 2), __ldg(rec + 3));
+    }
     return false;
 }
 
-// Evaluates the triangles of one leaf (:237-314).
-__device__ __forceinline__ void walk_leaf(MeshWalk& w, const MeshTables& mt, v3 p, float eps_md, float eps2,
-                                          uint32_t lo, uint32_t hi) {
+// One triangle of a leaf (:239-313) from its four cache words (a, tri id), (b, |e0|^2),
+// (c, |e1|^2), (unit normal, |e2|^2); degenerate triangles (:250-251) are skipped by
+// the caller (normal word w < 0).
+template <class W>
+__device__ __forceinline__ void walk_tri(W& w, v3 p, float eps_md, float eps2, float4 qa, float4 qb, float4 qc,
+                                         float4 qn) {
     const float PI_ = 3.14159265359f;
-    for (uint32_t pc = lo; pc < hi; pc++) {
-        const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
-        if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
-        const float4 qa = __ldg(&mt.tri_cache[pc * 4]), qb = __ldg(&mt.tri_cache[pc * 4 + 1]),
-                     qc = __ldg(&mt.tri_cache[pc * 4 + 2]);
-        const uint32_t t = __float_as_uint(qa.w);
-        const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
-        const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
-        const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
-        v3 cp, tb;
-        closest_point_triangle(p, a, b, c, cp, tb);
-        if (w.wt) {
-            const v3 diff = vsub(cp, p);
-            const float dist_sq = vdot(diff, diff);
-            if (dist_sq < w.min_dist_sq) {
-                w.min_dist_sq = dist_sq;
-                w.min_face = t;
-                w.sv_v = tb.y;
-                w.sv_w = tb.z;
-                w.found = true;
+    const uint32_t t = __float_as_uint(qa.w);
+    const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
+    const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+    const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
+    v3 cp, tb;
+    closest_point_triangle(p, a, b, c, cp, tb);
+    if (w.wt) {
+        const v3 diff = vsub(cp, p);
+        const float dist_sq = vdot(diff, diff);
+        if (dist_sq < w.min_dist_sq) {
+            w.min_dist_sq = dist_sq;
+            w.min_face = t;
+            w.sv_v = tb.y;
+            w.sv_w = tb.z;
+            w.found = true;
+        }
+    } else {
+        const float dist = exact_length(vsub(cp, p));
+        if (dist < w.min_dist + eps_md) {
+            float weight;
+            const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
+            const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
+            if (lcp < eps2) {
+                weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
+            } else if (lcq < eps2) {
+                weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
+            } else if (lcr < eps2) {
+                weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
+            } else {
+                const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
+                if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
+                    (lcp * e1n - e1cp * e1cp < eps2 * e1n))
+                    weight = PI_;
+                else
+                    weight = 2.0f * PI_;
             }
-        } else {
-            const float dist = exact_length(vsub(cp, p));
-            if (dist < w.min_dist + eps_md) {
-                float weight;
-                const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
-                const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
-                if (lcp < eps2) {
-                    weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
-                } else if (lcq < eps2) {
-                    weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
-                } else if (lcr < eps2) {
-                    weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
-                } else {
-                    const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
-                    if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
-                        (lcp * e1n - e1cp * e1cp < eps2 * e1n))
-                        weight = PI_;
-                    else
-                        weight = 2.0f * PI_;
-                }
-                if (dist > w.min_dist - eps_md) {
-                    w.acc = vadd(w.acc, vmuls(tn, weight));
-                    if (dist < w.min_dist) {
-                        w.min_dist = dist;
-                        w.min_face = t;
-                        w.sv_v = tb.y;
-                        w.sv_w = tb.z;
-                    }
-                } else {
+            if (dist > w.min_dist - eps_md) {
+                w.acc = vadd(w.acc, vmuls(tn, weight));
+                if (dist < w.min_dist) {
                     w.min_dist = dist;
                     w.min_face = t;
                     w.sv_v = tb.y;
                     w.sv_w = tb.z;
-                    w.acc = vmuls(tn, weight);
                 }
-                w.found = true;
+            } else {
+                w.min_dist = dist;
+                w.min_face = t;
+                w.sv_v = tb.y;
+                w.sv_w = tb.z;
+                w.acc = vmuls(tn, weight);
             }
+            w.found = true;
         }
     }
 }
 
+// Evaluates the triangles of one leaf (:237-314).
+template <class W>
+__device__ __forceinline__ void walk_leaf(W& w, const MeshTables& mt, v3 p, float eps_md, float eps2,
+                                          uint32_t lo, uint32_t hi) {
+    for (uint32_t pc = lo; pc < hi; pc++) {
+        const float4 qn = __ldg(&mt.tri_cache[pc * 4 + 3]);
+        if (qn.w < 0.0f) continue;  // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (:250-251)
+        walk_tri(w, p, eps_md, eps2, __ldg(&mt.tri_cache[pc * 4]), __ldg(&mt.tri_cache[pc * 4 + 1]),
+                 __ldg(&mt.tri_cache[pc * 4 + 2]), qn);
+    }
+}
+
 // Contact emission after the traversal of mesh ci (:333-411).
-__device__ __forceinline__ bool walk_finish(MeshWalk& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
+template <class W>
+__device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
                                             v3& shape_v, v3& nrm) {
     if (w.wt) w.min_dist = exact_sqrt(w.min_dist_sq);
     if (!(w.found && w.min_dist < w.max_dist)) return false;
@@ -292,7 +338,7 @@ __device__ __forceinline__ bool mesh_query(const MeshTables& mt, int ci, float r
                                            v3& shape_v, v3& nrm, bool& overflow) {
     const float eps_md = mt.avg_edge * 1e-3f;
     const float eps2 = eps_md * eps_md;
-    MeshWalk w;
+    MeshWalk<LocalStack> w;
     w.overflow = false;
     walk_begin(w, mt, ci, radius, p);
     while (w.sp > 0) {

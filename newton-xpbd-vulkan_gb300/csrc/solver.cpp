@@ -358,6 +358,10 @@ void Solver::finalize_meshes() {
             launch_lbvh_build(stream_, (int)pcnt[c], verts_.p, tris_.p + (size_t)prim_offsets_[c] * 3,
                               (uint32_t)node_offsets_[c], (uint32_t)prim_offsets_[c], (uint32_t)prim_offsets_[c],
                               nl_.p, nu_.p, prim_.p, roots_.p + c, topology(c), bvh_scratch_.p, status_.p);
+        node_pair_.alloc(total_nodes * 4, false);
+        for (size_t c = 0; c < nm; c++)
+            launch_node_pairs(stream_, (int)pcnt[c], (uint32_t)node_offsets_[c], topo_reachable_.p + node_offsets_[c],
+                              nl_.p, nu_.p, node_pair_.p);
         avg_edge0_ = meshes_[0].avg_edge;  // mesh 0's average edge for every mesh (scene.cpp:325)
         tri_cache_.alloc(total_prims * 4, false);
         launch_tri_cache(stream_, 0, (int64_t)total_prims, prim_.p, tris_.p, verts_.p, tri_cache_.p);
@@ -428,6 +432,7 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
                               cudaMemcpyHostToDevice, stream_));
     launch_lbvh_refit(stream_, (int)nt, verts_.p, tris_.p + pb * 3, topology(mi), nl_.p + nb, nu_.p + nb,
                       bvh_scratch_.p);
+    launch_node_pairs(stream_, (int)nt, (uint32_t)nb, topo_reachable_.p + nb, nl_.p, nu_.p, node_pair_.p);
     launch_tri_cache(stream_, (int64_t)pb, (int64_t)nt, prim_.p, tris_.p, verts_.p, tri_cache_.p);
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
@@ -710,6 +715,7 @@ MeshTables Solver::mesh_tables() const {
     m.prim_off = prim_off_.p;
     m.prim_cnt = prim_cnt_.p;
     m.tri_cache = tri_cache_.p;
+    m.pair = node_pair_.p;
     m.pose = body_q_.p;
     m.posed = dyn_any_ ? posed_.p : nullptr;
     m.walk_list = dyn_any_ ? walk_list_.p : nullptr;

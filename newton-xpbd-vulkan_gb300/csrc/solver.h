@@ -280,6 +280,7 @@ class Solver {
     DevBuf<float> verts_, vels_;
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
     DevBuf<float4> tri_cache_;
+    DevBuf<float4> node_pair_;  // MeshTables::pair, 4 per node slot
     DevBuf<int> topo_parent_, topo_child_l_, topo_child_r_;
     DevBuf<uint8_t> topo_marked_, topo_reachable_;
     DevBuf<uint32_t> topo_prim_, bvh_scratch_;
