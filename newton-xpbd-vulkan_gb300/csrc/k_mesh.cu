@@ -12,25 +12,79 @@
 
 namespace xpbd {
 
-// Contact generation with persistent warps. Lanes take particles from a work
-// queue (in the previous substep's hash-grid order, so a warp's particles are
-// neighbours), a warp refilling its lanes once none of them is busy. Every
-// iteration each busy lane advances its own traversal by one step: it pops stack
-// entries until one needs a load (pruned entries cost no load), and then either
-// tests one triangle of the leaf it holds or orders the children of an inner node;
-// both read one 64-byte record (triangle cache entry, or the sibling record of the
-// children), issued together. A warp is therefore never held back by a lane with
-// a long run of inner nodes before its next leaf: its time is set by its longest
-// particle, not by the sum of its per-leaf maxima. Each particle's own sequence of
-// node visits and triangle tests is that of the shader, so its contacts are
-// unchanged.
+// first walk index >= wi whose mesh p may reach (mesh_far), nwalk if none: the
+// meshes skipped would end their queries without a contact
+__device__ __forceinline__ int first_near(const MeshTables& mt, int wi, int nwalk, v3 p) {
+    for (; wi < nwalk; wi++)
+        if (!mesh_far(mt, mt.walk_list ? __ldg(&mt.walk_list[wi]) : wi, p)) break;
+    return wi;
+}
+
+// Triage before the traversal (one thread per particle, in queue order): the plane
+// test (generate_plane_contacts.comp:37-38) for every particle; particles that may
+// reach a mesh (mesh_far) are appended to the near list, in queue order within a
+// warp, and every other particle's contact info is final here.
+__global__ void __launch_bounds__(256) k_collide_triage(int64_t n, const uint32_t* __restrict__ order,
+                                                        const float4* __restrict__ x, const float* __restrict__ r,
+                                                        const int* __restrict__ flags, PlaneParams pl,
+                                                        MeshTables mt, uint32_t* __restrict__ cinfo,
+                                                        uint32_t* ccount, uint32_t* queue, uint32_t* near) {
+    __shared__ uint32_t s_warp[8];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int nwalk = mt.walk_list ? mt.walk_count : mt.n_meshes;
+    bool is_near = false;
+    uint32_t count = 0;
+    int64_t i = -1;
+    if (t < n) {
+        i = order ? (int64_t)__ldg(&order[t]) : t;
+        uint32_t info = 0;
+        if (flags[i] & 1) {
+            const v3 p = xyz(x[i]);
+            if (pl.enabled) {
+                const float dist = p.z - pl.altitude;
+                if (dist < pl.margin + r[i]) info |= kPlaneBit;
+            }
+            is_near = first_near(mt, 0, nwalk, p) < nwalk;
+        }
+        if (!is_near) {
+            cinfo[i] = info;
+            count = info & kPlaneBit;
+        }
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, is_near);
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(queue + 1, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (is_near) near[base + __popc(m & lanemask_lt())] = (uint32_t)i;
+    }
+    const uint32_t tot = block_sum(count, s_warp);
+    if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
+}
+
+// Contact generation with persistent warps over the near list (k_collide_triage).
+// kCollideLanes lanes of each warp take particles; a warp refills them from the list
+// once none of them is busy. Every iteration each busy lane advances its own
+// traversal by one step: it pops stack entries until one needs a load (pruned
+// entries cost no load), then either orders the children of an inner node (one
+// 64-byte sibling record) or tests one triangle of the leaf it holds (one 64-byte
+// triangle cache entry). A warp is never held back by a lane with a long run of
+// inner nodes before its next leaf: its time is set by its longest particle, not by
+// the sum of its per-leaf maxima. The time of the kernel is that of its longest
+// chains of dependent steps, so fewer particles per warp (more warps sharing the
+// near list, fewer divergent paths per iteration) is faster, up to the resident
+// warps. Each particle's own sequence of node visits and triangle tests is that of
+// the shader, so its contacts are unchanged.
 constexpr int kCollideThreads = 128;
-__global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const uint32_t* __restrict__ order,
-                                                 const float4* __restrict__ x, const float* __restrict__ r,
-                                                 const int* __restrict__ flags, PlaneParams pl, MeshTables mt,
+constexpr int kCollideLanes = 8;
+
+__global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const float4* __restrict__ x,
+                                                 const float* __restrict__ r, PlaneParams pl, MeshTables mt,
                                                  int slot_cap, uint32_t* __restrict__ cinfo,
                                                  float4* __restrict__ cslot, uint32_t* ccount, uint32_t* queue,
-                                                 DeviceStatus* st) {
+                                                 const uint32_t* __restrict__ near, DeviceStatus* st) {
     __shared__ uint32_t s_warp[kCollideThreads / 32];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -38,7 +92,7 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
     const float eps_md = mt.avg_edge * 1e-3f;
     const float eps2 = eps_md * eps_md;
     int64_t i = -1;
-    bool done = false, stack_ovf = false, slot_ovf = false;
+    bool done = lane >= kCollideLanes, stack_ovf = false, slot_ovf = false;
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
     uint32_t info = 0, count = 0;
@@ -46,46 +100,40 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
     int used = 0, ci = 0, wi = 0;
     // meshes walked here: all of them, or the static ones when some belong to dynamic bodies
     const int nwalk = mt.walk_list ? mt.walk_count : mt.n_meshes;
+    const uint64_t n_near = queue[1];  // written by k_collide_triage
     MeshWalk<LocalStack> w;
     w.sp = 0;
     w.overflow = false;
     while (true) {
-        // refill once no lane is busy: lanes without a particle take the next queue
-        // entries; particles with no mesh work (inactive, or no mesh) complete here
+        // refill once no lane is busy
         if (__ballot_sync(FULL, i >= 0) == 0) {
-            while (true) {
-                const bool need = !done && i < 0;
-                const uint32_t m = __ballot_sync(FULL, need);
-                if (!m) break;
+            const bool need = !done && i < 0;
+            const uint32_t m = __ballot_sync(FULL, need);
+            if (m) {
                 const int leader = __ffs(m) - 1;
                 uint32_t base = 0;
                 if (lane == leader) base = atomicAdd(queue, (uint32_t)__popc(m));
                 base = __shfl_sync(FULL, base, leader);
                 if (need) {
                     const uint64_t t = (uint64_t)base + (uint64_t)__popc(m & lt);
-                    if (t >= (uint64_t)n) {
+                    if (t >= n_near) {
                         done = true;
                     } else {
-                        i = order ? (int64_t)__ldg(&order[t]) : (int64_t)t;
+                        i = (int64_t)__ldg(&near[t]);
+                        p = xyz(x[i]);
+                        radius = r[i];
                         info = 0;
                         used = 0;
-                        bool traverse = false;
-                        if (flags[i] & 1) {
-                            p = xyz(x[i]);
-                            radius = r[i];
-                            if (pl.enabled) {  // generate_plane_contacts.comp:37-38
-                                const float dist = p.z - pl.altitude;
-                                if (dist < pl.margin + radius) info |= kPlaneBit;
-                            }
-                            if (nwalk > 0) {
-                                wi = 0;
-                                ci = mt.walk_list ? __ldg(&mt.walk_list[0]) : 0;
-                                walk_begin(w, mt, ci, radius, p);
-                                pc = phi = 0;
-                                traverse = true;
-                            }
+                        if (pl.enabled) {  // generate_plane_contacts.comp:37-38
+                            const float dist = p.z - pl.altitude;
+                            if (dist < pl.margin + radius) info |= kPlaneBit;
                         }
-                        if (!traverse) {
+                        wi = first_near(mt, 0, nwalk, p);  // < nwalk: the triage listed it
+                        if (wi < nwalk) {
+                            ci = mt.walk_list ? __ldg(&mt.walk_list[wi]) : wi;
+                            walk_begin(w, mt, ci, radius, p);
+                            pc = phi = 0;
+                        } else {
                             cinfo[i] = info;
                             count += info & kPlaneBit;
                             i = -1;
@@ -96,32 +144,31 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
         }
         if (__all_sync(FULL, done)) break;
         if (i < 0) continue;
-        // one step: pop until an entry needs a load, then one triangle or one inner node
-        int kind = 0;  // 1: triangle pc, 2: children (ca, cb) of an inner node
+        // one step: pop until an entry needs a load, then an inner node or one triangle
         uint32_t ca = 0, cb = 0;
+        bool inner = false;
         while (pc >= phi && w.sp > 0) {
             const int e = walk_pop_entry(w, eps_md, ca, cb);
             if (e == 1) {
                 pc = ca;
                 phi = cb;
             } else if (e == 2) {
-                kind = 2;
+                inner = true;
                 break;
             }
         }
-        if (pc < phi) kind = 1;
-        if (kind) {
-            const float4* rec = kind == 1 ? mt.tri_cache + (size_t)pc * 4 : mt.pair + (size_t)ca * 4;
+        if (inner || pc < phi) {
+            const float4* rec = inner ? mt.pair + (size_t)ca * 4 : mt.tri_cache + (size_t)pc * 4;
             const float4 f0 = __ldg(rec), f1 = __ldg(rec + 1), f2 = __ldg(rec + 2), f3 = __ldg(rec + 3);
-            if (kind == 1) {
+            if (inner) {
+                walk_children(w, p, eps_md, f0, f1, f2, f3);
+            } else {
                 // degenerate: |cross|/(|e0|^2+|e1|^2+|e2|^2) < 1e-6 (generate_mesh_contacts.comp:250-251)
                 if (f3.w >= 0.0f) walk_tri(w, p, eps_md, eps2, f0, f1, f2, f3);
                 pc++;
-            } else {
-                walk_children(w, p, eps_md, f0, f1, f2, f3);
             }
         }
-        if (pc >= phi && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
+        while (pc >= phi && w.sp == 0) {  // mesh ci done: emit its contact, move to the next mesh
             v3 bp, bv, nn;
             if (walk_finish(w, mt, ci, p, bp, bv, nn)) {
                 if (used < slot_cap) {
@@ -136,16 +183,18 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
             }
             stack_ovf |= w.overflow;
             w.overflow = false;
-            if (++wi < nwalk) {
+            wi = first_near(mt, wi + 1, nwalk, p);
+            if (wi < nwalk) {
                 ci = mt.walk_list ? __ldg(&mt.walk_list[wi]) : wi;
                 walk_begin(w, mt, ci, radius, p);
                 pc = phi = 0;
-            } else {
-                info |= (uint32_t)used << 1;
-                cinfo[i] = info;
-                count += (info & kPlaneBit) + (uint32_t)used;
-                i = -1;
+                break;
             }
+            info |= (uint32_t)used << 1;
+            cinfo[i] = info;
+            count += (info & kPlaneBit) + (uint32_t)used;
+            i = -1;
+            break;
         }
     }
     if (stack_ovf) {
@@ -162,11 +211,13 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
 
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st) {
+                    uint32_t* ccount, uint32_t* queue, uint32_t* near, DeviceStatus* st) {
     if (n <= 0) return;
+    k_collide_triage<<<(int)((n + 255) / 256), 256, 0, s>>>(n, order, x, r, flags, pl, mt, cinfo, ccount, queue,
+                                                             near);
     const int threads = kCollideThreads;
-    const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 8);
-    k_collide<<<blocks, threads, 0, s>>>(n, order, x, r, flags, pl, mt, slot_cap, cinfo, cslot, ccount, queue, st);
+    const int blocks = (int)std::min<int64_t>((n * (32 / kCollideLanes) + threads - 1) / threads, 152 * 8);
+    k_collide<<<blocks, threads, 0, s>>>(n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
 }
 
 // Triangle data that generate_mesh_contacts.comp:239-251 and :117 recompute on

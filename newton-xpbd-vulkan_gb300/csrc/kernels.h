@@ -82,6 +82,14 @@ struct MeshTables {
     // sibling records keyed by left child: pair[a*4 .. a*4+3] = nl[a], nu[a], nl[b], nu[b]
     // for every inner node with children (a, b), so one pop reads one 64-byte record
     const float4* pair;
+    // reach grids (one per mesh, null: none): bit set for every cell within reach of a
+    // leaf box. cull_org[m] = (origin.xyz, 1/cell), cull_dim[m] = (nx, ny, nz, dilation
+    // in cells; nx = 0: no grid), words of mesh m from cull_off[m], x fastest, 32 cells
+    // per word. A particle in a clear cell (or outside the grid) cannot reach any leaf.
+    const float4* cull_org;
+    const int4* cull_dim;
+    const uint32_t* cull_off;
+    const uint32_t* cull_bits;
     // meshes whose body is dynamic hold body-frame vertices: pose = the bodies' state
     // (2 float4 per mesh), posed[m] != 0 for those meshes, walk_list = the other meshes
     // (null: every mesh is static)
@@ -161,9 +169,10 @@ void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const
                          int4* table, const uint32_t* stamp, float4* rx, float4* rv, int* rf);
 // plane + mesh contact generation over the particles order[0..n) (any permutation);
 // *queue is the work-queue counter and must be zero at launch
+// queue: 2 zeroed words (work counter, near-list length); near: n words of scratch
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, uint32_t* queue, DeviceStatus* st);
+                    uint32_t* ccount, uint32_t* queue, uint32_t* near, DeviceStatus* st);
 // per-leaf-slot triangle cache for the slots [first, first + count)
 void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
                       const float* verts, float4* cache);
@@ -291,6 +300,12 @@ struct LbvhTopology {
     uint32_t* prim_local;  // triangle of each leaf slot, mesh-local
 };
 size_t lbvh_scratch_words(int num_tris);
+// Reach grids of all meshes (MeshTables::cull_*): mark the cells of every reachable
+// leaf box of node slots [0, total_nodes) (node_off: first slot of each mesh, nm + 1
+// entries), then dilate by each grid's reach along x, y and z. tmp has total_words.
+void launch_cull_build(cudaStream_t s, int nm, const uint32_t* node_off, int64_t total_nodes,
+                       const uint8_t* reachable, const float4* nl, const float4* nu, const float4* org,
+                       const int4* dim, const uint32_t* off, int64_t total_words, uint32_t* bits, uint32_t* tmp);
 // Sibling records of one mesh's reachable inner nodes (MeshTables::pair), after a
 // build or refit of its node slots [node_base, node_base + 2 num_tris).
 void launch_node_pairs(cudaStream_t s, int num_tris, uint32_t node_base, const uint8_t* reachable, const float4* nl,

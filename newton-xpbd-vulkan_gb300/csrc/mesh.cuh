@@ -15,6 +15,25 @@ __device__ __forceinline__ float dist_sq_aabb(v3 p, v3 lo, v3 hi) {  // generate
 
 __device__ __forceinline__ float comp(v3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
 
+// True when p (in mesh ci's frame) lies in a clear cell of the mesh's reach grid or
+// outside it, or is not finite: then no leaf box is within the traversal's initial
+// bound (margin + shape margin + radius + eps) and the query ends without testing
+// a triangle, i.e. without a contact (the bound only shrinks once a triangle is
+// tested, and a node's box distance never exceeds its descendants').
+__device__ __forceinline__ bool mesh_far(const MeshTables& mt, int ci, v3 p) {
+    if (!mt.cull_bits) return false;
+    const int4 d = __ldg(&mt.cull_dim[ci]);
+    if (d.x == 0) return false;
+    const float4 o = __ldg(&mt.cull_org[ci]);
+    const float fx = (p.x - o.x) * o.w, fy = (p.y - o.y) * o.w, fz = (p.z - o.z) * o.w;
+    if (!(fx >= 0.0f && fx < (float)d.x && fy >= 0.0f && fy < (float)d.y && fz >= 0.0f && fz < (float)d.z))
+        return true;
+    const int ix = min((int)fx, d.x - 1), iy = min((int)fy, d.y - 1), iz = min((int)fz, d.z - 1);
+    const uint32_t nwx = ((uint32_t)d.x + 31u) >> 5;
+    const uint32_t word = __ldg(&mt.cull_off[ci]) + ((uint32_t)iz * (uint32_t)d.y + (uint32_t)iy) * nwx + ((uint32_t)ix >> 5);
+    return ((__ldg(&mt.cull_bits[word]) >> (ix & 31)) & 1u) == 0u;
+}
+
 // generate_mesh_contacts.comp:77-113
 static __device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
     const v3 adir = mk3(fabsf(dir.x), fabsf(dir.y), fabsf(dir.z));
@@ -222,67 +241,98 @@ __device__ __forceinline__ bool walk_pop(W& w, const MeshTables& mt, v3 p, float
     return false;
 }
 
-// One triangle of a leaf (:239-313) from its four cache words (a, tri id), (b, |e0|^2),
-// (c, |e1|^2), (unit normal, |e2|^2); degenerate triangles (:250-251) are skipped by
-// the caller (normal word w < 0).
-template <class W>
-__device__ __forceinline__ void walk_tri(W& w, v3 p, float eps_md, float eps2, float4 qa, float4 qb, float4 qc,
-                                         float4 qn) {
+// Test of one triangle against p (:239-313), the part that does not depend on the
+// traversal state: closest point, its distance (squared for watertight meshes) and,
+// for open meshes when the distance is below `below`, the angle weight of the
+// triangle normal at the closest point.
+struct TriHit {
+    float d;       // squared distance (watertight) or exact_length distance (open)
+    float v, w;    // barycentric v, w of the closest point
+    float weight;  // normal weight (open meshes, when d < below)
+    v3 tn;         // unit normal
+    uint32_t t;    // triangle
+};
+
+// From the triangle's four cache words (a, tri id), (b, |e0|^2), (c, |e1|^2),
+// (unit normal, |e2|^2); degenerate triangles (:250-251) are skipped by the caller
+// (normal word w < 0).
+__device__ __forceinline__ TriHit tri_hit(bool wt, v3 p, float eps2, float below, float4 qa, float4 qb, float4 qc,
+                                          float4 qn) {
     const float PI_ = 3.14159265359f;
-    const uint32_t t = __float_as_uint(qa.w);
-    const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc), tn = xyz(qn);
-    const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
-    const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
+    TriHit h;
+    h.t = __float_as_uint(qa.w);
+    const v3 a = xyz(qa), b = xyz(qb), c = xyz(qc);
+    h.tn = xyz(qn);
     v3 cp, tb;
     closest_point_triangle(p, a, b, c, cp, tb);
-    if (w.wt) {
+    h.v = tb.y;
+    h.w = tb.z;
+    h.weight = 0.0f;
+    if (wt) {
         const v3 diff = vsub(cp, p);
-        const float dist_sq = vdot(diff, diff);
-        if (dist_sq < w.min_dist_sq) {
-            w.min_dist_sq = dist_sq;
-            w.min_face = t;
-            w.sv_v = tb.y;
-            w.sv_w = tb.z;
-            w.found = true;
-        }
+        h.d = vdot(diff, diff);
     } else {
-        const float dist = exact_length(vsub(cp, p));
-        if (dist < w.min_dist + eps_md) {
-            float weight;
+        h.d = exact_length(vsub(cp, p));
+        if (h.d < below) {
+            const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
+            const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
             const v3 cp_p = vsub(cp, a), cq_p = vsub(cp, b), cr_p = vsub(cp, c);
             const float lcp = vdot(cp_p, cp_p), lcq = vdot(cq_p, cq_p), lcr = vdot(cr_p, cr_p);
             if (lcp < eps2) {
-                weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
+                h.weight = series_acos(gclamp(vdot(vnormalize(e0), vnormalize(e1)), -1.0f, 1.0f));
             } else if (lcq < eps2) {
-                weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
+                h.weight = series_acos(gclamp(vdot(vnormalize(e2), vnormalize(vneg(e0))), -1.0f, 1.0f));
             } else if (lcr < eps2) {
-                weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
+                h.weight = series_acos(gclamp(vdot(vnormalize(vneg(e1)), vnormalize(vneg(e2))), -1.0f, 1.0f));
             } else {
                 const float e0cp = vdot(e0, cp_p), e2cq = vdot(e2, cq_p), e1cp = vdot(e1, cp_p);
                 if ((lcp * e0n - e0cp * e0cp < eps2 * e0n) || (lcq * e2n - e2cq * e2cq < eps2 * e2n) ||
                     (lcp * e1n - e1cp * e1cp < eps2 * e1n))
-                    weight = PI_;
+                    h.weight = PI_;
                 else
-                    weight = 2.0f * PI_;
+                    h.weight = 2.0f * PI_;
             }
-            if (dist > w.min_dist - eps_md) {
-                w.acc = vadd(w.acc, vmuls(tn, weight));
-                if (dist < w.min_dist) {
-                    w.min_dist = dist;
-                    w.min_face = t;
-                    w.sv_v = tb.y;
-                    w.sv_w = tb.z;
-                }
-            } else {
-                w.min_dist = dist;
-                w.min_face = t;
-                w.sv_v = tb.y;
-                w.sv_w = tb.z;
-                w.acc = vmuls(tn, weight);
-            }
-            w.found = true;
         }
     }
+    return h;
+}
+
+// The traversal state update of one tested triangle (:257-313), in test order.
+template <class W>
+__device__ __forceinline__ void walk_apply(W& w, const TriHit& h, float eps_md) {
+    if (w.wt) {
+        if (h.d < w.min_dist_sq) {
+            w.min_dist_sq = h.d;
+            w.min_face = h.t;
+            w.sv_v = h.v;
+            w.sv_w = h.w;
+            w.found = true;
+        }
+    } else if (h.d < w.min_dist + eps_md) {
+        if (h.d > w.min_dist - eps_md) {
+            w.acc = vadd(w.acc, vmuls(h.tn, h.weight));
+            if (h.d < w.min_dist) {
+                w.min_dist = h.d;
+                w.min_face = h.t;
+                w.sv_v = h.v;
+                w.sv_w = h.w;
+            }
+        } else {
+            w.min_dist = h.d;
+            w.min_face = h.t;
+            w.sv_v = h.v;
+            w.sv_w = h.w;
+            w.acc = vmuls(h.tn, h.weight);
+        }
+        w.found = true;
+    }
+}
+
+// One triangle of a leaf tested and applied by one thread.
+template <class W>
+__device__ __forceinline__ void walk_tri(W& w, v3 p, float eps_md, float eps2, float4 qa, float4 qb, float4 qc,
+                                         float4 qn) {
+    walk_apply(w, tri_hit(w.wt, p, eps2, w.min_dist + eps_md, qa, qb, qc, qn), eps_md);
 }
 
 // Evaluates the triangles of one leaf (:237-314).
@@ -298,9 +348,12 @@ __device__ __forceinline__ void walk_leaf(W& w, const MeshTables& mt, v3 p, floa
 }
 
 // Contact emission after the traversal of mesh ci (:333-411).
+// The ray-parity loop of watertight meshes is split over the `nsub` lanes of a group
+// (lane `sub`, lanes `gmask`) when nsub > 1; every lane of the group gets the result.
 template <class W>
 __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
-                                            v3& shape_v, v3& nrm) {
+                                            v3& shape_v, v3& nrm, int sub = 0, int nsub = 1,
+                                            unsigned gmask = 0xffffffffu) {
     if (w.wt) w.min_dist = exact_sqrt(w.min_dist_sq);
     if (!(w.found && w.min_dist < w.max_dist)) return false;
     const float u_mesh = (1.0f - w.sv_v) - w.sv_w;
@@ -317,10 +370,11 @@ __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, 
         const v3 ray_dir = mk3(1.029700994f, 1.086472273f, 1.034694910f);
         uint32_t hits = 0;
         const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
-        for (uint32_t ti = 0; ti < pn; ti++) {
+        for (uint32_t ti = (uint32_t)sub; ti < pn; ti += (uint32_t)nsub) {
             const float4* q = mt.tri_cache + (size_t)(po + ti) * 4;
             if (intersect_ray_tri_woop(p, ray_dir, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
         }
+        for (int o = 1; o < nsub; o <<= 1) hits += __shfl_xor_sync(gmask, hits, o);
         sign = (hits & 1u) ? -1.0f : 1.0f;
     } else {
         sign = vdot(w.acc, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;

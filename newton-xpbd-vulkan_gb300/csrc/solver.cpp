@@ -134,6 +134,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     table_.alloc((size_t)n_scenes * kNumCells);
     stamp_.alloc(1);
     cinfo_.alloc(n_);
+    near_.alloc(n_, false);
     slot_cap_ = 1;
     cslot_.alloc(std::max<size_t>(n_, 1) * 3);
     ensure_substep_capacity(16);
@@ -160,8 +161,8 @@ void Solver::apply_sort_plan(int bits, int items) {
     hist_off_ = 0;
     lb_off_ = (size_t)plan_.passes << plan_.bits;
     tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
-    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter
-    sort_scratch_.alloc(cq_off_ + 1);
+    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter, near-list length
+    sort_scratch_.alloc(cq_off_ + 2);
     // the final sort buffer doubles as the collision pass's thread -> particle order (any
     // permutation gives the same contacts)
     launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
@@ -358,6 +359,11 @@ void Solver::finalize_meshes() {
             launch_lbvh_build(stream_, (int)pcnt[c], verts_.p, tris_.p + (size_t)prim_offsets_[c] * 3,
                               (uint32_t)node_offsets_[c], (uint32_t)prim_offsets_[c], (uint32_t)prim_offsets_[c],
                               nl_.p, nu_.p, prim_.p, roots_.p + c, topology(c), bvh_scratch_.p, status_.p);
+        std::vector<uint32_t> noff(nm + 1);
+        for (size_t c = 0; c < nm; c++) noff[c] = (uint32_t)node_offsets_[c];
+        noff[nm] = (uint32_t)total_nodes;
+        up(node_off_dev_, noff);
+        cull_dirty_ = true;
         node_pair_.alloc(total_nodes * 4, false);
         for (size_t c = 0; c < nm; c++)
             launch_node_pairs(stream_, (int)pcnt[c], (uint32_t)node_offsets_[c], topo_reachable_.p + node_offsets_[c],
@@ -399,7 +405,24 @@ void Solver::set_particles(const float* q, const float* qd, const float* inv_mas
         XPBD_CUDA(cudaStreamSynchronize(stream_));
     };
     if (inv_mass) up(w_.p, inv_mass);
-    if (radii) up(r_.p, radii);
+    if (radii) {
+        up(r_.p, radii);
+        float lo = 0.0f, hi = 0.0f;
+        bool fin = true, first = true;
+        for (size_t i = 0; i < n; i++) {
+            if (!std::isfinite(radii[i])) {
+                fin = false;
+                continue;
+            }
+            lo = first ? radii[i] : std::min(lo, radii[i]);
+            hi = first ? radii[i] : std::max(hi, radii[i]);
+            first = false;
+        }
+        if (lo != r_min_ || hi != r_max_ || fin != r_finite_) cull_dirty_ = true;
+        r_min_ = lo;
+        r_max_ = hi;
+        r_finite_ = fin;
+    }
     if (flags) {
         up(flags_.p, flags);
         bool all = true;
@@ -434,6 +457,7 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
                       bvh_scratch_.p);
     launch_node_pairs(stream_, (int)nt, (uint32_t)nb, topo_reachable_.p + nb, nl_.p, nu_.p, node_pair_.p);
     launch_tri_cache(stream_, (int64_t)pb, (int64_t)nt, prim_.p, tris_.p, verts_.p, tri_cache_.p);
+    cull_dirty_ = true;
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -701,6 +725,99 @@ void Solver::get_bodies(float* q, float* qd, size_t nb) {
     }
 }
 
+// Reach grid of each mesh, in the mesh's own frame: cells of about a quarter of the
+// reach, covering the mesh's vertex box padded by the reach plus slack. The reach
+// bounds |margin + shape margin + r + eps| + |eps| over the particles' radii (both
+// extremes, since the traversal squares the bound) with a relative and an absolute
+// slack for rounding. A mesh gets no grid (is never culled) when a radius, the
+// margin or a vertex is not finite, or once 2^23 words are spent.
+void Solver::ensure_cull() {
+    if (!cull_dirty_ || !finalized_) return;
+    cull_dirty_ = false;
+    const size_t nm = meshes_.size();
+    if (nm == 0) return;
+    const double eps = (double)(avg_edge0_ * 1e-3f);
+    const bool ok = r_finite_ && std::isfinite(cfg_.soft_contact_margin) && std::isfinite(eps);
+    std::vector<float4> org(nm, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    std::vector<int4> dim(nm, make_int4(0, 0, 0, 0));
+    std::vector<uint32_t> off(nm + 1, 0);
+    const uint64_t kMeshCells = 1ull << 24, kTotalWords = 1ull << 23;
+    uint64_t words = 0;
+    for (size_t c = 0; c < nm; c++) {
+        off[c] = (uint32_t)words;
+        off[c + 1] = (uint32_t)words;
+        const MeshData& m = meshes_[c];
+        const size_t v0 = vert_offsets_[c], nv = m.vertices.size() / 3;
+        if (!ok || nv == 0 || !std::isfinite(m.shape_margin)) continue;
+        double lo[3], hi[3], amax = 0.0;
+        bool fin = true;
+        for (int k = 0; k < 3; k++) lo[k] = hi[k] = all_verts_[v0 * 3 + k];
+        for (size_t v = 0; v < nv; v++)
+            for (int k = 0; k < 3; k++) {
+                const double q = all_verts_[(v0 + v) * 3 + k];
+                fin = fin && std::isfinite(q);
+                lo[k] = std::min(lo[k], q);
+                hi[k] = std::max(hi[k], q);
+                amax = std::max(amax, std::fabs(q));
+            }
+        if (!fin) continue;
+        const double base = (double)cfg_.soft_contact_margin + (double)m.shape_margin;
+        const double reach =
+            std::max(std::fabs(base + r_max_ + eps), std::fabs(base + r_min_ + eps)) + std::fabs(eps);
+        const double R = reach * 1.001 + 1e-6 * (1.0 + amax);
+        double ext = 0.0;
+        for (int k = 0; k < 3; k++) ext = std::max(ext, hi[k] - lo[k]);
+        double cell = std::max(R * 0.25, (ext + 2.0 * R) * 1e-4);
+        int dims[3] = {0, 0, 0}, kd = 0;
+        uint64_t cells = 0;
+        for (int attempt = 0; attempt < 8; attempt++) {
+            kd = (int)std::ceil(R / cell) + 1;
+            const double pad = (kd + 2) * cell;
+            cells = 1;
+            for (int k = 0; k < 3; k++) {
+                dims[k] = (int)std::ceil((hi[k] - lo[k] + 2.0 * pad) / cell) + 1;
+                cells *= (uint64_t)dims[k];
+            }
+            if (cells <= kMeshCells) break;
+            cell *= std::cbrt((double)cells / (double)kMeshCells) * 1.01;
+        }
+        const uint64_t w = (uint64_t)((dims[0] + 31) / 32) * (uint64_t)dims[1] * (uint64_t)dims[2];
+        if (kd >= 32 || cells > kMeshCells || words + w > kTotalWords) continue;
+        const double pad = (kd + 2) * cell;
+        org[c] = make_float4((float)(lo[0] - pad), (float)(lo[1] - pad), (float)(lo[2] - pad), (float)(1.0 / cell));
+        dim[c] = make_int4(dims[0], dims[1], dims[2], kd);
+        words += w;
+        off[c + 1] = (uint32_t)words;
+    }
+    if (words == 0) {
+        if (cull_bits_.n) clear_graphs();  // the frame graphs hold the grid pointers
+        cull_bits_.release();
+        cull_tmp_.release();
+        return;
+    }
+    bool moved = false;
+    auto put = [&](auto& dev, const auto& host) {
+        if (dev.n < host.size()) {
+            dev.alloc(host.size(), false);
+            moved = true;
+        }
+        XPBD_CUDA(cudaMemcpy(dev.p, host.data(), host.size() * sizeof(host[0]), cudaMemcpyHostToDevice));
+    };
+    put(cull_org_, org);
+    put(cull_dim_, dim);
+    put(cull_off_, off);
+    if (cull_bits_.n < words) {
+        cull_bits_.alloc(words, false);
+        cull_tmp_.alloc(words, false);
+        moved = true;
+    }
+    if (moved) clear_graphs();
+    launch_cull_build(stream_, (int)nm, node_off_dev_.p, (int64_t)nl_.n, topo_reachable_.p, nl_.p, nu_.p,
+                      cull_org_.p, cull_dim_.p, cull_off_.p, (int64_t)words, cull_bits_.p, cull_tmp_.p);
+    XPBD_CUDA(cudaGetLastError());
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
 MeshTables Solver::mesh_tables() const {
     MeshTables m{};
     m.nl = nl_.p;
@@ -716,6 +833,10 @@ MeshTables Solver::mesh_tables() const {
     m.prim_cnt = prim_cnt_.p;
     m.tri_cache = tri_cache_.p;
     m.pair = node_pair_.p;
+    m.cull_org = cull_org_.p;
+    m.cull_dim = cull_dim_.p;
+    m.cull_off = cull_off_.p;
+    m.cull_bits = cull_bits_.n ? cull_bits_.p : nullptr;
     m.pose = body_q_.p;
     m.posed = dyn_any_ ? posed_.p : nullptr;
     m.walk_list = dyn_any_ ? walk_list_.p : nullptr;
@@ -778,8 +899,8 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     }
     if (mesh_pass) {
         launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
-                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, st);
-        count_kernel();
+                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, near_.p, st);
+        count_kernel(2);  // triage + traversal
         prof_mark(P_CONTACT);
     }
     if (bodies) {
@@ -909,6 +1030,7 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     rollout_valid_ = false;  // the stored rollout no longer ends at the current state
     ensure_substep_capacity(substeps);
     if (n_ == 0) return;
+    ensure_cull();
     if (!sort_tuned_ && n_ >= (1u << 20)) {  // large scenes: pick the sort variant on the real keys
         const int cc = contact_count_;
         autotune_sort(nullptr, nullptr);
@@ -1067,10 +1189,12 @@ void Solver::collide_only() {
     pl.margin = cfg_.soft_contact_margin;
     pl.altitude = cfg_.ground_plane_altitude;
     ensure_substep_capacity(1);
+    ensure_cull();
     XPBD_CUDA(cudaMemsetAsync(ccount_.p, 0, sizeof(uint32_t), stream_));
-    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p + cq_off_, 0, sizeof(uint32_t), stream_));
+    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p + cq_off_, 0, 2 * sizeof(uint32_t), stream_));
     launch_collide(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p, x_[cur_].p, r_.p, flags_.p, pl,
-                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount_.p, sort_scratch_.p + cq_off_, status_.p);
+                   mesh_tables(), slot_cap_, cinfo_.p, cslot_.p, ccount_.p, sort_scratch_.p + cq_off_, near_.p,
+                   status_.p);
     last_collide_src_ = cur_;
     finish_frame(1);
 }
@@ -1357,6 +1481,7 @@ void Solver::update_config(const xpbd_config& c) {
         XPBD_CUDA(cudaMemcpy(shape_mu_.p, smu.data(), smu.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     clear_graphs();  // the frame graphs carry the parameters
+    cull_dirty_ = true;
     rollout_valid_ = false;
 }
 

@@ -180,6 +180,7 @@ class Solver {
     };
     void require_init() const;
     void clear_graphs();
+    void ensure_cull();
     void ensure_substep_capacity(int substeps);
     void record_frame(Mode mode, float dt, int substeps, int iterations, int parity);
     void record_substep(Mode mode, int sub, int iterations, float sdt, int src);
@@ -281,6 +282,15 @@ class Solver {
     DevBuf<uint32_t> tris_, prim_, roots_, prim_off_, prim_cnt_;
     DevBuf<float4> tri_cache_;
     DevBuf<float4> node_pair_;  // MeshTables::pair, 4 per node slot
+    // reach grids (MeshTables::cull_*), rebuilt by ensure_cull when meshes, radii or
+    // the contact margin change
+    DevBuf<float4> cull_org_;
+    DevBuf<int4> cull_dim_;
+    DevBuf<uint32_t> cull_off_, cull_bits_, cull_tmp_, node_off_dev_;
+    DevBuf<uint32_t> near_;  // particles the collision kernel traverses, per substep
+    bool cull_dirty_ = true;
+    float r_min_ = 0.0f, r_max_ = 0.0f;
+    bool r_finite_ = true;
     DevBuf<int> topo_parent_, topo_child_l_, topo_child_r_;
     DevBuf<uint8_t> topo_marked_, topo_reachable_;
     DevBuf<uint32_t> topo_prim_, bvh_scratch_;
