@@ -74,11 +74,11 @@ __global__ void __launch_bounds__(256) k_collide_triage(int64_t n, const uint32_
 // inner nodes before its next leaf: its time is set by its longest particle, not by
 // the sum of its per-leaf maxima. The time of the kernel is that of its longest
 // chains of dependent steps, so fewer particles per warp (more warps sharing the
-// near list, fewer divergent paths per iteration) is faster, up to the resident
-// warps. Each particle's own sequence of node visits and triangle tests is that of
-// the shader, so its contacts are unchanged.
+// near list, fewer divergent paths per iteration) is faster as long as the list
+// fits the resident warps in one round: a warp uses ceil(near / warps) lanes.
+// Each particle's own sequence of node visits and triangle tests is that of the
+// shader, so its contacts are unchanged.
 constexpr int kCollideThreads = 128;
-constexpr int kCollideLanes = 8;
 
 __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const float4* __restrict__ x,
                                                  const float* __restrict__ r, PlaneParams pl, MeshTables mt,
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
     const float eps_md = mt.avg_edge * 1e-3f;
     const float eps2 = eps_md * eps_md;
     int64_t i = -1;
-    bool done = lane >= kCollideLanes, stack_ovf = false, slot_ovf = false;
+    bool stack_ovf = false, slot_ovf = false;
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
     uint32_t info = 0, count = 0;
@@ -101,6 +101,10 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
     // meshes walked here: all of them, or the static ones when some belong to dynamic bodies
     const int nwalk = mt.walk_list ? mt.walk_count : mt.n_meshes;
     const uint64_t n_near = queue[1];  // written by k_collide_triage
+    const uint64_t warps = (uint64_t)gridDim.x * (kCollideThreads / 32);
+    const uint64_t per_warp = (n_near + warps - 1) / warps;
+    const int lanes = per_warp < 1 ? 1 : (per_warp > 32 ? 32 : (int)per_warp);
+    bool done = lane >= lanes;
     MeshWalk<LocalStack> w;
     w.sp = 0;
     w.overflow = false;
@@ -216,7 +220,7 @@ void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const floa
     k_collide_triage<<<(int)((n + 255) / 256), 256, 0, s>>>(n, order, x, r, flags, pl, mt, cinfo, ccount, queue,
                                                              near);
     const int threads = kCollideThreads;
-    const int blocks = (int)std::min<int64_t>((n * (32 / kCollideLanes) + threads - 1) / threads, 152 * 8);
+    const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads, 152 * 8);
     k_collide<<<blocks, threads, 0, s>>>(n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
 }
 
