@@ -208,12 +208,16 @@ int xpbd_record_start(xpbd_solver* s, const char* directory, int first_frame);
 int xpbd_record_stop(xpbd_solver* s, int* frames_written);
 
 /* Sort autotuner (the north star's "autotuned sort parameters"): times every
- * onesweep variant (digit width 8 or 7 bits, 8 to 32 keys per thread) on the
+ * onesweep variant (digit width 8 or 7 bits, 2 to 32 keys per thread) on the
  * scene's current keys and keeps the fastest. Runs by itself on the first step of a
- * solver with 1M particles or more; results never depend on the choice (the sort
- * is stable). best = {bits, keys per thread}; times_us[4] = the four variants. */
+ * solver with XPBD_AUTOTUNE_MIN particles or more; results never depend on the
+ * choice (the sort is stable). best = {bits, keys per thread};
+ * times_us[XPBD_SORT_VARIANTS] = the variants in the order
+ * (8,2) (8,4) (8,8) (8,16) (7,4) (7,8) (7,16) (7,32). */
+#define XPBD_SORT_VARIANTS 8
+#define XPBD_AUTOTUNE_MIN 65536
 int xpbd_autotune(xpbd_solver* s, int best[2], double* times_us);
-/* Fixes the sort variant instead: (bits, keys per thread) = (8, 8), (8, 16), (7, 16) or (7, 32). */
+/* Fixes the sort variant instead: (bits, keys per thread) among the variants above. */
 int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread);
 
 /* New contact / material parameters after init (e.g. between rollouts of an

@@ -95,6 +95,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
+constexpr int kLookWindow = 8;
 
 template <int THREADS>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_scan, uint32_t& total) {
@@ -189,7 +190,11 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
     const uint32_t tile_excl = block_excl_scan<THREADS>(tot, s_scan, dummy);
     const uint32_t glob_excl = block_excl_scan<THREADS>(hist[tid], s_scan, dummy);
 
-    // decoupled look-back for digit `tid`
+    // decoupled look-back for digit `tid`, kLookWindow predecessors per round trip: when
+    // all tiles start together every predecessor holds only its aggregate at first, and
+    // a one-tile-at-a-time walk costs one dependent load per tile. A status word holds
+    // its flag and count together and nothing else a predecessor wrote is read here, so
+    // relaxed loads (all of a window in flight at once) suffice.
     uint32_t* my = lookback + (size_t)tile * BINS + tid;
     uint32_t prev = 0;
     if (tile == 0) {
@@ -198,10 +203,24 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
         st_release(my, kFlagAgg | tot);
         int64_t p = (int64_t)tile - 1;
         uint64_t t0 = 0;
-        while (p >= 0) {
-            const uint32_t sv = ld_acquire(lookback + (size_t)p * BINS + tid);
-            const uint32_t flag = sv & ~kCountMask;
-            if (flag == 0) {
+        bool found = false;
+        while (!found) {
+            uint32_t sv[kLookWindow];
+#pragma unroll
+            for (int j = 0; j < kLookWindow; j++)
+                sv[j] = p - j >= 0 ? ld_relaxed(lookback + (size_t)(p - j) * BINS + tid) : kFlagInc;
+            int used = 0;  // leading published entries consumed, nearest first
+#pragma unroll
+            for (int j = 0; j < kLookWindow; j++) {
+                if (used != j || found) continue;
+                const uint32_t flag = sv[j] & ~kCountMask;
+                if (flag == 0) continue;  // not published yet: resume from here
+                prev += sv[j] & kCountMask;
+                used = j + 1;
+                if (flag == kFlagInc) found = true;
+            }
+            if (found) break;
+            if (used == 0) {
                 const uint64_t now = globaltimer_ns();
                 if (t0 == 0) {
                     t0 = now;
@@ -213,9 +232,7 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
                 __nanosleep(32);
                 continue;
             }
-            prev += sv & kCountMask;
-            if (flag == kFlagInc) break;
-            p--;
+            p -= used;
             t0 = 0;
         }
         st_release(my, kFlagInc | ((prev + tot) & kCountMask));
@@ -284,8 +301,12 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
     if (sp.bits == B && sp.items == I)                                                                     \
         return onesweep_variant<B, I>(s, n, sp, pass, keys_in, vals_in, keys_out, vals_out, hist_pass, \
                                       lookback, tile_counter, st, n_dev);
+    XPBD_OS(8, 2)
+    XPBD_OS(8, 4)
     XPBD_OS(8, 8)
     XPBD_OS(8, 16)
+    XPBD_OS(7, 4)
+    XPBD_OS(7, 8)
     XPBD_OS(7, 16)
     XPBD_OS(7, 32)
 #undef XPBD_OS

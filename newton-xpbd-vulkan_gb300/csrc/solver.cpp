@@ -175,7 +175,7 @@ void Solver::apply_sort_plan(int bits, int items) {
 std::vector<double> Solver::autotune_sort(int* best_bits, int* best_items) {
     require_init();
     sync();
-    static const int kCand[][2] = {{8, 8}, {8, 16}, {7, 16}, {7, 32}};
+    static const int kCand[][2] = {{8, 2}, {8, 4}, {8, 8}, {8, 16}, {7, 4}, {7, 8}, {7, 16}, {7, 32}};
     std::vector<double> us;
     double best = 1e30;
     int bb = plan_.bits, bi = plan_.items;
@@ -229,8 +229,10 @@ std::vector<double> Solver::autotune_sort(int* best_bits, int* best_items) {
 void Solver::set_sort_variant(int bits, int items) {
     require_init();
     sync();
-    if (!((bits == 8 && (items == 8 || items == 16)) || (bits == 7 && (items == 16 || items == 32))))
-        throw std::runtime_error("set_sort_variant: (8, 8), (8, 16), (7, 16) or (7, 32)");
+    if (!((bits == 8 && (items == 2 || items == 4 || items == 8 || items == 16)) ||
+          (bits == 7 && (items == 4 || items == 8 || items == 16 || items == 32))))
+        throw std::runtime_error("set_sort_variant: bits 8 with 2, 4, 8 or 16 keys per thread, or bits 7 with 4, 8, "
+                                 "16 or 32");
     apply_sort_plan(bits, items);
     sort_tuned_ = true;  // an explicit choice is kept
 }

@@ -197,11 +197,11 @@ class XpbdSolver:
     def autotune(self):
         """Pick the fastest sort variant on the current keys (xpbd_autotune)."""
         best = (C.c_int * 2)()
-        t = (C.c_double * 4)()
+        names = ["8b x2", "8b x4", "8b x8", "8b x16", "7b x4", "7b x8", "7b x16", "7b x32"]
+        t = (C.c_double * len(names))()
         _check(_lib.xpbd_autotune(self._h, best, t))
-        names = ["8b x8", "8b x16", "7b x16", "7b x32"]
         return {"bits": int(best[0]), "keys_per_thread": int(best[1]),
-                "sort_us": {names[k]: float(t[k]) for k in range(4)}}
+                "sort_us": {names[k]: float(t[k]) for k in range(len(names))}}
 
     def set_sort_variant(self, bits, keys_per_thread):
         _check(_lib.xpbd_set_sort_variant(self._h, int(bits), int(keys_per_thread)))
