@@ -16,7 +16,7 @@
 namespace xpbd {
 
 constexpr int kSolveThreads = 128;
-constexpr int kPairCap = 16;  // accepted neighbours buffered per thread before the pair math runs
+constexpr int kPairCap = 12;  // accepted neighbours buffered per thread before the pair math runs
 
 // Pair math of solve_particle_particle_contacts.comp:159-207 for the neighbours
 // buffered in shared memory (slot kk, distance d), accumulated in buffer order.

@@ -144,7 +144,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     status_.alloc(1);
     diag_header_.alloc(2);
     xyz_stage_.alloc(std::max<size_t>(n_, 1) * 3);
-    pinned_words_ = std::max<size_t>(n_ * 4, 64);
+    pinned_words_ = 64;  // the per-frame readback (contact count, status)
     XPBD_CUDA(cudaMallocHost(&pinned_, pinned_words_ * sizeof(float)));
     if (cfg_.enable_diagnostics) {
         delta_.alloc(std::max<size_t>(n_, 1) * 3);
@@ -389,21 +389,14 @@ void Solver::set_particles(const float* q, const float* qd, const float* inv_mas
     sync();
     rollout_valid_ = false;
     if (n == 0) return;
-    std::memcpy(pinned_, q, n * 3 * sizeof(float));
-    XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
-    launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, x_[cur_].p);
-    XPBD_CUDA(cudaStreamSynchronize(stream_));
-    if (qd) {
-        std::memcpy(pinned_, qd, n * 3 * sizeof(float));
-        XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
-        launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, v_[cur_].p);
-    } else {
+    upload_xyz(q, x_[cur_].p, n);
+    if (qd)
+        upload_xyz(qd, v_[cur_].p, n);
+    else
         XPBD_CUDA(cudaMemsetAsync(v_[cur_].p, 0, n * sizeof(float4), stream_));
-    }
     XPBD_CUDA(cudaStreamSynchronize(stream_));
     auto up = [&](void* dst, const void* src) {
-        std::memcpy(pinned_, src, n * 4);
-        XPBD_CUDA(cudaMemcpyAsync(dst, pinned_, n * 4, cudaMemcpyHostToDevice, stream_));
+        XPBD_CUDA(cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyHostToDevice, stream_));
         XPBD_CUDA(cudaStreamSynchronize(stream_));
     };
     if (inv_mass) up(w_.p, inv_mass);
@@ -1244,16 +1237,28 @@ void Solver::set_contact_data(const int32_t* part, const int32_t* shape, const f
     injected_ = true;
 }
 
+// Host xyz arrays <-> device float4 state: one copy straight from or to the caller's
+// (pageable) memory plus a pack / unpack kernel; on Grace the driver moves pageable
+// memory over NVLink-C2C directly, several times faster than staging it through a
+// pinned buffer with a host memcpy.
+void Solver::upload_xyz(const float* h, float4* d, size_t n) {
+    XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, h, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
+    launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, d);
+}
+
+void Solver::download_xyz(const float4* d, float* h, size_t n) {
+    launch_unpack_xyz(stream_, (int64_t)n, d, xyz_stage_.p);
+    XPBD_CUDA(cudaMemcpyAsync(h, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void Solver::get_positions(float* out, size_t n) {
     if (!initialized_) return;
     n = std::min(n, n_);
     if (n == 0) return;
     XPBD_CUDA(cudaSetDevice(device_));
     sync();
-    launch_unpack_xyz(stream_, (int64_t)n, x_[cur_].p, xyz_stage_.p);
-    XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
-    XPBD_CUDA(cudaStreamSynchronize(stream_));
-    std::memcpy(out, pinned_, n * 3 * sizeof(float));
+    download_xyz(x_[cur_].p, out, n);
 }
 
 void Solver::get_velocities(float* out, size_t n) {
@@ -1262,10 +1267,7 @@ void Solver::get_velocities(float* out, size_t n) {
     if (n == 0) return;
     XPBD_CUDA(cudaSetDevice(device_));
     sync();
-    launch_unpack_xyz(stream_, (int64_t)n, v_[cur_].p, xyz_stage_.p);
-    XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
-    XPBD_CUDA(cudaStreamSynchronize(stream_));
-    std::memcpy(out, pinned_, n * 3 * sizeof(float));
+    download_xyz(v_[cur_].p, out, n);
 }
 
 void Solver::compact_contacts() {
@@ -1574,9 +1576,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     // upstream gradients (host xyz -> device float4)
     auto upload = [&](const float* h, float4* d) {
         if (h) {
-            std::memcpy(pinned_, h, n * 3 * sizeof(float));
-            XPBD_CUDA(cudaMemcpyAsync(xyz_stage_.p, pinned_, n * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
-            launch_pack_xyz(stream_, (int64_t)n, xyz_stage_.p, d);
+            upload_xyz(h, d, n);
             XPBD_CUDA(cudaStreamSynchronize(stream_));
         } else {
             XPBD_CUDA(cudaMemsetAsync(d, 0, n * sizeof(float4), stream_));
@@ -1660,10 +1660,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     XPBD_CUDA(cudaStreamSynchronize(stream_));
     auto download = [&](const float4* d, float* h) {
         if (!h) return;
-        launch_unpack_xyz(stream_, (int64_t)n, d, xyz_stage_.p);
-        XPBD_CUDA(cudaMemcpyAsync(pinned_, xyz_stage_.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, stream_));
-        XPBD_CUDA(cudaStreamSynchronize(stream_));
-        std::memcpy(h, pinned_, n * 3 * sizeof(float));
+        download_xyz(d, h, n);
     };
     download(gx_.p, gx0);
     download(gv_.p, gv0);

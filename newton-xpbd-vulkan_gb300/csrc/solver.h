@@ -181,6 +181,8 @@ class Solver {
     void require_init() const;
     void clear_graphs();
     void ensure_cull();
+    void upload_xyz(const float* h, float4* d, size_t n);
+    void download_xyz(const float4* d, float* h, size_t n);
     void ensure_substep_capacity(int substeps);
     void record_frame(Mode mode, float dt, int substeps, int iterations, int parity);
     void record_substep(Mode mode, int sub, int iterations, float sdt, int src);
@@ -317,7 +319,7 @@ class Solver {
     DeviceStatus host_status_{};
     // staging
     DevBuf<float> xyz_stage_;
-    float* pinned_ = nullptr;  // max(4n, ...) floats
+    float* pinned_ = nullptr;  // 64 words: the per-frame readback
     size_t pinned_words_ = 0;
     DevBuf<int32_t> c_part_, c_shape_;
     DevBuf<float> c_bpos_, c_bvel_, c_nrm_;
