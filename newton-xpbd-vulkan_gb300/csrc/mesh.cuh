@@ -34,9 +34,17 @@ __device__ __forceinline__ bool mesh_far(const MeshTables& mt, int ci, v3 p) {
     return ((__ldg(&mt.cull_bits[word]) >> (ix & 31)) & 1u) == 0u;
 }
 
-// generate_mesh_contacts.comp:77-113
-static __device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
+// generate_mesh_contacts.comp:77-113, split into the part that depends on the ray
+// only (axis order and shear constants, computed once per ray) and the per-triangle
+// test; the operations and their order are the shader's.
+struct WoopRay {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ WoopRay woop_setup(v3 dir) {
     const v3 adir = mk3(fabsf(dir.x), fabsf(dir.y), fabsf(dir.z));
+    WoopRay r;
     int kz = 0;
     if (adir.y > adir.x) kz = 1;
     if (adir.z > (kz == 1 ? adir.y : adir.x)) kz = 2;
@@ -49,20 +57,27 @@ static __device__ bool intersect_ray_tri_woop(v3 p, v3 dir, v3 a, v3 b, v3 c) {
         kx = ky;
         ky = t;
     }
-    const float Sx = __fdiv_rn(comp(dir, kx), comp(dir, kz));
-    const float Sy = __fdiv_rn(comp(dir, ky), comp(dir, kz));
-    const float Sz = __fdiv_rn(1.0f, comp(dir, kz));
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = __fdiv_rn(comp(dir, kx), comp(dir, kz));
+    r.Sy = __fdiv_rn(comp(dir, ky), comp(dir, kz));
+    r.Sz = __fdiv_rn(1.0f, comp(dir, kz));
+    return r;
+}
+
+__device__ __forceinline__ bool woop_hit(const WoopRay& r, v3 p, v3 a, v3 b, v3 c) {
     const v3 A = vsub(a, p), B = vsub(b, p), C = vsub(c, p);
-    const float Ax = comp(A, kx) - Sx * comp(A, kz), Ay = comp(A, ky) - Sy * comp(A, kz);
-    const float Bx = comp(B, kx) - Sx * comp(B, kz), By = comp(B, ky) - Sy * comp(B, kz);
-    const float Cx = comp(C, kx) - Sx * comp(C, kz), Cy = comp(C, ky) - Sy * comp(C, kz);
+    const float Ax = comp(A, r.kx) - r.Sx * comp(A, r.kz), Ay = comp(A, r.ky) - r.Sy * comp(A, r.kz);
+    const float Bx = comp(B, r.kx) - r.Sx * comp(B, r.kz), By = comp(B, r.ky) - r.Sy * comp(B, r.kz);
+    const float Cx = comp(C, r.kx) - r.Sx * comp(C, r.kz), Cy = comp(C, r.ky) - r.Sy * comp(C, r.kz);
     const float U = diff_product(Cx, By, Cy, Bx);
     const float V = diff_product(Ax, Cy, Ay, Cx);
     const float W = diff_product(Bx, Ay, By, Ax);
     if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
     const float det = U + V + W;
     if (det == 0.0f) return false;
-    const float Az = Sz * comp(A, kz), Bz = Sz * comp(B, kz), Cz = Sz * comp(C, kz);
+    const float Az = r.Sz * comp(A, r.kz), Bz = r.Sz * comp(B, r.kz), Cz = r.Sz * comp(C, r.kz);
     const float T = U * Az + V * Bz + W * Cz;
     if ((T < 0.0f && det > 0.0f) || (T > 0.0f && det < 0.0f)) return false;
     return true;
@@ -367,12 +382,12 @@ __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, 
     shape_v = vfma_vs(vel2, w_eval, vfma_vs(vel0, u_mesh, vmuls(vel1, v_mesh)));
     float sign;
     if (w.wt) {
-        const v3 ray_dir = mk3(1.029700994f, 1.086472273f, 1.034694910f);
+        const WoopRay ray = woop_setup(mk3(1.029700994f, 1.086472273f, 1.034694910f));
         uint32_t hits = 0;
         const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
         for (uint32_t ti = (uint32_t)sub; ti < pn; ti += (uint32_t)nsub) {
             const float4* q = mt.tri_cache + (size_t)(po + ti) * 4;
-            if (intersect_ray_tri_woop(p, ray_dir, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
+            if (woop_hit(ray, p, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
         }
         for (int o = 1; o < nsub; o <<= 1) hits += __shfl_xor_sync(gmask, hits, o);
         sign = (hits & 1u) ? -1.0f : 1.0f;
