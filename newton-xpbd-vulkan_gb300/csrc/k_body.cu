@@ -229,58 +229,87 @@ __device__ __forceinline__ uint32_t box_cell_hash(int ix, int iy, int iz, int si
 }
 __device__ __forceinline__ int cell_of(float v, float cs) { return f2i(floorf(v / cs)); }
 
-// each dynamic body's widened world box counts itself into the buckets of the cells it covers
-__global__ void k_boxgrid_count(RigidTables rt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rt.n_dyn) return;
+// cell (x, y, z) of the widened world box of dynamic body i that thread slot c (0 ..
+// kBoxCells - 1, 4 x 4 x 4 cells from the box's lowest cell) stands for; false past
+// the box's own cell range
+__device__ __forceinline__ bool box_cell(const RigidTables& rt, int i, int c, int& x, int& y, int& z) {
     const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
     const float e = rt.grid_reach + l.w;
-    for (int z = cell_of(l.z - e, rt.grid_cs); z <= cell_of(h.z + e, rt.grid_cs); z++)
-        for (int y = cell_of(l.y - e, rt.grid_cs); y <= cell_of(h.y + e, rt.grid_cs); y++)
-            for (int x = cell_of(l.x - e, rt.grid_cs); x <= cell_of(h.x + e, rt.grid_cs); x++)
-                atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.grid_size)], 1u);
+    x = cell_of(l.x - e, rt.grid_cs) + (c & 3);
+    y = cell_of(l.y - e, rt.grid_cs) + ((c >> 2) & 3);
+    z = cell_of(l.z - e, rt.grid_cs) + (c >> 4);
+    return x <= cell_of(h.x + e, rt.grid_cs) && y <= cell_of(h.y + e, rt.grid_cs) && z <= cell_of(h.z + e, rt.grid_cs);
 }
 
-// exclusive scan of the bucket counts (one block); the counts become fill cursors
+// each dynamic body's widened world box counts itself into the buckets of the cells it
+// covers, one thread per (body, cell)
+__global__ void k_boxgrid_count(RigidTables rt, DeviceStatus* st) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= rt.n_dyn * kBoxCells) return;
+    const int i = g / kBoxCells, c = g % kBoxCells;
+    int x, y, z;
+    if (box_cell(rt, i, c, x, y, z)) atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.grid_size)], 1u);
+    if (c == kBoxCells - 1) {  // a box wider than 4 cells per axis would lose cells: report it
+        const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
+        const float e = rt.grid_reach + l.w;
+        if (cell_of(h.x + e, rt.grid_cs) - cell_of(l.x - e, rt.grid_cs) > 3 ||
+            cell_of(h.y + e, rt.grid_cs) - cell_of(l.y - e, rt.grid_cs) > 3 ||
+            cell_of(h.z + e, rt.grid_cs) - cell_of(l.z - e, rt.grid_cs) > 3)
+            atomicOr(&st->error_bits, kErrBodyOverflow);
+    }
+}
+
+// exclusive scan of the bucket counts (one block, tiles of 4 counts per thread read
+// as one coalesced uint4); the counts become fill cursors
 __global__ void __launch_bounds__(1024) k_boxgrid_scan(RigidTables rt) {
-    __shared__ uint32_t s_sum[1024];
-    const int per = (rt.grid_size + 1023) / 1024;
-    const int b0 = threadIdx.x * per;
-    uint32_t t = 0;
-    for (int k = 0; k < per; k++)
-        if (b0 + k < rt.grid_size) t += rt.grid_count[b0 + k];
-    s_sum[threadIdx.x] = t;
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_carry = 0;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t v = threadIdx.x >= o ? s_sum[threadIdx.x - o] : 0u;
-        __syncthreads();
-        s_sum[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = s_sum[threadIdx.x] - t;
-    for (int k = 0; k < per; k++) {
-        const int b = b0 + k;
-        if (b < rt.grid_size) {
-            rt.grid_start[b] = run;
-            run += rt.grid_count[b];
-            rt.grid_count[b] = 0;
+    for (int base = 0; base < rt.grid_size; base += 4096) {  // grid_size is a power of two >= 64
+        const int b = base + tid * 4;
+        uint4 c = make_uint4(0u, 0u, 0u, 0u);
+        if (b < rt.grid_size) c = *reinterpret_cast<const uint4*>(rt.grid_count + b);
+        const uint32_t own = c.x + c.y + c.z + c.w;
+        uint32_t incl = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
         }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = s_warp[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            s_warp[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        const uint32_t start = carry + (warp ? s_warp[warp - 1] : 0u) + incl - own;
+        if (b < rt.grid_size) {
+            *reinterpret_cast<uint4*>(rt.grid_start + b) =
+                make_uint4(start, start + c.x, start + c.x + c.y, start + c.x + c.y + c.z);
+            *reinterpret_cast<uint4*>(rt.grid_count + b) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
+        if (tid == 0) s_carry = carry + s_warp[31];
+        __syncthreads();
     }
-    if (threadIdx.x == 1023) rt.grid_start[rt.grid_size] = s_sum[1023];
+    if (tid == 0) rt.grid_start[rt.grid_size] = s_carry;
 }
 
 __global__ void k_boxgrid_fill(RigidTables rt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rt.n_dyn) return;
-    const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
-    const float e = rt.grid_reach + l.w;
-    for (int z = cell_of(l.z - e, rt.grid_cs); z <= cell_of(h.z + e, rt.grid_cs); z++)
-        for (int y = cell_of(l.y - e, rt.grid_cs); y <= cell_of(h.y + e, rt.grid_cs); y++)
-            for (int x = cell_of(l.x - e, rt.grid_cs); x <= cell_of(h.x + e, rt.grid_cs); x++) {
-                const uint32_t b = box_cell_hash(x, y, z, rt.grid_size);
-                const uint32_t at = rt.grid_start[b] + atomicAdd(&rt.grid_count[b], 1u);
-                if (at < (uint32_t)rt.n_dyn * 8u) rt.grid_list[at] = (uint32_t)i;  // 8 cells per box at most
-            }
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= rt.n_dyn * kBoxCells) return;
+    const int i = g / kBoxCells, c = g % kBoxCells;
+    int x, y, z;
+    if (!box_cell(rt, i, c, x, y, z)) return;
+    const uint32_t b = box_cell_hash(x, y, z, rt.grid_size);
+    rt.grid_list[rt.grid_start[b] + atomicAdd(&rt.grid_count[b], 1u)] = make_int4(i, x, y, z);
 }
 
 void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
@@ -289,9 +318,10 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
     k_body_bounds<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(ba, rt, mt);
     k_body_pairs<<<(rt.n_dyn * 32 + 127) / 128, 128, 0, s>>>(rt, rp, st);
     cudaMemsetAsync(rt.grid_count, 0, sizeof(uint32_t) * (size_t)rt.grid_size, s);
-    k_boxgrid_count<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(rt);
+    const int cells = (rt.n_dyn * kBoxCells + 127) / 128;
+    k_boxgrid_count<<<cells, 128, 0, s>>>(rt, st);
     k_boxgrid_scan<<<1, 1024, 0, s>>>(rt);
-    k_boxgrid_fill<<<(rt.n_dyn + 127) / 128, 128, 0, s>>>(rt);
+    k_boxgrid_fill<<<cells, 128, 0, s>>>(rt);
 }
 
 // ---------------------------------------------------------------- rigid contacts ----
@@ -433,65 +463,110 @@ void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTa
 // of the box grid whose widened world box holds the particle are queried in their body
 // frame (generate_mesh_contacts.comp with the pose inverted); each contact is inserted
 // into the particle's slots at its mesh's place, so the list order does not matter.
-__global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t* __restrict__ order,
+// Boxes of the box grid that a particle at p (radius r) may touch, in bucket order:
+// f(ci, mesh, q, rot) for each dynamic body ci whose widened world box holds p and whose
+// root box (body frame, q = p in that frame) is within the traversal's first bound.
+template <class F>
+__device__ __forceinline__ void posed_candidates(const MeshTables& mt, const RigidTables& rt, v3 p, float radius,
+                                                 F&& f) {
+    const int cx = cell_of(p.x, rt.grid_cs), cy = cell_of(p.y, rt.grid_cs), cz = cell_of(p.z, rt.grid_cs);
+    const uint32_t b = box_cell_hash(cx, cy, cz, rt.grid_size);
+    const uint32_t k0 = rt.grid_start[b], k1 = rt.grid_start[b + 1];
+    for (uint32_t k = k0; k < k1; k++) {
+        const int4 en = __ldg(&rt.grid_list[k]);
+        if (en.y != cx || en.z != cy || en.w != cz) continue;  // another cell of this bucket
+        const int ci = en.x;
+        const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
+        const float e = (mt.soft_margin + l.w) + radius + rt.pad;
+        if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
+              p.z <= h.z + e))
+            continue;
+        const int mesh = rt.dyn[ci];
+        const v3 pos_m = xyz(mt.pose[mesh * 2]);
+        const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+        const v3 q = quat_rotate_inv(rot_m, vsub(p, pos_m));
+        {  // the traversal's first test (root box in the body frame) without starting a traversal
+            const uint32_t root = __ldg(&mt.roots[mesh]);
+            const float md = mt.soft_margin + l.w + radius;  // walk_begin's max_dist
+            if (dist_sq_aabb(q, xyz(__ldg(&mt.nl[root])), xyz(__ldg(&mt.nu[root]))) > md * md) continue;
+        }
+        if (!f(mesh, q, rot_m)) return;
+    }
+}
+
+// Triage (one thread per particle, in the previous substep's grid order): particles with
+// at least one candidate moving mesh go to the posed list, in grid order within a warp.
+__global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t* __restrict__ order,
                                                       const float4* __restrict__ x, const float* __restrict__ r,
                                                       const int* __restrict__ flags, MeshTables mt, RigidTables rt,
-                                                      int slot_cap, uint32_t* __restrict__ cinfo,
-                                                      float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+                                                      uint32_t* counter, uint32_t* list) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool any = false;
+    int64_t i = -1;
+    if (t < n) {
+        i = order ? (int64_t)order[t] : t;
+        if (flags[i] & 1)
+            posed_candidates(mt, rt, xyz(x[i]), r[i], [&](int, v3, q4) {
+                any = true;
+                return false;
+            });
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, any);
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (any) list[base + __popc(m & lanemask_lt())] = (uint32_t)i;
+    }
+}
+
+// Particles against the moving meshes (generate_mesh_contacts.comp:197-411 in each body's
+// frame) for the posed list: one thread per listed particle queries its candidate meshes
+// and inserts each contact into its slots in mesh order (the shader's mesh loop order).
+__global__ void __launch_bounds__(128) k_collide_posed(const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ counter,
+                                                      const float4* __restrict__ x, const float* __restrict__ r,
+                                                      MeshTables mt, RigidTables rt, int slot_cap,
+                                                      uint32_t* __restrict__ cinfo, float4* __restrict__ cslot,
+                                                      uint32_t* ccount, DeviceStatus* st) {
     __shared__ uint32_t s_warp[4];
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t entry = t < (int64_t)*counter ? t : -1;
     int used0 = 0, used = 0;
     bool slot_ovf = false, stack_ovf = false;
-    if (t < n) {
-        const int64_t i = order ? (int64_t)order[t] : t;
-        if (flags[i] & 1) {
-            const v3 p = xyz(x[i]);
-            const float radius = r[i];
-            const uint32_t info = cinfo[i];
-            used0 = used = info_slots(info);
-            const uint32_t b = box_cell_hash(cell_of(p.x, rt.grid_cs), cell_of(p.y, rt.grid_cs),
-                                             cell_of(p.z, rt.grid_cs), rt.grid_size);
-            const uint32_t k0 = rt.grid_start[b], k1 = rt.grid_start[b + 1];
-            for (uint32_t k = k0; k < k1; k++) {
-                const int ci = (int)rt.grid_list[k];
-                const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
-                const float e = (mt.soft_margin + l.w) + radius + rt.pad;
-                if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
-                      p.z <= h.z + e))
-                    continue;
-                const int mesh = rt.dyn[ci];
-                const v3 pos_m = xyz(mt.pose[mesh * 2]);
-                const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
-                const v3 q = quat_rotate_inv(rot_m, vsub(p, pos_m));
-                {  // the traversal's first test (root box in the body frame) without starting a traversal
-                    const uint32_t root = __ldg(&mt.roots[mesh]);
-                    const float md = mt.soft_margin + l.w + radius;  // walk_begin's max_dist
-                    if (dist_sq_aabb(q, xyz(__ldg(&mt.nl[root])), xyz(__ldg(&mt.nu[root]))) > md * md) continue;
-                }
-                v3 bp, bv, nn;
-                if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) continue;
-                const v3 nw = quat_rotate(rot_m, nn);
-                if (used >= slot_cap) {
-                    slot_ovf = true;
-                    continue;
-                }
-                float4* base = cslot + (size_t)i * slot_cap * 3;
-                int pos = used;
-                while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
-                for (int k2 = used; k2 > pos; k2--) {
-                    base[k2 * 3] = base[(k2 - 1) * 3];
-                    base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
-                    base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
-                }
-                base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
-                base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
-                base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
-                used++;
+    if (entry >= 0) {
+        const int64_t i = (int64_t)list[entry];
+        const v3 p = xyz(x[i]);
+        const float radius = r[i];
+        const uint32_t info = cinfo[i];
+        used0 = used = info_slots(info);
+        float4* base = cslot + (size_t)i * slot_cap * 3;
+        posed_candidates(mt, rt, p, radius, [&](int mesh, v3 q, q4 rot_m) {
+            v3 bp, bv, nn;
+            if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) return true;
+            const v3 nw = quat_rotate(rot_m, nn);
+            if (used >= slot_cap) {
+                slot_ovf = true;
+                return true;
             }
-            // every slot added here belongs to a dynamic body
-            if (used != used0)
-                cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
-        }
+            int pos = used;
+            while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
+            for (int k2 = used; k2 > pos; k2--) {
+                base[k2 * 3] = base[(k2 - 1) * 3];
+                base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
+                base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
+            }
+            base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
+            base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
+            base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+            used++;
+            return true;
+        });
+        // every slot added here belongs to a dynamic body
+        if (used != used0)
+            cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
     }
     if (slot_ovf) {
         atomicOr(&st->error_bits, kErrSlotOverflow);
@@ -507,10 +582,11 @@ __global__ void __launch_bounds__(128) k_collide_posed(int64_t n, const uint32_t
 
 void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                           const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
-                          float4* cslot, uint32_t* ccount, DeviceStatus* st) {
+                          float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st) {
     if (n <= 0 || rt.n_dyn <= 0) return;
     const int blocks = (int)((n + 127) / 128);
-    k_collide_posed<<<blocks, 128, 0, s>>>(n, order, x, r, flags, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+    k_posed_triage<<<blocks, 128, 0, s>>>(n, order, x, r, flags, mt, rt, counter, list);
+    k_collide_posed<<<blocks, 128, 0, s>>>(list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
 }
 
 // ---------------------------------------------------------------- body-delta entries ----

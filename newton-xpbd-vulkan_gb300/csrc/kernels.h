@@ -253,15 +253,18 @@ struct RigidTables {
     int* rc_count;
     float pad;                    // conservative widening of the world boxes
     int n_vert;                   // dv_start[nb]
-    // coarse hashed grid of the dynamic bodies' world boxes (widened by grid_reach) for the
-    // particle queries: cell size grid_cs >= any widened box, so a box covers <= 8 cells;
-    // bucket h lists its bodies (dyn indices, any order) in grid_list[grid_start[h] ..)
+    // hashed grid of the dynamic bodies' world boxes (widened by grid_reach) for the particle
+    // queries: cell size grid_cs >= a third of any widened box, so a box covers at most
+    // kBoxCells cells; bucket h lists (dyn index, cell x, y, z) entries, any order, in
+    // grid_list[grid_start[h] ..); a particle takes only the entries of its own cell
+    // (hash collisions never list a body twice for one cell)
     int grid_size;                // buckets (power of two)
     float grid_cs, grid_reach;
     uint32_t* grid_count;         // [grid_size]
     uint32_t* grid_start;         // [grid_size + 1]
-    uint32_t* grid_list;          // [8 * n_dyn]
+    int4* grid_list;              // [kBoxCells * n_dyn]
 };
+constexpr int kBoxCells = 64;
 // integrate_bodies.comp for every body; saves the pre-integration state to q_prev
 void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp);
 // world boxes of the dynamic bodies and their overlapping pairs
@@ -269,10 +272,11 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
 // rigid contacts of every dynamic-body vertex against the plane and the other meshes
 void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                            DeviceStatus* st);
-// particle contacts against the meshes of dynamic bodies, merged into the slots in mesh order
+// particle contacts against the meshes of dynamic bodies, merged into the slots in mesh order;
+// counter: one zeroed word, list: n words of scratch
 void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                           const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
-                          float4* cslot, uint32_t* ccount, DeviceStatus* st);
+                          float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st);
 // body-delta entries: key = body of each dynamic slot at position rank[i].x + j, digit histograms
 void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank,
                      uint32_t cap, const SortPlan& sp, uint32_t* keys, uint32_t* hist, DeviceStatus* st);

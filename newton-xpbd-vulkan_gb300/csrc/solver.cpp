@@ -161,8 +161,8 @@ void Solver::apply_sort_plan(int bits, int items) {
     hist_off_ = 0;
     lb_off_ = (size_t)plan_.passes << plan_.bits;
     tc_off_ = lb_off_ + (size_t)plan_.passes * sort_lookback_words(plan_);
-    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work-queue counter, near-list length
-    sort_scratch_.alloc(cq_off_ + 2);
+    cq_off_ = tc_off_ + (size_t)plan_.passes;  // collision work counter, near-list and posed-list lengths
+    sort_scratch_.alloc(cq_off_ + 3);
     // the final sort buffer doubles as the collision pass's thread -> particle order (any
     // permutation gives the same contacts)
     launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
@@ -413,7 +413,10 @@ void Solver::set_particles(const float* q, const float* qd, const float* inv_mas
             hi = first ? radii[i] : std::max(hi, radii[i]);
             first = false;
         }
-        if (lo != r_min_ || hi != r_max_ || fin != r_finite_) cull_dirty_ = true;
+        if (lo != r_min_ || hi != r_max_ || fin != r_finite_) {
+            cull_dirty_ = true;
+            if (hi != r_max_) clear_graphs();  // the frame graphs carry the box grid's reach
+        }
         r_min_ = lo;
         r_max_ = hi;
         r_finite_ = fin;
@@ -532,10 +535,11 @@ RigidTables Solver::rigid_tables() const {
     t.pad = 1e-3f;
     t.n_vert = n_dyn_verts_;
     // box grid: a particle's side of the widening (soft margin + radius + pad, radii bounded
-    // by particle_max_radius as for the neighbour search); cells larger than any widened box
+    // by the larger of particle_max_radius and the largest finite radius set); cells a
+    // third of the largest widened box, so a box covers at most 4 cells per axis
     t.grid_size = grid_size_;
-    t.grid_reach = cfg_.soft_contact_margin + cfg_.particle_max_radius + 2.0f * t.pad;
-    t.grid_cs = (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f + 1e-4f;
+    t.grid_reach = cfg_.soft_contact_margin + std::max(cfg_.particle_max_radius, r_max_) + 2.0f * t.pad;
+    t.grid_cs = (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f / 3.0f + 1e-4f;
     t.grid_count = grid_count_.p;
     t.grid_start = grid_start_.p;
     t.grid_list = grid_list_.p;
@@ -659,7 +663,8 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     while ((size_t)grid_size_ < 16 * dyn_list_.size()) grid_size_ *= 2;
     grid_count_.alloc((size_t)grid_size_, true);
     grid_start_.alloc((size_t)grid_size_ + 1, true);
-    grid_list_.alloc(std::max<size_t>(dyn_list_.size() * 8, 1), true);
+    grid_list_.alloc(std::max<size_t>(dyn_list_.size() * kBoxCells, 1), true);
+    posed_list_.alloc(std::max<size_t>(n_, 1), false);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);
     up(posed_, posed);
@@ -900,8 +905,9 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     }
     if (bodies) {
         launch_collide_posed(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p,
-                             mesh_tables(), rt, slot_cap_, cinfo_.p, cslot_.p, ccount, st);
-        count_kernel();
+                             mesh_tables(), rt, slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_ + 2,
+                             posed_list_.p, st);
+        count_kernel(2);  // triage + queries
         prof_mark(P_POSED);
         launch_rigid_contacts(stream_, ba, rt, mesh_tables(), rp, st);
         count_kernel();

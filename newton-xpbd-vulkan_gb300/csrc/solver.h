@@ -268,7 +268,9 @@ class Solver {
     DevBuf<int> dyn_, dyn_index_, posed_, walk_list_, partners_, partner_count_, rc_count_;
     int walk_count_ = 0, n_dyn_verts_ = 0, grid_size_ = 0;
     float dyn_half_diag_ = 0.0f, dyn_max_margin_ = 0.0f;
-    DevBuf<uint32_t> grid_count_, grid_start_, grid_list_;
+    DevBuf<uint32_t> grid_count_, grid_start_;
+    DevBuf<int4> grid_list_;
+    DevBuf<uint32_t> posed_list_;  // particles with candidate moving meshes, per substep
     DevBuf<uint32_t> dv_start_;
     DevBuf<float4> dv_local_, wbox_, rc_;
     uint32_t entry_cap_ = 0;
