@@ -58,3 +58,22 @@ def test_mixed_small_bitexact():
 def test_particle_weighting_off_bitexact():
     sc = box_scene(n_side=8, positions=((0.035, 0.035, 0.12),))
     _run(sc, 10, body_params=dict(particle_contact_con_weighting=0, rigid_contact_con_weighting=0))
+
+
+def test_box_shell_grid_collisions_bitexact():
+    """Particles in a shell around one large box (radii up to 0.012 above particle_max_radius).
+    With one dynamic body the box grid has 64 buckets for up to 64 cells, so the box's own
+    cells collide in the hash; each particle must still take the box exactly once, and the
+    grid's reach must cover the largest radius set."""
+    sc = box_scene(n_side=2, boxes=((0.08, 0.06, 0.05),), positions=((0.0, 0.0, 0.3),))
+    rng = np.random.default_rng(9)
+    n = 2500
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pos = np.array([0.0, 0.0, 0.3]) + d * rng.uniform(0.05, 0.13, (n, 1))
+    sc.positions = pos.astype(np.float32)
+    sc.velocities = np.zeros_like(sc.positions)
+    sc.inv_mass = np.full(n, 1000.0, np.float32)
+    sc.radii = rng.uniform(0.003, 0.012, n).astype(np.float32)
+    sc.flags = np.ones(n, np.int32)
+    _run(sc, 3, substeps=4)
