@@ -523,47 +523,120 @@ __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t*
 }
 
 // Particles against the moving meshes (generate_mesh_contacts.comp:197-411 in each body's
-// frame) for the posed list: one thread per listed particle queries its candidate meshes
-// and inserts each contact into its slots in mesh order (the shader's mesh loop order).
-__global__ void __launch_bounds__(128) k_collide_posed(const uint32_t* __restrict__ list,
-                                                      const uint32_t* __restrict__ counter,
-                                                      const float4* __restrict__ x, const float* __restrict__ r,
-                                                      MeshTables mt, RigidTables rt, int slot_cap,
-                                                      uint32_t* __restrict__ cinfo, float4* __restrict__ cslot,
-                                                      uint32_t* ccount, DeviceStatus* st) {
-    __shared__ uint32_t s_warp[4];
+// frame) for the posed list, one warp per 32 listed particles. Each lane lists its
+// particle's first kPosedCand candidate meshes in shared memory; the warp then runs all
+// (particle, mesh) queries of those lists one per lane, so lanes with one candidate do not
+// wait for lanes with three; finally each lane inserts its particle's contacts into its
+// slots in mesh order (the shader's mesh loop order; candidates past kPosedCand are
+// queried by their own lane afterwards, in candidate order).
+constexpr int kPosedCand = 3;
+constexpr int kPosedWarps = 4;
+
+struct PosedHit {
+    float4 a, b, c;  // (body_pos, found), (normal, 0), (body_vel, 0)
+};
+
+__device__ __forceinline__ void posed_insert(float4* base, int& used, int slot_cap, bool& slot_ovf, int mesh,
+                                             v3 bp, v3 nw, v3 bv) {
+    if (used >= slot_cap) {
+        slot_ovf = true;
+        return;
+    }
+    int pos = used;
+    while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
+    for (int k2 = used; k2 > pos; k2--) {
+        base[k2 * 3] = base[(k2 - 1) * 3];
+        base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
+        base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
+    }
+    base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
+    base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
+    base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
+    used++;
+}
+
+__global__ void __launch_bounds__(32 * kPosedWarps) k_collide_posed(
+    const uint32_t* __restrict__ list, const uint32_t* __restrict__ counter, const float4* __restrict__ x,
+    const float* __restrict__ r, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* __restrict__ cinfo,
+    float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+    __shared__ uint32_t s_warp[kPosedWarps];
+    __shared__ int s_cand[kPosedWarps][32][kPosedCand];
+    __shared__ float4 s_pos[kPosedWarps][32];
+    __shared__ uint32_t s_off[kPosedWarps][33];
+    __shared__ PosedHit s_res[kPosedWarps][32 * kPosedCand];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t entry = t < (int64_t)*counter ? t : -1;
+    const bool valid = t < (int64_t)*counter;
+    int64_t i = -1;
+    v3 p = mk3(0.0f, 0.0f, 0.0f);
+    float radius = 0.0f;
+    int ncand = 0;  // all candidates of this lane's particle
+    if (valid) {
+        i = (int64_t)list[t];
+        p = xyz(x[i]);
+        radius = r[i];
+        posed_candidates(mt, rt, p, radius, [&](int mesh, v3, q4) {
+            if (ncand < kPosedCand) s_cand[warp][lane][ncand] = mesh;
+            ncand++;
+            return true;
+        });
+    }
+    s_pos[warp][lane] = make_float4(p.x, p.y, p.z, radius);
+    const uint32_t own = (uint32_t)min(ncand, kPosedCand);
+    uint32_t incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    s_off[warp][lane] = incl - own;
+    if (lane == 31) s_off[warp][32] = incl;
+    __syncwarp();
+    const uint32_t total = s_off[warp][32];
+    bool stack_ovf = false, slot_ovf = false;
+    // the warp's (particle, mesh) queries, one per lane
+    for (uint32_t pr = (uint32_t)lane; pr < total; pr += 32) {
+        int o = 0;
+        while (o < 31 && s_off[warp][o + 1] <= pr) o++;
+        const int mesh = s_cand[warp][o][pr - s_off[warp][o]];
+        const float4 po = s_pos[warp][o];
+        const v3 pos_m = xyz(mt.pose[mesh * 2]);
+        const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+        const v3 q = quat_rotate_inv(rot_m, vsub(xyz(po), pos_m));  // as posed_candidates computes it
+        v3 bp, bv, nn;
+        PosedHit h;
+        if (mesh_query(mt, mesh, po.w, q, bp, bv, nn, stack_ovf)) {
+            const v3 nw = quat_rotate(rot_m, nn);
+            h.a = make_float4(bp.x, bp.y, bp.z, 1.0f);
+            h.b = make_float4(nw.x, nw.y, nw.z, 0.0f);
+            h.c = make_float4(bv.x, bv.y, bv.z, 0.0f);
+        } else {
+            h.a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        s_res[warp][pr] = h;
+    }
+    __syncwarp();
     int used0 = 0, used = 0;
-    bool slot_ovf = false, stack_ovf = false;
-    if (entry >= 0) {
-        const int64_t i = (int64_t)list[entry];
-        const v3 p = xyz(x[i]);
-        const float radius = r[i];
+    if (valid) {
         const uint32_t info = cinfo[i];
         used0 = used = info_slots(info);
         float4* base = cslot + (size_t)i * slot_cap * 3;
-        posed_candidates(mt, rt, p, radius, [&](int mesh, v3 q, q4 rot_m) {
-            v3 bp, bv, nn;
-            if (!mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf)) return true;
-            const v3 nw = quat_rotate(rot_m, nn);
-            if (used >= slot_cap) {
-                slot_ovf = true;
+        const uint32_t off = s_off[warp][lane];
+        for (uint32_t k = 0; k < own; k++) {
+            const PosedHit h = s_res[warp][off + k];
+            if (h.a.w != 0.0f)
+                posed_insert(base, used, slot_cap, slot_ovf, s_cand[warp][lane][k], xyz(h.a), xyz(h.b), xyz(h.c));
+        }
+        if (ncand > kPosedCand) {  // the rest, by this lane, in candidate order
+            int k = 0;
+            posed_candidates(mt, rt, p, radius, [&](int mesh, v3 q, q4 rot_m) {
+                if (k++ < kPosedCand) return true;
+                v3 bp, bv, nn;
+                if (mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf))
+                    posed_insert(base, used, slot_cap, slot_ovf, mesh, bp, quat_rotate(rot_m, nn), bv);
                 return true;
-            }
-            int pos = used;
-            while (pos > 0 && __float_as_int(base[(pos - 1) * 3].w) > mesh + 1) pos--;
-            for (int k2 = used; k2 > pos; k2--) {
-                base[k2 * 3] = base[(k2 - 1) * 3];
-                base[k2 * 3 + 1] = base[(k2 - 1) * 3 + 1];
-                base[k2 * 3 + 2] = base[(k2 - 1) * 3 + 2];
-            }
-            base[pos * 3] = make_float4(bp.x, bp.y, bp.z, __int_as_float(mesh + 1));
-            base[pos * 3 + 1] = make_float4(nw.x, nw.y, nw.z, 0.0f);
-            base[pos * 3 + 2] = make_float4(bv.x, bv.y, bv.z, 0.0f);
-            used++;
-            return true;
-        });
+            });
+        }
         // every slot added here belongs to a dynamic body
         if (used != used0)
             cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
@@ -586,7 +659,8 @@ void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, cons
     if (n <= 0 || rt.n_dyn <= 0) return;
     const int blocks = (int)((n + 127) / 128);
     k_posed_triage<<<blocks, 128, 0, s>>>(n, order, x, r, flags, mt, rt, counter, list);
-    k_collide_posed<<<blocks, 128, 0, s>>>(list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+    k_collide_posed<<<(int)((n + 32 * kPosedWarps - 1) / (32 * kPosedWarps)), 32 * kPosedWarps, 0, s>>>(
+        list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
 }
 
 // ---------------------------------------------------------------- body-delta entries ----
