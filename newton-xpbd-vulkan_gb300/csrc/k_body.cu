@@ -664,31 +664,41 @@ void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, cons
 }
 
 // ---------------------------------------------------------------- body-delta entries ----
-__global__ void k_dyn_emit(int64_t n, const uint32_t* __restrict__ cinfo, DynSlots ds, const uint2* __restrict__ rank,
-                           uint32_t cap, int bits, int passes, uint32_t* __restrict__ keys, uint32_t* hist,
-                           DeviceStatus* st) {
+// Body-delta entry keys (the body of each dynamic slot, at entry rank[i].x + j) and the
+// digit histograms of the sort passes, counted per block in shared memory first: the
+// keys are few bodies, so direct global atomics would pile onto a handful of bins.
+__global__ void __launch_bounds__(256) k_dyn_emit(int64_t n, const uint32_t* __restrict__ cinfo, DynSlots ds,
+                                                  const uint2* __restrict__ rank, uint32_t cap, int bits, int passes,
+                                                  uint32_t* __restrict__ keys, uint32_t* hist, DeviceStatus* st) {
+    __shared__ uint32_t s_hist[4 * 256];
+    const int nb = passes << bits;  // passes <= 4, bits <= 8
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) s_hist[k] = 0;
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t info = cinfo[i];
-    if (info_dyn(info) == 0) return;
-    const int used = info_slots(info);
-    uint32_t e = rank[i].x;
     bool ovf = false;
-    for (int j = 0; j < used; j++) {
-        const int shape = __float_as_int(ds.cslot[((size_t)i * ds.slot_cap + j) * 3].w);
-        const int body = ds.shape_body[shape];
-        if (body >= 0 && ds.body_invm[body] > 0.0f) {
-            if (e < cap) {
-                keys[e] = (uint32_t)body;
-                for (int p = 0; p < passes; p++)
-                    atomicAdd(&hist[(p << bits) + (((uint32_t)body >> (p * bits)) & ((1u << bits) - 1u))], 1u);
-            } else {
-                ovf = true;
+    const uint32_t info = i < n ? cinfo[i] : 0u;
+    if (info_dyn(info) != 0) {
+        const int used = info_slots(info);
+        uint32_t e = rank[i].x;
+        for (int j = 0; j < used; j++) {
+            const int shape = __float_as_int(ds.cslot[((size_t)i * ds.slot_cap + j) * 3].w);
+            const int body = ds.shape_body[shape];
+            if (body >= 0 && ds.body_invm[body] > 0.0f) {
+                if (e < cap) {
+                    keys[e] = (uint32_t)body;
+                    for (int p = 0; p < passes; p++)
+                        atomicAdd(&s_hist[(p << bits) + (((uint32_t)body >> (p * bits)) & ((1u << bits) - 1u))], 1u);
+                } else {
+                    ovf = true;
+                }
+                e++;
             }
-            e++;
         }
     }
     if (ovf) atomicOr(&st->error_bits, kErrBodyOverflow);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb; k += blockDim.x)
+        if (s_hist[k]) atomicAdd(&hist[k], s_hist[k]);
 }
 
 void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank, uint32_t cap,
