@@ -725,36 +725,53 @@ void launch_body_segments(cudaStream_t s, uint32_t cap, const uint32_t* count, c
 // One warp per body: the body's particle-contact deltas summed in entry order (the
 // canonical contact order), then apply_body_deltas.comp with their count as the
 // constraint weight (or none when particle_weighting is off).
-__global__ void k_body_particles(BodyArrays ba, const uint2* __restrict__ seg, const uint32_t* __restrict__ sorted,
-                                 const float4* __restrict__ bdel, const float4* __restrict__ q_in,
-                                 const float4* __restrict__ qd_in, float4* __restrict__ q_out,
-                                 float4* __restrict__ qd_out, RigidParams rp) {
+__global__ void __launch_bounds__(128) k_body_particles(BodyArrays ba, const uint2* __restrict__ seg,
+                                                       const uint32_t* __restrict__ sorted,
+                                                       const float4* __restrict__ bdel,
+                                                       const float4* __restrict__ q_in,
+                                                       const float4* __restrict__ qd_in, float4* __restrict__ q_out,
+                                                       float4* __restrict__ qd_out, RigidParams rp) {
+    // the warp stages 32 entries at a time in shared memory (the next 32 already loading)
+    // and lane 0 sums them in entry order
+    __shared__ float4 s_a[4][32], s_c[4][32];
     const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (b >= ba.nb) return;
     v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
     float cnt = 0.0f;
     if (ba.invm[b] > 0.0f) {
         const uint2 sg = seg[b];
+        const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float4 a = zero, c = zero;
+        if (sg.x + lane < sg.y) {
+            const uint32_t e = sorted[sg.x + lane];
+            a = bdel[(size_t)e * 2];
+            c = bdel[(size_t)e * 2 + 1];
+        }
         for (uint32_t base = sg.x; base < sg.y; base += 32) {
-            float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = a;
-            if (base + lane < sg.y) {
-                const uint32_t e = sorted[base + lane];
+            s_a[w][lane] = a;
+            s_c[w][lane] = c;
+            __syncwarp();
+            a = zero;
+            c = zero;
+            if (base + 32 + lane < sg.y) {
+                const uint32_t e = sorted[base + 32 + lane];
                 a = bdel[(size_t)e * 2];
                 c = bdel[(size_t)e * 2 + 1];
             }
-            const int m = (int)min(32u, sg.y - base);
-            for (int l = 0; l < m; l++) {
-                const float ax = __shfl_sync(0xffffffffu, a.x, l), ay = __shfl_sync(0xffffffffu, a.y, l),
-                            az = __shfl_sync(0xffffffffu, a.z, l), aw = __shfl_sync(0xffffffffu, a.w, l);
-                const float cx = __shfl_sync(0xffffffffu, c.x, l), cy = __shfl_sync(0xffffffffu, c.y, l),
-                            cz = __shfl_sync(0xffffffffu, c.z, l);
-                if (aw != 0.0f) {
-                    lin = vadd(lin, mk3(ax, ay, az));
-                    ang = vadd(ang, mk3(cx, cy, cz));
-                    cnt += 1.0f;
+            if (lane == 0) {
+                const int m = (int)min(32u, sg.y - base);
+#pragma unroll 8
+                for (int l = 0; l < m; l++) {
+                    const float4 al = s_a[w][l], cl = s_c[w][l];
+                    if (al.w != 0.0f) {
+                        lin = vadd(lin, xyz(al));
+                        ang = vadd(ang, xyz(cl));
+                        cnt += 1.0f;
+                    }
                 }
             }
+            __syncwarp();
         }
     }
     if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.particle_weighting, q_out, qd_out);
