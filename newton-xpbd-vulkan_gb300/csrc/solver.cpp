@@ -81,6 +81,12 @@ void Solver::clear_graphs() {
         for (auto& m : kv.second.marks) cudaEventDestroy(m.first);
     }
     graphs_.clear();
+    clear_backward_graphs();
+}
+
+void Solver::clear_backward_graphs() {
+    for (auto& kv : bwd_graphs_) cudaGraphExecDestroy(kv.second);
+    bwd_graphs_.clear();
 }
 
 void Solver::init(const xpbd_config& cfg, size_t num_particles, size_t max_contacts) {
@@ -1564,21 +1570,32 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     const float sdt = ro_dt_ / (float)ro_substeps_;  // as record_frame computes it
     const int n_seg = (ro_frames_ + ro_ckpt_ - 1) / ro_ckpt_;
     const size_t nn = std::max<size_t>(n, 1);
-    gx_.alloc(nn, false);
-    gv_.alloc(nn, false);
-    gw_.alloc(nn, true);
-    gacc_.alloc(nn, false);
-    part_xp_.alloc(nn, false);
-    part_vp_.alloc(nn, false);
-    part_x0_.alloc(nn, false);
-    part_v0_.alloc(nn, false);
-    part_gd_.alloc(nn, false);
+    // buffers keep their addresses between calls (the segment graphs hold them)
+    bool moved = false;
+    auto ensure = [&](auto& buf, size_t count) {
+        if (buf.n != count) {
+            buf.alloc(count, false);
+            moved = true;
+        }
+    };
+    ensure(gx_, nn);
+    ensure(gv_, nn);
+    ensure(gw_, nn);
+    ensure(gacc_, nn);
+    ensure(part_xp_, nn);
+    ensure(part_vp_, nn);
+    ensure(part_x0_, nn);
+    ensure(part_v0_, nn);
+    ensure(part_gd_, nn);
     const size_t blocks = adjoint_block_count((int64_t)n);
-    block_params_.alloc(std::max<size_t>(blocks, 1) * 3, false);
-    param_acc_.alloc(3, true);
+    ensure(block_params_, std::max<size_t>(blocks, 1) * 3);
+    ensure(param_acc_, 3);
     // per replayed substep: start state (x, v) and the sorted (key, id) pairs
-    traj_.alloc((size_t)ro_ckpt_ * ro_substeps_ * 2 * nn, false);
-    traj_keys_.alloc((size_t)ro_ckpt_ * ro_substeps_ * 2 * nn, false);
+    ensure(traj_, (size_t)ro_ckpt_ * ro_substeps_ * 2 * nn);
+    ensure(traj_keys_, (size_t)ro_ckpt_ * ro_substeps_ * 2 * nn);
+    if (moved) clear_backward_graphs();
+    XPBD_CUDA(cudaMemsetAsync(gw_.p, 0, gw_.bytes(), stream_));
+    XPBD_CUDA(cudaMemsetAsync(param_acc_.p, 0, param_acc_.bytes(), stream_));
     // upstream gradients (host xyz -> device float4)
     auto upload = [&](const float* h, float4* d) {
         if (h) {
@@ -1625,13 +1642,12 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     a.rv = rv_[0].p;
     a.x0 = x_[0].p;
     a.v0 = v_[0].p;
-    for (int c = n_seg - 1; c >= 0; c--) {
-        const int nf = std::min(ro_ckpt_, ro_frames_ - c * ro_ckpt_);
-        const int S = nf * ro_substeps_;
-        // replay the segment from its checkpoint, keeping every substep's start state
-        const float4* ck = ckpt_.p + (size_t)c * 2 * n;
-        XPBD_CUDA(cudaMemcpyAsync(x_[0].p, ck, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
-        XPBD_CUDA(cudaMemcpyAsync(v_[0].p, ck + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+    // one segment: replay from the checkpoint already in x_[0], v_[0] keeping every
+    // substep's start state and sort, then the adjoint of its substeps, last first (cell
+    // table and sorted records rebuilt from the stored sort); captured once per segment
+    // length and step, replayed for every segment
+    const PredictParams pp = predict_params(sdt);
+    auto segment = [&](int S) {
         int src = 0;
         const int fin = (plan_.passes - 1) & 1;
         for (int t = 0; t < S; t++) {
@@ -1648,20 +1664,43 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
             XPBD_CUDA(cudaMemcpyAsync(tk, pair_k_[fin].p, n * 4, cudaMemcpyDeviceToDevice, stream_));
             XPBD_CUDA(cudaMemcpyAsync(tk + n, pair_v_[fin].p, n * 4, cudaMemcpyDeviceToDevice, stream_));
         }
-        // adjoint of the segment's substeps, last first: cell table and sorted records
-        // rebuilt from the stored sort
-        const PredictParams pp = predict_params(sdt);
         for (int t = S - 1; t >= 0; t--) {
             const float4* tr = traj_.p + (size_t)t * 2 * n;
             const uint32_t* tk = traj_keys_.p + (size_t)t * 2 * n;
             launch_bump_stamp(stream_, stamp_.p);
             launch_cells_gather(stream_, (int64_t)n, tk, tk + n, tr, tr + n, w_.p, r_.p, flags_.p, pp, table_.p,
                                 stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
-            a.sids = tk + n;
-            a.x0 = tr;
-            a.v0 = tr + n;
-            launch_adjoint_substep(stream_, a);
+            AdjointArgs at = a;
+            at.sids = tk + n;
+            at.x0 = tr;
+            at.v0 = tr + n;
+            launch_adjoint_substep(stream_, at);
         }
+    };
+    for (int c = n_seg - 1; c >= 0; c--) {
+        const int nf = std::min(ro_ckpt_, ro_frames_ - c * ro_ckpt_);
+        const int S = nf * ro_substeps_;
+        const float4* ck = ckpt_.p + (size_t)c * 2 * n;
+        XPBD_CUDA(cudaMemcpyAsync(x_[0].p, ck, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        XPBD_CUDA(cudaMemcpyAsync(v_[0].p, ck + n, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_));
+        const std::pair<int, uint32_t> key(S, f2u(sdt));
+        auto it = bwd_graphs_.find(key);
+        if (it == bwd_graphs_.end()) {
+            cudaGraph_t g;
+            XPBD_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            try {
+                segment(S);
+            } catch (...) {
+                cudaStreamEndCapture(stream_, &g);
+                throw;
+            }
+            XPBD_CUDA(cudaStreamEndCapture(stream_, &g));
+            cudaGraphExec_t exec;
+            XPBD_CUDA(cudaGraphInstantiate(&exec, g, 0));
+            cudaGraphDestroy(g);
+            it = bwd_graphs_.emplace(key, exec).first;
+        }
+        XPBD_CUDA(cudaGraphLaunch(it->second, stream_));
     }
     XPBD_CUDA(cudaStreamSynchronize(stream_));
     auto download = [&](const float4* d, float* h) {

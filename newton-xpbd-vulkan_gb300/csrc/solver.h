@@ -180,6 +180,7 @@ class Solver {
     };
     void require_init() const;
     void clear_graphs();
+    void clear_backward_graphs();
     void ensure_cull();
     void upload_xyz(const float* h, float4* d, size_t n);
     void download_xyz(const float4* d, float* h, size_t n);
@@ -328,6 +329,7 @@ class Solver {
     DevBuf<int32_t> cell_starts_, cell_ends_;
     // graphs
     std::map<GraphKey, FrameGraph> graphs_;
+    std::map<std::pair<int, uint32_t>, cudaGraphExec_t> bwd_graphs_;  // rollout_backward segments by (substeps, dt)
     FrameGraph* recording_ = nullptr;  // graph being captured (marks and node counts go here)
     int pending_substeps_ = 0;         // frame launched by step_async and not yet synced
     uint64_t frames_run_ = 0;
