@@ -174,13 +174,23 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
                         lo = e.x;
                         hi = e.y;
                     }
-                    for (int kk = lo; kk < hi; kk++) {
+                    // candidates in groups of 4: the group's records are loaded together,
+                    // then tested one by one in order
+                    for (int kk0 = lo; kk0 < hi; kk0 += 4) {
+                        float4 nxs[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+                            nxs[u] = kk0 + u < hi ? __ldg(&rx[kk0 + u]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                        const int kk = kk0 + u;
+                        if (kk >= hi) break;
                         if (kk == k) continue;
                         const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
                         if ((nflag & 1) == 0) continue;
                         if (!ALL_ACTIVE && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
                             continue;
-                        const float4 nx = __ldg(&rx[kk]);
+                        const float4 nx = nxs[u];
                         const v3 raw = vsub(xp, xyz(nx));
                         if (fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R) continue;
                         // exact_length's squared sum; a candidate whose distance provably exceeds
@@ -197,6 +207,7 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
                         if (++np == kPairCap) {
                             pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
                             np = 0;
+                        }
                         }
                     }
                 }
