@@ -207,6 +207,8 @@ def run_gpu(args):
             parts["mixed"] = measure_mixed(args, dev)
         if "diff" in args.only:
             parts["diff"] = measure_diff(args, dev)
+        if "pile" in args.only:
+            parts["pile_1m"] = measure_pile(args, dev)
         print(json.dumps(parts), flush=True)
         return
     if world > 1:
@@ -311,7 +313,8 @@ def run_gpu(args):
     del solver
     for name, on, fn in (("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev, flush)),
                          ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev)),
-                         ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev))):
+                         ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev)),
+                         ("pile_1m", args.pile_frames > 0, lambda: measure_pile(args, dev))):
         if rank == 0 and on:
             try:
                 result[name] = fn()
@@ -492,6 +495,56 @@ def measure_mixed(args, dev):
             "box_height_range": [round(float(np.nanmin(bq[:, 2])), 3), round(float(np.nanmax(bq[:, 2])), 3)]}
 
 
+def measure_pile(args, dev):
+    """Plain step at 1M particles: the 4,096-particle pile recipe (r 0.01 m, spacing 0.02 m,
+    jitter +/-0.002 m, seed 42, plane + particle contacts, cell 0.02 m) on a 128x128x64
+    lattice (1,048,576 particles), 10 substeps x 1 iteration per frame, device-timed frames
+    after a pre-roll (the lattice has settled into contact). Reported beside the HBM roofline
+    of the whole substep (76 B per particle-substep)."""
+    import torch
+    import vkxpbd
+    from vkxpbd import scenes
+
+    sc = scenes.pile(dims=(128, 128, 64), name="pile_1m")
+    cfg = vkxpbd.SolverConfig()
+    sc.apply_config(cfg)
+    cfg.device_index = dev.index
+    s = vkxpbd.XpbdSolver()
+    s.init(cfg, sc.n)
+    s.finalize_meshes()
+    s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+    for _ in range(args.pile_preroll + args.warmup):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
+    frames = args.pile_frames
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    torch.cuda.synchronize(dev)
+    for k in range(frames):
+        ev[k][0].record(stream)
+        s.step_async(DT, SUBSTEPS, ITERATIONS)
+        ev[k][1].record(stream)
+    s.sync()
+    torch.cuda.synchronize(dev)
+    dev_s = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
+    launches = s.get_frame_stats()["kernels_per_frame"]
+    s.set_profiling(True)
+    s.reset_stage_times()
+    for _ in range(min(frames, 5)):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    stage_ms, prof_substeps = s.get_stage_times()
+    s.set_profiling(False)
+    peak, peak_kind = measured_peak_hbm()
+    work = sc.n * SUBSTEPS * frames
+    step_gbs = STEP_ALG_BYTES * work / dev_s / 1e9
+    return {"workload": "pile_1m", "particles": sc.n, "preroll_frames": args.pile_preroll, "frames": frames,
+            "value": work / dev_s, "unit": UNIT, "ms_per_frame": dev_s / frames * 1e3,
+            "launches_per_frame": int(launches), "contacts_last_substep": int(s.last_contact_count),
+            "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
+                              "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
+                              "peak_source": peak_kind},
+            "stages": stage_table(stage_ms, prof_substeps, sc.n, peak)}
+
+
 def measure_cache(args, solver, sc):
     """The add-on's per-frame cache (step, then np.save of the positions): done synchronously
     as the add-on does, and with the frame recorder (copy + file write overlap the next frame)."""
@@ -624,7 +677,9 @@ def main():
     ap.add_argument("--diff-frames", type=int, default=60, help="0 skips the differentiable rollout measurement")
     ap.add_argument("--cache-frames", type=int, default=50, help="0 skips the frame-cache measurement")
     ap.add_argument("--diff-reps", type=int, default=3)
-    ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed (default all)")
+    ap.add_argument("--pile-frames", type=int, default=10, help="0 skips the 1M-particle plain pile measurement")
+    ap.add_argument("--pile-preroll", type=int, default=20)
+    ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed,diff,pile (default all)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
