@@ -363,12 +363,9 @@ __device__ __forceinline__ void walk_leaf(W& w, const MeshTables& mt, v3 p, floa
 }
 
 // Contact emission after the traversal of mesh ci (:333-411).
-// The ray-parity loop of watertight meshes is split over the `nsub` lanes of a group
-// (lane `sub`, lanes `gmask`) when nsub > 1; every lane of the group gets the result.
 template <class W>
 __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, v3 p, v3& body_pos,
-                                            v3& shape_v, v3& nrm, int sub = 0, int nsub = 1,
-                                            unsigned gmask = 0xffffffffu) {
+                                            v3& shape_v, v3& nrm) {
     if (w.wt) w.min_dist = exact_sqrt(w.min_dist_sq);
     if (!(w.found && w.min_dist < w.max_dist)) return false;
     const float u_mesh = (1.0f - w.sv_v) - w.sv_w;
@@ -385,11 +382,10 @@ __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, 
         const WoopRay ray = woop_setup(mk3(1.029700994f, 1.086472273f, 1.034694910f));
         uint32_t hits = 0;
         const uint32_t po = __ldg(&mt.prim_off[ci]), pn = __ldg(&mt.prim_cnt[ci]);
-        for (uint32_t ti = (uint32_t)sub; ti < pn; ti += (uint32_t)nsub) {
+        for (uint32_t ti = 0; ti < pn; ti++) {
             const float4* q = mt.tri_cache + (size_t)(po + ti) * 4;
             if (woop_hit(ray, p, xyz(__ldg(q)), xyz(__ldg(q + 1)), xyz(__ldg(q + 2)))) hits++;
         }
-        for (int o = 1; o < nsub; o <<= 1) hits += __shfl_xor_sync(gmask, hits, o);
         sign = (hits & 1u) ? -1.0f : 1.0f;
     } else {
         sign = vdot(w.acc, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
