@@ -252,13 +252,16 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(AdjointArgs a) {
     }
 }
 
-// Adds the per-block parameter gradients to the double accumulators, in block order.
+// Adds the per-block parameter gradients to the double accumulators in a fixed order:
+// one warp per parameter, lane l summing blocks l, l + 32, ... and the lanes combined by
+// a fixed shuffle tree (deterministic run to run).
 __global__ void k_adj_params(int blocks, const float* __restrict__ block_params, double* acc) {
-    const int lane = threadIdx.x;
-    if (lane >= 3) return;
+    const int p = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (p >= 3) return;
     double t = 0.0;
-    for (int b = 0; b < blocks; b++) t += (double)block_params[(size_t)b * 3 + lane];
-    acc[lane] += t;
+    for (int b = lane; b < blocks; b += 32) t += (double)block_params[(size_t)b * 3 + p];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) acc[p] += t;
 }
 
 __global__ void k_bump_stamp(uint32_t* stamp) { *stamp += 1u; }
@@ -270,7 +273,7 @@ void launch_adjoint_substep(cudaStream_t s, const AdjointArgs& a) {
     const int blocks = (int)((a.n + kAdjThreads - 1) / kAdjThreads);
     k_adj_local<<<blocks, kAdjThreads, 0, s>>>(a);
     k_adj_pairs<<<blocks, kAdjThreads, 0, s>>>(a);
-    k_adj_params<<<1, 32, 0, s>>>(blocks, a.block_params, a.param_acc);
+    k_adj_params<<<1, 96, 0, s>>>(blocks, a.block_params, a.param_acc);
 }
 
 size_t adjoint_block_count(int64_t n) { return (size_t)((n + kAdjThreads - 1) / kAdjThreads); }
