@@ -77,3 +77,21 @@ def test_box_shell_grid_collisions_bitexact():
     sc.radii = rng.uniform(0.003, 0.012, n).astype(np.float32)
     sc.flags = np.ones(n, np.int32)
     _run(sc, 3, substeps=4)
+
+
+def test_particles_between_eight_boxes_bitexact():
+    """Particles in the gap between eight small boxes: each particle has up to eight
+    candidate moving meshes, past the per-particle share the query kernel lists for the
+    warp (the rest are queried by the particle's own lane, in candidate order)."""
+    he, c = 0.02, 0.0215
+    pos = [(sx * c, sy * c, 0.3 + sz * c) for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]
+    sc = box_scene(n_side=2, boxes=[(he, he, he)] * 8, positions=pos, seed=5)
+    rng = np.random.default_rng(21)
+    n = 600
+    p = (rng.random((n, 3)) - 0.5) * 0.012 + np.array([0.0, 0.0, 0.3])
+    sc.positions = p.astype(np.float32)
+    sc.velocities = np.zeros_like(sc.positions)
+    sc.inv_mass = np.full(n, 1000.0, np.float32)
+    sc.radii = np.full(n, 0.004, np.float32)
+    sc.flags = np.ones(n, np.int32)
+    _run(sc, 3, substeps=4)
