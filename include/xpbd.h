@@ -182,6 +182,11 @@ int xpbd_set_body_params(xpbd_solver* s, const xpbd_body_params* p);
 int xpbd_set_bodies(xpbd_solver* s, const float* q, const float* qd, const float* com, const float* inertia,
                     const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t num_bodies);
 int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t num_bodies);
+/* Batched solvers (xpbd_batch_init): the scene of each body, -1 for a static body shared
+ * by every scene. A dynamic body then meets only the particles and dynamic bodies of its
+ * own scene, so each scene steps as it would alone (with the batch's mesh 0 supplying
+ * the average edge length, as mesh 0 does in a single scene). Default: scene 0. */
+int xpbd_set_body_scenes(xpbd_solver* s, const int32_t* scene_of_body, size_t num_bodies);
 
 /* Differentiable rollout — an extension with no reference counterpart: the
  * hand-written adjoint of the substep (integration, ground-plane and

@@ -293,6 +293,10 @@ int xpbd_get_bodies(xpbd_solver* s, float* q, float* qd, size_t nb) {
     return guarded([&] { S(s).get_bodies(q, qd, nb); });
 }
 
+int xpbd_set_body_scenes(xpbd_solver* s, const int32_t* scene_of_body, size_t nb) {
+    return guarded([&] { S(s).set_body_scenes(scene_of_body, nb); });
+}
+
 int xpbd_record_start(xpbd_solver* s, const char* directory, int first_frame) {
     return guarded([&] {
         if (!directory) throw std::runtime_error("xpbd_record_start: directory is NULL");

@@ -203,7 +203,7 @@ __global__ void k_body_pairs(RigidTables rt, RigidParams rp, DeviceStatus* st) {
     for (int j0 = 0; j0 < rt.n_dyn; j0 += 32) {
         const int j = j0 + lane;
         bool ov = false;
-        if (j < rt.n_dyn && j != i) {
+        if (j < rt.n_dyn && j != i && rt.dyn_scene[j] == rt.dyn_scene[i]) {
             const float4 jl = rt.wbox[j * 2], jh = rt.wbox[j * 2 + 1];
             const float ej = rp.margin + jl.w + rt.pad;
             ov = (il.x - ei <= jh.x + ej) && (jl.x - ej <= ih.x + ei) && (il.y - ei <= jh.y + ej) &&
@@ -223,8 +223,9 @@ __global__ void k_body_pairs(RigidTables rt, RigidParams rp, DeviceStatus* st) {
 }
 
 // ------------------------------------------------------------- box grid ----
-__device__ __forceinline__ uint32_t box_cell_hash(int ix, int iy, int iz, int size) {
-    return (((uint32_t)ix * 73856093u) ^ ((uint32_t)iy * 19349663u) ^ ((uint32_t)iz * 83492791u)) &
+__device__ __forceinline__ uint32_t box_cell_hash(int ix, int iy, int iz, int scene, int size) {
+    return (((uint32_t)ix * 73856093u) ^ ((uint32_t)iy * 19349663u) ^ ((uint32_t)iz * 83492791u) ^
+            ((uint32_t)scene * 2654435761u)) &
            (uint32_t)(size - 1);
 }
 __device__ __forceinline__ int cell_of(float v, float cs) { return f2i(floorf(v / cs)); }
@@ -248,7 +249,8 @@ __global__ void k_boxgrid_count(RigidTables rt, DeviceStatus* st) {
     if (g >= rt.n_dyn * kBoxCells) return;
     const int i = g / kBoxCells, c = g % kBoxCells;
     int x, y, z;
-    if (box_cell(rt, i, c, x, y, z)) atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.grid_size)], 1u);
+    if (box_cell(rt, i, c, x, y, z))
+        atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.dyn_scene[i], rt.grid_size)], 1u);
     if (c == kBoxCells - 1) {  // a box wider than 4 cells per axis would lose cells: report it
         const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
         const float e = rt.grid_reach + l.w;
@@ -308,7 +310,7 @@ __global__ void k_boxgrid_fill(RigidTables rt) {
     const int i = g / kBoxCells, c = g % kBoxCells;
     int x, y, z;
     if (!box_cell(rt, i, c, x, y, z)) return;
-    const uint32_t b = box_cell_hash(x, y, z, rt.grid_size);
+    const uint32_t b = box_cell_hash(x, y, z, rt.dyn_scene[i], rt.grid_size);
     rt.grid_list[rt.grid_start[b] + atomicAdd(&rt.grid_count[b], 1u)] = make_int4(i, x, y, z);
 }
 
@@ -463,19 +465,21 @@ void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTa
 // of the box grid whose widened world box holds the particle are queried in their body
 // frame (generate_mesh_contacts.comp with the pose inverted); each contact is inserted
 // into the particle's slots at its mesh's place, so the list order does not matter.
-// Boxes of the box grid that a particle at p (radius r) may touch, in bucket order:
-// f(ci, mesh, q, rot) for each dynamic body ci whose widened world box holds p and whose
-// root box (body frame, q = p in that frame) is within the traversal's first bound.
+// Boxes of the box grid that a particle at p (radius r, scene `scene`) may touch, in
+// bucket order: f(mesh, q, rot) for each dynamic body of the particle's scene whose
+// widened world box holds p and whose root box (body frame, q = p in that frame) is
+// within the traversal's first bound.
 template <class F>
 __device__ __forceinline__ void posed_candidates(const MeshTables& mt, const RigidTables& rt, v3 p, float radius,
-                                                 F&& f) {
+                                                 int scene, F&& f) {
     const int cx = cell_of(p.x, rt.grid_cs), cy = cell_of(p.y, rt.grid_cs), cz = cell_of(p.z, rt.grid_cs);
-    const uint32_t b = box_cell_hash(cx, cy, cz, rt.grid_size);
+    const uint32_t b = box_cell_hash(cx, cy, cz, scene, rt.grid_size);
     const uint32_t k0 = rt.grid_start[b], k1 = rt.grid_start[b + 1];
     for (uint32_t k = k0; k < k1; k++) {
         const int4 en = __ldg(&rt.grid_list[k]);
         if (en.y != cx || en.z != cy || en.w != cz) continue;  // another cell of this bucket
         const int ci = en.x;
+        if (rt.dyn_scene[ci] != scene) continue;  // another scene's body in this cell
         const float4 l = rt.wbox[ci * 2], h = rt.wbox[ci * 2 + 1];
         const float e = (mt.soft_margin + l.w) + radius + rt.pad;
         if (!(p.x >= l.x - e && p.x <= h.x + e && p.y >= l.y - e && p.y <= h.y + e && p.z >= l.z - e &&
@@ -507,7 +511,7 @@ __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t*
     if (t < n) {
         i = order ? (int64_t)order[t] : t;
         if (flags[i] & 1)
-            posed_candidates(mt, rt, xyz(x[i]), r[i], [&](int, v3, q4) {
+            posed_candidates(mt, rt, xyz(x[i]), r[i], rt.pscene ? (int)rt.pscene[i] : 0, [&](int, v3, q4) {
                 any = true;
                 return false;
             });
@@ -572,11 +576,13 @@ __global__ void __launch_bounds__(32 * kPosedWarps) k_collide_posed(
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
     int ncand = 0;  // all candidates of this lane's particle
+    int scene = 0;
     if (valid) {
         i = (int64_t)list[t];
         p = xyz(x[i]);
         radius = r[i];
-        posed_candidates(mt, rt, p, radius, [&](int mesh, v3, q4) {
+        scene = rt.pscene ? (int)rt.pscene[i] : 0;
+        posed_candidates(mt, rt, p, radius, scene, [&](int mesh, v3, q4) {
             if (ncand < kPosedCand) s_cand[warp][lane][ncand] = mesh;
             ncand++;
             return true;
@@ -629,7 +635,7 @@ __global__ void __launch_bounds__(32 * kPosedWarps) k_collide_posed(
         }
         if (ncand > kPosedCand) {  // the rest, by this lane, in candidate order
             int k = 0;
-            posed_candidates(mt, rt, p, radius, [&](int mesh, v3 q, q4 rot_m) {
+            posed_candidates(mt, rt, p, radius, scene, [&](int mesh, v3 q, q4 rot_m) {
                 if (k++ < kPosedCand) return true;
                 v3 bp, bv, nn;
                 if (mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf))

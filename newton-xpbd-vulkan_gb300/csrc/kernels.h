@@ -253,6 +253,10 @@ struct RigidTables {
     int* rc_count;
     float pad;                    // conservative widening of the world boxes
     int n_vert;                   // dv_start[nb]
+    // batched scenes: the scene of each dynamic body and of each particle (null: all in
+    // scene 0); bodies meet only bodies and particles of their own scene
+    const int* dyn_scene;
+    const uint32_t* pscene;
     // hashed grid of the dynamic bodies' world boxes (widened by grid_reach) for the particle
     // queries: cell size grid_cs >= a third of any widened box, so a box covers at most
     // kBoxCells cells; bucket h lists (dyn index, cell x, y, z) entries, any order, in

@@ -540,6 +540,8 @@ RigidTables Solver::rigid_tables() const {
     t.rc_count = rc_count_.p;
     t.pad = 1e-3f;
     t.n_vert = n_dyn_verts_;
+    t.dyn_scene = dyn_scene_.p;
+    t.pscene = pscene_.p;
     // box grid: a particle's side of the widening (soft margin + radius + pad, radii bounded
     // by the larger of particle_max_radius and the largest finite radius set); cells a
     // third of the largest widened box, so a box covers at most 4 cells per axis
@@ -573,6 +575,33 @@ RigidParams Solver::rigid_params(float sdt) const {
 void Solver::set_body_params(const xpbd_body_params& p) {
     body_params_ = p;
     clear_graphs();
+}
+
+// Scene of each body in a batched solver (-1: shared by every scene, for static
+// bodies). A dynamic body meets only the particles and dynamic bodies of its scene.
+void Solver::set_body_scenes(const int32_t* scenes, size_t nb) {
+    if (!finalized_) throw std::runtime_error("set_body_scenes: call finalize_meshes() first");
+    if (nb != meshes_.size()) throw std::runtime_error("set_body_scenes: one scene per mesh");
+    const int ns = (int)scene_off_.size() - 1;
+    for (size_t b = 0; b < nb; b++)
+        if (scenes[b] < -1 || scenes[b] >= ns) throw std::runtime_error("set_body_scenes: scene out of range");
+    XPBD_CUDA(cudaSetDevice(device_));
+    sync();
+    body_scene_.assign(scenes, scenes + nb);
+    if (dyn_any_) upload_dyn_scenes();
+    clear_graphs();
+}
+
+void Solver::upload_dyn_scenes() {
+    std::vector<int> ds(std::max<size_t>(dyn_list_.size(), 1), 0);
+    for (size_t k = 0; k < dyn_list_.size(); k++) {
+        const int b = dyn_list_[k];
+        ds[k] = (size_t)b < body_scene_.size() ? body_scene_[b] : 0;
+        if (ds[k] < 0)
+            throw std::runtime_error("set_body_scenes: a dynamic body needs a scene (-1 is for static bodies)");
+    }
+    dyn_scene_.alloc(ds.size(), false);
+    XPBD_CUDA(cudaMemcpy(dyn_scene_.p, ds.data(), ds.size() * sizeof(int), cudaMemcpyHostToDevice));
 }
 
 void Solver::set_bodies(const float* q, const float* qd, const float* com, const float* inertia,
@@ -673,6 +702,7 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     posed_list_.alloc(std::max<size_t>(n_, 1), false);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);
+    upload_dyn_scenes();
     up(posed_, posed);
     up(walk_list_, walk);
     walk_count_ = (int)walk.size();

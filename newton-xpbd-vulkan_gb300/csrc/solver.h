@@ -114,6 +114,8 @@ class Solver {
     void set_bodies(const float* q, const float* qd, const float* com, const float* inertia,
                     const float* inv_inertia, const float* inv_mass, const int32_t* flags, size_t nb);
     void get_bodies(float* q, float* qd, size_t nb);
+    // batched: scene of each body (-1: static, shared by every scene)
+    void set_body_scenes(const int32_t* scenes, size_t nb);
     // frame cache: positions of every later step written to dir/frame_%04d.npy
     void record_start(const std::string& dir, int first_frame);
     int record_stop();
@@ -182,6 +184,7 @@ class Solver {
     void clear_graphs();
     void clear_backward_graphs();
     void ensure_cull();
+    void upload_dyn_scenes();
     void upload_xyz(const float* h, float4* d, size_t n);
     void download_xyz(const float4* d, float* h, size_t n);
     void ensure_substep_capacity(int substeps);
@@ -272,6 +275,8 @@ class Solver {
     DevBuf<uint32_t> grid_count_, grid_start_;
     DevBuf<int4> grid_list_;
     DevBuf<uint32_t> posed_list_;  // particles with candidate moving meshes, per substep
+    std::vector<int32_t> body_scene_;  // batched: scene of each body (-1: every scene)
+    DevBuf<int> dyn_scene_;            // scene of each dynamic body (dyn index)
     DevBuf<uint32_t> dv_start_;
     DevBuf<float4> dv_local_, wbox_, rc_;
     uint32_t entry_cap_ = 0;

@@ -159,6 +159,12 @@ class XpbdSolver:
         fl = None if flags is None else _i32(flags).reshape(-1)
         _check(_lib.xpbd_set_bodies(self._h, *[_ptr(a, _FP) for a in arrs], _ptr(fl, _IP), nb))
 
+    def set_body_scenes(self, scenes):
+        """Batched solvers: the scene of each body (one per mesh), -1 for static bodies
+        shared by every scene (xpbd_set_body_scenes)."""
+        sc = _i32(scenes).reshape(-1)
+        _check(_lib.xpbd_set_body_scenes(self._h, _ptr(sc, _IP), sc.size))
+
     def get_body_q(self):
         nb = self.mesh_count
         q = np.zeros((nb, 7), np.float32)

@@ -106,6 +106,7 @@ SIGNATURES = {
     "xpbd_body_params_default": (None, [C.POINTER(BodyParams)]),
     "xpbd_set_body_params": (C.c_int, [_P, C.POINTER(BodyParams)]),
     "xpbd_set_bodies": (C.c_int, [_P, _F, _F, _F, _F, _F, _F, _I, _Z]),
+    "xpbd_set_body_scenes": (C.c_int, [_P, _I, _Z]),
     "xpbd_get_bodies": (C.c_int, [_P, _F, _F, _Z]),
     "xpbd_update_config": (C.c_int, [_P, C.POINTER(Config)]),
     "xpbd_autotune": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),

@@ -230,6 +230,50 @@ class Batch:
         return np.ascontiguousarray(np.concatenate([getattr(s, attr) for s in self.scenes]))
 
 
+def batch_bodies(batch: "Batch", shared: int = 1):
+    """Meshes, body table and body scenes of one batched solver for scenes that each list
+    the same `shared` static meshes first and then their own meshes: the shared meshes
+    once (scene -1), then every scene's own meshes in scene order (scene s).
+    Returns (meshes, Bodies, scene_of_body)."""
+    first = batch.scenes[0]
+    meshes = list(first.meshes[:shared])
+    rows = [(first.bodies, b) for b in range(shared)]
+    scene_of_body = [-1] * shared
+    for s, sc in enumerate(batch.scenes):
+        for b in range(shared, len(sc.meshes)):
+            meshes.append(sc.meshes[b])
+            rows.append((sc.bodies, b))
+            scene_of_body.append(s)
+    nb = len(meshes)
+    out = Bodies.static(nb)
+    for k, (src, b) in enumerate(rows):
+        for name in ("q", "qd", "com", "inertia", "inv_inertia", "inv_mass", "flags"):
+            getattr(out, name)[k] = getattr(src, name)[b]
+    return meshes, out, np.array(scene_of_body, np.int32)
+
+
+def batched_piles_with_boxes(n_scenes=512, lo=1024, hi=65536, max_boxes=16, seed=SEED_BATCH,
+                             frames=100) -> Batch:
+    """The batched piles with 0..max_boxes dynamic boxes per scene (uniform integer count,
+    half-extents U[0.02, 0.08], density 1000, orientations uniform on SO(3), dropped in a
+    column above the pile; seed + s per scene). Every scene lists the same static anchor
+    mesh first (a small box far below the plane) so that mesh 0 is common to all scenes."""
+    av, at = box_mesh((0.05, 0.05, 0.05), center=(0.0, 0.0, -10.0))
+    counts = batch_counts(n_scenes, lo, hi, seed)
+    out = []
+    for s, c in enumerate(counts):
+        rng = np.random.default_rng(seed + s)
+        sc = pile_of(c, seed=seed + s, frames=frames, name=f"pile{s}")
+        sc.meshes.append((av, at, 0.0, True))
+        top = float(sc.positions[:, 2].max()) if c else 0.0
+        nb = int(rng.integers(0, max_boxes + 1))
+        he = rng.uniform(0.02, 0.08, (nb, 3)).astype(np.float32)
+        xy = (rng.random((nb, 2)) - 0.5) * 0.1
+        pos = [(float(xy[k, 0]), float(xy[k, 1]), top + 0.2 + 0.2 * k) for k in range(nb)]
+        out.append(add_boxes(sc, [tuple(h) for h in he], pos, random_quats(nb, rng)))
+    return Batch(out)
+
+
 def batched_piles(n_scenes=512, lo=1024, hi=65536, seed=SEED_BATCH, frames=100) -> Batch:
     """Batched uneven scenes: n_scenes piles with log-uniform particle counts, scene s
     jittered with seed `seed + s`; plane only."""

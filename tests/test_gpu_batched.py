@@ -118,3 +118,34 @@ def test_every_sort_variant_bitexact(bits, items):
         g.step(1.0 / 60.0, 10, 1)
         orc.step(1.0 / 60.0, 10, 1)
         assert_bitexact(g.get_positions(), orc.get_positions(), f"frame {f}")
+
+
+def test_batched_scenes_with_boxes_bitexact():
+    """Uneven piles with 0-3 dynamic boxes each in one batched solver (bodies assigned to
+    their scenes): every scene's particles and boxes equal that scene stepped alone."""
+    full = scenes.batched_piles_with_boxes(n_scenes=4, lo=150, hi=900, max_boxes=3, seed=52)
+    batch = scenes.Batch(full.scenes)
+    cfg = config_for(batch)
+    import vkxpbd
+
+    g = vkxpbd.XpbdSolver()
+    g.init_batched(cfg, batch.counts)
+    meshes, bodies, body_scene = scenes.batch_bodies(batch)
+    for (v, t, margin, wt) in meshes:
+        g.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
+    g.finalize_meshes()
+    g.set_bodies(bodies.q, bodies.qd, bodies.com, bodies.inertia, bodies.inv_inertia, bodies.inv_mass,
+                 bodies.flags)
+    g.set_body_scenes(body_scene)
+    g.set_particles(batch.concat("positions"), batch.concat("velocities"), batch.concat("inv_mass"),
+                    batch.concat("radii"), batch.concat("flags"))
+    assert sum(len(sc.meshes) - 1 for sc in batch.scenes) > 0, "the seed must give some boxes"
+    oracles = [make_pair(sc, cfg, gpu=False)[1] for sc in batch.scenes]
+    off = g.scene_offsets()
+    for f in range(30):
+        g.step(1.0 / 60.0, 10, 1)
+        x, q = g.get_positions(), g.get_body_q()
+        for s, orc in enumerate(oracles):
+            orc.step(1.0 / 60.0, 10, 1)
+            assert_bitexact(x[off[s]:off[s + 1]], orc.get_positions(), f"scene {s} positions frame {f}")
+            assert_bitexact(q[body_scene == s], orc.get_body_q()[1:], f"scene {s} boxes frame {f}")
