@@ -332,21 +332,43 @@ def run_gpu(args):
 
 def measure_batched(args, dev, flush):
     """Batched uneven scenes: 512 piles with log-uniform counts in [1024, 65536] (seed 46),
-    plane + particle-particle contacts, 10 substeps x 1 iteration per frame. "batched" is one
-    solver stepping all scenes (one graph per frame, one launch per kernel for all scenes);
-    "plain" is one solver per scene, each frame stepped scene by scene with the blocking
-    step(), as a reference user drives several scenes. Aggregate particle-substeps/s."""
+    each with 0..16 dynamic boxes (--batched-boxes; half-extents U[0.02, 0.08], seed 46 + s)
+    dropped onto it, plane + particle-particle + box contacts, 10 substeps x 1 iteration per
+    frame. "batched" is one solver stepping all scenes (one graph per frame, one launch per
+    kernel for all scenes, every box assigned to its scene); "plain" is one solver per scene,
+    each frame stepped scene by scene with the blocking step(), as a reference user drives
+    several scenes. Aggregate particle-substeps/s."""
     import torch
     import vkxpbd
     from vkxpbd import scenes
 
-    batch = scenes.batched_piles(args.batched_scenes)
+    if args.batched_boxes > 0:
+        batch = scenes.batched_piles_with_boxes(args.batched_scenes, max_boxes=args.batched_boxes)
+    else:
+        batch = scenes.batched_piles(args.batched_scenes)
     cfg = vkxpbd.SolverConfig()
     batch.apply_config(cfg)
     cfg.device_index = dev.index
     g = vkxpbd.XpbdSolver()
     g.init_batched(cfg, batch.counts)
-    g.finalize_meshes()
+
+    def add_bodies(solver, meshes, bodies, body_scene=None):
+        for (v, t, margin, wt) in meshes:
+            solver.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
+        solver.finalize_meshes()
+        if bodies is not None:
+            solver.set_bodies(bodies.q, bodies.qd, bodies.com, bodies.inertia, bodies.inv_inertia,
+                              bodies.inv_mass, bodies.flags)
+            if body_scene is not None:
+                solver.set_body_scenes(body_scene)
+
+    n_boxes = 0
+    if args.batched_boxes > 0:
+        meshes, bodies, body_scene = scenes.batch_bodies(batch)
+        add_bodies(g, meshes, bodies, body_scene)
+        n_boxes = int((body_scene >= 0).sum())
+    else:
+        g.finalize_meshes()
     g.set_particles(batch.concat("positions"), batch.concat("velocities"), batch.concat("inv_mass"),
                     batch.concat("radii"), batch.concat("flags"))
     frames = args.batched_frames
@@ -393,7 +415,7 @@ def measure_batched(args, dev, flush):
     for sc in batch.scenes:
         s = vkxpbd.XpbdSolver()
         s.init(cfg, sc.n)
-        s.finalize_meshes()
+        add_bodies(s, sc.meshes, sc.bodies)
         s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
         plain.append(s)
     for _ in range(args.warmup):
@@ -408,7 +430,7 @@ def measure_batched(args, dev, flush):
     wall_p = time.perf_counter() - t0
     launches_p = sum(s.get_frame_stats()["kernels_per_frame"] for s in plain)
     del plain
-    return {"workload": "batched_piles", "scenes": len(batch.scenes), "particles": batch.n,
+    return {"workload": "batched_piles", "scenes": len(batch.scenes), "particles": batch.n, "boxes": n_boxes,
             "counts": "log-uniform 1024-65536, seed 46", "frames": frames, "warmup": args.warmup,
             "batched_value": work / dev_b, "batched_wall_value": work / wall_b, "plain_value": work / wall_p,
             "unit": UNIT, "batched_over_plain": (work / wall_b) / (work / wall_p),
@@ -418,7 +440,7 @@ def measure_batched(args, dev, flush):
                               "peak_source": peak_kind},
             "stages": stages,
             "note": "batched_value device-timed (CUDA events); *_wall_value and plain_value host wall clock "
-                    "around stepping; boxes (0-16 per scene) not included"}
+                    "around stepping"}
 
 
 def stage_table(stage_ms, prof_substeps, n, peak):
@@ -672,6 +694,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-scenes", type=int, default=512, help="0 skips the batched-scenes measurement")
     ap.add_argument("--batched-frames", type=int, default=10)
+    ap.add_argument("--batched-boxes", type=int, default=16, help="0..N dynamic boxes per batched scene (0: none)")
     ap.add_argument("--mixed-frames", type=int, default=10, help="0 skips the particles + boxes measurement")
     ap.add_argument("--mixed-preroll", type=int, default=20)
     ap.add_argument("--diff-frames", type=int, default=60, help="0 skips the differentiable rollout measurement")
