@@ -287,7 +287,17 @@ __device__ __forceinline__ TriHit tri_hit(bool wt, v3 p, float eps2, float below
         const v3 diff = vsub(cp, p);
         h.d = vdot(diff, diff);
     } else {
-        h.d = exact_length(vsub(cp, p));
+        // exact_length's squared sum; a triangle whose distance provably reaches `below`
+        // (1.5e-5 relative margin, far above the rounding of the test) cannot change the
+        // traversal state, which acts only on d < below, and skips the refined root
+        const v3 dd = vsub(cp, p);
+        const float sq = __fmaf_rn(dd.z, dd.z, __fmaf_rn(dd.x, dd.x, dd.y * dd.y));
+        const float lim = below * 1.0000153f;
+        if (sq > lim * lim) {
+            h.d = __int_as_float(0x7f800000);  // +inf
+            return h;
+        }
+        h.d = exact_sqrt(sq);
         if (h.d < below) {
             const v3 e0 = vsub(b, a), e1 = vsub(c, a), e2 = vsub(c, b);
             const float e0n = qb.w, e1n = qc.w, e2n = qn.w;
