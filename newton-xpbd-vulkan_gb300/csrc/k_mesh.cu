@@ -213,15 +213,28 @@ __global__ void __launch_bounds__(kCollideThreads, 8) k_collide(int64_t n, const
     if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
 }
 
-void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
-                    const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
-                    uint32_t* ccount, uint32_t* queue, uint32_t* near, DeviceStatus* st) {
+void launch_collide_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                           const int* flags, PlaneParams pl, MeshTables mt, uint32_t* cinfo, uint32_t* ccount,
+                           uint32_t* queue, uint32_t* near) {
     if (n <= 0) return;
     k_collide_triage<<<(int)((n + 255) / 256), 256, 0, s>>>(n, order, x, r, flags, pl, mt, cinfo, ccount, queue,
                                                              near);
+}
+
+void launch_collide_walk(cudaStream_t s, int64_t n, const float4* x, const float* r, PlaneParams pl, MeshTables mt,
+                         int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* queue,
+                         const uint32_t* near, DeviceStatus* st) {
+    if (n <= 0) return;
     const int threads = kCollideThreads;
     const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads, 152 * 8);
     k_collide<<<blocks, threads, 0, s>>>(n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
+}
+
+void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                    const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
+                    uint32_t* ccount, uint32_t* queue, uint32_t* near, DeviceStatus* st) {
+    launch_collide_triage(s, n, order, x, r, flags, pl, mt, cinfo, ccount, queue, near);
+    launch_collide_walk(s, n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
 }
 
 // Triangle data that generate_mesh_contacts.comp:239-251 and :117 recompute on

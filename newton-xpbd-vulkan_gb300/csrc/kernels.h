@@ -173,6 +173,14 @@ void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const
 void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                     const int* flags, PlaneParams pl, MeshTables mt, int slot_cap, uint32_t* cinfo, float4* cslot,
                     uint32_t* ccount, uint32_t* queue, uint32_t* near, DeviceStatus* st);
+// the two halves of launch_collide: the triage (reads `order`, writes the near list and the
+// contact words of the particles it settles) and the traversal of the near list
+void launch_collide_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                           const int* flags, PlaneParams pl, MeshTables mt, uint32_t* cinfo, uint32_t* ccount,
+                           uint32_t* queue, uint32_t* near);
+void launch_collide_walk(cudaStream_t s, int64_t n, const float4* x, const float* r, PlaneParams pl, MeshTables mt,
+                         int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* queue,
+                         const uint32_t* near, DeviceStatus* st);
 // per-leaf-slot triangle cache for the slots [first, first + count)
 void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
                       const float* verts, float4* cache);

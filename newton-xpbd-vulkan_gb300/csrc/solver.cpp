@@ -68,6 +68,9 @@ Solver::~Solver() {
     clear_graphs();
     if (pinned_) cudaFreeHost(pinned_);
     if (stream_) cudaStreamDestroy(stream_);
+    if (aux_) cudaStreamDestroy(aux_);
+    if (fork_) cudaEventDestroy(fork_);
+    if (join_) cudaEventDestroy(join_);
 }
 
 void Solver::require_init() const {
@@ -111,6 +114,9 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     if (device_ >= ndev) throw std::runtime_error("device_index out of range");
     XPBD_CUDA(cudaSetDevice(device_));
     XPBD_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    XPBD_CUDA(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+    XPBD_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    XPBD_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
 
     for (int p = 0; p < 2; p++) {
         x_[p].alloc(n_);
@@ -933,9 +939,25 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         count_kernel(2);
         prof_mark(P_BODY_CONTACT);
     }
+    // Without dynamic bodies the traversal of the near list forks onto the second stream
+    // once the triage has read the previous order (which the sort below overwrites); the
+    // integrate / sort / gather chain reads neither contacts nor their counters, and the
+    // join comes before the first reader of contacts. Profiling keeps one stream so that
+    // each stage's events bracket its own kernels.
+    const bool fork = mesh_pass && !bodies && !profiling_;
     if (mesh_pass) {
-        launch_collide(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mesh_tables(),
-                       slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_, near_.p, st);
+        const MeshTables mt = mesh_tables();
+        launch_collide_triage(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mt,
+                              cinfo_.p, ccount, sort_scratch_.p + cq_off_, near_.p);
+        cudaStream_t ws = stream_;
+        if (fork) {
+            XPBD_CUDA(cudaEventRecord(fork_, stream_));
+            XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+            ws = aux_;
+        }
+        launch_collide_walk(ws, n, x_[src].p, r_.p, pl, mt, slot_cap_, cinfo_.p, cslot_.p, ccount,
+                            sort_scratch_.p + cq_off_, near_.p, st);
+        if (fork) XPBD_CUDA(cudaEventRecord(join_, aux_));
         count_kernel(2);  // triage + traversal
         prof_mark(P_CONTACT);
     }
@@ -999,6 +1021,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const uint32_t* sids = vin;
     const uint32_t* info = injected_ && !gen ? inj_info_.p : cinfo_.p;
     const float4* slots = injected_ && !gen ? inj_slot_.p : cslot_.p;
+    launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
+                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
+    count_kernel();
+    prof_mark(P_CELLS);
+    if (fork) XPBD_CUDA(cudaStreamWaitEvent(stream_, join_, 0));  // contacts complete
     ContactRanks cr{nullptr, nullptr};
     if (gen && need_ranks_) {
         launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, nullptr, st);
@@ -1007,10 +1034,6 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         cr.rank = rank_.p;
         cr.totals = totals_.p;
     }
-    launch_cells_gather(stream_, n, skeys, sids, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pp, table_.p,
-                        stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
-    count_kernel();
-    prof_mark(P_CELLS);
     SolveDiag dg{nullptr, nullptr, nullptr, 0};
     if (cfg_.enable_diagnostics) {
         dg.delta_out = delta_.p;

@@ -216,6 +216,10 @@ class Solver {
     int64_t contact_max_ = 0;
     int contact_count_ = 0;
     cudaStream_t stream_ = nullptr;
+    // second stream of the frame graph: the mesh traversal runs on it beside the
+    // integrate / sort / gather chain, which does not read contacts
+    cudaStream_t aux_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
 
     std::vector<MeshData> meshes_;
     std::vector<size_t> vert_offsets_, node_offsets_, prim_offsets_;
