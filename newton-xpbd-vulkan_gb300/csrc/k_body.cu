@@ -659,14 +659,25 @@ __global__ void __launch_bounds__(32 * kPosedWarps) k_collide_posed(
     if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
 }
 
+void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                         const int* flags, MeshTables mt, RigidTables rt, uint32_t* counter, uint32_t* list) {
+    if (n <= 0 || rt.n_dyn <= 0) return;
+    k_posed_triage<<<(int)((n + 127) / 128), 128, 0, s>>>(n, order, x, r, flags, mt, rt, counter, list);
+}
+
+void launch_posed_queries(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
+                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* counter,
+                          uint32_t* list, DeviceStatus* st) {
+    if (n <= 0 || rt.n_dyn <= 0) return;
+    k_collide_posed<<<(int)((n + 32 * kPosedWarps - 1) / (32 * kPosedWarps)), 32 * kPosedWarps, 0, s>>>(
+        list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+}
+
 void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                           const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
                           float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st) {
-    if (n <= 0 || rt.n_dyn <= 0) return;
-    const int blocks = (int)((n + 127) / 128);
-    k_posed_triage<<<blocks, 128, 0, s>>>(n, order, x, r, flags, mt, rt, counter, list);
-    k_collide_posed<<<(int)((n + 32 * kPosedWarps - 1) / (32 * kPosedWarps)), 32 * kPosedWarps, 0, s>>>(
-        list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+    launch_posed_triage(s, n, order, x, r, flags, mt, rt, counter, list);
+    launch_posed_queries(s, n, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, counter, list, st);
 }
 
 // ---------------------------------------------------------------- body-delta entries ----

@@ -289,6 +289,13 @@ void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTa
 void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                           const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
                           float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st);
+// its two halves: the triage (reads `order`, lists the particles near a moving mesh) and
+// the queries of the listed particles
+void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
+                         const int* flags, MeshTables mt, RigidTables rt, uint32_t* counter, uint32_t* list);
+void launch_posed_queries(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
+                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* counter,
+                          uint32_t* list, DeviceStatus* st);
 // body-delta entries: key = body of each dynamic slot at position rank[i].x + j, digit histograms
 void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank,
                      uint32_t cap, const SortPlan& sp, uint32_t* keys, uint32_t* hist, DeviceStatus* st);

@@ -939,47 +939,58 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         count_kernel(2);
         prof_mark(P_BODY_CONTACT);
     }
-    // Without dynamic bodies the traversal of the near list forks onto the second stream
-    // once the triage has read the previous order (which the sort below overwrites); the
-    // integrate / sort / gather chain reads neither contacts nor their counters, and the
-    // join comes before the first reader of contacts. Profiling keeps one stream so that
-    // each stage's events bracket its own kernels.
-    const bool fork = mesh_pass && !bodies && !profiling_;
+    // Contact generation forks onto the second stream once the triages have read the
+    // previous order (which the sort below overwrites): the static-mesh traversal, then the
+    // moving-mesh queries, rigid contacts and body-delta entries. The integrate / sort /
+    // gather chain reads none of their outputs (nor the body poses they read before the
+    // bodies integrate), and the join comes before the body integration and the first
+    // reader of contacts. Profiling keeps one stream in the original order so that each
+    // stage's events bracket its own kernels.
+    const bool fork = mesh_pass && !profiling_;
+    const MeshTables mt = mesh_tables();
+    const uint32_t* prev_order = pair_v_[(plan_.passes - 1) & 1].p;
+    uint32_t* posed_counter = sort_scratch_.p + cq_off_ + 2;
+    cudaStream_t cs = stream_;
+    if (fork) {
+        launch_collide_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, pl, mt, cinfo_.p, ccount,
+                              sort_scratch_.p + cq_off_, near_.p);
+        if (bodies)
+            launch_posed_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, mt, rt, posed_counter,
+                                posed_list_.p);
+        XPBD_CUDA(cudaEventRecord(fork_, stream_));
+        XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+        cs = aux_;
+    }
     if (mesh_pass) {
-        const MeshTables mt = mesh_tables();
-        launch_collide_triage(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p, pl, mt,
-                              cinfo_.p, ccount, sort_scratch_.p + cq_off_, near_.p);
-        cudaStream_t ws = stream_;
-        if (fork) {
-            XPBD_CUDA(cudaEventRecord(fork_, stream_));
-            XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
-            ws = aux_;
-        }
-        launch_collide_walk(ws, n, x_[src].p, r_.p, pl, mt, slot_cap_, cinfo_.p, cslot_.p, ccount,
+        if (!fork)
+            launch_collide_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, pl, mt, cinfo_.p, ccount,
+                                  sort_scratch_.p + cq_off_, near_.p);
+        launch_collide_walk(cs, n, x_[src].p, r_.p, pl, mt, slot_cap_, cinfo_.p, cslot_.p, ccount,
                             sort_scratch_.p + cq_off_, near_.p, st);
-        if (fork) XPBD_CUDA(cudaEventRecord(join_, aux_));
         count_kernel(2);  // triage + traversal
         prof_mark(P_CONTACT);
     }
     if (bodies) {
-        launch_collide_posed(stream_, n, pair_v_[(plan_.passes - 1) & 1].p, x_[src].p, r_.p, flags_.p,
-                             mesh_tables(), rt, slot_cap_, cinfo_.p, cslot_.p, ccount, sort_scratch_.p + cq_off_ + 2,
+        if (!fork)
+            launch_posed_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, mt, rt, posed_counter,
+                                posed_list_.p);
+        launch_posed_queries(cs, n, x_[src].p, r_.p, mt, rt, slot_cap_, cinfo_.p, cslot_.p, ccount, posed_counter,
                              posed_list_.p, st);
         count_kernel(2);  // triage + queries
         prof_mark(P_POSED);
-        launch_rigid_contacts(stream_, ba, rt, mesh_tables(), rp, st);
+        launch_rigid_contacts(cs, ba, rt, mt, rp, st);
         count_kernel();
         prof_mark(P_RIGID);
         // body-delta entries: dynamic slots in contact order, grouped by body (stable sort)
-        launch_dyn_scan(stream_, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
-        launch_dyn_emit(stream_, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
+        launch_dyn_scan(cs, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
+        launch_dyn_emit(cs, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
                         esort_scratch_.p + ehist_off_, st);
         count_kernel(4);
         const uint32_t* ek = ekeys_.p;
         const uint32_t* ev = nullptr;
         const size_t elbw = sort_lookback_words(eplan_);
         for (int p = 0; p < eplan_.passes; p++) {
-            launch_onesweep_pass(stream_, (int64_t)entry_cap_, eplan_, p, ek, ev, epk_[p & 1].p, epv_[p & 1].p,
+            launch_onesweep_pass(cs, (int64_t)entry_cap_, eplan_, p, ek, ev, epk_[p & 1].p, epv_[p & 1].p,
                                  esort_scratch_.p + ehist_off_ + ((size_t)p << eplan_.bits),
                                  esort_scratch_.p + elb_off_ + (size_t)p * elbw, esort_scratch_.p + etc_off_ + p, st,
                                  dyn_totals_.p);
@@ -987,22 +998,18 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
             ek = epk_[p & 1].p;
             ev = epv_[p & 1].p;
         }
-        launch_body_segments(stream_, entry_cap_, dyn_totals_.p, ek, seg_.p);
+        launch_body_segments(cs, entry_cap_, dyn_totals_.p, ek, seg_.p);
         count_kernel();
         sorted_entries_ = ev;
         prof_mark(P_BODY_ENTRIES);
     }
+    if (fork) XPBD_CUDA(cudaEventRecord(join_, aux_));
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pscene_.p, pp, pl, keys_.p, plan_,
                         sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
-    if (bodies) {
-        launch_body_integrate(stream_, ba, body_q_prev_.p, body_qd_prev_.p, rp);
-        count_kernel();
-        prof_mark(P_BODY_INTEGRATE);
-    }
     const uint32_t* kin = keys_.p;
     const uint32_t* vin = nullptr;
     const size_t lbw = sort_lookback_words(plan_);
@@ -1026,6 +1033,11 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     count_kernel();
     prof_mark(P_CELLS);
     if (fork) XPBD_CUDA(cudaStreamWaitEvent(stream_, join_, 0));  // contacts complete
+    if (bodies) {  // after every reader of the substep-start poses
+        launch_body_integrate(stream_, ba, body_q_prev_.p, body_qd_prev_.p, rp);
+        count_kernel();
+        prof_mark(P_BODY_INTEGRATE);
+    }
     ContactRanks cr{nullptr, nullptr};
     if (gen && need_ranks_) {
         launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, nullptr, st);
