@@ -79,7 +79,105 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
     }
 }
 
-template <bool LAST, bool ALL_ACTIVE, bool DIAG>
+// The particle-particle part of one particle's iteration (solve_particle_particle_contacts.comp:
+// 116-217 and the relaxation of apply_particle_deltas.comp): the candidate filter (:145-157)
+// runs first and buffers accepted neighbours; the pair math then runs over the buffer in
+// candidate order, so lanes stay in step. Returns the relaxed total delta.
+template <bool ALL_ACTIVE, bool DIAG>
+__device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1, uint32_t id,
+                                       const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                       const int* __restrict__ rf, const int4* __restrict__ table, uint32_t stamp,
+                                       const uint32_t* __restrict__ sids, const SolveParams& sp, const SolveDiag& dg,
+                                       int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
+    const int is_proxy = pflag & 2;
+    const float R = radius + sp.max_radius + sp.k_coh;
+    const float inv = sp.inv;
+    const int32_t xs = f2i(floorf((xp.x - R) * inv)), ys = f2i(floorf((xp.y - R) * inv)),
+                  zs = f2i(floorf((xp.z - R) * inv));
+    const int32_t xe = min(f2i(floorf((xp.x + R) * inv)), xs + kGridDim - 1);
+    const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
+    const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
+    v3 acc = mk3(0.0f, 0.0f, 0.0f);
+    int np = 0;
+    // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
+    // or is clamped at 0; their particles then form one run of the sorted order, in the
+    // reference's visit order (x ascending, then sorted order within a cell)
+    const int32_t xo = xs + kGridOrigin;
+    const bool row_run = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
+    for (int32_t cz = zs; cz <= ze; cz++) {
+        for (int32_t cy = ys; cy <= ye; cy++) {
+            for (int32_t cx = xs; cx <= xe; cx++) {
+                int lo, hi;
+                if (row_run) {
+                    const int c0 = cell_index(xs, cy, cz);
+                    lo = 0x7fffffff;
+                    hi = -1;
+                    for (int j = 0; j <= xe - xs; j++) {
+                        const int4 e = __ldg(&table[c0 + j]);
+                        if ((uint32_t)e.z == stamp) {
+                            lo = min(lo, e.x);
+                            hi = max(hi, e.y);
+                        }
+                    }
+                    cx = xe;  // the run covers the whole row
+                } else {
+                    const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                    if ((uint32_t)e.z != stamp) continue;
+                    lo = e.x;
+                    hi = e.y;
+                }
+                // candidates in groups of 4: the group's records are loaded together,
+                // then tested one by one in order
+                for (int kk0 = lo; kk0 < hi; kk0 += 4) {
+                    float4 nxs[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        nxs[u] = kk0 + u < hi ? __ldg(&rx[kk0 + u]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int kk = kk0 + u;
+                        if (kk >= hi) break;
+                        if (kk == k) continue;
+                        const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
+                        if ((nflag & 1) == 0) continue;
+                        if (!ALL_ACTIVE && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
+                            continue;
+                        const float4 nx = nxs[u];
+                        const v3 raw = vsub(xp, xyz(nx));
+                        if (fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R) continue;
+                        // exact_length's squared sum; a candidate whose distance provably exceeds
+                        // r_i + r_j + cohesion (1.5e-5 relative margin, far above the rounding of
+                        // the filter) is rejected before the refined square root
+                        const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
+                        const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
+                        if (sq > reach * reach) continue;
+                        const float d = exact_sqrt(sq);
+                        const float err = d - radius - nx.w;
+                        if (err > sp.k_coh || d <= 0.0f) continue;
+                        s_kk[np][threadIdx.x] = kk;
+                        s_d[np][threadIdx.x] = d;
+                        if (++np == kPairCap) {
+                            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+                            np = 0;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+    const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
+    return mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f), __fmaf_rn(dw.z, sp.relax, 0.0f));
+}
+
+// Fused XPBD iteration of one particle in sorted order. PP selects how the
+// particle-particle total is obtained: kPPFused computes it here; kPPOnly computes only it
+// and writes it to pp[k] (no other output; run beside the contact generation, which it
+// does not read); kPPApply reads it from pp[k] and does the rest. Both ways add the same
+// total to the shape deltas in the same order.
+enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
+
+template <bool LAST, bool ALL_ACTIVE, bool DIAG, int PP>
 __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     int64_t n, const uint32_t* __restrict__ sids, const uint32_t* __restrict__ skeys, const float4* __restrict__ rx,
     const float4* __restrict__ rv, const int* __restrict__ rf, const int4* __restrict__ table_all,
@@ -87,19 +185,26 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     const float4* __restrict__ x0a, const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo,
     const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ rx_out,
     float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg,
-    BodyDeltaOut bo) {
-    __shared__ int s_kk[kPairCap][kSolveThreads];
-    __shared__ float s_d[kPairCap][kSolveThreads];
+    BodyDeltaOut bo, float4* __restrict__ pp) {
+    __shared__ int s_kk[PP == kPPApply ? 1 : kPairCap][kSolveThreads];
+    __shared__ float s_d[PP == kPPApply ? 1 : kPairCap][kSolveThreads];
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const uint32_t stamp = *stamp_p;
     const uint32_t id = sids[k];
-    // this particle's scene table (scene-major keys); one scene: the whole table
-    const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
     const float4 ox = rx[k], ov = rv[k];
     const int pflag = ALL_ACTIVE ? 1 : rf[k];
     const v3 xp = xyz(ox), vp = xyz(ov);
     const float radius = ox.w, w1 = ov.w;
+    if constexpr (PP == kPPOnly) {
+        v3 total = mk3(0.0f, 0.0f, 0.0f);
+        if (pflag & 1) {
+            const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, *stamp_p, sids,
+                                               sp, dg, s_kk, s_d);
+        }
+        pp[k] = make_float4(total.x, total.y, total.z, 0.0f);
+        return;
+    }
     v3 x_new = xp, v_new = vp;
     v3 delta = mk3(0.0f, 0.0f, 0.0f);
 
@@ -134,89 +239,15 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
                 }
             }
         }
-        // particle-particle contacts (solve_particle_particle_contacts.comp:116-217): the
-        // candidate filter (:145-157) runs first and buffers accepted neighbours; the pair
-        // math then runs over the buffer in candidate order, so lanes stay in step
-        const int is_proxy = pflag & 2;
-        const float R = radius + sp.max_radius + sp.k_coh;
-        const float inv = sp.inv;
-        const int32_t xs = f2i(floorf((xp.x - R) * inv)), ys = f2i(floorf((xp.y - R) * inv)),
-                      zs = f2i(floorf((xp.z - R) * inv));
-        const int32_t xe = min(f2i(floorf((xp.x + R) * inv)), xs + kGridDim - 1);
-        const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
-        const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
-        v3 acc = mk3(0.0f, 0.0f, 0.0f);
-        int np = 0;
-        // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
-        // or is clamped at 0; their particles then form one run of the sorted order, in the
-        // reference's visit order (x ascending, then sorted order within a cell)
-        const int32_t xo = xs + kGridOrigin;
-        const bool row_run = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
-        for (int32_t cz = zs; cz <= ze; cz++) {
-            for (int32_t cy = ys; cy <= ye; cy++) {
-                for (int32_t cx = xs; cx <= xe; cx++) {
-                    int lo, hi;
-                    if (row_run) {
-                        const int c0 = cell_index(xs, cy, cz);
-                        lo = 0x7fffffff;
-                        hi = -1;
-                        for (int j = 0; j <= xe - xs; j++) {
-                            const int4 e = __ldg(&table[c0 + j]);
-                            if ((uint32_t)e.z == stamp) {
-                                lo = min(lo, e.x);
-                                hi = max(hi, e.y);
-                            }
-                        }
-                        cx = xe;  // the run covers the whole row
-                    } else {
-                        const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
-                        if ((uint32_t)e.z != stamp) continue;
-                        lo = e.x;
-                        hi = e.y;
-                    }
-                    // candidates in groups of 4: the group's records are loaded together,
-                    // then tested one by one in order
-                    for (int kk0 = lo; kk0 < hi; kk0 += 4) {
-                        float4 nxs[4];
-#pragma unroll
-                        for (int u = 0; u < 4; u++)
-                            nxs[u] = kk0 + u < hi ? __ldg(&rx[kk0 + u]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                        const int kk = kk0 + u;
-                        if (kk >= hi) break;
-                        if (kk == k) continue;
-                        const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
-                        if ((nflag & 1) == 0) continue;
-                        if (!ALL_ACTIVE && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
-                            continue;
-                        const float4 nx = nxs[u];
-                        const v3 raw = vsub(xp, xyz(nx));
-                        if (fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R) continue;
-                        // exact_length's squared sum; a candidate whose distance provably exceeds
-                        // r_i + r_j + cohesion (1.5e-5 relative margin, far above the rounding of
-                        // the filter) is rejected before the refined square root
-                        const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
-                        const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
-                        if (sq > reach * reach) continue;
-                        const float d = exact_sqrt(sq);
-                        const float err = d - radius - nx.w;
-                        if (err > sp.k_coh || d <= 0.0f) continue;
-                        s_kk[np][threadIdx.x] = kk;
-                        s_d[np][threadIdx.x] = d;
-                        if (++np == kPairCap) {
-                            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
-                            np = 0;
-                        }
-                        }
-                    }
-                }
-            }
+        v3 total;
+        if constexpr (PP == kPPApply) {
+            total = xyz(pp[k]);
+        } else {
+            // this particle's scene table (scene-major keys); one scene: the whole table
+            const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, *stamp_p, sids,
+                                               sp, dg, s_kk, s_d);
         }
-        pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
-        const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
-        const v3 total = mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f),
-                             __fmaf_rn(dw.z, sp.relax, 0.0f));
         delta = vadd(delta, total);
         // apply_particle_deltas.comp:43-54
         x_new = vadd(xp, delta);
@@ -295,25 +326,33 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
                   const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr,
                   BodyTables bt, SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out,
-                  SolveDiag dg, BodyDeltaOut bo) {
+                  SolveDiag dg, BodyDeltaOut bo, int pp_mode, float4* pp) {
     if (n <= 0) return;
     const int threads = kSolveThreads;
     const int blocks = (int)((n + threads - 1) / threads);
     const bool diag = dg.pair_header != nullptr;
-#define XPBD_SOLVE(L, A, D)                                                                                         \
-    if (last == L && all_active == A && diag == D) {                                                                \
-        k_solve<L, A, D><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo, cslot, \
-                                                    cr, bt, sp, rx_out, rv_out, x_out, v_out, dg, bo);              \
+#define XPBD_SOLVE(L, A, D, P)                                                                                     \
+    if (last == L && all_active == A && diag == D && pp_mode == P) {                                              \
+        k_solve<L, A, D, P><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo,   \
+                                                       cslot, cr, bt, sp, rx_out, rv_out, x_out, v_out, dg, bo, pp); \
         return;                                                                                                     \
     }
-    XPBD_SOLVE(true, true, false)
-    XPBD_SOLVE(true, false, false)
-    XPBD_SOLVE(false, true, false)
-    XPBD_SOLVE(false, false, false)
-    XPBD_SOLVE(true, true, true)
-    XPBD_SOLVE(true, false, true)
-    XPBD_SOLVE(false, true, true)
-    XPBD_SOLVE(false, false, true)
+    XPBD_SOLVE(true, true, false, kPPFused)
+    XPBD_SOLVE(true, false, false, kPPFused)
+    XPBD_SOLVE(false, true, false, kPPFused)
+    XPBD_SOLVE(false, false, false, kPPFused)
+    XPBD_SOLVE(true, true, true, kPPFused)
+    XPBD_SOLVE(true, false, true, kPPFused)
+    XPBD_SOLVE(false, true, true, kPPFused)
+    XPBD_SOLVE(false, false, true, kPPFused)
+    // the split (no diagnostics): the particle-particle part alone, then the rest
+    if (pp_mode == kPPOnly) last = false;  // writes pp only
+    XPBD_SOLVE(false, true, false, kPPOnly)
+    XPBD_SOLVE(false, false, false, kPPOnly)
+    XPBD_SOLVE(true, true, false, kPPApply)
+    XPBD_SOLVE(true, false, false, kPPApply)
+    XPBD_SOLVE(false, true, false, kPPApply)
+    XPBD_SOLVE(false, false, false, kPPApply)
 #undef XPBD_SOLVE
 }
 

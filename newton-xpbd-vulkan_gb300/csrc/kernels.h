@@ -187,13 +187,15 @@ void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32
 void launch_iota(cudaStream_t s, int64_t n, uint32_t* out);
 // fused shape solve + particle-particle solve + apply (+ restitution on the last iteration)
 // skeys (sorted keys) is passed for batched scenes so that each particle looks up its own
-// scene's table; null for one scene
+// scene's table; null for one scene. pp_mode 1 computes only the particle-particle totals
+// (pp[k], sorted order; reads no contact), pp_mode 2 is the rest of the iteration taking
+// its totals from pp; 0 does both (required with diagnostics)
 void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const uint32_t* skeys,
                   const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
                   const float4* x0,
                   const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
                   SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg,
-                  BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr});
+                  BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr}, int pp_mode = 0, float4* pp = nullptr);
 // restitution (apply_particle_shape_restitution.comp) after the body passes of the last
 // iteration, scattering the sorted final state to particle order
 void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const float4* rx, const float4* rv,

@@ -71,6 +71,9 @@ Solver::~Solver() {
     if (aux_) cudaStreamDestroy(aux_);
     if (fork_) cudaEventDestroy(fork_);
     if (join_) cudaEventDestroy(join_);
+    for (auto& e : split_ev_)
+        for (auto& x : e)
+            if (x) cudaEventDestroy(x);
 }
 
 void Solver::require_init() const {
@@ -85,6 +88,8 @@ void Solver::clear_graphs() {
     }
     graphs_.clear();
     clear_backward_graphs();
+    split_choice_ = -1;
+    split_trials_ = 0;
 }
 
 void Solver::clear_backward_graphs() {
@@ -124,6 +129,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
         rx_[p].alloc(n_);
         rv_[p].alloc(n_);
     }
+    pp_.alloc(n_);
     w_.alloc(n_);
     r_.alloc(n_);
     flags_.alloc(n_);
@@ -1032,6 +1038,24 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
                         stamp_.p, rx_[0].p, rv_[0].p, rf_.p);
     count_kernel();
     prof_mark(P_CELLS);
+    SolveDiag dg{nullptr, nullptr, nullptr, 0};
+    if (cfg_.enable_diagnostics) {
+        dg.delta_out = delta_.p;
+        dg.pair_header = diag_header_.p;
+        dg.pairs = diag_pairs_.p;
+        dg.max_pairs = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
+    }
+    const BodyTables bt = body_tables();
+    const BodyDeltaOut bo{bodies ? bdel_.p : nullptr, bodies ? dyn_rank_.p : nullptr};
+    // the first iteration's particle-particle part reads no contact: it runs before the join
+    const bool split = fork && split_now_ && iterations > 0 && !cfg_.enable_diagnostics;
+    if (split) {
+        launch_solve(stream_, n, false, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[0].p, rv_[0].p, rf_.p,
+                     table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, ContactRanks{nullptr, nullptr}, bt,
+                     solve_params(sdt, 0), nullptr, nullptr, nullptr, nullptr, dg, BodyDeltaOut{nullptr, nullptr}, 1,
+                     pp_.p);
+        count_kernel();
+    }
     if (fork) XPBD_CUDA(cudaStreamWaitEvent(stream_, join_, 0));  // contacts complete
     if (bodies) {  // after every reader of the substep-start poses
         launch_body_integrate(stream_, ba, body_q_prev_.p, body_qd_prev_.p, rp);
@@ -1046,21 +1070,13 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         cr.rank = rank_.p;
         cr.totals = totals_.p;
     }
-    SolveDiag dg{nullptr, nullptr, nullptr, 0};
-    if (cfg_.enable_diagnostics) {
-        dg.delta_out = delta_.p;
-        dg.pair_header = diag_header_.p;
-        dg.pairs = diag_pairs_.p;
-        dg.max_pairs = cfg_.max_diag_pairs ? cfg_.max_diag_pairs : 100000u;
-    }
-    const BodyTables bt = body_tables();
-    const BodyDeltaOut bo{bodies ? bdel_.p : nullptr, bodies ? dyn_rank_.p : nullptr};
     for (int it = 0; it < iterations; it++) {
         // with dynamic bodies the restitution waits for the last body pass
         const bool last = it == iterations - 1 && !bodies;
         launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p,
                      rv_[it & 1].p, rf_.p, table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, cr, bt,
-                     solve_params(sdt, it), rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo);
+                     solve_params(sdt, it), rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo,
+                     split && it == 0 ? 2 : 0, pp_.p);
         count_kernel();
         prof_mark(P_SOLVE);
         if (bodies) {
@@ -1109,7 +1125,16 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
         contact_count_ = cc;
     }
     auto t0 = std::chrono::high_resolution_clock::now();
-    GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0};
+    const bool split_ok = mode == Mode::Step && !meshes_.empty() && !profiling_ && iterations > 0 &&
+                          !cfg_.enable_diagnostics;
+    int trial = -1;
+    if (split_ok && split_choice_ < 0) {
+        trial = split_trials_++;
+        split_now_ = (trial & 1) != 0;
+    } else {
+        split_now_ = split_ok && split_choice_ == 1;
+    }
+    GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0, split_now_ ? 1 : 0};
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         FrameGraph fg;
@@ -1130,7 +1155,25 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
         cudaGraphDestroy(g);
         it = graphs_.emplace(key, std::move(fg)).first;
     }
+    if (trial >= 0) {
+        for (auto& x : split_ev_[trial])
+            if (!x) XPBD_CUDA(cudaEventCreate(&x));
+        XPBD_CUDA(cudaEventRecord(split_ev_[trial][0], stream_));
+    }
     XPBD_CUDA(cudaGraphLaunch(it->second.exec, stream_));
+    if (trial >= 0) {
+        XPBD_CUDA(cudaEventRecord(split_ev_[trial][1], stream_));
+        if (trial == kSplitTrials - 1) {  // both ways timed: keep the faster (first use of each skipped)
+            XPBD_CUDA(cudaEventSynchronize(split_ev_[trial][1]));
+            float best[2] = {3.0e38f, 3.0e38f};
+            for (int t = 2; t < kSplitTrials; t++) {
+                float ms = 0.0f;
+                XPBD_CUDA(cudaEventElapsedTime(&ms, split_ev_[t][0], split_ev_[t][1]));
+                best[t & 1] = std::min(best[t & 1], ms);
+            }
+            split_choice_ = best[1] < best[0] ? 1 : 0;
+        }
+    }
     if (recorder_.active()) {  // this frame's positions to the writer thread (after the graph)
         launch_unpack_xyz(stream_, (int64_t)n_, x_[cur_ ^ (substeps & 1)].p, rec_stage_.p);
         recorder_.enqueue(stream_, rec_stage_.p);
@@ -1712,6 +1755,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     // table and sorted records rebuilt from the stored sort); captured once per segment
     // length and step, replayed for every segment
     const PredictParams pp = predict_params(sdt);
+    split_now_ = false;  // the replayed substeps keep the fused solve
     auto segment = [&](int S) {
         int src = 0;
         const int fin = (plan_.passes - 1) & 1;

@@ -169,10 +169,10 @@ class Solver {
     enum class Mode { Step, SolveOnly };
     struct GraphKey {
         uint32_t dt_bits;
-        int substeps, iterations, parity, mode, timed;
+        int substeps, iterations, parity, mode, timed, split;
         bool operator<(const GraphKey& o) const {
-            return std::tie(dt_bits, substeps, iterations, parity, mode, timed) <
-                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode, o.timed);
+            return std::tie(dt_bits, substeps, iterations, parity, mode, timed, split) <
+                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode, o.timed, o.split);
         }
     };
     struct FrameGraph {
@@ -220,6 +220,16 @@ class Solver {
     // integrate / sort / gather chain, which does not read contacts
     cudaStream_t aux_ = nullptr;
     cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    // Whether the first iteration's particle-particle part runs before the join, beside the
+    // contact generation (split) or after it, fused with the rest (the faster depends on how
+    // long the contact chain is next to the sort and the solve): -1 undecided, in which case
+    // the next kSplitTrials frames alternate both ways under events and the faster is kept
+    // until the graphs are rebuilt. Results are the same either way.
+    static constexpr int kSplitTrials = 6;
+    int split_choice_ = -1;
+    int split_trials_ = 0;
+    bool split_now_ = false;
+    cudaEvent_t split_ev_[kSplitTrials][2] = {};
 
     std::vector<MeshData> meshes_;
     std::vector<size_t> vert_offsets_, node_offsets_, prim_offsets_;
@@ -243,6 +253,7 @@ class Solver {
     DevBuf<int4> table_;
     DevBuf<uint32_t> stamp_;
     DevBuf<float4> rx_[2], rv_[2];
+    DevBuf<float4> pp_;  // first iteration's particle-particle totals (sorted order) when split
     DevBuf<int> rf_;
     // contacts
     int slot_cap_ = 1;
