@@ -83,7 +83,7 @@ __device__ __forceinline__ void for_cells(v3 x, float R, float inv, const int4* 
     for (int32_t cz = zs; cz <= ze; cz++)
         for (int32_t cy = ys; cy <= ye; cy++)
             for (int32_t cx = xs; cx <= xe; cx++) {
-                const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                const int4 e = __ldg(&table[cell_index(cx, cy, cz, true)]);  // one scene: split keys
                 if ((uint32_t)e.z != stamp) continue;
                 for (int kk = e.x; kk < e.y; kk++) f(kk);
             }

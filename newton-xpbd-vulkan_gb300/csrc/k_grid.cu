@@ -40,8 +40,8 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
             const int fl = flags[i];
             v3 xp, vp;
             predict(xf, v[i], w[i], fl, pp, xp, vp);
-            key = hash_grid_index(xp, pp.inv);
-            if (pscene) key |= pscene[i] << 21;  // scene-major key = entry of the scene's table
+            // one scene: split key; batched: scene-major key = entry of the scene's table
+            key = pscene ? (hash_grid_index(xp, pp.inv, false) | (pscene[i] << 21)) : hash_grid_index(xp, pp.inv, true);
             keys[i] = key;
             if (cinfo) {  // generate_plane_contacts.comp:32-38 on the pre-integration position
                 uint32_t info = 0;
@@ -77,6 +77,51 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
     size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
     k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pscene, pp, pl, keys, sp.bits, sp.passes, hist,
                                             cinfo, ccount, stamp);
+}
+
+// out[i] = keys[i] & mask and the digit histograms of every pass (the reference-layout view
+// of split keys, sorted on demand for the sorted-order getters)
+__global__ void __launch_bounds__(256) k_mask_keys(int64_t n, const uint32_t* __restrict__ keys, uint32_t mask,
+                                                   uint32_t* __restrict__ out, int bits, int passes,
+                                                   uint32_t* __restrict__ hist) {
+    extern __shared__ uint32_t s_hist[];  // passes << bits
+    const int bins = 1 << bits;
+    for (int i = threadIdx.x; i < passes * bins; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t key = keys[i] & mask;
+        out[i] = key;
+        for (int p = 0; p < passes; p++) atomicAdd(&s_hist[p * bins + ((key >> (p * bits)) & (uint32_t)(bins - 1))], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * bins; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+void launch_mask_keys(cudaStream_t s, int64_t n, const uint32_t* keys, uint32_t mask, uint32_t* out,
+                      const SortPlan& sp, uint32_t* hist) {
+    if (n <= 0) return;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    k_mask_keys<<<blocks, 256, sizeof(uint32_t) * ((size_t)sp.passes << sp.bits), s>>>(n, keys, mask, out, sp.bits,
+                                                                                      sp.passes, hist);
+}
+
+// grid_offsets.comp:16-34 over sorted keys of the reference layout (starts and ends zeroed
+// first, as the zero fills of scene.cpp:918-922)
+__global__ void k_cell_bounds(int64_t n, const uint32_t* __restrict__ skeys, int32_t* __restrict__ starts,
+                              int32_t* __restrict__ ends) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t c = skeys[t];
+    if (t == 0 || skeys[t - 1] != c) starts[c] = (int32_t)t;
+    if (t == n - 1 || skeys[t + 1] != c) ends[c] = (int32_t)(t + 1);
+}
+
+void launch_cell_bounds(cudaStream_t s, int64_t n, const uint32_t* skeys, int32_t* starts, int32_t* ends) {
+    cudaMemsetAsync(starts, 0, sizeof(int32_t) * kNumCells, s);
+    cudaMemsetAsync(ends, 0, sizeof(int32_t) * kNumCells, s);
+    if (n > 0) k_cell_bounds<<<(int)((n + 255) / 256), 256, 0, s>>>(n, skeys, starts, ends);
 }
 
 // ---------------------------------------------------------------------------

@@ -86,7 +86,8 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
 template <bool ALL_ACTIVE, bool DIAG>
 __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1, uint32_t id,
                                        const float4* __restrict__ rx, const float4* __restrict__ rv,
-                                       const int* __restrict__ rf, const int4* __restrict__ table, uint32_t stamp,
+                                       const int* __restrict__ rf, const int4* __restrict__ table, bool split,
+                                       uint32_t stamp,
                                        const uint32_t* __restrict__ sids, const SolveParams& sp, const SolveDiag& dg,
                                        int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
     const int is_proxy = pflag & 2;
@@ -100,8 +101,9 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
     v3 acc = mk3(0.0f, 0.0f, 0.0f);
     int np = 0;
     // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
-    // or is clamped at 0; their particles then form one run of the sorted order, in the
-    // reference's visit order (x ascending, then sorted order within a cell)
+    // or is clamped at 0 (then the alias bit of x is the same for the whole row); their
+    // particles then form one run of the sorted order, in the reference's visit order (x
+    // ascending, then sorted order within a cell)
     const int32_t xo = xs + kGridOrigin;
     const bool row_run = xo >= 0 && (xo % kGridDim) + (xe - xs) < kGridDim;
     for (int32_t cz = zs; cz <= ze; cz++) {
@@ -109,7 +111,7 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
             for (int32_t cx = xs; cx <= xe; cx++) {
                 int lo, hi;
                 if (row_run) {
-                    const int c0 = cell_index(xs, cy, cz);
+                    const int c0 = cell_index(xs, cy, cz, split);
                     lo = 0x7fffffff;
                     hi = -1;
                     for (int j = 0; j <= xe - xs; j++) {
@@ -121,7 +123,7 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
                     }
                     cx = xe;  // the run covers the whole row
                 } else {
-                    const int4 e = __ldg(&table[cell_index(cx, cy, cz)]);
+                    const int4 e = __ldg(&table[cell_index(cx, cy, cz, split)]);
                     if ((uint32_t)e.z != stamp) continue;
                     lo = e.x;
                     hi = e.y;
@@ -199,8 +201,8 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
         v3 total = mk3(0.0f, 0.0f, 0.0f);
         if (pflag & 1) {
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
-            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, *stamp_p, sids,
-                                               sp, dg, s_kk, s_d);
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, skeys == nullptr,
+                                               *stamp_p, sids, sp, dg, s_kk, s_d);
         }
         pp[k] = make_float4(total.x, total.y, total.z, 0.0f);
         return;
@@ -245,8 +247,8 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
         } else {
             // this particle's scene table (scene-major keys); one scene: the whole table
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
-            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, *stamp_p, sids,
-                                               sp, dg, s_kk, s_d);
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, skeys == nullptr,
+                                               *stamp_p, sids, sp, dg, s_kk, s_d);
         }
         delta = vadd(delta, total);
         // apply_particle_deltas.comp:43-54

@@ -12,6 +12,7 @@ namespace xpbd {
 
 constexpr int kGridDim = 128;                                   // hash grid, src/scene.cpp:17-18
 constexpr int kNumCells = kGridDim * kGridDim * kGridDim;
+constexpr int kSplitKeyBits = 24;  // one scene: the reference's 21-bit key + 3 alias bits
 constexpr int kGridOrigin = 1 << 20;                            // grid_cell_indices.comp:20
 
 // Device-side status word read back after every frame. A kernel that gives
@@ -221,6 +222,11 @@ void launch_contact_compact(cudaStream_t s, int64_t n, const uint32_t* cinfo, co
                             float altitude, int32_t* part, int32_t* shape, float* bpos, float* bvel, float* nrm);
 // reference-layout cell tables from the stamped table (table of one scene)
 void launch_cell_tables(cudaStream_t s, const int4* table, const uint32_t* stamp, int32_t* starts, int32_t* ends);
+// out = keys & mask with the digit histograms of every pass of sp added to hist
+void launch_mask_keys(cudaStream_t s, int64_t n, const uint32_t* keys, uint32_t mask, uint32_t* out,
+                      const SortPlan& sp, uint32_t* hist);
+// per-cell [start, end) of sorted 21-bit keys over the 128^3 cells (0 for empty cells)
+void launch_cell_bounds(cudaStream_t s, int64_t n, const uint32_t* skeys, int32_t* starts, int32_t* ends);
 // stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
 void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,
                        cudaStream_t s);

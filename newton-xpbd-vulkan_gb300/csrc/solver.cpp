@@ -112,6 +112,8 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     contact_max_ = (int64_t)(max_contacts ? max_contacts : num_particles * 2);  // scene.cpp:68
     key_bits_ = 21;
     while (n_scenes > 1 && (size_t(1) << (key_bits_ - 21)) < n_scenes) key_bits_++;
+    split_keys_ = n_scenes == 1;
+    if (split_keys_) key_bits_ = kSplitKeyBits;
     int ndev = 0;
     XPBD_CUDA(cudaGetDeviceCount(&ndev));
     if (ndev == 0) throw std::runtime_error("no CUDA device");
@@ -149,7 +151,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     // digit width 8, 16 keys per thread above 1M particles, 8 below (more tiles per SM);
     // scenes of 1M particles and more are re-tuned on their first step (autotune_sort)
     apply_sort_plan(8, n_ >= (1u << 20) ? 16 : 8);
-    table_.alloc((size_t)n_scenes * kNumCells);
+    table_.alloc(split_keys_ ? (size_t(1) << kSplitKeyBits) : (size_t)n_scenes * kNumCells);
     stamp_.alloc(1);
     cinfo_.alloc(n_);
     near_.alloc(n_, false);
@@ -1430,13 +1432,42 @@ void Solver::get_contacts(int32_t* part, int32_t* shape, float* nrm, float* bpos
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
+// The last sort in the reference's layout: the stable sort of the 21-bit cell keys (the
+// split keys of the last substep, still in keys_ in particle order, with the alias bits
+// cleared) from particle order, as gpu_sort.h sorts them. Its scratch is the substep's,
+// which every substep clears first.
+const uint32_t* Solver::sort_reference_layout(const uint32_t** ids) {
+    if (!ref_k_[0].p)
+        for (int p = 0; p < 2; p++) {
+            ref_k_[p].alloc(n_, false);
+            ref_v_[p].alloc(n_, false);
+        }
+    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
+    launch_mask_keys(stream_, (int64_t)n_, keys_.p, (1u << 21) - 1u, ref_k_[1].p, plan_, sort_scratch_.p + hist_off_);
+    const uint32_t* kin = ref_k_[1].p;
+    const uint32_t* vin = nullptr;
+    const size_t lbw = sort_lookback_words(plan_);
+    for (int p = 0; p < plan_.passes; p++) {
+        launch_onesweep_pass(stream_, (int64_t)n_, plan_, p, kin, vin, ref_k_[p & 1].p, ref_v_[p & 1].p,
+                             sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
+                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, status_.p);
+        kin = ref_k_[p & 1].p;
+        vin = ref_v_[p & 1].p;
+    }
+    *ids = vin;
+    return kin;
+}
+
 void Solver::get_sorted(uint32_t* cells, uint32_t* ids, size_t n) {
     if (!initialized_) return;
     n = std::min(n, n_);
     XPBD_CUDA(cudaSetDevice(device_));
     const int fin = (plan_.passes - 1) & 1;
-    if (cells) XPBD_CUDA(cudaMemcpyAsync(cells, pair_k_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
-    if (ids) XPBD_CUDA(cudaMemcpyAsync(ids, pair_v_[fin].p, n * 4, cudaMemcpyDeviceToHost, stream_));
+    const uint32_t* sk = pair_k_[fin].p;
+    const uint32_t* sv = pair_v_[fin].p;
+    if (split_keys_ && n_ > 0) sk = sort_reference_layout(&sv);
+    if (cells) XPBD_CUDA(cudaMemcpyAsync(cells, sk, n * 4, cudaMemcpyDeviceToHost, stream_));
+    if (ids) XPBD_CUDA(cudaMemcpyAsync(ids, sv, n * 4, cudaMemcpyDeviceToHost, stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -1447,7 +1478,13 @@ void Solver::get_cell_tables(int32_t* starts, int32_t* ends) {
         cell_starts_.alloc(kNumCells, false);
         cell_ends_.alloc(kNumCells, false);
     }
-    launch_cell_tables(stream_, table_.p, stamp_.p, cell_starts_.p, cell_ends_.p);
+    if (split_keys_) {
+        const uint32_t* sv = nullptr;
+        const uint32_t* sk = sort_reference_layout(&sv);
+        launch_cell_bounds(stream_, (int64_t)n_, sk, cell_starts_.p, cell_ends_.p);
+    } else {
+        launch_cell_tables(stream_, table_.p, stamp_.p, cell_starts_.p, cell_ends_.p);
+    }
     if (starts) XPBD_CUDA(cudaMemcpyAsync(starts, cell_starts_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
     if (ends) XPBD_CUDA(cudaMemcpyAsync(ends, cell_ends_.p, kNumCells * 4, cudaMemcpyDeviceToHost, stream_));
     XPBD_CUDA(cudaStreamSynchronize(stream_));

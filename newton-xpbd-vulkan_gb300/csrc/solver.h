@@ -248,6 +248,11 @@ class Solver {
     // hash grid and sort
     SortPlan plan_{};
     DevBuf<uint32_t> keys_, pair_k_[2], pair_v_[2];
+    // one scene sorts split keys (the reference's cell key + 3 alias bits); the sorted-order
+    // getters re-sort the reference's 21-bit keys on demand into ref_k_ / ref_v_
+    bool split_keys_ = false;
+    DevBuf<uint32_t> ref_k_[2], ref_v_[2];
+    const uint32_t* sort_reference_layout(const uint32_t** ids);
     DevBuf<uint32_t> sort_scratch_;  // hist | lookback | tile counters (cleared per substep)
     size_t hist_off_ = 0, lb_off_ = 0, tc_off_ = 0, cq_off_ = 0;
     DevBuf<int4> table_;

@@ -132,19 +132,31 @@ __device__ __forceinline__ int32_t f2i(float f) {
 }
 __device__ __forceinline__ int32_t imax0(int32_t a) { return a < 0 ? 0 : a; }
 
-// grid_cell_indices.comp:17-25
-__device__ __forceinline__ uint32_t hash_grid_index(v3 p, float inv) {
-    int32_t gx = imax0(f2i(floorf(p.x * inv)) + kGridOrigin);
-    int32_t gy = imax0(f2i(floorf(p.y * inv)) + kGridOrigin);
-    int32_t gz = imax0(f2i(floorf(p.z * inv)) + kGridOrigin);
-    return (uint32_t)((gz % kGridDim) * (kGridDim * kGridDim) + (gy % kGridDim) * kGridDim + (gx % kGridDim));
+// Hash-grid keys. The reference's key (grid_cell_indices.comp:17-25,
+// solve_particle_particle_contacts.comp:67-79) is the cell index on a 128^3 grid that wraps
+// every 128 cells per axis, so cells 128 apart share a key ("aliens"): the neighbour loop
+// visits their particles and rejects them by distance. With `split` the key also carries
+// bit 7 of each axis' unwrapped cell coordinate in bits 21..23 (the grid wraps every 256
+// cells). The sort is stable from particle order, so a cell's particles are in particle
+// order either way and the particles of one true cell appear in a split key's range in the
+// same relative order as in the reference's range; only aliens 128 cells away are gone,
+// and those are never accepted. Bits 0..20 are the reference's key.
+__device__ __forceinline__ uint32_t grid_key(int32_t gx, int32_t gy, int32_t gz, bool split) {
+    // g* = imax0(cell + kGridOrigin) >= 0
+    const uint32_t k = (uint32_t)((gz % kGridDim) * (kGridDim * kGridDim) + (gy % kGridDim) * kGridDim +
+                                  (gx % kGridDim));
+    if (!split) return k;
+    return k | ((((uint32_t)gx >> 7) & 1u) << 21) | ((((uint32_t)gy >> 7) & 1u) << 22) |
+           ((((uint32_t)gz >> 7) & 1u) << 23);
 }
-// solve_particle_particle_contacts.comp:67-79
-__device__ __forceinline__ int32_t cell_index(int32_t x, int32_t y, int32_t z) {
-    x = imax0(x + kGridOrigin);
-    y = imax0(y + kGridOrigin);
-    z = imax0(z + kGridOrigin);
-    return (z % kGridDim) * (kGridDim * kGridDim) + (y % kGridDim) * kGridDim + (x % kGridDim);
+__device__ __forceinline__ uint32_t hash_grid_index(v3 p, float inv, bool split) {
+    const int32_t gx = imax0(f2i(floorf(p.x * inv)) + kGridOrigin);
+    const int32_t gy = imax0(f2i(floorf(p.y * inv)) + kGridOrigin);
+    const int32_t gz = imax0(f2i(floorf(p.z * inv)) + kGridOrigin);
+    return grid_key(gx, gy, gz, split);
+}
+__device__ __forceinline__ int32_t cell_index(int32_t x, int32_t y, int32_t z, bool split) {
+    return (int32_t)grid_key(imax0(x + kGridOrigin), imax0(y + kGridOrigin), imax0(z + kGridOrigin), split);
 }
 
 struct q4 {
