@@ -559,7 +559,7 @@ __device__ __forceinline__ void posed_insert(float4* base, int& used, int slot_c
     used++;
 }
 
-__global__ void __launch_bounds__(32 * kPosedWarps) k_collide_posed(
+__global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ counter, const float4* __restrict__ x,
     const float* __restrict__ r, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* __restrict__ cinfo,
     float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
