@@ -225,6 +225,15 @@ int xpbd_autotune(xpbd_solver* s, int best[2], double* times_us);
 /* Fixes the sort variant instead: (bits, keys per thread) among the variants above. */
 int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread);
 
+/* How the first solver iteration of a substep with meshes is ordered against contact
+ * generation (no counterpart in the reference; results are identical either way):
+ * 0 = fused after the contacts, 1 = its particle-particle part computed beside contact
+ * generation and the rest after it, -1 (default) = each solver times both over its first
+ * frames and keeps the faster. xpbd_get_solve_split reports the form in use (-1 while
+ * undecided). */
+int xpbd_set_solve_split(xpbd_solver* s, int mode);
+int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
+
 /* New contact / material parameters after init (e.g. between rollouts of an
  * optimisation): every numeric field of cfg except device_index and the
  * diagnostics / profiling switches, which stay as at init. */

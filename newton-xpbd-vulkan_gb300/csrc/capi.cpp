@@ -34,6 +34,10 @@ xpbd::Solver& S(xpbd_solver* s) {
     if (!s) throw std::runtime_error("null solver handle");
     return s->impl;
 }
+const xpbd::Solver& CS(const xpbd_solver* s) {
+    if (!s) throw std::runtime_error("null solver handle");
+    return s->impl;
+}
 }  // namespace
 
 extern "C" {
@@ -326,6 +330,17 @@ int xpbd_autotune(xpbd_solver* s, int best[2], double* times_us) {
 
 int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread) {
     return guarded([&] { S(s).set_sort_variant(bits, keys_per_thread); });
+}
+
+int xpbd_set_solve_split(xpbd_solver* s, int mode) {
+    return guarded([&] { S(s).set_solve_split(mode); });
+}
+
+int xpbd_get_solve_split(const xpbd_solver* s, int* mode) {
+    return guarded([&] {
+        if (!mode) throw std::runtime_error("xpbd_get_solve_split: mode is NULL");
+        *mode = CS(s).solve_split();
+    });
 }
 
 int xpbd_update_config(xpbd_solver* s, const xpbd_config* cfg) {

@@ -88,7 +88,7 @@ void Solver::clear_graphs() {
     }
     graphs_.clear();
     clear_backward_graphs();
-    split_choice_ = -1;
+    split_choice_ = split_forced_;
     split_trials_ = 0;
 }
 
@@ -244,6 +244,15 @@ std::vector<double> Solver::autotune_sort(int* best_bits, int* best_items) {
     if (best_bits) *best_bits = bb;
     if (best_items) *best_items = bi;
     return us;
+}
+
+void Solver::set_solve_split(int mode) {
+    require_init();
+    if (mode < -1 || mode > 1) throw std::runtime_error("set_solve_split: -1 (timed choice), 0 (fused) or 1 (split)");
+    sync();
+    split_forced_ = mode;
+    split_choice_ = mode;
+    split_trials_ = 0;
 }
 
 void Solver::set_sort_variant(int bits, int items) {

@@ -129,6 +129,8 @@ class Solver {
     // returns the times (us) of {8b x 8, 8b x 16, 7b x 16, 7b x 32}
     std::vector<double> autotune_sort(int* best_bits, int* best_items);
     void set_sort_variant(int bits, int items);
+    void set_solve_split(int mode);               // -1 timed choice, 0 fused, 1 split
+    int solve_split() const { return split_choice_; }
     void rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
                           double* params);
     void step(float dt, int substeps, int iterations);
@@ -227,6 +229,7 @@ class Solver {
     // until the graphs are rebuilt. Results are the same either way.
     static constexpr int kSplitTrials = 6;
     int split_choice_ = -1;
+    int split_forced_ = -1;  // set_solve_split: kept across graph rebuilds
     int split_trials_ = 0;
     bool split_now_ = false;
     cudaEvent_t split_ev_[kSplitTrials][2] = {};

@@ -212,6 +212,18 @@ class XpbdSolver:
     def set_sort_variant(self, bits, keys_per_thread):
         _check(_lib.xpbd_set_sort_variant(self._h, int(bits), int(keys_per_thread)))
 
+    def set_solve_split(self, mode):
+        """First iteration against contact generation: 0 fused after it, 1 particle-particle
+        part beside it, -1 (default) timed on the first frames (xpbd_set_solve_split)."""
+        _check(_lib.xpbd_set_solve_split(self._h, int(mode)))
+
+    @property
+    def solve_split(self):
+        """The form in use: 0 fused, 1 split, -1 not decided yet."""
+        v = C.c_int(0)
+        _check(_lib.xpbd_get_solve_split(self._h, C.byref(v)))
+        return int(v.value)
+
     def update_config(self, config):
         """New contact / material parameters after init (xpbd_update_config)."""
         _check(_lib.xpbd_update_config(self._h, C.byref(config._c)))
