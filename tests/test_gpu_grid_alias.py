@@ -84,3 +84,29 @@ def test_aliased_clusters_two_iterations_with_cohesion():
         assert_bitexact(g.get_positions(), orc.get_positions(), f"positions frame {f}")
         assert_bitexact(g.get_velocities(), orc.get_velocities(), f"velocities frame {f}")
     _check_grid(g, orc, "cohesion")
+
+
+def test_far_and_clamped_coordinates_bitexact():
+    """Particles beyond 2^20 cells clamp to cell 0 on each axis (grid_cell_indices.comp:21-23)
+    under both keys; far particles share wrapped cells with the pile near the origin."""
+    sc = _alias_scene(seed=9, n_side=5)
+    rng = np.random.default_rng(9)
+    far = np.array([[-3.0e4, 0.0, 0.5], [-3.0e4, 0.005, 0.5], [2.0e4, -2.0e4, 1.0], [5.12, 5.12, 5.12],
+                    [-5.12, 0.01, 0.3], [1.0e5, 1.0e5, 1.0e5]], np.float32)
+    far = np.concatenate([far, far + rng.uniform(-0.004, 0.004, far.shape).astype(np.float32)])
+    n0 = sc.n
+    sc.positions = np.concatenate([sc.positions, far]).astype(np.float32)
+    k = far.shape[0]
+    sc.velocities = np.concatenate([sc.velocities, np.zeros((k, 3), np.float32)])
+    sc.inv_mass = np.concatenate([sc.inv_mass, np.full(k, 1000.0, np.float32)])
+    sc.radii = np.concatenate([sc.radii, np.full(k, 0.01, np.float32)])
+    sc.flags = np.concatenate([sc.flags, np.ones(k, np.int32)])
+    assert sc.n == n0 + k
+    cfg = config_for(sc)
+    g, orc = make_pair(sc, cfg)
+    for f in range(4):
+        g.step(1.0 / 60.0, 4, 1)
+        orc.step(1.0 / 60.0, 4, 1)
+        assert_bitexact(g.get_positions(), orc.get_positions(), f"positions frame {f}")
+        assert_bitexact(g.get_velocities(), orc.get_velocities(), f"velocities frame {f}")
+    _check_grid(g, orc, "far")
