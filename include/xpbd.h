@@ -212,7 +212,7 @@ int xpbd_set_body_scenes(xpbd_solver* s, const int32_t* scene_of_body, size_t nu
 int xpbd_record_start(xpbd_solver* s, const char* directory, int first_frame);
 int xpbd_record_stop(xpbd_solver* s, int* frames_written);
 
-/* Sort autotuner (the north star's "autotuned sort parameters"): times every
+/* Sort autotuner (autotuned sort parameters for batched scenes): times every
  * onesweep variant (digit width 8 or 7 bits, 2 to 32 keys per thread) on the
  * scene's current keys and keeps the fastest. Runs by itself on the first step of a
  * solver with XPBD_AUTOTUNE_MIN particles or more; results never depend on the

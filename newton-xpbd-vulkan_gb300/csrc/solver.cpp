@@ -1369,7 +1369,7 @@ void Solver::set_contact_data(const int32_t* part, const int32_t* shape, const f
 }
 
 // Host xyz arrays <-> device float4 state: one copy straight from or to the caller's
-// (pageable) memory plus a pack / unpack kernel; on Grace the driver moves pageable
+// (pageable) memory plus a pack / unpack kernel; on Grace the CUDA driver moves pageable
 // memory over NVLink-C2C directly, several times faster than staging it through a
 // pinned buffer with a host memcpy.
 void Solver::upload_xyz(const float* h, float4* d, size_t n) {

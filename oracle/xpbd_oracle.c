@@ -136,7 +136,7 @@ static inline real diff_product(real a, real b, real c, real d) {
 }
 
 /*
- * acos(x), x in [-1,1]. GLSL leaves acos's rounding to the driver; this build
+ * acos(x), x in [-1,1]. GLSL leaves acos's rounding to the GPU driver; this code
  * fixes it to a Taylor series of asin (coefficients (2n)!/(4^n (n!)^2 (2n+1)),
  * n=1..11, rounded to float) evaluated by Horner in t^2, with the half-angle
  * identity acos(x) = 2 asin(sqrt((1-x)/2)) for |x| > 1/2. Max error ~1 ulp.
