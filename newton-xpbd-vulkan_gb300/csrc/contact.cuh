@@ -152,6 +152,7 @@ __device__ __forceinline__ bool restitution_dv(const Contact& ct, v3 v_new, v3 p
 __device__ __forceinline__ bool contact_kept(uint32_t info, int k, const ContactRanks& cr, uint32_t id,
                                              int64_t contact_max) {
     if (!cr.rank) return true;
+    if (cr.count && (int64_t)*cr.count <= contact_max) return true;  // nothing over the cap
     const uint2 rk = cr.rank[id];
     if ((info & kPlaneBit) && k == 0) return (int64_t)rk.x < contact_max;
     const int j = k - (int)(info & kPlaneBit);

@@ -25,7 +25,9 @@ __device__ __forceinline__ uint2 particle_counts(const uint32_t* __restrict__ ci
 
 // phase 1: per-tile sums
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int64_t n, const uint32_t* __restrict__ cinfo,
-                                                             DynSlots ds, uint32_t* __restrict__ tile_sums) {
+                                                             DynSlots ds, uint32_t* __restrict__ tile_sums,
+                                                             const uint32_t* skip, int64_t cap) {
+    if (skip && (int64_t)*skip <= cap) return;
     __shared__ uint32_t s_a[kScanThreads / 32], s_b[kScanThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     uint32_t a = 0, b = 0;
@@ -60,7 +62,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int64_t n, const u
 
 // phase 2: one block scans the tile sums in place (exclusive) and writes the totals
 __global__ void __launch_bounds__(1024) k_scan_tiles(int tiles, uint32_t* __restrict__ tile_sums,
-                                                    uint32_t* __restrict__ totals) {
+                                                    uint32_t* __restrict__ totals, const uint32_t* skip, int64_t cap) {
+    if (skip && (int64_t)*skip <= cap) return;
     __shared__ uint32_t s_a[32], s_b[32];
     __shared__ uint32_t carry_a, carry_b;
     if (threadIdx.x == 0) carry_a = carry_b = 0;
@@ -111,7 +114,8 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(int tiles, uint32_t* __rest
 // phase 3: per-particle exclusive ranks
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(int64_t n, const uint32_t* __restrict__ cinfo,
                                                            DynSlots ds, const uint32_t* __restrict__ tile_sums,
-                                                           uint2* __restrict__ rank) {
+                                                           uint2* __restrict__ rank, const uint32_t* skip, int64_t cap) {
+    if (skip && (int64_t)*skip <= cap) return;
     __shared__ uint32_t s_a[kScanThreads / 32], s_b[kScanThreads / 32];
     // thread t owns kScanItems consecutive particles of the tile
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
@@ -153,16 +157,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(int64_t n, const uin
 }
 
 void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2* rank, uint32_t* totals,
-                         uint32_t* workspace, uint32_t* /*unused*/, DeviceStatus* /*unused*/) {
+                         uint32_t* workspace, const uint32_t* skip_count, int64_t cap) {
     if (n <= 0) {
         cudaMemsetAsync(totals, 0, 2 * sizeof(uint32_t), s);
         return;
     }
     const int tiles = (int)((n + kScanTile - 1) / kScanTile);
     const DynSlots none{nullptr, 0, nullptr, nullptr};
-    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace);
-    k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals);
-    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace, rank);
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace, skip_count, cap);
+    k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals, skip_count, cap);
+    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, none, workspace, rank, skip_count, cap);
 }
 
 void launch_dyn_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, uint2* rank, uint32_t* totals,
@@ -172,9 +176,9 @@ void launch_dyn_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots 
         return;
     }
     const int tiles = (int)((n + kScanTile - 1) / kScanTile);
-    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace);
-    k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals);
-    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace, rank);
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace, nullptr, 0);
+    k_scan_tiles<<<1, 1024, 0, s>>>(tiles, workspace, totals, nullptr, 0);
+    k_scan_down<<<tiles, kScanThreads, 0, s>>>(n, cinfo, ds, workspace, rank, nullptr, 0);
 }
 
 __global__ void k_contact_compact(int64_t n, const uint32_t* __restrict__ cinfo, const float4* __restrict__ cslot,

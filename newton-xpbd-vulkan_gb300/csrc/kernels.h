@@ -136,6 +136,9 @@ struct SolveDiag {
 struct ContactRanks {
     const uint2* rank;        // per particle (exclusive plane count, exclusive slot count), or null
     const uint32_t* totals;   // [2] total plane contacts, total slot contacts
+    // the substep's contact count, or null: when it is at most contact_max every contact
+    // is kept and the ranks (not computed then) are not read
+    const uint32_t* count = nullptr;
 };
 
 // ---------------------------------------------------------------- sort ----
@@ -204,8 +207,9 @@ void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const flo
                       ContactRanks cr, BodyTables bt, SolveParams sp, float4* x_out, float4* v_out);
 // exclusive scan of per-particle (plane bit, slot count) for the contact_max cap / compaction
 size_t contact_scan_words(int64_t n);
+// (skip_count, cap): the scan does nothing when *skip_count <= cap (no contact over the cap)
 void launch_contact_scan(cudaStream_t s, int64_t n, const uint32_t* cinfo, uint2* rank, uint32_t* totals,
-                         uint32_t* lookback, uint32_t* tile_counter, DeviceStatus* st);
+                         uint32_t* workspace, const uint32_t* skip_count = nullptr, int64_t cap = 0);
 // exclusive scan of each particle's number of contact slots with a dynamic body
 // (rank[i].x; totals[0] = all of them)
 struct DynSlots {

@@ -1075,11 +1075,14 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     }
     ContactRanks cr{nullptr, nullptr};
     if (gen && need_ranks_) {
-        launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, nullptr, st);
+        // contacts past contact_max are dropped in the canonical order; a substep with at
+        // most contact_max contacts keeps them all and skips the scan on the device
+        launch_contact_scan(stream_, n, info, rank_.p, totals_.p, scan_ws_.p, ccount, contact_max_);
         count_kernel(3);
         prof_mark(P_RANKS);
         cr.rank = rank_.p;
         cr.totals = totals_.p;
+        cr.count = ccount;
     }
     for (int it = 0; it < iterations; it++) {
         // with dynamic bodies the restitution waits for the last body pass
@@ -1410,7 +1413,7 @@ void Solver::compact_contacts() {
         c_bvel_.alloc(cm * 3, false);
         c_nrm_.alloc(cm * 3, false);
     }
-    launch_contact_scan(stream_, (int64_t)n_, cinfo_.p, rank_.p, totals_.p, scan_ws_.p, nullptr, status_.p);
+    launch_contact_scan(stream_, (int64_t)n_, cinfo_.p, rank_.p, totals_.p, scan_ws_.p);
     launch_contact_compact(stream_, (int64_t)n_, cinfo_.p, cslot_.p, slot_cap_, rank_.p, totals_.p, contact_max_,
                            x_[last_collide_src_].p, cfg_.ground_plane_altitude, c_part_.p, c_shape_.p, c_bpos_.p,
                            c_bvel_.p, c_nrm_.p);

@@ -124,6 +124,25 @@ def test_contact_max_cap_bitexact():
     _step_compare(g, orc, 4, 1.0 / 60.0, 5, 1, "capped")
 
 
+def test_contact_max_cap_crossed_during_run_bitexact():
+    """A pile falling onto the heightfield: early substeps stay under the cap (every contact
+    kept, the rank scan skipped on the device), later ones exceed it (contacts past the cap
+    dropped in the canonical order)."""
+    sc = mesh_pile(12, 24)
+    cfg = config_for(sc)
+    cap = 400
+    g, orc = make_pair(sc, cfg, max_contacts=cap)
+    counts = []
+    for f in range(10):
+        g.step(1.0 / 60.0, 5, 1)
+        orc.step(1.0 / 60.0, 5, 1)
+        assert_bitexact(g.get_positions(), orc.get_positions(), f"positions frame {f}")
+        assert_bitexact(g.get_velocities(), orc.get_velocities(), f"velocities frame {f}")
+        assert g.last_contact_count == orc.last_contact_count, f"contact count frame {f}"
+        counts.append(g.last_contact_count)
+    assert min(counts) < cap and max(counts) == cap, counts
+
+
 def test_step_solve_only_bitexact():
     sc = small_pile(8)
     sc.positions[:, 2] -= 0.05
