@@ -284,44 +284,40 @@ __global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
     }
 }
 
-// apply_particle_shape_restitution.comp:248-316 after the body passes: one thread per
-// particle in sorted order reads its final state, adds the restitution increments of its
-// contacts (canonical order, pre-restitution velocity) and writes particle order.
+// apply_particle_shape_restitution.comp:48-116 after the body passes: the last iteration
+// has written the final state in particle order; one thread per particle (particle order,
+// so the contact headers are read coalesced) adds the restitution increments of its
+// contacts (canonical order, on the pre-restitution velocity) to its velocity. Particles
+// without a contact, and inactive ones (:256), keep their state.
 __global__ void __launch_bounds__(kSolveThreads) k_restitute(
-    int64_t n, const uint32_t* __restrict__ sids, const float4* __restrict__ rx, const float4* __restrict__ rv,
-    const int* __restrict__ rf, const float4* __restrict__ x0a, const float4* __restrict__ v0a,
-    const uint32_t* __restrict__ cinfo, const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt,
-    SolveParams sp, float4* __restrict__ x_out, float4* __restrict__ v_out) {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t id = sids[k];
-    const float4 ox = rx[k], ov = rv[k];
-    v3 v_new = xyz(ov);
-    const uint32_t info = cinfo[id];
+    int64_t n, const int* __restrict__ flags, const float* __restrict__ radii, const float4* __restrict__ x0a,
+    const float4* __restrict__ v0a, const uint32_t* __restrict__ cinfo, const float4* __restrict__ cslot,
+    ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ v_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t info = cinfo[i];
     const int ncon = (int)(info & kPlaneBit) + info_slots(info);
-    // inactive particles keep their predicted state and take no restitution (:256)
-    if (sp.enable_restitution && ncon && (rf[k] & 1)) {
-        const v3 x0 = xyz(x0a[id]), v_old = xyz(v0a[id]);
-        const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
-        const v3 v_snap = v_new;
-        for (int c = 0; c < ncon; c++) {
-            if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
-            const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
-            v3 dv;
-            if (restitution_dv(ct, v_snap, x0, v_old, ox.w, bt, sp, dv)) v_new = vadd(v_new, dv);
-        }
+    if (ncon == 0 || !(flags[i] & 1)) return;
+    const uint32_t id = (uint32_t)i;
+    const v3 x0 = xyz(x0a[i]), v_old = xyz(v0a[i]);
+    const float4* slots = cslot + (size_t)i * sp.slot_cap * 3;
+    const v3 v_snap = xyz(v_out[i]);
+    v3 v_new = v_snap;
+    for (int c = 0; c < ncon; c++) {
+        if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;
+        const Contact ct = load_contact(info, c, slots, x0, sp.altitude);
+        v3 dv;
+        if (restitution_dv(ct, v_snap, x0, v_old, radii[i], bt, sp, dv)) v_new = vadd(v_new, dv);
     }
-    x_out[id] = make_float4(ox.x, ox.y, ox.z, 0.0f);
-    v_out[id] = make_float4(v_new.x, v_new.y, v_new.z, 0.0f);
+    v_out[i] = make_float4(v_new.x, v_new.y, v_new.z, 0.0f);
 }
 
-void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const float4* rx, const float4* rv,
-                      const int* rf, const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot,
-                      ContactRanks cr, BodyTables bt, SolveParams sp, float4* x_out, float4* v_out) {
+void launch_restitute(cudaStream_t s, int64_t n, const int* flags, const float* radii, const float4* x0,
+                      const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
+                      SolveParams sp, float4* v_out) {
     if (n <= 0) return;
     const int blocks = (int)((n + kSolveThreads - 1) / kSolveThreads);
-    k_restitute<<<blocks, kSolveThreads, 0, s>>>(n, sids, rx, rv, rf, x0, v0, cinfo, cslot, cr, bt, sp, x_out,
-                                                 v_out);
+    k_restitute<<<blocks, kSolveThreads, 0, s>>>(n, flags, radii, x0, v0, cinfo, cslot, cr, bt, sp, v_out);
 }
 
 void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const uint32_t* sids, const uint32_t* skeys,

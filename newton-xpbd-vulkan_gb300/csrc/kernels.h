@@ -201,10 +201,10 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg,
                   BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr}, int pp_mode = 0, float4* pp = nullptr);
 // restitution (apply_particle_shape_restitution.comp) after the body passes of the last
-// iteration, scattering the sorted final state to particle order
-void launch_restitute(cudaStream_t s, int64_t n, const uint32_t* sids, const float4* rx, const float4* rv,
-                      const int* rf, const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot,
-                      ContactRanks cr, BodyTables bt, SolveParams sp, float4* x_out, float4* v_out);
+// iteration, in particle order on the final state the last iteration wrote (v_out)
+void launch_restitute(cudaStream_t s, int64_t n, const int* flags, const float* radii, const float4* x0,
+                      const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
+                      SolveParams sp, float4* v_out);
 // exclusive scan of per-particle (plane bit, slot count) for the contact_max cap / compaction
 size_t contact_scan_words(int64_t n);
 // (skip_count, cap): the scan does nothing when *skip_count <= cap (no contact over the cap)

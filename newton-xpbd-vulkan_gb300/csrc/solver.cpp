@@ -1085,11 +1085,14 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         cr.count = ccount;
     }
     for (int it = 0; it < iterations; it++) {
-        // with dynamic bodies the restitution waits for the last body pass
-        const bool last = it == iterations - 1 && !bodies;
+        // the last iteration writes the final state in particle order; with dynamic bodies
+        // its restitution waits for the last body pass (below)
+        const bool last = it == iterations - 1;
+        SolveParams sp = solve_params(sdt, it);
+        if (bodies) sp.enable_restitution = 0;
         launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p,
-                     rv_[it & 1].p, rf_.p, table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, cr, bt,
-                     solve_params(sdt, it), rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo,
+                     rv_[it & 1].p, rf_.p, table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, cr, bt, sp,
+                     rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo,
                      split && it == 0 ? 2 : 0, pp_.p);
         count_kernel();
         prof_mark(P_SOLVE);
@@ -1103,9 +1106,9 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
             prof_mark(P_BODY_RIGID_ITER);
         }
     }
-    if (bodies && iterations > 0) {
-        launch_restitute(stream_, n, sids, rx_[iterations & 1].p, rv_[iterations & 1].p, rf_.p, x_[src].p,
-                         v_[src].p, info, slots, cr, bt, solve_params(sdt, iterations - 1), x_[dst].p, v_[dst].p);
+    if (bodies && iterations > 0 && cfg_.enable_restitution) {
+        launch_restitute(stream_, n, flags_.p, r_.p, x_[src].p, v_[src].p, info, slots, cr, bt,
+                         solve_params(sdt, iterations - 1), v_[dst].p);
         count_kernel();
         prof_mark(P_RESTITUTION);
     }
