@@ -1145,9 +1145,15 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     const bool split_ok = mode == Mode::Step && !meshes_.empty() && !profiling_ && iterations > 0 &&
                           !cfg_.enable_diagnostics;
     int trial = -1;
+    if (split_ok && split_forced_ < 0 && split_choice_ >= 0 && ++split_frames_ >= kSplitRetime) {
+        split_choice_ = -1;  // time both ways again, without the first-use frames
+        split_trials_ = 2;
+    }
     if (split_ok && split_choice_ < 0) {
+        // frames 0 and 1 build each graph (not compared); then fused, split, split, fused,
+        // so that a steady change of the frame time between frames cancels in the sums
         trial = split_trials_++;
-        split_now_ = (trial & 1) != 0;
+        split_now_ = trial == 1 || trial == 3 || trial == 4;
     } else {
         split_now_ = split_ok && split_choice_ == 1;
     }
@@ -1180,15 +1186,16 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     XPBD_CUDA(cudaGraphLaunch(it->second.exec, stream_));
     if (trial >= 0) {
         XPBD_CUDA(cudaEventRecord(split_ev_[trial][1], stream_));
-        if (trial == kSplitTrials - 1) {  // both ways timed: keep the faster (first use of each skipped)
+        if (trial == kSplitTrials - 1) {  // both ways timed: keep the faster
             XPBD_CUDA(cudaEventSynchronize(split_ev_[trial][1]));
-            float best[2] = {3.0e38f, 3.0e38f};
+            float sum[2] = {0.0f, 0.0f};
             for (int t = 2; t < kSplitTrials; t++) {
                 float ms = 0.0f;
                 XPBD_CUDA(cudaEventElapsedTime(&ms, split_ev_[t][0], split_ev_[t][1]));
-                best[t & 1] = std::min(best[t & 1], ms);
+                sum[(t == 3 || t == 4) ? 1 : 0] += ms;
             }
-            split_choice_ = best[1] < best[0] ? 1 : 0;
+            split_choice_ = sum[1] < sum[0] ? 1 : 0;
+            split_frames_ = 0;
         }
     }
     if (recorder_.active()) {  // this frame's positions to the writer thread (after the graph)

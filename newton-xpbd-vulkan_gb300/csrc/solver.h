@@ -225,10 +225,15 @@ class Solver {
     // Whether the first iteration's particle-particle part runs before the join, beside the
     // contact generation (split) or after it, fused with the rest (the faster depends on how
     // long the contact chain is next to the sort and the solve): -1 undecided, in which case
-    // the next kSplitTrials frames alternate both ways under events and the faster is kept
-    // until the graphs are rebuilt. Results are the same either way.
+    // the next kSplitTrials frames run both ways under events and the faster is kept.
+    // Results are the same either way.
+    // The choice is timed again every kSplitRetime frames (both graphs exist by then, so
+    // two frames each way): a scene's balance moves as it evolves (bodies settling into a
+    // pile multiply the moving-mesh queries).
     static constexpr int kSplitTrials = 6;
+    static constexpr int kSplitRetime = 16;
     int split_choice_ = -1;
+    int split_frames_ = 0;  // frames since the last choice
     int split_forced_ = -1;  // set_solve_split: kept across graph rebuilds
     int split_trials_ = 0;
     bool split_now_ = false;
