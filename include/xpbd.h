@@ -155,6 +155,9 @@ int xpbd_reset_stage_times(xpbd_solver* s);
 const char* xpbd_stage_name(int index);
 /* out = {kernel launches per frame, memset nodes per frame, frames run, cached graphs} */
 int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]);
+/* Kernels launched by all frames run so far (the frame graphs' kernel nodes, frame by
+ * frame: exact also when consecutive frames replay different graphs). */
+int xpbd_get_kernels_launched(xpbd_solver* s, uint64_t* total);
 
 /* Rigid bodies — an extension: the reference's body table is static
  * (src/scene.cpp:220-238) and its body shaders (integrate_bodies.comp,

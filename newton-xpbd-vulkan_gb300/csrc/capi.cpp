@@ -269,6 +269,13 @@ int xpbd_get_frame_stats(xpbd_solver* s, uint64_t out[4]) {
     return guarded([&] { S(s).frame_stats(out); });
 }
 
+int xpbd_get_kernels_launched(xpbd_solver* s, uint64_t* total) {
+    return guarded([&] {
+        if (!total) throw std::runtime_error("xpbd_get_kernels_launched: total is NULL");
+        *total = S(s).kernels_launched();
+    });
+}
+
 void xpbd_body_params_default(xpbd_body_params* p) {
     if (!p) return;
     p->angular_damping = 0.0f;

@@ -1203,6 +1203,7 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
         recorder_.enqueue(stream_, rec_stage_.p);
     }
     last_kernels_ = it->second.kernels;
+    kernels_total_ += it->second.kernels + (recorder_.active() ? 1 : 0);
     last_memsets_ = it->second.memsets;
     frames_run_++;
     last_collide_src_ = cur_ ^ ((substeps - 1) & 1);

@@ -131,6 +131,7 @@ class Solver {
     void set_sort_variant(int bits, int items);
     void set_solve_split(int mode);               // -1 timed choice, 0 fused, 1 split
     int solve_split() const { return split_choice_; }
+    uint64_t kernels_launched() const { return kernels_total_; }
     void rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
                           double* params);
     void step(float dt, int substeps, int iterations);
@@ -367,6 +368,7 @@ class Solver {
     int pending_substeps_ = 0;         // frame launched by step_async and not yet synced
     uint64_t frames_run_ = 0;
     uint64_t last_kernels_ = 0, last_memsets_ = 0;
+    uint64_t kernels_total_ = 0;  // kernels launched by all frames run
     // profiler (stage names follow scene.cpp:1481-1505 where the stages correspond)
     bool profiling_ = false;
     double prof_ms_[kMaxStages] = {0};

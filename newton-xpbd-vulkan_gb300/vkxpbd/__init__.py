@@ -520,6 +520,13 @@ class XpbdSolver:
     def reset_stage_times(self):
         _check(_lib.xpbd_reset_stage_times(self._h))
 
+    @property
+    def kernels_launched(self):
+        """Kernels launched by all frames run so far (xpbd_get_kernels_launched)."""
+        v = C.c_uint64(0)
+        _check(_lib.xpbd_get_kernels_launched(self._h, C.byref(v)))
+        return int(v.value)
+
     def get_frame_stats(self):
         """{kernels, memsets} per frame of the last launched graph, frames run, cached graphs."""
         out = (C.c_uint64 * 4)()
