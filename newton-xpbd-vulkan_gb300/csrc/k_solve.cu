@@ -15,7 +15,7 @@
 
 namespace xpbd {
 
-constexpr int kSolveThreads = 128;
+constexpr int kSolveThreads = 64;
 constexpr int kPairCap = 12;  // accepted neighbours buffered per thread before the pair math runs
 
 // Pair math of solve_particle_particle_contacts.comp:159-207 for the neighbours
@@ -180,7 +180,7 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
 enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
 
 template <bool LAST, bool ALL_ACTIVE, bool DIAG, int PP>
-__global__ void __launch_bounds__(kSolveThreads, 8) k_solve(
+__global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     int64_t n, const uint32_t* __restrict__ sids, const uint32_t* __restrict__ skeys, const float4* __restrict__ rx,
     const float4* __restrict__ rv, const int* __restrict__ rf, const int4* __restrict__ table_all,
     const uint32_t* __restrict__ stamp_p,
