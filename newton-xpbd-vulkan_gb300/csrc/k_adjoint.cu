@@ -73,8 +73,8 @@ __device__ __forceinline__ v3 pair_backward(v3 raw, v3 vrel, float ri, float rj,
 // Visits the particles of the cells covering [x - R, x + R] (the forward's cell walk,
 // solve_particle_particle_contacts.comp:126-141) and calls f(sorted index).
 template <class F>
-__device__ __forceinline__ void for_cells(v3 x, float R, float inv, const int4* __restrict__ table, uint32_t stamp,
-                                          F&& f) {
+__device__ __forceinline__ void for_cells(v3 x, float R, float inv, bool split, const int4* __restrict__ table,
+                                          uint32_t stamp, F&& f) {
     const int32_t xs = f2i(floorf((x.x - R) * inv)), ys = f2i(floorf((x.y - R) * inv)),
                   zs = f2i(floorf((x.z - R) * inv));
     const int32_t xe = min(f2i(floorf((x.x + R) * inv)), xs + kGridDim - 1);
@@ -83,7 +83,7 @@ __device__ __forceinline__ void for_cells(v3 x, float R, float inv, const int4* 
     for (int32_t cz = zs; cz <= ze; cz++)
         for (int32_t cy = ys; cy <= ye; cy++)
             for (int32_t cx = xs; cx <= xe; cx++) {
-                const int4 e = __ldg(&table[cell_index(cx, cy, cz, true)]);  // one scene: split keys
+                const int4 e = __ldg(&table[cell_index(cx, cy, cz, split)]);
                 if ((uint32_t)e.z != stamp) continue;
                 for (int kk = e.x; kk < e.y; kk++) f(kk);
             }
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(AdjointArgs a) {
         float gw = 0.0f;
         v3 acc = mk3(0.0f, 0.0f, 0.0f);
         const float R = r + a.max_radius + a.k_coh;
-        for_cells(xp, R, a.inv, a.table, *a.stamp, [&](int kk) {
+        for_cells(xp, R, a.inv, a.split_keys != 0, a.table, *a.stamp, [&](int kk) {
             if (kk == (int)k) return;
             const float4 nx = __ldg(&a.rx[kk]);
             const v3 raw = vsub(xp, xyz(nx));

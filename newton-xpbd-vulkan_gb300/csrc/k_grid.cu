@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(256) k_predict_keys(int64_t n, const float4* _
             v3 xp, vp;
             predict(xf, v[i], w[i], fl, pp, xp, vp);
             // one scene: split key; batched: scene-major key = entry of the scene's table
-            key = pscene ? (hash_grid_index(xp, pp.inv, false) | (pscene[i] << 21)) : hash_grid_index(xp, pp.inv, true);
+            key = pscene ? (hash_grid_index(xp, pp.inv, false) | (pscene[i] << 21))
+                         : hash_grid_index(xp, pp.inv, pp.split_keys != 0);
             keys[i] = key;
             if (cinfo) {  // generate_plane_contacts.comp:32-38 on the pre-integration position
                 uint32_t info = 0;

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
         v3 total = mk3(0.0f, 0.0f, 0.0f);
         if (pflag & 1) {
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
-            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, skeys == nullptr,
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
                                                *stamp_p, sids, sp, dg, s_kk, s_d);
         }
         pp[k] = make_float4(total.x, total.y, total.z, 0.0f);
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
         } else {
             // this particle's scene table (scene-major keys); one scene: the whole table
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
-            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, skeys == nullptr,
+            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
                                                *stamp_p, sids, sp, dg, s_kk, s_d);
         }
         delta = vadd(delta, total);

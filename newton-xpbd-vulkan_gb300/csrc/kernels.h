@@ -13,6 +13,9 @@ namespace xpbd {
 constexpr int kGridDim = 128;                                   // hash grid, src/scene.cpp:17-18
 constexpr int kNumCells = kGridDim * kGridDim * kGridDim;
 constexpr int kSplitKeyBits = 24;  // one scene: the reference's 21-bit key + 3 alias bits
+// one-scene solvers from this many particles sort split keys (their cell table has 2^24
+// entries, 256 MiB); smaller ones sort the reference's keys (128^3 entries, 32 MiB)
+constexpr size_t kSplitKeysMinParticles = 32768;
 constexpr int kGridOrigin = 1 << 20;                            // grid_cell_indices.comp:20
 
 // Device-side status word read back after every frame. A kernel that gives
@@ -44,6 +47,7 @@ __host__ __device__ __forceinline__ int info_dyn(uint32_t info) { return (int)(i
 
 struct PredictParams {
     float dt, v_max, gx, gy, gz, inv;
+    int split_keys;  // one scene with split cell keys (the reference's key + alias bits)
 };
 struct PlaneParams {
     int enabled;
@@ -112,6 +116,7 @@ struct SolveParams {
     float altitude;
     int slot_cap;             // generic contact slots per particle
     int iter_index;
+    int split_keys;           // cell keys of the sort: split (one scene) or the reference's
     int64_t contact_max;
 };
 
@@ -384,7 +389,7 @@ struct AdjointArgs {
     float* block_params;  // 3 per block
     double* param_acc;    // [3]: plane mu (effective), particle mu, restitution
     float dt, inv, relax, ka, altitude, margin, mu_plane, k_mu, k_coh, max_radius, restitution;
-    int restitution_on, plane_on;
+    int restitution_on, plane_on, split_keys;
 };
 void launch_adjoint_substep(cudaStream_t s, const AdjointArgs& a);
 // new generation for the stamped cell table (before a cell table is rebuilt without the key kernel)

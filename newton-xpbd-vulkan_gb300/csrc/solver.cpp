@@ -112,7 +112,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     contact_max_ = (int64_t)(max_contacts ? max_contacts : num_particles * 2);  // scene.cpp:68
     key_bits_ = 21;
     while (n_scenes > 1 && (size_t(1) << (key_bits_ - 21)) < n_scenes) key_bits_++;
-    split_keys_ = n_scenes == 1;
+    split_keys_ = n_scenes == 1 && (num_particles >= kSplitKeysMinParticles || env_on("VKXPBD_SPLIT_KEYS"));
     if (split_keys_) key_bits_ = kSplitKeyBits;
     int ndev = 0;
     XPBD_CUDA(cudaGetDeviceCount(&ndev));
@@ -496,6 +496,7 @@ PredictParams Solver::predict_params(float sdt) const {
     p.gy = cfg_.gravity[1];
     p.gz = cfg_.gravity[2];
     p.inv = 1.0f / cfg_.search_radius;
+    p.split_keys = split_keys_ ? 1 : 0;
     return p;
 }
 
@@ -516,6 +517,7 @@ SolveParams Solver::solve_params(float sdt, int it) const {
     s.slot_cap = injected_ ? inj_cap_ : slot_cap_;
     s.iter_index = it;
     s.contact_max = contact_max_;
+    s.split_keys = split_keys_ ? 1 : 0;
     return s;
 }
 
@@ -1806,6 +1808,7 @@ void Solver::rollout_backward(const float* gx_final, const float* gv_final, floa
     a.max_radius = cfg_.particle_max_radius;
     a.restitution = cfg_.soft_contact_restitution;
     a.restitution_on = cfg_.enable_restitution ? 1 : 0;
+    a.split_keys = split_keys_ ? 1 : 0;
     a.rx = rx_[0].p;
     a.rv = rv_[0].p;
     a.x0 = x_[0].p;

@@ -1,8 +1,9 @@
 """Hash-grid aliasing: particles 128 cells apart share the reference's 21-bit cell key.
 
-With one scene the CUDA path sorts split keys (the reference's key plus bit 7 of each axis'
-unwrapped cell coordinate) so that the neighbour loop skips particles 128 cells away, which
-the reference visits and rejects by distance. These scenes put clusters exactly 128 and 256
+One-scene solvers of 32,768 particles or more (or with VKXPBD_SPLIT_KEYS set, as here) sort
+split keys (the reference's key plus bit 7 of each axis' unwrapped cell coordinate) so that
+the neighbour loop skips particles 128 cells away, which the reference visits and rejects by
+distance. These scenes put clusters exactly 128 and 256
 cells apart along x, y and z, one cluster across the 128-cell boundary and one at negative
 coordinates, so that wrapped cells hold several clusters. Bar: bit-exact states, contacts and
 the sorted-order getters (which report the reference's 21-bit layout) against the oracle.
@@ -14,6 +15,13 @@ from helpers import assert_bitexact, config_for, make_pair
 from vkxpbd import scenes
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _split_keys(monkeypatch):
+    # these scenes are below the particle count from which solvers sort split keys by
+    # themselves; the variable makes them sort split keys too
+    monkeypatch.setenv("VKXPBD_SPLIT_KEYS", "1")
 
 
 def _alias_scene(seed=21, n_side=7):
