@@ -1,26 +1,30 @@
 """Benchmark: particle-substeps/s of the XPBD substep on one GB300.
 
-Workload (default): the particles-on-a-mesh scene — 262,144 particles
-(64^3 lattice, r = 0.005 m, seeded jitter) falling onto a 256x256-vertex
-sum-of-sines heightfield (130,050 triangles) with plane, mesh and
-particle-particle contacts, dt = 1/60 s, 10 substeps, 1 solver iteration,
-FP32. One step = one frame (10 substeps) of one continuous run: the scene is
-pre-rolled for --preroll frames (so the pile is in contact), then --warmup
-frames, then --steps timed frames. L2 is flushed (256 MiB write on the
-solver's stream) between timed frames; frame times come from CUDA events on
-the solver's stream.
+Contract line (default): the mixed particles-and-rigid-bodies workload —
+1,048,576 particles (128x128x64 lattice, r = 0.005 m, seeded jitter) on the
+ground plane and a 256x256-vertex sum-of-sines heightfield (130,050
+triangles), plus 1,024 dynamic boxes (half-extents U[0.02, 0.08] m, density
+1000 kg/m^3, orientations uniform on SO(3)) dropped onto the pile; plane,
+heightfield, moving-box and particle-particle contacts, body contact solve and
+body delta apply, dt = 1/60 s, 10 substeps, 1 solver iteration, FP32. One step
+= one frame (10 substeps) of one continuous run: the scene is pre-rolled for
+--preroll frames (boxes landing in the pile), then --warmup frames, then
+--steps timed frames. L2 is flushed (256 MiB write on the solver's stream)
+between timed frames; frame times are CUDA events on the solver's stream.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--preroll P] [--impl reference]
 
-The same line carries "batched": 512 independent piles (log-uniform 1,024-65,536
-particles, seed 46, plane + particle-particle contacts) stepped by one batched
-solver against the same scenes stepped one solver at a time (--batched-scenes 0
-skips it).
+The same line carries the other workloads under their own keys:
+"particles_on_mesh" (262,144 particles on the heightfield), "pile_1m" (the
+plain step at 1,048,576 particles), "batched" (512 uneven scenes in one
+batched solver against one solver per scene and against the plain 1M step),
+"diff" (forward + backward of the 32,768-particle throw over 600 substeps);
+the last key, "headline", repeats each workload's figure.
 
 --impl reference times the CPU restatement of the reference's shaders (the
-oracle, all host threads) on the same pre-rolled scene, one substep per step.
-Under torchrun every rank steps its own replica of the scene (the path does
-not shard); rank 0 prints one JSON line.
+oracle, all host threads; no product library is loaded) on the same mixed
+workload, one substep per step. Under torchrun every rank steps its own
+replica of the scene (the path does not shard); rank 0 prints one JSON line.
 """
 from __future__ import annotations
 
@@ -52,6 +56,9 @@ FLUSH_BYTES = 256 << 20
 # traffic is 76 B per particle-substep at one iteration.
 ALG_BYTES = {
     "1. Contact Gen (plane + mesh)": 24,       # x, r, flags in; contact header out
+    "1d. Contacts on Moving Meshes": 24,       # x, r, flags in; contact header out
+    "1b. Contact Ranks (cap)": 12,             # header in; rank out
+    "1f. Body Delta Entries (scan, sort)": 4,  # header in
     "2b. Integrate + Cell Keys": 40,           # x, v, w, flags, r in; key, header out
     "2e. Onesweep Pass 0": 12,                 # key in; key, id out
     "2e. Onesweep Pass 1": 16,                 # key, id in and out
@@ -59,6 +66,7 @@ ALG_BYTES = {
     "2e. Onesweep Pass 3": 16,
     "2g. Cell Table + Gather": 76,             # sorted key, id, x, v, w, r, flags in; records out
     "3. Solve+Apply(+Restitution)": 96,        # records, id, x0, v0, header in; x, v out
+    "3c. Restitution (bodies)": 52,            # header, x0, v0, v in; v out
 }
 STEP_ALG_BYTES = 76
 
@@ -88,13 +96,8 @@ def barrier(world: int) -> None:
         dist.barrier()
 
 
-def build_scene(args):
-    from vkxpbd import scenes
-
-    return scenes.particles_on_mesh(frames=300)
-
-
 def make_solver(sc, device_index=-1):
+    """A vkxpbd solver holding scene `sc` (meshes, bodies, particles)."""
     import vkxpbd
 
     cfg = vkxpbd.SolverConfig()
@@ -105,6 +108,9 @@ def make_solver(sc, device_index=-1):
     for (v, t, margin, wt) in sc.meshes:
         s.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
     s.finalize_meshes()
+    b = getattr(sc, "bodies", None)
+    if b is not None:
+        s.set_bodies(b.q, b.qd, b.com, b.inertia, b.inv_inertia, b.inv_mass, b.flags)
     s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
     return s, cfg
 
@@ -161,54 +167,181 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def dram_traffic(kernel_stage: str):
+def dram_traffic(workload: str, kernel_stage: str):
     """Per-launch DRAM bytes of a kernel at this workload from the committed ncu summary, or None."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as fh:
-            return json.load(fh).get(kernel_stage)
+            entry = json.load(fh).get(workload, {})
+        return entry.get(kernel_stage) if isinstance(entry, dict) else None
     except (OSError, ValueError):
         return None
 
 
-def cpu_baseline_sample(sc, cfg, x, v, budget_s=15.0):
-    """Oracle (CPU restatement, all host threads) on the pre-rolled state: a bounded number of substeps."""
+def launches_of(stage, prof_substeps):
+    per_iteration = stage.startswith(("3.", "3b", "3d"))
+    return prof_substeps * (ITERATIONS if per_iteration else 1)
+
+
+def stage_table(stage_ms, prof_substeps, n, peak):
+    out = {}
+    for k, v in stage_ms.items():
+        if v <= 0:
+            continue
+        us = v / launches_of(k, prof_substeps) * 1e3
+        st = {"us_per_launch": round(us, 2)}
+        if k in ALG_BYTES:
+            gbs = ALG_BYTES[k] * n / (us * 1e-6) / 1e9
+            st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
+        out[k] = st
+    return out
+
+
+def profile_stages(solver, frames, flush=None):
+    """Per-kernel device times from event-record nodes inside the frame graph (a separate,
+    serialised pass: the timed frames run two streams)."""
+    solver.set_profiling(True)
+    solver.reset_stage_times()
+    for _ in range(frames):
+        if flush is not None:
+            flush()
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+    stage_ms, prof_substeps = solver.get_stage_times()
+    solver.set_profiling(False)
+    return stage_ms, prof_substeps
+
+
+def roofline_of(workload, stage_ms, prof_substeps, n, step_ms, peak, peak_kind):
+    """Dominant kernel (most device time among the kernels with algorithmic bytes) against
+    the measured HBM copy bandwidth, and the whole substep with 76 B per particle-substep."""
+    ranked = sorted(((v, k) for k, v in stage_ms.items() if k in ALG_BYTES and v > 0), reverse=True)
+    if not ranked:
+        raise RuntimeError(f"no per-kernel stage times were recorded: {stage_ms}")
+    dom_ms, dom = ranked[0]
+    avg_ms = dom_ms / launches_of(dom, prof_substeps)
+    achieved = ALG_BYTES[dom] * n / (avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "alg_bytes_per_launch": ALG_BYTES[dom] * n, "avg_launch_us": round(avg_ms * 1e3, 2),
+                "traffic": dram_traffic(workload, dom),
+                "share_of_step": round(dom_ms / sum(v for v in stage_ms.values() if v > 0), 3)}
+    step_gbs = STEP_ALG_BYTES * n * SUBSTEPS * ITERATIONS / (step_ms * 1e-3) / 1e9
+    roofline_step = {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4), "peak_source": peak_kind}
+    return roofline, roofline_step
+
+
+def timed_frames(solver, stream, frames, flush=None):
+    """Device time (ms) of `frames` frames, CUDA events on the solver's stream."""
+    import torch
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    for k in range(frames):
+        if flush is not None:
+            flush()
+        ev[k][0].record(stream)
+        solver.step_async(DT, SUBSTEPS, ITERATIONS)
+        ev[k][1].record(stream)
+    solver.sync()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev)
+
+
+def e2e_frames(solver, frames, x, v, body_q=None, body_qd=None, flush=None, sync=None):
+    """The same frames through the public API with host buffers: every frame uploads the state
+    (set_particles, and set_bodies for bodies), steps, and reads the state back. Returns
+    (seconds, h2d bytes per frame, d2h bytes per frame)."""
+    x_h, v_h = x.copy(), v.copy()
+    q_h = None if body_q is None else body_q.copy()
+    qd_h = None if body_qd is None else body_qd.copy()
+    nbytes = x_h.nbytes + v_h.nbytes + (0 if q_h is None else q_h.nbytes + qd_h.nbytes)
+    total = 0.0
+    for _ in range(frames):
+        if flush is not None:
+            flush()
+        if sync is not None:
+            sync()
+        t0 = time.perf_counter()
+        solver.set_particles(x_h, v_h)
+        if q_h is not None:
+            solver.set_bodies(q_h, qd_h)
+        solver.step(DT, SUBSTEPS, ITERATIONS)
+        x_h = solver.get_positions()
+        v_h = solver.get_velocities()
+        if q_h is not None:
+            q_h = solver.get_body_q()
+            qd_h = solver.get_body_qd()
+        total += time.perf_counter() - t0
+    return total, nbytes, nbytes
+
+
+def cpu_baseline_sample(sc, x, v, body_q=None, body_qd=None, budget_s=15.0):
+    """Oracle (CPU restatement, all host threads) on the pre-rolled state: a bounded number of
+    substeps of the same workload."""
     import oracle as O
-    from helpers import make_pair
+    from helpers import config_for, make_pair
 
     O.load("f32").or_set_threads(os.cpu_count() or 1)
+    cfg = config_for(sc, gpu=False)
     _, orc = make_pair(sc, cfg, gpu=False)
     orc.set_particles(x, v)
+    if body_q is not None:
+        orc.set_bodies(body_q, body_qd)
+    sdt = DT / SUBSTEPS
     t0 = time.perf_counter()
-    orc.step(DT, SUBSTEPS, ITERATIONS)  # one frame = SUBSTEPS substeps (dt/substeps each)
+    orc.step(sdt, 1, ITERATIONS)
     t1 = time.perf_counter() - t0
-    substeps = SUBSTEPS
-    frames = max(0, min(20, int(budget_s / max(t1, 1e-3)) - 1))
+    more = max(0, min(10 * SUBSTEPS, int(budget_s / max(t1, 1e-3)) - 1))
     t0 = time.perf_counter()
-    for _ in range(frames):
-        orc.step(DT, SUBSTEPS, ITERATIONS)
+    for _ in range(more):
+        orc.step(sdt, 1, ITERATIONS)
     t2 = time.perf_counter() - t0
-    total_t, total_sub = t1 + t2, substeps * (1 + frames)
+    total_t, total_sub = t1 + t2, 1 + more
     return {"value": sc.n * total_sub / total_t, "unit": UNIT, "cores": int(O.load("f32").or_get_threads()),
             "kind": "port",
-            "sample": f"{total_sub} substeps of the pre-rolled {sc.n}-particle scene ({total_t:.1f} s)"}
+            "sample": f"{total_sub} substeps (dt/10 each) of the pre-rolled {sc.n}-particle {sc.name} state "
+                      f"({total_t:.1f} s)"}
+
+
+def headline(result):
+    """Each workload's figure, repeated compactly at the end of the line."""
+    head = {"mixed": result["value"], "mixed_e2e": result["e2e"]["value"],
+            "mixed_roofline_frac": result["roofline"]["frac"]}
+    pom = result.get("particles_on_mesh", {})
+    if "value" in pom:
+        head["particles_on_mesh"] = pom["value"]
+        head["particles_on_mesh_e2e"] = pom["e2e"]["value"]
+    pile = result.get("pile_1m", {})
+    if "value" in pile:
+        head["pile_1m"] = pile["value"]
+        head["pile_1m_roofline_step_frac"] = pile["roofline_step"]["frac"]
+    bat = result.get("batched", {})
+    for k, name in (("batched_value", "batched"), ("plain_value", "batched_plain"),
+                    ("batched_over_plain", "batched_over_plain"), ("batched_over_pile_1m", "batched_over_pile_1m")):
+        if k in bat:
+            head[name] = bat[k]
+    diff = result.get("diff", {})
+    for k in ("fwd_bwd_over_fwd", "forward_value"):
+        if k in diff:
+            head["diff_" + k] = diff[k]
+    if "cpu_baseline" in result:
+        head["cpu_baseline"] = result["cpu_baseline"]["value"]
+    return head
 
 
 def run_gpu(args):
     import torch
 
+    import scenes
+
     rank, world, local = dist_env()
     if args.only and "main" not in args.only.split(","):  # sub-measurements alone (not the contract line)
         dev = torch.device("cuda", local)
         parts = {}
-        if "batched" in args.only:
-            parts["batched"] = measure_batched(args, dev, None)
-        if "mixed" in args.only:
-            parts["mixed"] = measure_mixed(args, dev)
-        if "diff" in args.only:
-            parts["diff"] = measure_diff(args, dev)
-        if "pile" in args.only:
-            parts["pile_1m"] = measure_pile(args, dev)
+        for key, name, fn in (("mesh", "particles_on_mesh", measure_mesh), ("batched", "batched", measure_batched),
+                              ("diff", "diff", measure_diff), ("pile", "pile_1m", measure_pile)):
+            if key in args.only.split(","):
+                parts[name] = fn(args, dev)
         print(json.dumps(parts), flush=True)
         return
     if world > 1:
@@ -216,13 +349,15 @@ def run_gpu(args):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    sc = build_scene(args)
-    solver, cfg = make_solver(sc, device_index=local)
+
+    dev = torch.device("cuda", local)
+    sc = scenes.mixed()
+    solver, _ = make_solver(sc, device_index=local)
     for _ in range(args.preroll):
         solver.step(DT, SUBSTEPS, ITERATIONS)
     x_snap, v_snap = solver.get_positions(), solver.get_velocities()
+    q_snap, qd_snap = solver.get_body_q(), solver.get_body_qd()
 
-    dev = torch.device("cuda", local)
     stream = torch.cuda.ExternalStream(solver.cuda_stream, device=dev)
     flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -233,97 +368,65 @@ def run_gpu(args):
     for _ in range(args.warmup):
         flush()
         solver.step(DT, SUBSTEPS, ITERATIONS)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = ClockSampler(local)
     barrier(world)
     torch.cuda.synchronize(dev)
     kernels_before = solver.kernels_launched
-    for k in range(args.steps):
-        flush()
-        starts[k].record(stream)
-        solver.step_async(DT, SUBSTEPS, ITERATIONS)
-        ends[k].record(stream)
-    solver.sync()
+    dev_ms = timed_frames(solver, stream, args.steps, flush)
     kernels_timed = solver.kernels_launched - kernels_before
     torch.cuda.synchronize(dev)
     barrier(world)
     clk = clocks.stop()
-    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     dev_ms_max = reduce_max(dev_ms, world)
     particle_substeps = sc.n * SUBSTEPS * args.steps * world
     value = particle_substeps / (dev_ms_max * 1e-3)
 
-    # per-kernel device times (event-record nodes inside the frame graph), separate pass
-    solver.set_profiling(True)
-    solver.reset_stage_times()
-    prof_frames = min(args.steps, 30)
-    for _ in range(prof_frames):
-        flush()
-        solver.step(DT, SUBSTEPS, ITERATIONS)
-    stage_ms, prof_substeps = solver.get_stage_times()
-    solver.set_profiling(False)
-    launches = {k: prof_substeps * (ITERATIONS if k.startswith("3.") else 1) for k in stage_ms}
-    ranked = sorted(((v, k) for k, v in stage_ms.items() if k in ALG_BYTES and v > 0), reverse=True)
-    if not ranked:
-        raise RuntimeError(f"no per-kernel stage times were recorded: {stage_ms}")
-    dom_ms, dom = ranked[0]
-    avg_ms = dom_ms / launches[dom]
+    stage_ms, prof_substeps = profile_stages(solver, min(args.steps, 10), flush)
     peak, peak_kind = measured_peak_hbm()
-    achieved = ALG_BYTES[dom] * sc.n / (avg_ms * 1e-3) / 1e9
-    step_gbs = STEP_ALG_BYTES * sc.n * SUBSTEPS * ITERATIONS / ((dev_ms / args.steps) * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "alg_bytes_per_launch": ALG_BYTES[dom] * sc.n, "avg_launch_us": round(avg_ms * 1e3, 2),
-                "traffic": dram_traffic(dom),
-                "share_of_step": round(dom_ms / sum(stage_ms.values()), 3)}
+    roofline, roofline_step = roofline_of("mixed", stage_ms, prof_substeps, sc.n, dev_ms / args.steps, peak,
+                                          peak_kind)
 
-    # end to end through the public API with host buffers: set_particles -> step -> readback
-    solver.set_particles(x_snap, v_snap)
-    x_h, v_h = x_snap.copy(), v_snap.copy()
-    e2e_s = 0.0
-    for k in range(args.steps):
-        flush()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        solver.set_particles(x_h, v_h)
-        solver.step(DT, SUBSTEPS, ITERATIONS)
-        x_h = solver.get_positions()
-        v_h = solver.get_velocities()
-        e2e_s += time.perf_counter() - t0
+    # end to end through the public API with host buffers: set_particles + set_bodies -> step -> readback
+    e2e_s, h2d, d2h = e2e_frames(solver, args.steps, x_snap, v_snap, q_snap, qd_snap, flush,
+                                 lambda: torch.cuda.synchronize(dev))
     e2e_s = reduce_max(e2e_s, world)
-    e2e = {"value": particle_substeps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(sc.n * 12 * 2),
-           "d2h_bytes_per_step": int(sc.n * 12 * 2)}
+    e2e = {"value": particle_substeps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+    bq, bqd = solver.get_body_q()[1:], solver.get_body_qd()[1:]
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded lattice + sum-of-sines heightfield)",
-        "config": {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
+        "dtype": "f32", "data": "synthetic (seeded lattice, sum-of-sines heightfield, seeded boxes)",
+        "config": {"workload": "mixed", "particles": sc.n, "boxes": len(sc.meshes) - 1,
+                   "triangles": int(sum(m[1].shape[0] for m in sc.meshes)),
                    "substeps": SUBSTEPS, "iterations": ITERATIONS, "dt": DT, "step": "one frame (10 substeps)",
                    "preroll_frames": args.preroll, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "roofline": roofline,
-        "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
-                          "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4)},
-        "stage_ms_per_substep": {k: round(v / max(prof_substeps, 1), 5) for k, v in stage_ms.items() if v > 0},
+        "roofline_step": roofline_step,
+        "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
+        "boxes_finite": bool(np.isfinite(bq).all() and np.isfinite(bqd).all()),
         "e2e": e2e, "gpu_launches": int(kernels_timed), "clocks": clk,
     }
-    if rank == 0 and args.cache_frames > 0:
-        result["frame_cache"] = measure_cache(args, solver, sc)
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline_sample(sc, x_snap, v_snap, q_snap, qd_snap, budget_s=args.cpu_budget)
     del solver
-    for name, on, fn in (("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev, flush)),
-                         ("mixed", args.mixed_frames > 0, lambda: measure_mixed(args, dev)),
-                         ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev)),
-                         ("pile_1m", args.pile_frames > 0, lambda: measure_pile(args, dev))):
+    for name, on, fn in (("particles_on_mesh", args.mesh_frames > 0, lambda: measure_mesh(args, dev)),
+                         ("pile_1m", args.pile_frames > 0, lambda: measure_pile(args, dev)),
+                         ("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev)),
+                         ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev))):
         if rank == 0 and on:
             try:
                 result[name] = fn()
             except RuntimeError as e:  # a device-side table overflow is reported, not fatal to the line
                 result[name] = {"error": str(e)}
-    if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline_sample(sc, cfg, x_snap, v_snap, budget_s=args.cpu_budget)
     if rank == 0:
+        pile = result.get("pile_1m", {}).get("value")
+        bat = result.get("batched", {})
+        if pile and bat.get("batched_value"):
+            bat["batched_over_pile_1m"] = bat["batched_value"] / pile
+        result["headline"] = headline(result)
         print(json.dumps(result), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -331,7 +434,52 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def measure_batched(args, dev, flush):
+def measure_mesh(args, dev):
+    """Particles on a mesh: 262,144 particles (64^3 lattice, r 0.005, seed 42) falling onto the
+    256x256 sum-of-sines heightfield (130,050 triangles, seed 44) with plane, mesh and
+    particle-particle contacts, 10 substeps x 1 iteration per frame, device-timed frames after
+    a pre-roll (the pile is in contact), L2 flushed between frames; plus the same frames end
+    to end through the public API with host buffers, and the frame cache."""
+    import torch
+
+    import scenes
+
+    sc = scenes.particles_on_mesh()
+    s, _ = make_solver(sc, device_index=dev.index)
+    for _ in range(args.mesh_preroll):
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    x_snap, v_snap = s.get_positions(), s.get_velocities()
+    stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
+    flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def flush():
+        with torch.cuda.stream(stream):
+            flush_buf.fill_(1.0)
+
+    for _ in range(args.warmup):
+        flush()
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    frames = args.mesh_frames
+    torch.cuda.synchronize(dev)
+    dev_ms = timed_frames(s, stream, frames, flush)
+    stage_ms, prof_substeps = profile_stages(s, min(frames, 30), flush)
+    peak, peak_kind = measured_peak_hbm()
+    roofline, roofline_step = roofline_of("particles_on_mesh", stage_ms, prof_substeps, sc.n, dev_ms / frames,
+                                          peak, peak_kind)
+    e2e_s, h2d, d2h = e2e_frames(s, frames, x_snap, v_snap, flush=flush, sync=lambda: torch.cuda.synchronize(dev))
+    work = sc.n * SUBSTEPS * frames
+    out = {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
+           "preroll_frames": args.mesh_preroll, "frames": frames, "value": work / (dev_ms * 1e-3), "unit": UNIT,
+           "ms_per_frame": dev_ms / frames, "roofline": roofline, "roofline_step": roofline_step,
+           "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
+           "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(d2h)}}
+    if args.cache_frames > 0:
+        out["frame_cache"] = measure_cache(args, s, sc)
+    return out
+
+
+def measure_batched(args, dev):
     """Batched uneven scenes: 512 piles with log-uniform counts in [1024, 65536] (seed 46),
     each with 0..16 dynamic boxes (--batched-boxes; half-extents U[0.02, 0.08], seed 46 + s)
     dropped onto it, plane + particle-particle + box contacts, 10 substeps x 1 iteration per
@@ -341,7 +489,8 @@ def measure_batched(args, dev, flush):
     several scenes. Aggregate particle-substeps/s."""
     import torch
     import vkxpbd
-    from vkxpbd import scenes
+
+    import scenes
 
     if args.batched_boxes > 0:
         batch = scenes.batched_piles_with_boxes(args.batched_scenes, max_boxes=args.batched_boxes)
@@ -376,38 +525,14 @@ def measure_batched(args, dev, flush):
     stream = torch.cuda.ExternalStream(g.cuda_stream, device=dev)
     for _ in range(args.warmup):
         g.step(DT, SUBSTEPS, ITERATIONS)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for k in range(frames):
-        ev[k][0].record(stream)
-        g.step_async(DT, SUBSTEPS, ITERATIONS)
-        ev[k][1].record(stream)
-    g.sync()
-    torch.cuda.synchronize(dev)
+    dev_b = timed_frames(g, stream, frames) * 1e-3
     wall_b = time.perf_counter() - t0
-    dev_b = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
     launches_b = g.get_frame_stats()["kernels_per_frame"]
     work = batch.n * SUBSTEPS * frames
-    # per-kernel device times (separate pass with event-record nodes in the graph)
-    g.set_profiling(True)
-    g.reset_stage_times()
-    for _ in range(min(frames, 5)):
-        g.step(DT, SUBSTEPS, ITERATIONS)
-    stage_ms, prof_substeps = g.get_stage_times()
-    g.set_profiling(False)
+    stage_ms, prof_substeps = profile_stages(g, min(frames, 5))
     peak, peak_kind = measured_peak_hbm()
-    stages = {}
-    for k, v in stage_ms.items():
-        if v <= 0:
-            continue
-        launches = prof_substeps * (ITERATIONS if k.startswith("3.") else 1)
-        us = v / launches * 1e3
-        st = {"us_per_launch": round(us, 2)}
-        if k in ALG_BYTES:
-            gbs = ALG_BYTES[k] * batch.n / (us * 1e-6) / 1e9
-            st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
-        stages[k] = st
     step_gbs = STEP_ALG_BYTES * work / dev_b / 1e9
     del g
     torch.cuda.synchronize(dev)
@@ -439,83 +564,9 @@ def measure_batched(args, dev, flush):
             "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
                               "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
                               "peak_source": peak_kind},
-            "stages": stages,
+            "stages": stage_table(stage_ms, prof_substeps, batch.n, peak),
             "note": "batched_value device-timed (CUDA events); *_wall_value and plain_value host wall clock "
-                    "around stepping"}
-
-
-def stage_table(stage_ms, prof_substeps, n, peak):
-    out = {}
-    for k, v in stage_ms.items():
-        if v <= 0:
-            continue
-        launches = prof_substeps * (ITERATIONS if k.startswith("3.") else 1)
-        us = v / launches * 1e3
-        st = {"us_per_launch": round(us, 2)}
-        if k in ALG_BYTES:
-            gbs = ALG_BYTES[k] * n / (us * 1e-6) / 1e9
-            st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
-        out[k] = st
-    return out
-
-
-def measure_mixed(args, dev):
-    """Mixed particles and rigid bodies: 1,048,576 particles (128x128x64 lattice, r 0.005) on the
-    plane and the 256x256 heightfield plus 1,024 dynamic boxes (half-extents U[0.02, 0.08],
-    density 1000, orientations uniform on SO(3), seed 45), 10 substeps x 1 iteration per frame,
-    body contact solve and body delta apply on. Device-timed frames after a pre-roll."""
-    import torch
-    import vkxpbd
-    from vkxpbd import scenes
-
-    sc = scenes.mixed()
-    cfg = vkxpbd.SolverConfig()
-    sc.apply_config(cfg)
-    cfg.device_index = dev.index
-    s = vkxpbd.XpbdSolver()
-    s.init(cfg, sc.n)
-    for (v, t, margin, wt) in sc.meshes:
-        s.add_mesh(v, t, shape_margin=margin, is_watertight=wt)
-    s.finalize_meshes()
-    b = sc.bodies
-    s.set_bodies(b.q, b.qd, b.com, b.inertia, b.inv_inertia, b.inv_mass, b.flags)
-    s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
-    for _ in range(args.mixed_preroll):
-        s.step(DT, SUBSTEPS, ITERATIONS)
-    for _ in range(args.warmup):
-        s.step(DT, SUBSTEPS, ITERATIONS)
-    stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
-    frames = args.mixed_frames
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
-    torch.cuda.synchronize(dev)
-    for k in range(frames):
-        ev[k][0].record(stream)
-        s.step_async(DT, SUBSTEPS, ITERATIONS)
-        ev[k][1].record(stream)
-    s.sync()
-    torch.cuda.synchronize(dev)
-    dev_s = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
-    launches = s.get_frame_stats()["kernels_per_frame"]
-    s.set_profiling(True)
-    s.reset_stage_times()
-    for _ in range(min(frames, 5)):
-        s.step(DT, SUBSTEPS, ITERATIONS)
-    stage_ms, prof_substeps = s.get_stage_times()
-    s.set_profiling(False)
-    peak, peak_kind = measured_peak_hbm()
-    work = sc.n * SUBSTEPS * frames
-    step_gbs = STEP_ALG_BYTES * work / dev_s / 1e9
-    bq, bqd = s.get_body_q()[1:], s.get_body_qd()[1:]
-    return {"workload": "mixed", "particles": sc.n, "boxes": len(sc.meshes) - 1,
-            "triangles": int(sum(m[1].shape[0] for m in sc.meshes)), "preroll_frames": args.mixed_preroll,
-            "frames": frames, "value": work / dev_s, "unit": UNIT, "ms_per_frame": dev_s / frames * 1e3,
-            "launches_per_frame": int(launches),
-            "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
-                              "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
-                              "peak_source": peak_kind},
-            "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
-            "boxes_finite": bool(np.isfinite(bq).all() and np.isfinite(bqd).all()),
-            "box_height_range": [round(float(np.nanmin(bq[:, 2])), 3), round(float(np.nanmax(bq[:, 2])), 3)]}
+                    "around stepping; batched_over_pile_1m = batched_value / the pile_1m value"}
 
 
 def measure_pile(args, dev):
@@ -525,46 +576,27 @@ def measure_pile(args, dev):
     after a pre-roll (the lattice has settled into contact). Reported beside the HBM roofline
     of the whole substep (76 B per particle-substep)."""
     import torch
-    import vkxpbd
-    from vkxpbd import scenes
+
+    import scenes
 
     sc = scenes.pile(dims=(128, 128, 64), name="pile_1m")
-    cfg = vkxpbd.SolverConfig()
-    sc.apply_config(cfg)
-    cfg.device_index = dev.index
-    s = vkxpbd.XpbdSolver()
-    s.init(cfg, sc.n)
-    s.finalize_meshes()
-    s.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
+    s, _ = make_solver(sc, device_index=dev.index)
     for _ in range(args.pile_preroll + args.warmup):
         s.step(DT, SUBSTEPS, ITERATIONS)
     stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
     frames = args.pile_frames
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
     torch.cuda.synchronize(dev)
-    for k in range(frames):
-        ev[k][0].record(stream)
-        s.step_async(DT, SUBSTEPS, ITERATIONS)
-        ev[k][1].record(stream)
-    s.sync()
-    torch.cuda.synchronize(dev)
-    dev_s = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
+    dev_s = timed_frames(s, stream, frames) * 1e-3
     launches = s.get_frame_stats()["kernels_per_frame"]
-    s.set_profiling(True)
-    s.reset_stage_times()
-    for _ in range(min(frames, 5)):
-        s.step(DT, SUBSTEPS, ITERATIONS)
-    stage_ms, prof_substeps = s.get_stage_times()
-    s.set_profiling(False)
+    stage_ms, prof_substeps = profile_stages(s, min(frames, 5))
     peak, peak_kind = measured_peak_hbm()
     work = sc.n * SUBSTEPS * frames
-    step_gbs = STEP_ALG_BYTES * work / dev_s / 1e9
+    roofline, roofline_step = roofline_of("pile_1m", stage_ms, prof_substeps, sc.n, dev_s * 1e3 / frames, peak,
+                                          peak_kind)
     return {"workload": "pile_1m", "particles": sc.n, "preroll_frames": args.pile_preroll, "frames": frames,
             "value": work / dev_s, "unit": UNIT, "ms_per_frame": dev_s / frames * 1e3,
             "launches_per_frame": int(launches), "contacts_last_substep": int(s.last_contact_count),
-            "roofline_step": {"alg_bytes_per_particle_substep": STEP_ALG_BYTES, "achieved": round(step_gbs, 1),
-                              "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
-                              "peak_source": peak_kind},
+            "roofline": roofline, "roofline_step": roofline_step,
             "stages": stage_table(stage_ms, prof_substeps, sc.n, peak)}
 
 
@@ -600,7 +632,8 @@ def measure_diff(args, dev):
     Forward = the checkpointed rollout; backward = replay + adjoint of every substep."""
     import torch
     import vkxpbd
-    from vkxpbd import scenes
+
+    import scenes
 
     sc = scenes.throw()
     target = scenes.throw_target()
@@ -650,18 +683,23 @@ def measure_diff(args, dev):
 
 
 def run_reference(args):
-    """The reference's CPU implementation of the path: the oracle port on all host threads."""
+    """The reference's CPU implementation of the path: the oracle port (a restatement of the
+    reference's shaders and host driver) on all host threads, on the mixed workload. Loads no
+    product library: the scene comes from the seeded generators and the configuration from
+    the oracle's own SolverConfig (the reference's defaults, src/scene.h:15-40)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle as O
     from helpers import config_for, make_pair
 
+    import scenes
+
     O.load("f32").or_set_threads(os.cpu_count() or 1)
-    sc = build_scene(args)
-    cfg = config_for(sc)
+    sc = scenes.mixed()
+    cfg = config_for(sc, gpu=False)
     _, orc = make_pair(sc, cfg, gpu=False)
-    for _ in range(args.preroll):
+    for _ in range(args.ref_preroll):
         orc.step(DT, SUBSTEPS, ITERATIONS)
     sdt = DT / SUBSTEPS  # one step = one substep of the frame (dt/10)
     for _ in range(args.warmup):
@@ -672,13 +710,17 @@ def run_reference(args):
     t = time.perf_counter() - t0
     value = sc.n * args.steps / t
     cores = int(O.load("f32").or_get_threads())
-    sample = f"{args.steps} substeps of the pre-rolled {sc.n}-particle scene after {args.preroll} pre-roll frames"
+    sample = (f"{args.steps} substeps (dt/10 each) of the mixed workload after {args.ref_preroll} pre-roll frames "
+              f"and {args.warmup} warm-up substeps; like the reference's shader, the oracle queries every particle "
+              f"against every mesh, a cost that does not depend on the pile's state")
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + sum-of-sines heightfield)",
-           "config": {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
-                      "substeps": SUBSTEPS, "iterations": ITERATIONS, "dt": DT, "step": "one substep (dt/10)",
-                      "preroll_frames": args.preroll, "parallelism": "cpu threads"},
+           "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded lattice, sum-of-sines heightfield, seeded boxes)",
+           "config": {"workload": "mixed", "particles": sc.n, "boxes": len(sc.meshes) - 1,
+                      "triangles": int(sum(m[1].shape[0] for m in sc.meshes)), "substeps": SUBSTEPS,
+                      "iterations": ITERATIONS, "dt": DT, "step": "one substep (dt/10)",
+                      "preroll_frames": args.ref_preroll, "parallelism": "cpu threads"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -687,23 +729,24 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=10)
-    ap.add_argument("--preroll", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--preroll", type=int, default=20, help="mixed workload frames before the timed frames")
+    ap.add_argument("--ref-preroll", type=int, default=0, help="reference arm: oracle frames before timing")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mesh-frames", type=int, default=100, help="0 skips the particles-on-mesh measurement")
+    ap.add_argument("--mesh-preroll", type=int, default=30)
     ap.add_argument("--batched-scenes", type=int, default=512, help="0 skips the batched-scenes measurement")
     ap.add_argument("--batched-frames", type=int, default=10)
     ap.add_argument("--batched-boxes", type=int, default=16, help="0..N dynamic boxes per batched scene (0: none)")
-    ap.add_argument("--mixed-frames", type=int, default=10, help="0 skips the particles + boxes measurement")
-    ap.add_argument("--mixed-preroll", type=int, default=20)
     ap.add_argument("--diff-frames", type=int, default=60, help="0 skips the differentiable rollout measurement")
     ap.add_argument("--cache-frames", type=int, default=50, help="0 skips the frame-cache measurement")
     ap.add_argument("--diff-reps", type=int, default=3)
     ap.add_argument("--pile-frames", type=int, default=10, help="0 skips the 1M-particle plain pile measurement")
     ap.add_argument("--pile-preroll", type=int, default=20)
-    ap.add_argument("--only", default="", help="comma list of parts to run: main,batched,mixed,diff,pile (default all)")
+    ap.add_argument("--only", default="", help="comma list of parts to run alone: mesh,batched,diff,pile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

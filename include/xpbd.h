@@ -138,6 +138,14 @@ int xpbd_print_profiler_summary(xpbd_solver* s);
 /* Device status bits of the last step (1 = look-back timeout, 2 = BVH stack
  * overflow, 4 = mesh contact slots full) and their counters. */
 int xpbd_get_status(xpbd_solver* s, uint32_t out[4]);
+/* Test hook of the sort's bounded wait (the reference's fence wait has none,
+ * src/scene.cpp:1003): process-wide, in every later step's particle sort and in
+ * xpbd_sort_keys_noalloc, tile `hold_tile` of the first radix pass never publishes
+ * its prefix, so the look-back wait of the tile after it gives up after wait_ns
+ * (0 < wait_ns <= 1e9) and the step fails with "device wait timed out" (its result
+ * is discarded; every index stays in range). hold_tile < 0 restores normal
+ * operation (waits bounded by 1 s). Solvers re-record their frame graphs. */
+int xpbd_debug_lookback_hold(int64_t hold_tile, uint64_t wait_ns);
 /* xpbd_step without the wait: the frame's graph is queued on the solver's
  * stream and the call returns. xpbd_sync (or any state call) waits, reads the
  * contact count and checks the status word. */
@@ -273,7 +281,13 @@ int xpbd_batch_scene_offsets(xpbd_solver* s, size_t* offsets, size_t cap);
  * that every GPU loading the library holds until exit, so n is limited to
  * XPBD_NOALLOC_MAX_KEYS. The first call on a device resolves that array's
  * device address (make it before any stream capture). All calls share the
- * array: calls that overlap on the GPU race and give wrong results. */
+ * array: calls that overlap on the GPU race and give wrong results. d_keys must
+ * not overlap d_sorted_keys or d_sorted_ids (rejected). The call returns once
+ * the sort has finished on `stream`: it reads back an 8-byte status word and
+ * fails ("device wait timed out") when a bounded wait inside the sort ran out,
+ * in which case the output is invalid. The array's device address is resolved
+ * once per device ordinal for the life of the process, so a cudaDeviceReset in
+ * between is not supported. */
 #define XPBD_NOALLOC_MAX_KEYS (1 << 20)
 int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint32_t* d_sorted_ids, size_t n,
                            int key_bits, void* stream);

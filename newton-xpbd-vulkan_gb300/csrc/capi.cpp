@@ -235,6 +235,10 @@ int xpbd_get_status(xpbd_solver* s, uint32_t out[4]) {
     return guarded([&] { S(s).status(out); });
 }
 
+int xpbd_debug_lookback_hold(int64_t hold_tile, uint64_t wait_ns) {
+    return guarded([&] { xpbd::set_lookback_debug(hold_tile, wait_ns); });
+}
+
 int xpbd_step_async(xpbd_solver* s, float dt, int substeps, int iterations) {
     return guarded([&] { S(s).step_async(dt, substeps, iterations); });
 }

@@ -3,13 +3,34 @@
 // histogram/scan/scatter passes (sort_histogram.comp, sort_scan_{a,b,c}.comp,
 // sort_scatter.comp) and grid_offsets.comp with its 16 MiB of fills.
 #include <algorithm>
+#include <atomic>
 #include <stdexcept>
+#include <string>
 
 #include "kernels.h"
 #include "particle.cuh"
 #include "xmath.cuh"
 
 namespace xpbd {
+
+namespace {
+std::atomic<int> g_sm_count[64];
+}  // namespace
+
+int device_sm_count() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetDevice failed: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) throw std::runtime_error("device ordinal out of range (at most 64 devices)");
+    int c = g_sm_count[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+    e = cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || c <= 0)
+        throw std::runtime_error(std::string("cudaDeviceGetAttribute(MultiProcessorCount) failed: ") +
+                                 cudaGetErrorString(e));
+    g_sm_count[dev].store(c, std::memory_order_relaxed);
+    return c;
+}
 
 // ---------------------------------------------------------------------------
 // Keys + digit histograms of every sort pass (+ plane contacts when no mesh)
@@ -74,7 +95,7 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo, uint32_t* ccount,
                          uint32_t* stamp) {
     if (n <= 0) return;
-    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 8);
     size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
     k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pscene, pp, pl, keys, sp.bits, sp.passes, hist,
                                             cinfo, ccount, stamp);
@@ -103,7 +124,7 @@ __global__ void __launch_bounds__(256) k_mask_keys(int64_t n, const uint32_t* __
 void launch_mask_keys(cudaStream_t s, int64_t n, const uint32_t* keys, uint32_t mask, uint32_t* out,
                       const SortPlan& sp, uint32_t* hist) {
     if (n <= 0) return;
-    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 8);
     k_mask_keys<<<blocks, 256, sizeof(uint32_t) * ((size_t)sp.passes << sp.bits), s>>>(n, keys, mask, out, sp.bits,
                                                                                       sp.passes, hist);
 }
@@ -142,6 +163,30 @@ constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
 constexpr int kLookWindow = 8;
+constexpr uint32_t kNoHold = 0xffffffffu;
+
+namespace {
+// test hook of the bounded wait (set_lookback_debug): tile g_hold_tile of the first pass
+// of every sort never publishes, and waits give up after g_wait_ns
+std::atomic<uint32_t> g_hold_tile{kNoHold};
+std::atomic<uint64_t> g_wait_ns{kWaitLimitNs};
+std::atomic<uint32_t> g_debug_generation{0};
+}  // namespace
+
+void set_lookback_debug(int64_t hold_tile, uint64_t wait_ns) {
+    if (hold_tile < 0) {
+        g_hold_tile.store(kNoHold);
+        g_wait_ns.store(kWaitLimitNs);
+    } else {
+        if (hold_tile >= (int64_t)kNoHold) throw std::runtime_error("set_lookback_debug: tile index too large");
+        if (wait_ns == 0 || wait_ns > kWaitLimitNs)
+            throw std::runtime_error("set_lookback_debug: wait limit must be in (0, 1 s]");
+        g_hold_tile.store((uint32_t)hold_tile);
+        g_wait_ns.store(wait_ns);
+    }
+    g_debug_generation.fetch_add(1u);
+}
+uint32_t lookback_debug_generation() { return g_debug_generation.load(); }
 
 template <int THREADS>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_scan, uint32_t& total) {
@@ -172,7 +217,8 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
                                                       uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                       const uint32_t* __restrict__ hist, uint32_t* lookback,
                                                       uint32_t* tile_counter, DeviceStatus* st,
-                                                      const uint32_t* __restrict__ n_dev) {
+                                                      const uint32_t* __restrict__ n_dev, uint32_t hold_tile,
+                                                      uint64_t wait_ns) {
     constexpr int BINS = 1 << BITS;
     constexpr int WARPS = THREADS / 32;
     constexpr int TILE = THREADS * ITEMS;
@@ -243,10 +289,12 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
     // relaxed loads (all of a window in flight at once) suffice.
     uint32_t* my = lookback + (size_t)tile * BINS + tid;
     uint32_t prev = 0;
+    // a held tile (test hook) publishes nothing: its successor's wait runs out
+    const bool publish = tile != hold_tile;
     if (tile == 0) {
-        st_release(my, kFlagInc | tot);
+        if (publish) st_release(my, kFlagInc | tot);
     } else {
-        st_release(my, kFlagAgg | tot);
+        if (publish) st_release(my, kFlagAgg | tot);
         int64_t p = (int64_t)tile - 1;
         uint64_t t0 = 0;
         bool found = false;
@@ -270,7 +318,7 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
                 const uint64_t now = globaltimer_ns();
                 if (t0 == 0) {
                     t0 = now;
-                } else if (now - t0 > kWaitLimitNs) {
+                } else if (now - t0 > wait_ns) {
                     atomicOr(&st->error_bits, kErrLookbackTimeout);
                     atomicAdd(&st->lookback_timeouts, 1u);
                     break;
@@ -281,7 +329,7 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
             p -= used;
             t0 = 0;
         }
-        st_release(my, kFlagInc | ((prev + tot) & kCountMask));
+        if (publish) st_release(my, kFlagInc | ((prev + tot) & kCountMask));
     }
     // output slot = s_gbase[d] + position in the tile's digit-sorted order (modular arithmetic)
     s_gbase[tid] = glob_excl + prev - tile_excl;
@@ -324,7 +372,7 @@ size_t sort_lookback_words(const SortPlan& p) { return (size_t)p.tiles << p.bits
 template <int BITS, int ITEMS>
 static void onesweep_variant(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* ki,
                              const uint32_t* vi, uint32_t* ko, uint32_t* vo, const uint32_t* hist, uint32_t* lb,
-                             uint32_t* tc, DeviceStatus* st, const uint32_t* n_dev) {
+                             uint32_t* tc, DeviceStatus* st, const uint32_t* n_dev, bool debug_hold) {
     constexpr int THREADS = 1 << BITS;
     constexpr int TILE = THREADS * ITEMS;
     size_t smem = sizeof(uint32_t) * ((size_t)(THREADS / 32) * (1 << BITS) + 2 * TILE + (1 << BITS));
@@ -334,19 +382,20 @@ static void onesweep_variant(cudaStream_t s, int64_t n, const SortPlan& sp, int 
                              (int)smem);
         attr_set = true;
     }
+    const uint32_t hold = (debug_hold && pass == 0) ? g_hold_tile.load() : kNoHold;
     k_onesweep<BITS, THREADS, ITEMS><<<sp.tiles, THREADS, smem, s>>>(n, pass * BITS, ki, vi, ko, vo, hist, lb, tc,
-                                                                     st, n_dev);
+                                                                     st, n_dev, hold, g_wait_ns.load());
 }
 
 void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
-                          DeviceStatus* st, const uint32_t* n_dev) {
+                          DeviceStatus* st, const uint32_t* n_dev, bool debug_hold) {
     if (n <= 0) return;
 #define XPBD_OS(B, I)                                                                                      \
     if (sp.bits == B && sp.items == I)                                                                     \
         return onesweep_variant<B, I>(s, n, sp, pass, keys_in, vals_in, keys_out, vals_out, hist_pass, \
-                                      lookback, tile_counter, st, n_dev);
+                                      lookback, tile_counter, st, n_dev, debug_hold);
     XPBD_OS(8, 2)
     XPBD_OS(8, 4)
     XPBD_OS(8, 8)

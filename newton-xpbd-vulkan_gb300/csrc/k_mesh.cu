@@ -221,7 +221,7 @@ void launch_collide_triage(cudaStream_t s, int64_t n, const uint32_t* order, con
                                                              near);
 }
 
-// One warp per block, 32 blocks per SM (the same 4,864 resident warps as four-warp blocks):
+// One warp per block, 32 blocks per SM (the same resident warps as four-warp blocks):
 // a block's registers are released as soon as its own warp is done, so the sort chain
 // running beside the traversal takes over the SMs of the warps that finish first
 // (bench frame 2.89 -> 2.80 ms; the traversal itself is as fast either way).
@@ -230,7 +230,7 @@ void launch_collide_walk(cudaStream_t s, int64_t n, const float4* x, const float
                          const uint32_t* near, DeviceStatus* st) {
     if (n <= 0) return;
     const int threads = kCollideThreads;
-    const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads, 152 * 32);
+    const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads, (int64_t)device_sm_count() * 32);
     k_collide<<<blocks, threads, 0, s>>>(n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
 }
 

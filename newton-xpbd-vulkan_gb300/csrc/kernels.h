@@ -167,11 +167,22 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
                          uint32_t* ccount, uint32_t* stamp);
 // one onesweep pass; vals_in == nullptr means vals are the element index; n_dev (optional)
-// holds the element count on the device (at most n, the capacity the grid is sized for)
+// holds the element count on the device (at most n, the capacity the grid is sized for).
+// debug_hold: the pass honours the look-back test hook (set_lookback_debug)
 void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pass, const uint32_t* keys_in,
                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           const uint32_t* hist_pass, uint32_t* lookback, uint32_t* tile_counter,
-                          DeviceStatus* st, const uint32_t* n_dev = nullptr);
+                          DeviceStatus* st, const uint32_t* n_dev = nullptr, bool debug_hold = false);
+// Test hook of the bounded look-back wait: in every later sort pass launched with
+// debug_hold (the particle sort of a step and the allocation-free sort), tile hold_tile of
+// the first pass never publishes its prefix, so its successors' waits run out after
+// wait_ns (0 < wait_ns <= 1 s) and set kErrLookbackTimeout. The output of such a sort is
+// wrong but every index stays in range. hold_tile < 0 restores normal operation.
+// lookback_debug_generation() changes on every call (solvers then re-record their graphs).
+void set_lookback_debug(int64_t hold_tile, uint64_t wait_ns);
+uint32_t lookback_debug_generation();
+// SM count of the current device (cudaDevAttrMultiProcessorCount), cached per device
+int device_sm_count();
 // cell table + sorted-order particle records
 void launch_cells_gather(cudaStream_t s, int64_t n, const uint32_t* skeys, const uint32_t* sids, const float4* x,
                          const float4* v, const float* w, const float* r, const int* flags, PredictParams pp,

@@ -13,7 +13,11 @@
 // held by every GPU that loads this module until the process exits. All calls
 // share it: calls that overlap on the GPU (different streams, or different host
 // threads without ordering) race on it and give wrong results. The histograms,
-// look-back words and tile counters are cleared at the start of every call.
+// look-back words, tile counters and status block are cleared at the start of
+// every call. The input must not overlap either output (a pass may write the
+// output while an earlier one still reads the input). A call returns once the
+// sort has finished on its stream: it reads back the status block, and a
+// look-back wait that ran out (the output is then wrong) makes the call fail.
 #include <cstdint>
 #include <mutex>
 #include <stdexcept>
@@ -99,11 +103,15 @@ void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* so
     if (key_bits < 1 || key_bits > 32) throw std::runtime_error("xpbd_sort_keys_noalloc: key_bits must be in 1..32");
     if (n == 0) return;
     if (!keys || !sorted_keys || !sorted_ids) throw std::runtime_error("xpbd_sort_keys_noalloc: null buffer");
+    const auto overlap = [n](const uint32_t* a, const uint32_t* b) { return a < b + n && b < a + n; };
+    if (overlap(keys, sorted_keys) || overlap(keys, sorted_ids) || overlap(sorted_keys, sorted_ids))
+        throw std::runtime_error("xpbd_sort_keys_noalloc: the input and output buffers must not overlap");
     uint32_t* base = scratch_for_current_device();
     const SortPlan plan = make_sort_plan(n, key_bits, kNoAllocBits, kNoAllocItems);
     // zero histograms, look-back words and tile counters (the key/id pair needs no clearing)
     XPBD_CUDA_NOALLOC(cudaMemsetAsync(base + kNaHist, 0, (size_t)(kNaWords - kNaHist) * sizeof(uint32_t), s));
-    const int blocks = (int)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
+    const int64_t max_blocks = (int64_t)device_sm_count() * 8;
+    const int blocks = (int)((n + 255) / 256 < max_blocks ? (n + 255) / 256 : max_blocks);
     k_key_hist<<<blocks, 256, 0, s>>>(n, keys, plan.bits, plan.passes, base + kNaHist);
     XPBD_CUDA_NOALLOC(cudaGetLastError());
     // ping-pong so that the last pass lands in the caller's output buffers
@@ -115,11 +123,20 @@ void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* so
         uint32_t* vo = to_out ? sorted_ids : base + kNaPairV;
         launch_onesweep_pass(s, n, plan, p, kin, vin, ko, vo, base + kNaHist + ((int64_t)p << plan.bits),
                              base + kNaLook + (int64_t)p * kNoAllocTiles * (1 << kNoAllocBits),
-                             base + kNaTiles + p, reinterpret_cast<DeviceStatus*>(base + kNaStatus));
+                             base + kNaTiles + p, reinterpret_cast<DeviceStatus*>(base + kNaStatus), nullptr,
+                             true);
         XPBD_CUDA(cudaGetLastError());
         kin = ko;
         vin = vo;
     }
+    // the status block of this call (a bounded look-back wait sets a bit instead of hanging)
+    DeviceStatus host{};
+    XPBD_CUDA_NOALLOC(
+        cudaMemcpyAsync(&host, base + kNaStatus, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+    XPBD_CUDA_NOALLOC(cudaStreamSynchronize(s));
+    if (host.error_bits & kErrLookbackTimeout)
+        throw std::runtime_error("xpbd_sort_keys_noalloc: device wait timed out in the onesweep look-back "
+                                 "(output invalid)");
 }
 
 }  // namespace xpbd

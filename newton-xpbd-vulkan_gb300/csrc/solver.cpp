@@ -1037,7 +1037,8 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         uint32_t* vo = pair_v_[p & 1].p;
         launch_onesweep_pass(stream_, n, plan_, p, kin, vin, ko, vo,
                              sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
-                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st);
+                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st,
+                             nullptr, true);
         count_kernel();
         prof_mark(P_SORT0 + std::min(p, 3));
         kin = ko;
@@ -1137,6 +1138,10 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     rollout_valid_ = false;  // the stored rollout no longer ends at the current state
     ensure_substep_capacity(substeps);
     if (n_ == 0) return;
+    if (lb_debug_seen_ != lookback_debug_generation()) {  // the sort's test hook changed: re-record
+        clear_graphs();
+        lb_debug_seen_ = lookback_debug_generation();
+    }
     ensure_cull();
     if (!sort_tuned_ && n_ >= (1u << 20)) {  // large scenes: pick the sort variant on the real keys
         const int cc = contact_count_;

@@ -209,6 +209,7 @@ class Solver {
     void prof_mark(int slot);
     void apply_sort_plan(int bits, int items);
     bool sort_tuned_ = false;
+    uint32_t lb_debug_seen_ = 0;  // lookback_debug_generation() the frame graphs were recorded under
     void count_kernel(int k = 1);
     void count_memset();
 

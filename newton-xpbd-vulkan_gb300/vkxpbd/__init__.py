@@ -130,6 +130,14 @@ def enumerate_devices():
     return out
 
 
+def debug_lookback_hold(hold_tile: int, wait_ns: int = 1_000_000) -> None:
+    """Test hook of the sort's bounded look-back wait (xpbd_debug_lookback_hold): tile
+    `hold_tile` of the first radix pass of every later particle sort never publishes, so
+    the next step fails with "device wait timed out" after wait_ns. hold_tile < 0 restores
+    normal operation."""
+    _check(_lib.xpbd_debug_lookback_hold(int(hold_tile), int(wait_ns)))
+
+
 class XpbdSolver:
     """vkx::XpbdSolver (src/scene.h:74-135) on the GPU."""
 

@@ -94,6 +94,7 @@ SIGNATURES = {
     "xpbd_get_aux_diag": (C.c_int, [_P, C.c_int, C.c_void_p, _Z, C.POINTER(_Z)]),
     "xpbd_print_profiler_summary": (C.c_int, [_P]),
     "xpbd_get_status": (C.c_int, [_P, _U]),
+    "xpbd_debug_lookback_hold": (C.c_int, [C.c_int64, C.c_uint64]),
     "xpbd_step_async": (C.c_int, [_P, C.c_float, C.c_int, C.c_int]),
     "xpbd_sync": (C.c_int, [_P]),
     "xpbd_stream": (C.c_void_p, [_P]),

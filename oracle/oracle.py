@@ -19,10 +19,21 @@ REFDIR = os.path.join(HERE, "_ref")
 NUM_CELLS = 128 ** 3
 
 
+def reference_checkout():
+    """The reference checkout the BVH shim is compiled from: $XPBD_REFERENCE_DIR, else the
+    build container's checkout; None where neither exists (the GPU machine has none)."""
+    for d in (os.environ.get("XPBD_REFERENCE_DIR"), "/root/reference"):
+        if d and os.path.exists(os.path.join(d, "src", "mesh_bvh.h")):
+            return d
+    return None
+
+
 def build() -> None:
     """Oracle libraries, plus the reference's BVH shim where the checkout exists (Makefile REF)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "-j2", "all"])
-    subprocess.check_call(["make", "-s", "-C", HERE, "ref-if-present"])
+    ref = reference_checkout()
+    if ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref-if-present", f"REF={ref}"])
 
 
 class Config(C.Structure):
@@ -50,6 +61,31 @@ class Config(C.Structure):
             else:
                 setattr(c, name, getattr(cfg, name))
         return c
+
+
+class SolverConfig:
+    """vkx::SolverConfig's numeric fields with the reference's defaults (src/scene.h:15-40),
+    as a plain object: the oracle's own configuration, built without the product library."""
+
+    def __init__(self):
+        self.dt = 1.0 / 60.0
+        self.substeps = 1
+        self.iterations = 2
+        self.particle_v_max = 1e5
+        self.soft_contact_mu = 0.5
+        self.shape_material_mu = 1.0
+        self.soft_contact_relaxation = 0.9
+        self.particle_adhesion = 0.0
+        self.particle_mu = 0.5
+        self.particle_cohesion = 0.0
+        self.particle_max_radius = 0.02
+        self.search_radius = 0.04
+        self.soft_contact_margin = 0.01
+        self.enable_restitution = False
+        self.soft_contact_restitution = 0.0
+        self.has_ground_plane = True
+        self.ground_plane_altitude = 0.0
+        self.gravity = [0.0, 0.0, -9.81]
 
 
 _P = C.c_void_p

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [os.path.join(ROOT, "oracle"), os.path.join(ROOT, "newton-xpbd-vulkan_gb300")]
 
 import oracle as O  # noqa: E402
-from vkxpbd import scenes  # noqa: E402
+import scenes  # noqa: E402
 
 
 def meshes():

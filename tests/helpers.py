@@ -4,13 +4,18 @@ from __future__ import annotations
 import numpy as np
 
 import oracle as O
-from vkxpbd import scenes
+import scenes
 
 
-def config_for(scene, **overrides):
-    import vkxpbd
+def config_for(scene, gpu=True, **overrides):
+    """The scene's configuration on vkxpbd.SolverConfig, or (gpu=False) on the oracle's own
+    SolverConfig with the same defaults (no product code loaded)."""
+    if gpu:
+        import vkxpbd
 
-    cfg = vkxpbd.SolverConfig()
+        cfg = vkxpbd.SolverConfig()
+    else:
+        cfg = O.SolverConfig()
     scene.apply_config(cfg)
     for k, v in overrides.items():
         setattr(cfg, k, v)
@@ -18,8 +23,9 @@ def config_for(scene, **overrides):
 
 
 def make_pair(scene, cfg, max_contacts=0, gpu=True, precision="f32", body_params=None):
-    """(gpu solver or None, oracle solver) with identical inputs."""
-    import vkxpbd
+    """(gpu solver or None, oracle solver) with identical inputs. gpu=False loads no product code."""
+    if gpu:
+        import vkxpbd
 
     body_params = dict(body_params or {})
     orc = O.OracleSolver(cfg, scene.n, max_contacts, precision=precision)

@@ -11,7 +11,7 @@ import pytest
 
 import oracle as O
 from helpers import config_for
-from vkxpbd import scenes
+import scenes
 
 FRAMES = 6
 

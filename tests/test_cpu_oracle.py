@@ -37,7 +37,7 @@ def test_oracle_bvh_matches_live_reference_build():
     ref = O.load_ref()
     if ref is None:
         pytest.skip("reference BVH shim not built here (needs the reference checkout)")
-    from vkxpbd import scenes
+    import scenes
 
     v, t = scenes.heightfield(256)  # the 130,050-triangle heightfield of the mesh workload
     a = O.bvh_build(v, t)
@@ -48,7 +48,7 @@ def test_oracle_bvh_matches_live_reference_build():
 
 
 def test_watertight_detection():
-    from vkxpbd import scenes
+    import scenes
 
     bv, bt = scenes.box_mesh((1, 1, 1))
     assert O.tris_watertight(bt, 8)
@@ -242,7 +242,7 @@ def test_enumerate_devices_is_a_list():
 def test_particle_exactly_on_mesh_surface_gives_finite_contact():
     """exact_sqrt(0): a particle whose closest surface point equals its position (seen in the
     mixed workload after boxes pressed particles into the heightfield) keeps a finite contact."""
-    from vkxpbd import scenes
+    import scenes
 
     sc = scenes.particles_on_mesh(dims=(1, 1, 1))
     p = np.array([[0.23391318321228027, -0.32021233439445496, 0.045575764030218124]], np.float32)

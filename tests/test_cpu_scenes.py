@@ -3,7 +3,7 @@ import math
 
 import numpy as np
 
-from vkxpbd import scenes
+import scenes
 
 
 def test_batch_counts_log_uniform_and_seeded():
@@ -38,3 +38,47 @@ def test_batch_concat_and_offsets():
     x = batch.concat("positions")
     assert x.shape == (15, 3) and x.dtype == np.float32
     assert np.array_equal(x[5:14], batch.scenes[1].positions)
+
+
+def test_oracle_config_has_the_reference_defaults():
+    """The oracle's own SolverConfig (used where no product code may load) carries the same
+    defaults as vkxpbd.SolverConfig (src/scene.h:15-40)."""
+    import oracle as O
+    import vkxpbd
+
+    a, b = O.SolverConfig(), vkxpbd.SolverConfig()
+    for k, va in vars(a).items():
+        vb = getattr(b, k)
+        if k == "gravity":
+            assert np.allclose(list(vb), va, rtol=1e-6), k
+        elif isinstance(va, bool):
+            assert bool(vb) == va, k
+        else:
+            assert abs(float(vb) - float(va)) <= 1e-6 * max(1.0, abs(float(va))), k
+
+
+def test_reference_arm_path_loads_no_product_code():
+    """The benchmark's reference arm builds its scene and configuration and steps the oracle
+    without importing vkxpbd or loading libxpbd_gb300.so."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys, os\n"
+        f"sys.path[:0] = [{os.path.join(root, 'newton-xpbd-vulkan_gb300')!r}, {os.path.join(root, 'oracle')!r}, "
+        f"{os.path.join(root, 'tests')!r}]\n"
+        "import scenes\n"
+        "from helpers import config_for, make_pair\n"
+        "sc = scenes.pile(dims=(6, 6, 6))\n"
+        "cfg = config_for(sc, gpu=False)\n"
+        "_, orc = make_pair(sc, cfg, gpu=False)\n"
+        "orc.step(1.0 / 60.0, 1, 1)\n"
+        "assert 'vkxpbd' not in sys.modules, 'vkxpbd imported'\n"
+        "maps = open('/proc/self/maps').read() if os.path.exists('/proc/self/maps') else ''\n"
+        "assert 'libxpbd_gb300' not in maps, 'product library loaded'\n"
+        "print('ok')\n"
+    )
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.strip().endswith("ok"), out.stderr

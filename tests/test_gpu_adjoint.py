@@ -4,7 +4,7 @@ import pytest
 
 import oracle as O
 from helpers import assert_bitexact, config_for
-from vkxpbd import scenes
+import scenes
 
 pytestmark = pytest.mark.gpu
 

@@ -49,7 +49,7 @@ def test_boxes_stack_and_heightfield_bitexact():
 
 def test_mixed_small_bitexact():
     """A scaled-down particles + heightfield + falling boxes scene (the mixed workload's recipe)."""
-    from vkxpbd import scenes
+    import scenes
 
     sc = scenes.mixed(dims=(24, 24, 12), n_boxes=24, hf_vertices=64)
     _run(sc, 20)

@@ -47,7 +47,7 @@ def test_gpu_bvh_matches_reference_golden(name):
 
 
 def test_gpu_bvh_of_several_meshes_and_bench_heightfield():
-    from vkxpbd import scenes
+    import scenes
 
     hv, ht = scenes.heightfield(256)
     bv, bt = scenes.box_mesh((0.1, 0.2, 0.05), center=(0.1, 0.0, 0.3), quat_xyzw=(0.2, 0.1, 0.0, 0.97))

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from helpers import assert_bitexact, config_for, make_pair
-from vkxpbd import scenes
+import scenes
 
 pytestmark = pytest.mark.gpu
 

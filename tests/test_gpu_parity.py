@@ -39,7 +39,7 @@ def test_grid_intermediates_bitexact():
 
 def test_pile_config1_bitexact():
     """The 4,096-particle pile (plane, particle-particle, restitution 0.2), 10 substeps x 1 iteration."""
-    from vkxpbd import scenes
+    import scenes
 
     sc = scenes.pile()
     cfg = config_for(sc)
@@ -87,7 +87,7 @@ def test_mesh_heightfield_bitexact():
 
 
 def test_watertight_box_bitexact():
-    from vkxpbd import scenes
+    import scenes
 
     sc = small_pile(8, spacing=0.02, radius=0.01, bottom_z=0.05)
     bv, bt = scenes.box_mesh((0.05, 0.05, 0.03), center=(0.0, 0.0, 0.03), quat_xyzw=(0.0, 0.0, 0.3826834, 0.9238795))
@@ -222,7 +222,7 @@ def test_tolerance_floor():
 
 
 def test_particle_exactly_on_mesh_surface_bitexact():
-    from vkxpbd import scenes
+    import scenes
 
     sc = scenes.particles_on_mesh(dims=(1, 1, 1))
     sc.positions = np.array([[0.23391318321228027, -0.32021233439445496, 0.045575764030218124]], np.float32)

@@ -29,7 +29,8 @@ def test_noalloc_sort_matches_solver_sort_twice():
     import torch
 
     from helpers import assert_bitexact, config_for, make_pair
-    from vkxpbd import _abi, scenes
+    import scenes
+    from vkxpbd import _abi
 
     lib = _abi.load()
     sc = scenes.pile(dims=(24, 24, 24))
@@ -54,6 +55,72 @@ def test_noalloc_sort_matches_solver_sort_twice():
         assert_bitexact(out_v, ref_ids, f"call {call}: sorted ids")
 
 
+def _noalloc_sort(lib, keys, key_bits, torch, dev):
+    n = keys.size
+    d_keys = torch.from_numpy(keys.view(np.int32).copy()).to(dev)
+    d_out_k = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    d_out_v = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    rc = lib.xpbd_sort_keys_noalloc(C.c_void_p(d_keys.data_ptr()), C.c_void_p(d_out_k.data_ptr()),
+                                    C.c_void_p(d_out_v.data_ptr()), n, key_bits, C.c_void_p(stream.cuda_stream))
+    torch.cuda.synchronize(dev)
+    return rc, d_out_k.cpu().numpy().view(np.uint32), d_out_v.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("n", [13_824, 1 << 20])
+@pytest.mark.parametrize("key_bits", [21, 32])
+def test_noalloc_sort_random_keys_stable(n, key_bits):
+    """Up to the stated maximum (1,048,576 keys: every look-back word of the array in use) and
+    with 32-bit keys (four radix passes, so the first pass writes the scratch pair): sorted
+    keys and ids against numpy's stable argsort, twice in a row on different keys."""
+    import torch
+
+    from helpers import assert_bitexact
+    from vkxpbd import _abi
+
+    lib = _abi.load()
+    dev = torch.device("cuda", 0)
+    for call in range(2):
+        rng = np.random.default_rng(1000 * call + key_bits)
+        hi = 1 << key_bits
+        # many equal keys as in a hash grid (a few values repeated), so stability matters
+        keys = rng.integers(0, min(hi, 4 * n), size=n, dtype=np.uint64)
+        if key_bits == 32:
+            keys = (keys * 2654435761) % hi  # spread over the whole word
+        keys = keys.astype(np.uint32)
+        rc, out_k, out_v = _noalloc_sort(lib, keys, key_bits, torch, dev)
+        assert rc == 0, lib.xpbd_last_error().decode()
+        order = np.argsort(keys, kind="stable").astype(np.uint32)
+        assert_bitexact(out_v, order, f"n={n} bits={key_bits} call {call}: ids")
+        assert_bitexact(out_k, keys[order], f"n={n} bits={key_bits} call {call}: keys")
+
+
+def test_noalloc_sort_reports_a_timed_out_wait():
+    """A look-back wait that runs out (one tile held back by the test hook, 1 ms limit) makes
+    the call fail instead of returning a wrong order; the next call is exact again."""
+    import torch
+
+    import vkxpbd
+    from helpers import assert_bitexact
+    from vkxpbd import _abi
+
+    lib = _abi.load()
+    dev = torch.device("cuda", 0)
+    keys = np.random.default_rng(5).integers(0, 1 << 21, size=20_000, dtype=np.uint32)
+    vkxpbd.debug_lookback_hold(2, 1_000_000)
+    try:
+        rc, _, _ = _noalloc_sort(lib, keys, 21, torch, dev)
+        assert rc != 0
+        assert "timed out" in lib.xpbd_last_error().decode()
+    finally:
+        vkxpbd.debug_lookback_hold(-1)
+    rc, out_k, out_v = _noalloc_sort(lib, keys, 21, torch, dev)
+    assert rc == 0, lib.xpbd_last_error().decode()
+    order = np.argsort(keys, kind="stable").astype(np.uint32)
+    assert_bitexact(out_v, order, "ids after the timed-out call")
+    assert_bitexact(out_k, keys[order], "keys after the timed-out call")
+
+
 def test_noalloc_sort_rejects_too_many_keys():
     from vkxpbd import _abi
 
@@ -61,3 +128,15 @@ def test_noalloc_sort_rejects_too_many_keys():
     rc = lib.xpbd_sort_keys_noalloc(C.c_void_p(16), C.c_void_p(16), C.c_void_p(16), (1 << 20) + 1, 21, None)
     assert rc != 0
     assert "at most 1048576" in lib.xpbd_last_error().decode()
+
+
+def test_noalloc_sort_rejects_overlapping_buffers():
+    """The input must not overlap an output: a pass could overwrite keys a later tile still reads."""
+    from vkxpbd import _abi
+
+    lib = _abi.load()
+    a, b = 1 << 20, 1 << 24
+    for keys, out_k, out_v in ((a, a, b), (a, b, a + 64), (a, b, b + 64)):
+        rc = lib.xpbd_sort_keys_noalloc(C.c_void_p(keys), C.c_void_p(out_k), C.c_void_p(out_v), 1000, 21, None)
+        assert rc != 0
+        assert "must not overlap" in lib.xpbd_last_error().decode()
