@@ -347,11 +347,18 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(int64_t n, int shift, cons
         }
     }
     __syncthreads();
+    // A slot is below n whenever the histograms match the input and every look-back
+    // completed. After a wait that ran out, this pass's slots are still below n, but the
+    // next pass's input then holds duplicates and holes that its (up-front) histograms do
+    // not count, so its slots could run past n: the bound keeps a failed sort in range.
+    const uint32_t n_out = (uint32_t)n;
     for (int i = tid; i < valid_n; i += THREADS) {
         const uint32_t key = s_keys[i];
         const uint32_t g = s_gbase[(key >> shift) & (BINS - 1)] + (uint32_t)i;
-        keys_out[g] = key;
-        vals_out[g] = s_vals[i];
+        if (g < n_out) {
+            keys_out[g] = key;
+            vals_out[g] = s_vals[i];
+        }
     }
 }
 

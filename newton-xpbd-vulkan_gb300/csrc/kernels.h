@@ -177,7 +177,8 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
 // debug_hold (the particle sort of a step and the allocation-free sort), tile hold_tile of
 // the first pass never publishes its prefix, so its successors' waits run out after
 // wait_ns (0 < wait_ns <= 1 s) and set kErrLookbackTimeout. The output of such a sort is
-// wrong but every index stays in range. hold_tile < 0 restores normal operation.
+// wrong (duplicates and holes holding earlier contents of the buffers) but every slot it
+// writes stays below n (the scatter is bounded). hold_tile < 0 restores normal operation.
 // lookback_debug_generation() changes on every call (solvers then re-record their graphs).
 void set_lookback_debug(int64_t hold_tile, uint64_t wait_ns);
 uint32_t lookback_debug_generation();

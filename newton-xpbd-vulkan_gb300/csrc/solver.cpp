@@ -1252,8 +1252,13 @@ void Solver::finish_frame(int substeps) {
     std::memcpy(&raw, pinned_, 4);
     std::memcpy(&host_status_, pinned_ + 1, sizeof(DeviceStatus));
     contact_count_ = (int)std::min<int64_t>((int64_t)raw, contact_max_);
-    if (host_status_.error_bits & kErrLookbackTimeout)
+    if (host_status_.error_bits & kErrLookbackTimeout) {
+        // the failed sort's ids (with duplicates and holes) would be the next collision
+        // pass's particle order: start it from the identity again
+        launch_iota(stream_, (int64_t)n_, pair_v_[(plan_.passes - 1) & 1].p);
+        XPBD_CUDA(cudaStreamSynchronize(stream_));
         throw std::runtime_error("device wait timed out in the onesweep look-back (result discarded)");
+    }
     if (host_status_.error_bits & kErrStackOverflow)
         throw std::runtime_error("BVH traversal stack overflow (more than 32 pending nodes)");
     if (host_status_.error_bits & kErrSlotOverflow)
