@@ -353,10 +353,17 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     sc = scenes.mixed()
     solver, _ = make_solver(sc, device_index=local)
-    for _ in range(args.preroll):
-        solver.step(DT, SUBSTEPS, ITERATIONS)
+    if args.load_state:  # a pre-rolled state saved by --save-state (short profiling runs)
+        st = np.load(args.load_state)
+        solver.set_particles(st["x"], st["v"])
+        solver.set_bodies(st["q"], st["qd"])
+    else:
+        for _ in range(args.preroll):
+            solver.step(DT, SUBSTEPS, ITERATIONS)
     x_snap, v_snap = solver.get_positions(), solver.get_velocities()
     q_snap, qd_snap = solver.get_body_q(), solver.get_body_qd()
+    if args.save_state:
+        np.savez(args.save_state, x=x_snap, v=v_snap, q=q_snap, qd=qd_snap)
 
     stream = torch.cuda.ExternalStream(solver.cuda_stream, device=dev)
     flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -733,6 +740,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--preroll", type=int, default=20, help="mixed workload frames before the timed frames")
     ap.add_argument("--ref-preroll", type=int, default=0, help="reference arm: oracle frames before timing")
+    ap.add_argument("--save-state", default="", help="save the mixed workload's pre-rolled state (.npz)")
+    ap.add_argument("--load-state", default="", help="start the mixed workload from a saved state (no pre-roll)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
