@@ -244,6 +244,14 @@ int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread);
  * reports the form in use (-1 while timing). */
 int xpbd_set_solve_split(xpbd_solver* s, int mode);
 int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
+/* Form of the solve kernel (no counterpart in the reference; results are identical either
+ * way): 0 = each thread computes the pair terms of its own particle's neighbours, 1 = the
+ * lanes of a warp compute their neighbours' pair terms together (balanced when neighbour
+ * counts differ), -1 (default) = a solver of 16,384 particles or more times both on its own
+ * last substep after its first frame and again every 64 frames, and keeps the faster.
+ * xpbd_get_solve_form reports the form in use. */
+int xpbd_set_solve_form(xpbd_solver* s, int form);
+int xpbd_get_solve_form(const xpbd_solver* s, int* form);
 
 /* New contact / material parameters after init (e.g. between rollouts of an
  * optimisation): every numeric field of cfg except device_index and the

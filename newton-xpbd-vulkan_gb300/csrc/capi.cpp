@@ -235,6 +235,17 @@ int xpbd_get_status(xpbd_solver* s, uint32_t out[4]) {
     return guarded([&] { S(s).status(out); });
 }
 
+int xpbd_set_solve_form(xpbd_solver* s, int form) {
+    return guarded([&] { S(s).set_solve_form(form); });
+}
+
+int xpbd_get_solve_form(const xpbd_solver* s, int* form) {
+    return guarded([&] {
+        if (!s) throw std::runtime_error("null solver");
+        if (form) *form = s->impl.solve_form();
+    });
+}
+
 int xpbd_debug_lookback_hold(int64_t hold_tile, uint64_t wait_ns) {
     return guarded([&] { xpbd::set_lookback_debug(hold_tile, wait_ns); });
 }

@@ -9,6 +9,8 @@
 // particle owns its contacts and sums them in the canonical order (plane, then
 // mesh slots, then the particle-particle total), which makes the step
 // deterministic and needs no delta buffer, no fill and no atomics.
+#include <stdexcept>
+
 #include "contact.cuh"
 #include "kernels.h"
 #include "xmath.cuh"
@@ -17,6 +19,39 @@ namespace xpbd {
 
 constexpr int kSolveThreads = 64;
 constexpr int kPairCap = 12;  // accepted neighbours buffered per thread before the pair math runs
+constexpr int kCoopCap = 12;  // accepted neighbours buffered per lane for the warp's pair pass
+// How a solve kernel computes the particle-particle totals (the solver times both on its scene
+// and keeps the faster; the results are the same bits): each thread its own neighbours' pair
+// terms, or the warp's pair pass
+enum { kFormThread = 0, kFormWarp = 1 };
+
+// Pair term of solve_particle_particle_contacts.comp:159-177: the delta of a particle at
+// (xp, vp), radius, inverse mass w1 from neighbour record (nx, nv) at distance d;
+// .w = 0 when the pair adds nothing (zero combined inverse mass, :166).
+__device__ __forceinline__ float4 pair_term_body(float4 nx, float4 nv, float d, v3 xp, v3 vp, float radius,
+                                                 float w1, float k_mu, float dt) {
+    const v3 raw = vsub(xp, xyz(nx));
+    const float err = d - radius - nx.w;
+    const float denom = w1 + nv.w;
+    if (denom <= 0.0f) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const v3 nn = exact_div(raw, d);
+    const v3 vrel = vsub(vp, xyz(nv));
+    const float vn = exact_dot(nn, vrel);
+    const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y), __fmaf_rn(vn, -nn.z, vrel.z));
+    const float vt_len = exact_length(vt);
+    const float lambda_f = gmax(k_mu * err, -vt_len * dt);
+    const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+    const v3 p2 = vmuls(nn, err);
+    const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
+                        __fmaf_rn(vt_dir.z, lambda_f, -p2.z));
+    const v3 pair_d = exact_div(diff, denom);
+    return make_float4(pair_d.x, pair_d.y, pair_d.z, 1.0f);
+}
+// the same, out of line (the rare path of a lane whose buffer fills)
+__device__ __noinline__ float4 pair_term(float4 nx, float4 nv, float d, v3 xp, v3 vp, float radius, float w1,
+                                         float k_mu, float dt) {
+    return pair_term_body(nx, nv, d, xp, vp, radius, w1, k_mu, dt);
+}
 
 // Pair math of solve_particle_particle_contacts.comp:159-207 for the neighbours
 // buffered in shared memory (slot kk, distance d), accumulated in buffer order.
@@ -79,17 +114,14 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
     }
 }
 
-// The particle-particle part of one particle's iteration (solve_particle_particle_contacts.comp:
-// 116-217 and the relaxation of apply_particle_deltas.comp): the candidate filter (:145-157)
-// runs first and buffers accepted neighbours; the pair math then runs over the buffer in
-// candidate order, so lanes stay in step. Returns the relaxed total delta.
-template <bool ALL_ACTIVE, bool DIAG>
-__device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1, uint32_t id,
-                                       const float4* __restrict__ rx, const float4* __restrict__ rv,
-                                       const int* __restrict__ rf, const int4* __restrict__ table, bool split,
-                                       uint32_t stamp,
-                                       const uint32_t* __restrict__ sids, const SolveParams& sp, const SolveDiag& dg,
-                                       int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
+// The candidate filter of solve_particle_particle_contacts.comp:116-157 for the particle in
+// sorted slot k: accept(kk, d) for every accepted neighbour slot kk at distance d, in the
+// shader's visit order (cells x fastest, then y, then z; sorted order within a cell).
+template <bool ALL_ACTIVE, class F>
+__device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float radius, const float4* __restrict__ rx,
+                                          const float4* __restrict__ rv, const int* __restrict__ rf,
+                                          const int4* __restrict__ table, bool split, uint32_t stamp,
+                                          const SolveParams& sp, F&& accept) {
     const int is_proxy = pflag & 2;
     const float R = radius + sp.max_radius + sp.k_coh;
     const float inv = sp.inv;
@@ -98,8 +130,6 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
     const int32_t xe = min(f2i(floorf((xp.x + R) * inv)), xs + kGridDim - 1);
     const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
     const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
-    v3 acc = mk3(0.0f, 0.0f, 0.0f);
-    int np = 0;
     // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
     // or is clamped at 0 (then the alias bit of x is the same for the whole row); their
     // particles then form one run of the sorted order, in the reference's visit order (x
@@ -156,18 +186,115 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
                         const float d = exact_sqrt(sq);
                         const float err = d - radius - nx.w;
                         if (err > sp.k_coh || d <= 0.0f) continue;
-                        s_kk[np][threadIdx.x] = kk;
-                        s_d[np][threadIdx.x] = d;
-                        if (++np == kPairCap) {
-                            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
-                            np = 0;
-                        }
+                        accept(kk, d);
                     }
                 }
             }
         }
     }
+}
+
+// The particle-particle part of one particle's iteration (solve_particle_particle_contacts.comp:
+// 116-217 and the relaxation of apply_particle_deltas.comp): the candidate filter (:145-157)
+// runs first and buffers accepted neighbours; the pair math then runs over the buffer in
+// candidate order, so lanes stay in step. Returns the relaxed total delta.
+template <bool ALL_ACTIVE, bool DIAG>
+__device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1, uint32_t id,
+                                       const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                       const int* __restrict__ rf, const int4* __restrict__ table, bool split,
+                                       uint32_t stamp,
+                                       const uint32_t* __restrict__ sids, const SolveParams& sp, const SolveDiag& dg,
+                                       int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
+    v3 acc = mk3(0.0f, 0.0f, 0.0f);
+    int np = 0;
+    pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float d) {
+        s_kk[np][threadIdx.x] = kk;
+        s_d[np][threadIdx.x] = d;
+        if (++np == kPairCap) {
+            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+            np = 0;
+        }
+    });
     pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+    const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
+    return mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f), __fmaf_rn(dw.z, sp.relax, 0.0f));
+}
+
+// Shared memory of one warp's pair pass (pp_total_warp).
+struct WarpPairs {
+    int kk[kCoopCap][32];  // accepted neighbour slots of each lane, candidate order
+    float d[kCoopCap][32];
+    float4 own_x[32];      // (xp, radius) of each lane's particle
+    float4 own_v[32];      // (vp, inverse mass)
+    uint32_t off[33];      // exclusive prefix of the lanes' buffered counts
+    float4 res[32];        // pair terms of the current 32 buffered neighbours
+};
+
+// pp_total for a whole warp (all 32 lanes call it; active = false for a lane with nothing to
+// add). Each lane filters its candidates in the shader's order and buffers the accepted ones;
+// the warp then computes the pair terms of all buffered neighbours 32 at a time, so a lane
+// with few neighbours does not idle while another works through many, and each lane adds its
+// own terms in its candidate order. A lane whose buffer fills before its filter is done adds
+// that buffer's terms itself first. Each particle's sum runs over the same terms in the same
+// order as pp_total, so both give the same bits.
+template <bool ALL_ACTIVE>
+__device__ __forceinline__ v3 pp_total_warp(bool active, int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1,
+                                            const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                            const int* __restrict__ rf, const int4* __restrict__ table, bool split,
+                                            uint32_t stamp, const SolveParams& sp, WarpPairs& wp) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    v3 acc = mk3(0.0f, 0.0f, 0.0f);
+    int np = 0;
+    if (active) {
+        pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float d) {
+            wp.kk[np][lane] = kk;
+            wp.d[np][lane] = d;
+            if (++np == kCoopCap) {
+                for (int q = 0; q < np; q++) {
+                    const int j = wp.kk[q][lane];
+                    const float4 t = pair_term(__ldg(&rx[j]), __ldg(&rv[j]), wp.d[q][lane], xp, vp, radius, w1,
+                                               sp.k_mu, sp.dt);
+                    if (t.w != 0.0f) acc = vadd(acc, xyz(t));
+                }
+                np = 0;
+            }
+        });
+    }
+    uint32_t incl = (uint32_t)np;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t my_off = incl - (uint32_t)np;
+    wp.off[lane] = my_off;
+    if (lane == 31) wp.off[32] = incl;
+    wp.own_x[lane] = make_float4(xp.x, xp.y, xp.z, radius);
+    wp.own_v[lane] = make_float4(vp.x, vp.y, vp.z, w1);
+    __syncwarp();
+    const uint32_t total = wp.off[32];
+    for (uint32_t c = 0; c < total; c += 32) {
+        const uint32_t t = c + (uint32_t)lane;
+        if (t < total) {
+            int o = 0;  // the lane whose buffer holds term t: the last o with off[o] <= t
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (o + step < 32 && wp.off[o + step] <= t) o += step;
+            const uint32_t q = t - wp.off[o];
+            const int j = wp.kk[q][o];
+            const float4 ox = wp.own_x[o], ov = wp.own_v[o];
+            wp.res[lane] = pair_term_body(__ldg(&rx[j]), __ldg(&rv[j]), wp.d[q][o], xyz(ox), xyz(ov), ox.w, ov.w,
+                                          sp.k_mu, sp.dt);
+        }
+        __syncwarp();
+        const uint32_t lo = max(my_off, c), hi = min(my_off + (uint32_t)np, c + 32u);
+        for (uint32_t u = lo; u < hi; u++) {
+            const float4 r = wp.res[u - c];
+            if (r.w != 0.0f) acc = vadd(acc, xyz(r));
+        }
+        __syncwarp();
+    }
     const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
     return mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f), __fmaf_rn(dw.z, sp.relax, 0.0f));
 }
@@ -179,7 +306,7 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
 // total to the shape deltas in the same order.
 enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
 
-template <bool LAST, bool ALL_ACTIVE, bool DIAG, int PP>
+template <bool LAST, bool ALL_ACTIVE, bool DIAG, int PP, int FORM>
 __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     int64_t n, const uint32_t* __restrict__ sids, const uint32_t* __restrict__ skeys, const float4* __restrict__ rx,
     const float4* __restrict__ rv, const int* __restrict__ rf, const int4* __restrict__ table_all,
@@ -188,21 +315,36 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     const float4* __restrict__ cslot, ContactRanks cr, BodyTables bt, SolveParams sp, float4* __restrict__ rx_out,
     float4* __restrict__ rv_out, float4* __restrict__ x_out, float4* __restrict__ v_out, SolveDiag dg,
     BodyDeltaOut bo, float4* __restrict__ pp) {
-    __shared__ int s_kk[PP == kPPApply ? 1 : kPairCap][kSolveThreads];
-    __shared__ float s_d[PP == kPPApply ? 1 : kPairCap][kSolveThreads];
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    // the warp's pair pass (pp_total_warp) computes the particle-particle totals; the
+    // diagnostic kernels keep the per-thread form, which records every pair as it is summed
+    constexpr bool WARP = FORM == kFormWarp && !DIAG && PP != kPPApply;
+    __shared__ int s_kk[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
+    __shared__ float s_d[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
+    __shared__ WarpPairs s_wp[WARP ? kSolveThreads / 32 : 1];
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (!WARP && k0 >= n) return;
+    const bool valid = k0 < n;  // every lane of a warp reaches the warp's pair pass
+    const int64_t k = valid ? k0 : n - 1;
     const uint32_t id = sids[k];
     const float4 ox = rx[k], ov = rv[k];
-    const int pflag = ALL_ACTIVE ? 1 : rf[k];
+    const int pflag = valid ? (ALL_ACTIVE ? 1 : rf[k]) : 0;
     const v3 xp = xyz(ox), vp = xyz(ov);
     const float radius = ox.w, w1 = ov.w;
+    v3 total = mk3(0.0f, 0.0f, 0.0f);
+    if constexpr (WARP) {
+        // this particle's scene table (scene-major keys); one scene: the whole table
+        const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
+        total = pp_total_warp<ALL_ACTIVE>((pflag & 1) != 0, k, pflag, xp, vp, radius, w1, rx, rv, rf, table,
+                                          sp.split_keys != 0, *stamp_p, sp, s_wp[threadIdx.x >> 5]);
+        if (!valid) return;
+    }
     if constexpr (PP == kPPOnly) {
-        v3 total = mk3(0.0f, 0.0f, 0.0f);
-        if (pflag & 1) {
-            const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
-            total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
-                                               *stamp_p, sids, sp, dg, s_kk, s_d);
+        if constexpr (!WARP) {
+            if (pflag & 1) {
+                const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
+                total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table,
+                                                   sp.split_keys != 0, *stamp_p, sids, sp, dg, s_kk, s_d);
+            }
         }
         pp[k] = make_float4(total.x, total.y, total.z, 0.0f);
         return;
@@ -241,10 +383,9 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
                 }
             }
         }
-        v3 total;
         if constexpr (PP == kPPApply) {
             total = xyz(pp[k]);
-        } else {
+        } else if constexpr (!WARP) {
             // this particle's scene table (scene-major keys); one scene: the whole table
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
             total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
@@ -324,34 +465,44 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   const float4* rx, const float4* rv, const int* rf, const int4* table, const uint32_t* stamp,
                   const float4* x0, const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr,
                   BodyTables bt, SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out,
-                  SolveDiag dg, BodyDeltaOut bo, int pp_mode, float4* pp) {
+                  SolveDiag dg, BodyDeltaOut bo, int pp_mode, float4* pp, int form) {
     if (n <= 0) return;
     const int threads = kSolveThreads;
     const int blocks = (int)((n + threads - 1) / threads);
     const bool diag = dg.pair_header != nullptr;
-#define XPBD_SOLVE(L, A, D, P)                                                                                     \
-    if (last == L && all_active == A && diag == D && pp_mode == P) {                                              \
-        k_solve<L, A, D, P><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo,   \
-                                                       cslot, cr, bt, sp, rx_out, rv_out, x_out, v_out, dg, bo, pp); \
+    // the warp form applies where the particle-particle totals are computed without diagnostics
+    if (diag || pp_mode == kPPApply) form = kFormThread;
+#define XPBD_SOLVE(L, A, D, P, F)                                                                                  \
+    if (last == L && all_active == A && diag == D && pp_mode == P && form == F) {                                 \
+        k_solve<L, A, D, P, F><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo, \
+                                                          cslot, cr, bt, sp, rx_out, rv_out, x_out, v_out, dg, bo,  \
+                                                          pp);                                                      \
         return;                                                                                                     \
     }
-    XPBD_SOLVE(true, true, false, kPPFused)
-    XPBD_SOLVE(true, false, false, kPPFused)
-    XPBD_SOLVE(false, true, false, kPPFused)
-    XPBD_SOLVE(false, false, false, kPPFused)
-    XPBD_SOLVE(true, true, true, kPPFused)
-    XPBD_SOLVE(true, false, true, kPPFused)
-    XPBD_SOLVE(false, true, true, kPPFused)
-    XPBD_SOLVE(false, false, true, kPPFused)
+    XPBD_SOLVE(true, true, false, kPPFused, kFormThread)
+    XPBD_SOLVE(true, false, false, kPPFused, kFormThread)
+    XPBD_SOLVE(false, true, false, kPPFused, kFormThread)
+    XPBD_SOLVE(false, false, false, kPPFused, kFormThread)
+    XPBD_SOLVE(true, true, false, kPPFused, kFormWarp)
+    XPBD_SOLVE(true, false, false, kPPFused, kFormWarp)
+    XPBD_SOLVE(false, true, false, kPPFused, kFormWarp)
+    XPBD_SOLVE(false, false, false, kPPFused, kFormWarp)
+    XPBD_SOLVE(true, true, true, kPPFused, kFormThread)
+    XPBD_SOLVE(true, false, true, kPPFused, kFormThread)
+    XPBD_SOLVE(false, true, true, kPPFused, kFormThread)
+    XPBD_SOLVE(false, false, true, kPPFused, kFormThread)
     // the split (no diagnostics): the particle-particle part alone, then the rest
     if (pp_mode == kPPOnly) last = false;  // writes pp only
-    XPBD_SOLVE(false, true, false, kPPOnly)
-    XPBD_SOLVE(false, false, false, kPPOnly)
-    XPBD_SOLVE(true, true, false, kPPApply)
-    XPBD_SOLVE(true, false, false, kPPApply)
-    XPBD_SOLVE(false, true, false, kPPApply)
-    XPBD_SOLVE(false, false, false, kPPApply)
+    XPBD_SOLVE(false, true, false, kPPOnly, kFormThread)
+    XPBD_SOLVE(false, false, false, kPPOnly, kFormThread)
+    XPBD_SOLVE(false, true, false, kPPOnly, kFormWarp)
+    XPBD_SOLVE(false, false, false, kPPOnly, kFormWarp)
+    XPBD_SOLVE(true, true, false, kPPApply, kFormThread)
+    XPBD_SOLVE(true, false, false, kPPApply, kFormThread)
+    XPBD_SOLVE(false, true, false, kPPApply, kFormThread)
+    XPBD_SOLVE(false, false, false, kPPApply, kFormThread)
 #undef XPBD_SOLVE
+    throw std::runtime_error("no solve kernel for these options");
 }
 
 }  // namespace xpbd

@@ -216,7 +216,11 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   const float4* x0,
                   const float4* v0, const uint32_t* cinfo, const float4* cslot, ContactRanks cr, BodyTables bt,
                   SolveParams sp, float4* rx_out, float4* rv_out, float4* x_out, float4* v_out, SolveDiag dg,
-                  BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr}, int pp_mode = 0, float4* pp = nullptr);
+                  BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr}, int pp_mode = 0, float4* pp = nullptr,
+                  int form = 0);
+// forms of the solve kernel (launch_solve's `form`): 0 = each thread sums its own neighbours'
+// pair terms, 1 = the lanes of a warp compute their neighbours' pair terms together; same bits
+constexpr int kSolveForms = 2;
 // restitution (apply_particle_shape_restitution.comp) after the body passes of the last
 // iteration, in particle order on the final state the last iteration wrote (v_out)
 void launch_restitute(cudaStream_t s, int64_t n, const int* flags, const float* radii, const float4* x0,

@@ -255,6 +255,69 @@ void Solver::set_solve_split(int mode) {
     split_trials_ = 0;
 }
 
+void Solver::set_solve_form(int form) {
+    require_init();
+    if (form < -1 || form >= kSolveForms) throw std::runtime_error("set_solve_form: -1 (timed choice), 0 or 1");
+    sync();
+    solve_form_forced_ = form;
+    if (form >= 0) solve_form_ = form;
+    solve_form_timed_ = false;
+}
+
+// Times every form of the solve kernel on the last substep of the last frame: its last
+// iteration is launched again on the records, cell table and contacts still in memory, with
+// its outputs in scratch buffers (the records of the other iteration parity, which that
+// iteration does not read, and the body-delta entries, which the next frame rebuilds), so the
+// state is untouched. The fastest form is kept; every form gives the same bits.
+void Solver::autotune_solve() {
+    sync();
+    const int it = last_iterations_ - 1;
+    SolveParams sp = solve_params(last_sdt_, it);
+    if (dyn_any_) sp.enable_restitution = 0;
+    ContactRanks cr{nullptr, nullptr};
+    if (need_ranks_) {
+        cr.rank = rank_.p;
+        cr.totals = totals_.p;
+        cr.count = ccount_.p + (last_substeps_ - 1);
+    }
+    const uint32_t* sids = pair_v_[(plan_.passes - 1) & 1].p;
+    const uint32_t* skeys = pscene_.p ? pair_k_[(plan_.passes - 1) & 1].p : nullptr;
+    const int src = last_collide_src_;
+    const BodyDeltaOut bo{dyn_any_ ? bdel_.p : nullptr, dyn_any_ ? dyn_rank_.p : nullptr};
+    const SolveDiag dg{nullptr, nullptr, nullptr, 0};
+    float4* sx = rx_[(it + 1) & 1].p;  // scratch outputs
+    float4* sv = rv_[(it + 1) & 1].p;
+    constexpr int kReps = 3;
+    cudaEvent_t ev[2 * kSolveForms * kReps];
+    for (auto& e : ev) XPBD_CUDA(cudaEventCreate(&e));
+    for (int rep = 0; rep <= kReps; rep++) {  // round 0 warms up
+        for (int f = 0; f < kSolveForms; f++) {
+            cudaEvent_t* e = ev + 2 * (f * kReps + std::max(rep - 1, 0));
+            if (rep) XPBD_CUDA(cudaEventRecord(e[0], stream_));
+            launch_solve(stream_, (int64_t)n_, true, all_active_, sids, skeys, rx_[it & 1].p, rv_[it & 1].p, rf_.p,
+                         table_.p, stamp_.p, x_[src].p, v_[src].p, cinfo_.p, cslot_.p, cr, body_tables(), sp,
+                         nullptr, nullptr, sx, sv, dg, bo, 0, nullptr, f);
+            if (rep) XPBD_CUDA(cudaEventRecord(e[1], stream_));
+        }
+    }
+    XPBD_CUDA(cudaGetLastError());
+    XPBD_CUDA(cudaStreamSynchronize(stream_));
+    double ms[kSolveForms] = {0.0};
+    for (int f = 0; f < kSolveForms; f++)
+        for (int r = 0; r < kReps; r++) {
+            float t = 0.0f;
+            XPBD_CUDA(cudaEventElapsedTime(&t, ev[2 * (f * kReps + r)], ev[2 * (f * kReps + r) + 1]));
+            ms[f] += t;
+        }
+    for (auto& e : ev) cudaEventDestroy(e);
+    int best = 0;
+    for (int f = 1; f < kSolveForms; f++)
+        if (ms[f] < ms[best]) best = f;
+    solve_form_ = best;
+    solve_form_timed_ = true;
+    solve_form_frame_ = frames_run_;
+}
+
 void Solver::set_sort_variant(int bits, int items) {
     require_init();
     sync();
@@ -1067,7 +1130,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         launch_solve(stream_, n, false, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[0].p, rv_[0].p, rf_.p,
                      table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, ContactRanks{nullptr, nullptr}, bt,
                      solve_params(sdt, 0), nullptr, nullptr, nullptr, nullptr, dg, BodyDeltaOut{nullptr, nullptr}, 1,
-                     pp_.p);
+                     pp_.p, solve_form_);
         count_kernel();
     }
     if (fork) XPBD_CUDA(cudaStreamWaitEvent(stream_, join_, 0));  // contacts complete
@@ -1096,7 +1159,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         launch_solve(stream_, n, last, all_active_, sids, pscene_.p ? skeys : nullptr, rx_[it & 1].p,
                      rv_[it & 1].p, rf_.p, table_.p, stamp_.p, x_[src].p, v_[src].p, info, slots, cr, bt, sp,
                      rx_[(it + 1) & 1].p, rv_[(it + 1) & 1].p, x_[dst].p, v_[dst].p, dg, bo,
-                     split && it == 0 ? 2 : 0, pp_.p);
+                     split && it == 0 ? 2 : 0, pp_.p, solve_form_);
         count_kernel();
         prof_mark(P_SOLVE);
         if (bodies) {
@@ -1148,6 +1211,9 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
         autotune_sort(nullptr, nullptr);
         contact_count_ = cc;
     }
+    if (solve_form_forced_ < 0 && last_was_step_ && n_ >= kSolveTuneMinParticles && !profiling_ &&
+        !cfg_.enable_diagnostics && (!solve_form_timed_ || frames_run_ - solve_form_frame_ >= kSolveRetime))
+        autotune_solve();
     auto t0 = std::chrono::high_resolution_clock::now();
     const bool split_ok = mode == Mode::Step && !meshes_.empty() && !profiling_ && iterations > 0 &&
                           !cfg_.enable_diagnostics;
@@ -1164,7 +1230,8 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     } else {
         split_now_ = split_ok && split_choice_ == 1;
     }
-    GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0, split_now_ ? 1 : 0};
+    GraphKey key{f2u(dt), substeps, iterations, cur_, (int)mode, profiling_ ? 1 : 0, split_now_ ? 1 : 0,
+                 solve_form_};
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         FrameGraph fg;
@@ -1214,6 +1281,10 @@ void Solver::run_frame(Mode mode, float dt, int substeps, int iterations, bool s
     last_memsets_ = it->second.memsets;
     frames_run_++;
     last_collide_src_ = cur_ ^ ((substeps - 1) & 1);
+    last_sdt_ = dt / (float)substeps;
+    last_substeps_ = substeps;
+    last_iterations_ = iterations;
+    last_was_step_ = mode == Mode::Step && iterations > 0;
     cur_ ^= (substeps & 1);
     pending_substeps_ = substeps;
     if (!sync_now) return;

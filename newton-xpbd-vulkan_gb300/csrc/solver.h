@@ -131,6 +131,9 @@ class Solver {
     void set_sort_variant(int bits, int items);
     void set_solve_split(int mode);               // -1 timed choice, 0 fused, 1 split
     int solve_split() const { return split_choice_; }
+    // form of the solve kernel (kernels.h kSolveForms): -1 timed choice (default), or a form
+    void set_solve_form(int form);
+    int solve_form() const { return solve_form_; }
     uint64_t kernels_launched() const { return kernels_total_; }
     void rollout_backward(const float* gx_final, const float* gv_final, float* gx0, float* gv0, float* gw,
                           double* params);
@@ -172,10 +175,10 @@ class Solver {
     enum class Mode { Step, SolveOnly };
     struct GraphKey {
         uint32_t dt_bits;
-        int substeps, iterations, parity, mode, timed, split;
+        int substeps, iterations, parity, mode, timed, split, form;
         bool operator<(const GraphKey& o) const {
-            return std::tie(dt_bits, substeps, iterations, parity, mode, timed, split) <
-                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode, o.timed, o.split);
+            return std::tie(dt_bits, substeps, iterations, parity, mode, timed, split, form) <
+                   std::tie(o.dt_bits, o.substeps, o.iterations, o.parity, o.mode, o.timed, o.split, o.form);
         }
     };
     struct FrameGraph {
@@ -209,6 +212,18 @@ class Solver {
     void prof_mark(int slot);
     void apply_sort_plan(int bits, int items);
     bool sort_tuned_ = false;
+    // Solve-kernel form: timed on the scene's own last substep (its last iteration launched
+    // again with its outputs in scratch buffers) after the first frame and again every
+    // kSolveRetime frames; every form gives the same bits.
+    static constexpr uint64_t kSolveRetime = 64;
+    static constexpr size_t kSolveTuneMinParticles = 16384;  // smaller scenes keep form 0
+    int solve_form_ = 0, solve_form_forced_ = -1;
+    uint64_t solve_form_frame_ = 0;
+    bool solve_form_timed_ = false;
+    float last_sdt_ = 0.0f;
+    int last_substeps_ = 0, last_iterations_ = 0;
+    bool last_was_step_ = false;
+    void autotune_solve();
     uint32_t lb_debug_seen_ = 0;  // lookback_debug_generation() the frame graphs were recorded under
     void count_kernel(int k = 1);
     void count_memset();

@@ -232,6 +232,18 @@ class XpbdSolver:
         _check(_lib.xpbd_get_solve_split(self._h, C.byref(v)))
         return int(v.value)
 
+    def set_solve_form(self, form):
+        """Solve-kernel form: 0 per-thread pair terms, 1 warp pair pass, -1 (default) timed on
+        the scene's own substeps (xpbd_set_solve_form). Results are identical."""
+        _check(_lib.xpbd_set_solve_form(self._h, int(form)))
+
+    @property
+    def solve_form(self):
+        """The solve-kernel form in use (0 or 1)."""
+        v = C.c_int(0)
+        _check(_lib.xpbd_get_solve_form(self._h, C.byref(v)))
+        return int(v.value)
+
     def update_config(self, config):
         """New contact / material parameters after init (xpbd_update_config)."""
         _check(_lib.xpbd_update_config(self._h, C.byref(config._c)))

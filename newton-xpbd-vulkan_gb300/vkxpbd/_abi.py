@@ -115,6 +115,8 @@ SIGNATURES = {
     "xpbd_set_solve_split": (C.c_int, [_P, C.c_int]),
     "xpbd_get_kernels_launched": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "xpbd_get_solve_split": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "xpbd_set_solve_form": (C.c_int, [_P, C.c_int]),
+    "xpbd_get_solve_form": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "xpbd_record_start": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "xpbd_record_stop": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "xpbd_rollout": (C.c_int, [_P, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
