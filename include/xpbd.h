@@ -248,7 +248,7 @@ int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
  * way): 0 = each thread computes the pair terms of its own particle's neighbours, 1 = the
  * lanes of a warp compute their neighbours' pair terms together (balanced when neighbour
  * counts differ), -1 (default) = a solver of 16,384 particles or more times both on its own
- * last substep after its first frame and again every 64 frames, and keeps the faster.
+ * last substep after its first frame and again every 16 frames, and keeps the faster.
  * xpbd_get_solve_form reports the form in use. */
 int xpbd_set_solve_form(xpbd_solver* s, int form);
 int xpbd_get_solve_form(const xpbd_solver* s, int* form);

@@ -287,11 +287,14 @@ void Solver::autotune_solve() {
     const SolveDiag dg{nullptr, nullptr, nullptr, 0};
     float4* sx = rx_[(it + 1) & 1].p;  // scratch outputs
     float4* sv = rv_[(it + 1) & 1].p;
-    constexpr int kReps = 3;
+    // two timed rounds, forms in opposite orders (a drift cancels); the first timing of a
+    // solver has a warm-up round before them (first launches load the kernels)
+    constexpr int kReps = 2;
     cudaEvent_t ev[2 * kSolveForms * kReps];
     for (auto& e : ev) XPBD_CUDA(cudaEventCreate(&e));
-    for (int rep = 0; rep <= kReps; rep++) {  // round 0 warms up
-        for (int f = 0; f < kSolveForms; f++) {
+    for (int rep = solve_form_timed_ ? 1 : 0; rep <= kReps; rep++) {
+        for (int k = 0; k < kSolveForms; k++) {
+            const int f = (rep & 1) ? k : kSolveForms - 1 - k;
             cudaEvent_t* e = ev + 2 * (f * kReps + std::max(rep - 1, 0));
             if (rep) XPBD_CUDA(cudaEventRecord(e[0], stream_));
             launch_solve(stream_, (int64_t)n_, true, all_active_, sids, skeys, rx_[it & 1].p, rv_[it & 1].p, rf_.p,

@@ -214,8 +214,9 @@ class Solver {
     bool sort_tuned_ = false;
     // Solve-kernel form: timed on the scene's own last substep (its last iteration launched
     // again with its outputs in scratch buffers) after the first frame and again every
-    // kSolveRetime frames; every form gives the same bits.
-    static constexpr uint64_t kSolveRetime = 64;
+    // kSolveRetime frames, as the scene evolves (in the mixed workload the warp form turns
+    // faster once the boxes press into the pile); every form gives the same bits.
+    static constexpr uint64_t kSolveRetime = 16;
     static constexpr size_t kSolveTuneMinParticles = 16384;  // smaller scenes keep form 0
     int solve_form_ = 0, solve_form_forced_ = -1;
     uint64_t solve_form_frame_ = 0;
