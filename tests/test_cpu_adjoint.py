@@ -107,3 +107,57 @@ def test_rollout_rejects_meshes():
     o.set_particles(sc.positions, sc.velocities, sc.inv_mass, sc.radii, sc.flags)
     with pytest.raises(RuntimeError):
         o.rollout(1.0 / 60.0, 10, 1)
+
+
+def _run_frames(sc, frames, prec="f64", cfg_over=None, v0=None):
+    o = O.OracleSolver(config_for(sc, **(cfg_over or {})), sc.n, 0, precision=prec)
+    o.finalize_meshes()
+    o.set_particles(sc.positions, sc.velocities if v0 is None else v0, sc.inv_mass, sc.radii, sc.flags)
+    o.rollout(1.0 / 60.0, 10, frames)
+    x = o.get_state64()[0] if prec == "f64" else o.get_positions().astype(np.float64)
+    m = x.mean(axis=0)
+    target = scenes.throw_target()
+    return o, float(((m - target) ** 2).sum()), m
+
+
+def test_fd_matches_at_70_substeps():
+    """The longest horizon of the 512-particle copy at which central differences at eps 1e-3
+    still match the exact gradient to 1e-3 (the block has just landed; measured 2e-4 for the
+    plane friction, 1e-5 for a uniform velocity shift). At 80 substeps eps 1e-3 straddles a
+    contact switch and only eps 1e-4 matches; from 90 on no step size does."""
+    sc = _scene()
+    o, _, m = _run_frames(sc, 7)
+    target = scenes.throw_target()
+    g = o.rollout_backward(np.tile((2.0 * (m - target) / sc.n).astype(np.float32), (sc.n, 1)))
+    eps = 1e-3
+    fd_mu = (_run_frames(sc, 7, cfg_over={"soft_contact_mu": 0.5 + eps})[1] -
+             _run_frames(sc, 7, cfg_over={"soft_contact_mu": 0.5 - eps})[1]) / (2 * eps)
+    assert abs(g["soft_contact_mu"] - fd_mu) <= 1e-3 * abs(fd_mu), (g["soft_contact_mu"], fd_mu)
+    d = np.zeros((sc.n, 3), np.float32)
+    d[:, 0] = 1.0
+    fd_v = (_run_frames(sc, 7, v0=sc.velocities + eps * d)[1] - _run_frames(sc, 7, v0=sc.velocities - eps * d)[1]) / (
+        2 * eps)
+    assert abs(float((g["v0"] * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
+
+
+def test_gradient_growth_beyond_the_fd_horizon_is_genuine():
+    """Past ~80 substeps the exact gradient of the throw grows exponentially (the Jacobian of the
+    Jacobi-style contact projection in the settled pile has modes above 1 per substep). Not an
+    FP32 artefact: the FP64 and FP32 adjoints reach the same magnitude at 240 substeps, and the
+    central difference, bounded over a finite step, grows toward it as the step shrinks."""
+    sc = _scene()
+    target = scenes.throw_target()
+    norms = {}
+    for prec in ("f64", "f32"):
+        o, _, m = _run_frames(sc, 24, prec)
+        g = o.rollout_backward(np.tile((2.0 * (m - target) / sc.n).astype(np.float32), (sc.n, 1)))
+        norms[prec] = float(np.linalg.norm(g["v0"]))
+    assert norms["f64"] > 1e5, norms
+    assert norms["f64"] / 3 < norms["f32"] < norms["f64"] * 3, norms
+    d = np.zeros((sc.n, 3), np.float32)
+    d[:, 0] = 1.0
+    fd = {}
+    for eps in (1e-3, 1e-6):
+        fd[eps] = (_run_frames(sc, 24, v0=sc.velocities + eps * d)[1] -
+                   _run_frames(sc, 24, v0=sc.velocities - eps * d)[1]) / (2 * eps)
+    assert abs(fd[1e-6]) > 10 * abs(fd[1e-3]), fd
