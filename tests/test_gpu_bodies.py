@@ -95,3 +95,52 @@ def test_particles_between_eight_boxes_bitexact():
     sc.radii = np.full(n, 0.004, np.float32)
     sc.flags = np.ones(n, np.int32)
     _run(sc, 3, substeps=4)
+
+
+def _icosphere(radius, subdivisions=1):
+    """Closed triangle mesh of a sphere: an icosahedron with each face split in four (80)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def m(a, b):
+            k = (min(a, b), max(a, b))
+            if k not in mid:
+                c = verts[a] + verts[b]
+                verts.append(c / np.linalg.norm(c))
+                mid[k] = len(verts) - 1
+            return mid[k]
+
+        f = [g for (a, b, c) in f for g in ((a, m(a, b), m(c, a)), (b, m(b, c), m(a, b)), (c, m(c, a), m(b, c)),
+                                            (m(a, b), m(b, c), m(c, a)))]
+    return (np.array(verts) * radius).astype(np.float32), np.array(f, np.uint32)
+
+
+def test_dynamic_mesh_larger_than_a_box_bitexact():
+    """A dynamic body whose mesh has 80 triangles (an icosphere) dropped on a particle pile: its
+    particle queries take the per-thread traversal with the shader's 32-entry stack, the boxes
+    of the other tests the shared-memory stack of small meshes."""
+    import scenes
+
+    sc = box_scene(n_side=8, positions=((0.035, 0.035, 0.2),))
+    v, t = _icosphere(0.04)
+    b = sc.bodies
+    sc.meshes.append((v, t, 0.0, True))
+    nb = len(sc.meshes)
+    nbod = scenes.Bodies.static(nb)
+    for name in ("q", "qd", "com", "inertia", "inv_inertia", "inv_mass", "flags"):
+        getattr(nbod, name)[: nb - 1] = getattr(b, name)
+    m = 1000.0 * 4.0 / 3.0 * np.pi * 0.04 ** 3
+    inertia = np.eye(3) * 0.4 * m * 0.04 ** 2
+    nbod.q[nb - 1] = (-0.03, -0.02, 0.16, 0.0, 0.0, 0.0, 1.0)
+    nbod.inertia[nb - 1] = inertia
+    nbod.inv_inertia[nb - 1] = np.linalg.inv(inertia)
+    nbod.inv_mass[nb - 1] = 1.0 / m
+    sc.bodies = nbod
+    _run(sc, 25)
