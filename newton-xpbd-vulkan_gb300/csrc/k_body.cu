@@ -567,11 +567,7 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     __shared__ int s_cand[kPosedWarps][32][kPosedCand];
     __shared__ float4 s_pos[kPosedWarps][32];
     __shared__ uint32_t s_off[kPosedWarps][33];
-    __shared__ PosedHit s_res[kPosedWarps][32];  // the results of the warp's current 32 queries
-    // traversal stacks of small meshes (boxes) in shared memory instead of local memory
-    __shared__ float s_snd[kPosedWarps][kSmallTris][32];
-    __shared__ uint32_t s_slw[kPosedWarps][kSmallTris][32];
-    __shared__ uint32_t s_suw[kPosedWarps][kSmallTris][32];
+    __shared__ PosedHit s_res[kPosedWarps][32 * kPosedCand];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -599,70 +595,51 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
         const uint32_t y = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += y;
     }
-    const uint32_t my_off = incl - own;
-    s_off[warp][lane] = my_off;
+    s_off[warp][lane] = incl - own;
     if (lane == 31) s_off[warp][32] = incl;
     __syncwarp();
     const uint32_t total = s_off[warp][32];
     bool stack_ovf = false, slot_ovf = false;
-    uint32_t info = 0;
+    // the warp's (particle, mesh) queries, one per lane
+    for (uint32_t pr = (uint32_t)lane; pr < total; pr += 32) {
+        int o = 0;
+        while (o < 31 && s_off[warp][o + 1] <= pr) o++;
+        const int mesh = s_cand[warp][o][pr - s_off[warp][o]];
+        const float4 po = s_pos[warp][o];
+        const v3 pos_m = xyz(mt.pose[mesh * 2]);
+        const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+        const v3 q = quat_rotate_inv(rot_m, vsub(xyz(po), pos_m));  // as posed_candidates computes it
+        v3 bp, bv, nn;
+        PosedHit h;
+        if (mesh_query(mt, mesh, po.w, q, bp, bv, nn, stack_ovf)) {
+            const v3 nw = quat_rotate(rot_m, nn);
+            h.a = make_float4(bp.x, bp.y, bp.z, 1.0f);
+            h.b = make_float4(nw.x, nw.y, nw.z, 0.0f);
+            h.c = make_float4(bv.x, bv.y, bv.z, 0.0f);
+        } else {
+            h.a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        s_res[warp][pr] = h;
+    }
+    __syncwarp();
     int used0 = 0, used = 0;
-    float4* slots = nullptr;
     if (valid) {
-        info = cinfo[i];
+        const uint32_t info = cinfo[i];
         used0 = used = info_slots(info);
-        slots = cslot + (size_t)i * slot_cap * 3;
-    }
-    const SmemStack sstk{&s_snd[warp][0][lane], &s_slw[warp][0][lane], &s_suw[warp][0][lane]};
-    // the warp's (particle, mesh) queries, 32 at a time, one per lane; after each round every
-    // lane inserts the results of its own queries
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t pr = base + (uint32_t)lane;
-        if (pr < total) {
-            int o = 0;  // the lane whose list holds query pr: the last o with off[o] <= pr
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (o + step < 32 && s_off[warp][o + step] <= pr) o += step;
-            const int mesh = s_cand[warp][o][pr - s_off[warp][o]];
-            const float4 po = s_pos[warp][o];
-            const v3 pos_m = xyz(mt.pose[mesh * 2]);
-            const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
-            const v3 q = quat_rotate_inv(rot_m, vsub(xyz(po), pos_m));  // as posed_candidates computes it
-            v3 bp, bv, nn;
-            PosedHit h;
-            const bool small = __ldg(&mt.prim_cnt[mesh]) <= kSmallTris;
-            const bool hit = small ? mesh_query_with(mt, mesh, po.w, q, bp, bv, nn, stack_ovf, sstk)
-                                   : mesh_query(mt, mesh, po.w, q, bp, bv, nn, stack_ovf);
-            if (hit) {
-                const v3 nw = quat_rotate(rot_m, nn);
-                h.a = make_float4(bp.x, bp.y, bp.z, 1.0f);
-                h.b = make_float4(nw.x, nw.y, nw.z, 0.0f);
-                h.c = make_float4(bv.x, bv.y, bv.z, 0.0f);
-            } else {
-                h.a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            }
-            s_res[warp][lane] = h;
+        float4* base = cslot + (size_t)i * slot_cap * 3;
+        const uint32_t off = s_off[warp][lane];
+        for (uint32_t k = 0; k < own; k++) {
+            const PosedHit h = s_res[warp][off + k];
+            if (h.a.w != 0.0f)
+                posed_insert(base, used, slot_cap, slot_ovf, s_cand[warp][lane][k], xyz(h.a), xyz(h.b), xyz(h.c));
         }
-        __syncwarp();
-        if (valid) {
-            const uint32_t lo = max(my_off, base), hi = min(my_off + own, base + 32u);
-            for (uint32_t u = lo; u < hi; u++) {
-                const PosedHit h = s_res[warp][u - base];
-                if (h.a.w != 0.0f)
-                    posed_insert(slots, used, slot_cap, slot_ovf, s_cand[warp][lane][u - my_off], xyz(h.a), xyz(h.b),
-                                 xyz(h.c));
-            }
-        }
-        __syncwarp();
-    }
-    if (valid) {
         if (ncand > kPosedCand) {  // the rest, by this lane, in candidate order
             int k = 0;
             posed_candidates(mt, rt, p, radius, scene, [&](int mesh, v3 q, q4 rot_m) {
                 if (k++ < kPosedCand) return true;
                 v3 bp, bv, nn;
                 if (mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf))
-                    posed_insert(slots, used, slot_cap, slot_ovf, mesh, bp, quat_rotate(rot_m, nn), bv);
+                    posed_insert(base, used, slot_cap, slot_ovf, mesh, bp, quat_rotate(rot_m, nn), bv);
                 return true;
             });
         }

@@ -148,7 +148,6 @@ __device__ __forceinline__ v3 ldv(const float* __restrict__ p, uint32_t i) {
 // the node, the squared box distance and the packed child words read when its parent
 // ordered its children, so a pop needs no load.
 struct LocalStack {
-    static constexpr uint32_t kCap = 32;  // the shader's stack depth
     float nds[32];
     uint32_t lw[32], uw[32];
     __device__ __forceinline__ void put(uint32_t k, float d, uint32_t l, uint32_t u) {
@@ -160,28 +159,6 @@ struct LocalStack {
     __device__ __forceinline__ void words(uint32_t k, uint32_t& l, uint32_t& u) const {
         l = lw[k];
         u = uw[k];
-    }
-};
-
-// Traversal stack in shared memory for meshes of at most kSmallTris triangles: entry k of a
-// thread at nds[k * 32] (one column per lane of a warp). A tree of that many triangles in
-// leaves of up to 4 is at most kSmallTris - 4 levels deep, and a depth-first walk holds at
-// most one pending sibling per level plus one node, so kCap entries never fill.
-constexpr uint32_t kSmallTris = 16;
-struct SmemStack {
-    static constexpr uint32_t kCap = kSmallTris;
-    float* nds;
-    uint32_t* lw;
-    uint32_t* uw;
-    __device__ __forceinline__ void put(uint32_t k, float d, uint32_t l, uint32_t u) {
-        nds[k * 32] = d;
-        lw[k * 32] = l;
-        uw[k * 32] = u;
-    }
-    __device__ __forceinline__ float dist(uint32_t k) const { return nds[k * 32]; }
-    __device__ __forceinline__ void words(uint32_t k, uint32_t& l, uint32_t& u) const {
-        l = lw[k * 32];
-        u = uw[k * 32];
     }
 };
 
@@ -199,7 +176,7 @@ struct MeshWalk {
 
 template <class W>
 __device__ __forceinline__ void walk_push(W& w, float nds, float4 lo4, float4 hi4) {
-    if (w.sp < decltype(w.stk)::kCap) {
+    if (w.sp < 32) {
         w.stk.put(w.sp, nds, __float_as_uint(lo4.w), __float_as_uint(hi4.w));
         w.sp++;
     } else {
@@ -429,25 +406,6 @@ __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, 
     const float d = delta_len * sign;
     body_pos = vfma_vs(vneg(nrm), d, p);
     return true;
-}
-
-// Whole query of point p (in the mesh's own frame) against mesh ci by one thread, with the
-// traversal stack `stk` (a LocalStack, or a SmemStack for meshes of at most kSmallTris triangles).
-template <class Stack>
-__device__ __forceinline__ bool mesh_query_with(const MeshTables& mt, int ci, float radius, v3 p, v3& body_pos,
-                                                v3& shape_v, v3& nrm, bool& overflow, Stack stk) {
-    const float eps_md = mt.avg_edge * 1e-3f;
-    const float eps2 = eps_md * eps_md;
-    MeshWalk<Stack> w;
-    w.stk = stk;
-    w.overflow = false;
-    walk_begin(w, mt, ci, radius, p);
-    while (w.sp > 0) {
-        uint32_t lo, hi;
-        if (walk_pop(w, mt, p, eps_md, lo, hi)) walk_leaf(w, mt, p, eps_md, eps2, lo, hi);
-    }
-    overflow |= w.overflow;
-    return walk_finish(w, mt, ci, p, body_pos, shape_v, nrm);
 }
 
 // Whole query of point p (in the mesh's own frame) against mesh ci by one thread.
