@@ -327,123 +327,33 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
 }
 
 // ---------------------------------------------------------------- rigid contacts ----
-// Rigid contacts of every vertex of a dynamic body's mesh: the vertex against the ground
-// plane, then the closest-point query of generate_mesh_contacts.comp (radius 0, the rigid
-// margin in place of the soft contact margin) against the static meshes and the overlapping
-// dynamic bodies' meshes, in mesh index order (the merge of the two ascending lists); the
-// first kRigidSlots contacts are kept. Slot record (5 float4): (p0, shape1 bits),
+// One warp per vertex of a dynamic body's mesh: the vertex against the ground plane,
+// then the closest-point query of generate_mesh_contacts.comp (radius 0, the rigid
+// margin in place of the soft contact margin) against the static meshes and the
+// overlapping dynamic bodies' meshes, in mesh index order (lane 0 merges the two
+// ascending lists 32 candidates at a time, each lane queries one). The first
+// kRigidSlots contacts are kept. Slot record (5 float4): (p0, shape1 bits),
 // (p1, thickness0), (normal, thickness1), (offset0, 0), (offset1, 0).
-//
-// One lane per vertex. Each lane lists its vertex's first kRigidCand candidate meshes (a
-// partner's mesh only when the vertex lies within the partner's widened world box; outside
-// it no contact is within the margin); the warp runs all listed (vertex, mesh) queries one per
-// lane, so a vertex with several candidates does not hold the others; each lane then writes
-// its vertex's contacts in candidate order and queries any candidates past the listed ones
-// itself, in order.
-constexpr int kRigidCand = 4;
-
-struct RigidHit {
-    float4 p;  // (body-side point, found)
-    float4 n;  // (normal in the queried mesh's frame, stack overflow)
-};
-
-__device__ __forceinline__ void rigid_emit(const BodyArrays& ba, const RigidTables& rt, const MeshTables& mt, int m,
-                                          v3 V, float th0, q4 rot_a, v3 bpos, v3 nrm, float4* out, int& cnt) {
-    if (cnt < kRigidSlots) {
-        const bool pz = rt.dyn_index[m] >= 0;
-        q4 rot_m;
-        rot_m.x = rot_m.y = rot_m.z = 0.0f;
-        rot_m.w = 1.0f;
-        if (pz) rot_m = f4q(ba.q[m * 2 + 1]);
-        const float th1 = mt.margins[m];
-        const v3 n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
-        const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0));
-        const v3 o1 = pz ? quat_rotate_inv(rot_m, vmuls(n, -th1)) : vmuls(n, -th1);
-        float4* o = out + cnt * 5;
-        o[0] = make_float4(V.x, V.y, V.z, __int_as_float(m + 1));
-        o[1] = make_float4(bpos.x, bpos.y, bpos.z, th0);
-        o[2] = make_float4(n.x, n.y, n.z, th1);
-        o[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
-        o[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
-    }
-    cnt++;
-}
-
-// The candidate meshes of vertex P of body a (mesh index order): f(m, Q) with Q the vertex in
-// m's frame, until f returns false.
-template <class F>
-__device__ __forceinline__ void rigid_candidates(const BodyArrays& ba, const RigidTables& rt, const MeshTables& mt,
-                                                 const RigidParams& rp, int a, v3 P, F&& f) {
-    const int ia = rt.dyn_index[a];
-    const int pc = rt.partner_count[ia];
-    const int* partners = rt.partners + ia * kPartnerCap;
-    int si = 0, pi = 0;
-    while (si < mt.walk_count || pi < pc) {
-        const int ms = si < mt.walk_count ? mt.walk_list[si] : 0x7fffffff;
-        const int mp = pi < pc ? partners[pi] : 0x7fffffff;
-        int m;
-        if (ms < mp) {
-            m = ms;
-            si++;
-        } else {
-            m = mp;
-            pi++;
-        }
-        if (m == a) continue;
-        v3 Q = P;
-        if (rt.dyn_index[m] >= 0) {  // the vertex is far outside the partner's world box: no contact within the margin
-            const int im = rt.dyn_index[m];
-            const float4 l = rt.wbox[im * 2], h = rt.wbox[im * 2 + 1];
-            const float e = rp.margin + l.w + rt.pad;
-            if (!(P.x >= l.x - e && P.x <= h.x + e && P.y >= l.y - e && P.y <= h.y + e && P.z >= l.z - e &&
-                  P.z <= h.z + e))
-                continue;
-            Q = quat_rotate_inv(f4q(ba.q[m * 2 + 1]), vsub(P, xyz(ba.q[m * 2])));
-        }
-        if (!f(m, Q)) return;
-    }
-}
-
 __global__ void __launch_bounds__(128) k_rigid_contacts(BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                                                        DeviceStatus* st) {
-    constexpr int QMAX = 32 * kRigidCand;
-    __shared__ int s_qm[4][QMAX];        // mesh of each listed query
-    __shared__ float4 s_qp[4][QMAX];     // the vertex in that mesh's frame
-    __shared__ uint32_t s_off[4][33];
-    __shared__ RigidHit s_res[4][32];    // the results of the warp's current 32 queries
-    const unsigned FULL = 0xffffffffu;
+    __shared__ int s_cand[4][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int d = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const bool valid = d < rt.n_vert;
-    MeshTables rmt = mt;
-    rmt.soft_margin = rp.margin;
-    int a = 0, cnt = 0, ncand = 0;
-    v3 V = mk3(0.0f, 0.0f, 0.0f), P = V;
-    q4 rot_a;
-    rot_a.x = rot_a.y = rot_a.z = 0.0f;
-    rot_a.w = 1.0f;
-    float th0 = 0.0f;
-    float4* out = nullptr;
-    bool stack_ovf = false;
-    int cm[kRigidCand];
-    v3 cq[kRigidCand];
-#pragma unroll
-    for (int k = 0; k < kRigidCand; k++) {
-        cm[k] = 0;
-        cq[k] = V;
-    }
-    if (valid) {
-        const float4 lv = rt.dv_local[d];
-        a = __float_as_int(lv.w);
-        V = xyz(lv);
-        const v3 pos_a = xyz(ba.q[a * 2]);
-        rot_a = f4q(ba.q[a * 2 + 1]);
-        P = vadd(pos_a, quat_rotate(rot_a, V));
-        th0 = mt.margins[a];
-        out = rt.rc + (size_t)d * kRigidSlots * 5;
-        if (rp.plane) {
-            const float dist = P.z - rp.altitude;
-            if (dist < rp.margin) {
+    const int d = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (d >= rt.n_vert) return;  // uniform per warp
+    const float4 lv = rt.dv_local[d];
+    const int a = __float_as_int(lv.w);
+    const v3 V = xyz(lv);
+    const v3 pos_a = xyz(ba.q[a * 2]);
+    const q4 rot_a = f4q(ba.q[a * 2 + 1]);
+    const v3 P = vadd(pos_a, quat_rotate(rot_a, V));
+    const float th0 = mt.margins[a];
+    float4* out = rt.rc + (size_t)d * kRigidSlots * 5;
+    int cnt = 0;
+    bool ovf = false, stack_ovf = false;
+    if (rp.plane) {
+        const float dist = P.z - rp.altitude;
+        if (dist < rp.margin) {
+            if (lane == 0) {
                 const v3 n = mk3(0.0f, 0.0f, -1.0f);
                 const float th1 = 0.0f;
                 const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0)), o1 = vmuls(n, -th1);
@@ -452,73 +362,92 @@ __global__ void __launch_bounds__(128) k_rigid_contacts(BodyArrays ba, RigidTabl
                 out[2] = make_float4(n.x, n.y, n.z, th1);
                 out[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
                 out[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
-                cnt = 1;
             }
+            cnt = 1;
         }
-        rigid_candidates(ba, rt, mt, rp, a, P, [&](int m, v3 Q) {
-#pragma unroll
-            for (int k = 0; k < kRigidCand; k++)
-                if (k == ncand) {
-                    cm[k] = m;
-                    cq[k] = Q;
+    }
+    MeshTables rmt = mt;
+    rmt.soft_margin = rp.margin;
+    const int ia = rt.dyn_index[a];
+    const int pc = rt.partner_count[ia];
+    const int* partners = rt.partners + ia * kPartnerCap;
+    const int total = mt.walk_count + pc;
+    int si = 0, pi = 0;  // merge cursors (lane 0)
+    for (int c0 = 0; c0 < total; c0 += 32) {
+        if (lane == 0) {
+            for (int k = 0; k < 32; k++) {
+                int m = -1;
+                if (si < mt.walk_count || pi < pc) {
+                    const int ms = si < mt.walk_count ? mt.walk_list[si] : 0x7fffffff;
+                    const int mp = pi < pc ? partners[pi] : 0x7fffffff;
+                    if (ms < mp) {
+                        m = ms;
+                        si++;
+                    } else {
+                        m = mp;
+                        pi++;
+                    }
                 }
-            ncand++;
-            return true;
-        });
-    }
-    const uint32_t own = (uint32_t)min(ncand, kRigidCand);
-    uint32_t incl = own;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += y;
-    }
-    const uint32_t my_off = incl - own;
-    s_off[warp][lane] = my_off;
-    if (lane == 31) s_off[warp][32] = incl;
-#pragma unroll
-    for (int k = 0; k < kRigidCand; k++)
-        if ((uint32_t)k < own) {
-            s_qm[warp][my_off + k] = cm[k];
-            s_qp[warp][my_off + k] = make_float4(cq[k].x, cq[k].y, cq[k].z, 0.0f);
-        }
-    __syncwarp();
-    const uint32_t total = s_off[warp][32];
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t pr = base + (uint32_t)lane;
-        if (pr < total) {
-            const int m = s_qm[warp][pr];
-            v3 bpos, bvel, nrm;
-            bool ovf = false;
-            const bool found = mesh_query(rmt, m, 0.0f, xyz(s_qp[warp][pr]), bpos, bvel, nrm, ovf);
-            s_res[warp][lane].p = make_float4(bpos.x, bpos.y, bpos.z, found ? 1.0f : 0.0f);
-            s_res[warp][lane].n = make_float4(nrm.x, nrm.y, nrm.z, ovf ? 1.0f : 0.0f);
-        }
-        __syncwarp();
-        if (valid) {
-            const uint32_t lo = max(my_off, base), hi = min(my_off + own, base + 32u);
-            for (uint32_t u = lo; u < hi; u++) {
-                const RigidHit h = s_res[warp][u - base];
-                stack_ovf |= h.n.w != 0.0f;
-                if (h.p.w != 0.0f) rigid_emit(ba, rt, mt, s_qm[warp][u], V, th0, rot_a, xyz(h.p), xyz(h.n), out, cnt);
+                s_cand[warp][k] = m;
             }
         }
         __syncwarp();
-    }
-    if (valid) {
-        if (ncand > kRigidCand) {  // the rest, by this lane, in candidate order
-            int k = 0;
-            rigid_candidates(ba, rt, mt, rp, a, P, [&](int m, v3 Q) {
-                if (k++ < kRigidCand) return true;
-                v3 bpos, bvel, nrm;
-                if (mesh_query(rmt, m, 0.0f, Q, bpos, bvel, nrm, stack_ovf))
-                    rigid_emit(ba, rt, mt, m, V, th0, rot_a, bpos, nrm, out, cnt);
-                return true;
-            });
+        const int m = s_cand[warp][lane];
+        __syncwarp();
+        bool found = false;
+        v3 bpos, nrm, pos_m = mk3(0.0f, 0.0f, 0.0f);
+        q4 rot_m;
+        rot_m.x = rot_m.y = rot_m.z = 0.0f;
+        rot_m.w = 1.0f;
+        bool pz = false;
+        if (m >= 0 && m != a) {
+            pz = rt.dyn_index[m] >= 0;
+            bool near = true;
+            if (pz) {  // the vertex is far outside the partner's world box: no contact within the margin
+                const int im = rt.dyn_index[m];
+                const float4 l = rt.wbox[im * 2], h = rt.wbox[im * 2 + 1];
+                const float e = rp.margin + l.w + rt.pad;
+                near = P.x >= l.x - e && P.x <= h.x + e && P.y >= l.y - e && P.y <= h.y + e && P.z >= l.z - e &&
+                       P.z <= h.z + e;
+            }
+            if (near) {
+                v3 Q = P;
+                if (pz) {
+                    pos_m = xyz(ba.q[m * 2]);
+                    rot_m = f4q(ba.q[m * 2 + 1]);
+                    Q = quat_rotate_inv(rot_m, vsub(P, pos_m));
+                }
+                v3 bvel;
+                found = mesh_query(rmt, m, 0.0f, Q, bpos, bvel, nrm, stack_ovf);
+            }
         }
-        rt.rc_count[d] = min(cnt, kRigidSlots);
-        if (cnt > kRigidSlots) atomicAdd(&st->rigid_slot_overflows, 1u);  // extra contacts dropped, in order
-        if (stack_ovf) {
+        const uint32_t fm = __ballot_sync(0xffffffffu, found);
+        if (found) {
+            const int slot = cnt + __popc(fm & lanemask_lt());
+            if (slot < kRigidSlots) {
+                const float th1 = mt.margins[m];
+                const v3 n = vneg(pz ? quat_rotate(rot_m, nrm) : nrm);
+                const v3 o0 = quat_rotate_inv(rot_a, vmuls(n, th0));
+                const v3 o1 = pz ? quat_rotate_inv(rot_m, vmuls(n, -th1)) : vmuls(n, -th1);
+                float4* o = out + slot * 5;
+                o[0] = make_float4(V.x, V.y, V.z, __int_as_float(m + 1));
+                o[1] = make_float4(bpos.x, bpos.y, bpos.z, th0);
+                o[2] = make_float4(n.x, n.y, n.z, th1);
+                o[3] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+                o[4] = make_float4(o1.x, o1.y, o1.z, 0.0f);
+            }
+        }
+        cnt += __popc(fm);
+    }
+    if (cnt > kRigidSlots) {
+        ovf = true;
+        cnt = kRigidSlots;
+    }
+    const bool any_stack = __any_sync(0xffffffffu, stack_ovf);
+    if (lane == 0) {
+        rt.rc_count[d] = cnt;
+        if (ovf) atomicAdd(&st->rigid_slot_overflows, 1u);  // extra contacts dropped, in order
+        if (any_stack) {
             atomicOr(&st->error_bits, kErrStackOverflow);
             atomicAdd(&st->stack_overflows, 1u);
         }
@@ -528,7 +457,7 @@ __global__ void __launch_bounds__(128) k_rigid_contacts(BodyArrays ba, RigidTabl
 void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                            DeviceStatus* st) {
     if (rt.n_vert <= 0) return;
-    k_rigid_contacts<<<(rt.n_vert + 127) / 128, 128, 0, s>>>(ba, rt, mt, rp, st);
+    k_rigid_contacts<<<(rt.n_vert * 32 + 127) / 128, 128, 0, s>>>(ba, rt, mt, rp, st);
 }
 
 // ---------------------------------------------------------------- particle contacts on moving meshes ----
@@ -872,15 +801,16 @@ __global__ void __launch_bounds__(128) k_body_particles(BodyArrays ba, const uin
             cp_async_wait_prev();                 // this chunk has arrived
             __syncwarp();
             if (lane == 0) {
+                // entries of contacts that produced no delta (w = 0) add +0: a sum that starts
+                // at +0 is never -0, so adding +0 leaves it unchanged and the loop needs no branch
                 const int m = (int)min((uint32_t)kBodyChunk, sg.y - base);
 #pragma unroll 8
                 for (int l = 0; l < m; l++) {
                     const float4 al = s_a[w][buf][l], cl = s_c[w][buf][l];
-                    if (al.w != 0.0f) {
-                        lin = vadd(lin, xyz(al));
-                        ang = vadd(ang, xyz(cl));
-                        cnt += 1.0f;
-                    }
+                    const bool on = al.w != 0.0f;
+                    lin = vadd(lin, on ? xyz(al) : mk3(0.0f, 0.0f, 0.0f));
+                    ang = vadd(ang, on ? xyz(cl) : mk3(0.0f, 0.0f, 0.0f));
+                    cnt += on ? 1.0f : 0.0f;
                 }
             }
             __syncwarp();  // the buffer is refilled by the next round's copies
