@@ -25,13 +25,17 @@ constexpr int kCoopCap = 12;  // accepted neighbours buffered per lane for the w
 // terms, or the warp's pair pass
 enum { kFormThread = 0, kFormWarp = 1 };
 
-// Pair term of solve_particle_particle_contacts.comp:159-177: the delta of a particle at
-// (xp, vp), radius, inverse mass w1 from neighbour record (nx, nv) at distance d;
-// .w = 0 when the pair adds nothing (zero combined inverse mass, :166).
-__device__ __forceinline__ float4 pair_term_body(float4 nx, float4 nv, float d, v3 xp, v3 vp, float radius,
-                                                 float w1, float k_mu, float dt) {
-    const v3 raw = vsub(xp, xyz(nx));
+// Pair term of solve_particle_particle_contacts.comp:153-177 for a candidate the filter kept
+// at squared distance sq (exact_length's sum): the refined distance, the neighbour test
+// (:157) and the delta of a particle at (xp, vp), radius, inverse mass w1 from neighbour
+// record (nx, nv); .w = 0 when the pair adds nothing (not a neighbour, or zero combined
+// inverse mass, :166).
+__device__ __forceinline__ float4 pair_term_body(float4 nx, float4 nv, float sq, v3 xp, v3 vp, float radius,
+                                                 float w1, float k_mu, float k_coh, float dt) {
+    const float d = exact_sqrt(sq);
     const float err = d - radius - nx.w;
+    if (err > k_coh || d <= 0.0f) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const v3 raw = vsub(xp, xyz(nx));
     const float denom = w1 + nv.w;
     if (denom <= 0.0f) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const v3 nn = exact_div(raw, d);
@@ -48,9 +52,9 @@ __device__ __forceinline__ float4 pair_term_body(float4 nx, float4 nv, float d, 
     return make_float4(pair_d.x, pair_d.y, pair_d.z, 1.0f);
 }
 // the same, out of line (the rare path of a lane whose buffer fills)
-__device__ __noinline__ float4 pair_term(float4 nx, float4 nv, float d, v3 xp, v3 vp, float radius, float w1,
-                                         float k_mu, float dt) {
-    return pair_term_body(nx, nv, d, xp, vp, radius, w1, k_mu, dt);
+__device__ __noinline__ float4 pair_term(float4 nx, float4 nv, float sq, v3 xp, v3 vp, float radius, float w1,
+                                         float k_mu, float k_coh, float dt) {
+    return pair_term_body(nx, nv, sq, xp, vp, radius, w1, k_mu, k_coh, dt);
 }
 
 // Pair math of solve_particle_particle_contacts.comp:159-207 for the neighbours
@@ -62,11 +66,12 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
                                            uint32_t id, const SolveParams& sp, const SolveDiag& dg, v3& acc) {
     for (int q = 0; q < np; q++) {
         const int kk = s_kk[q][threadIdx.x];
-        const float d = s_d[q][threadIdx.x];
         const float4 nx = __ldg(&rx[kk]);
         const float4 nv = __ldg(&rv[kk]);
-        const v3 raw = vsub(xp, xyz(nx));
+        const float d = exact_sqrt(s_d[q][threadIdx.x]);  // the buffer holds squared distances
         const float err = d - radius - nx.w;
+        if (err > sp.k_coh || d <= 0.0f) continue;  // :157
+        const v3 raw = vsub(xp, xyz(nx));
         const float denom = w1 + nv.w;
         if (denom <= 0.0f) continue;
         const v3 nn = exact_div(raw, d);
@@ -115,7 +120,8 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
 }
 
 // The candidate filter of solve_particle_particle_contacts.comp:116-157 for the particle in
-// sorted slot k: accept(kk, d) for every accepted neighbour slot kk at distance d, in the
+// sorted slot k: accept(kk, sq) for every candidate slot kk within reach (squared distance sq,
+// the refined distance and the neighbour test of :153-157 follow in the pair term), in the
 // shader's visit order (cells x fastest, then y, then z; sorted order within a cell).
 template <bool ALL_ACTIVE, class F>
 __device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float radius, const float4* __restrict__ rx,
@@ -183,10 +189,7 @@ __device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float rad
                         const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
                         const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
                         if (sq > reach * reach) continue;
-                        const float d = exact_sqrt(sq);
-                        const float err = d - radius - nx.w;
-                        if (err > sp.k_coh || d <= 0.0f) continue;
-                        accept(kk, d);
+                        accept(kk, sq);
                     }
                 }
             }
@@ -207,9 +210,9 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
                                        int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
     v3 acc = mk3(0.0f, 0.0f, 0.0f);
     int np = 0;
-    pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float d) {
+    pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float sq) {
         s_kk[np][threadIdx.x] = kk;
-        s_d[np][threadIdx.x] = d;
+        s_d[np][threadIdx.x] = sq;
         if (++np == kPairCap) {
             pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
             np = 0;
@@ -223,7 +226,7 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
 // Shared memory of one warp's pair pass (pp_total_warp).
 struct WarpPairs {
     int kk[kCoopCap][32];  // accepted neighbour slots of each lane, candidate order
-    float d[kCoopCap][32];
+    float sq[kCoopCap][32];  // their squared distances
     float4 own_x[32];      // (xp, radius) of each lane's particle
     float4 own_v[32];      // (vp, inverse mass)
     uint32_t off[33];      // exclusive prefix of the lanes' buffered counts
@@ -247,14 +250,14 @@ __device__ __forceinline__ v3 pp_total_warp(bool active, int64_t k, int pflag, v
     v3 acc = mk3(0.0f, 0.0f, 0.0f);
     int np = 0;
     if (active) {
-        pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float d) {
+        pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float sq) {
             wp.kk[np][lane] = kk;
-            wp.d[np][lane] = d;
+            wp.sq[np][lane] = sq;
             if (++np == kCoopCap) {
                 for (int q = 0; q < np; q++) {
                     const int j = wp.kk[q][lane];
-                    const float4 t = pair_term(__ldg(&rx[j]), __ldg(&rv[j]), wp.d[q][lane], xp, vp, radius, w1,
-                                               sp.k_mu, sp.dt);
+                    const float4 t = pair_term(__ldg(&rx[j]), __ldg(&rv[j]), wp.sq[q][lane], xp, vp, radius, w1,
+                                               sp.k_mu, sp.k_coh, sp.dt);
                     if (t.w != 0.0f) acc = vadd(acc, xyz(t));
                 }
                 np = 0;
@@ -284,8 +287,8 @@ __device__ __forceinline__ v3 pp_total_warp(bool active, int64_t k, int pflag, v
             const uint32_t q = t - wp.off[o];
             const int j = wp.kk[q][o];
             const float4 ox = wp.own_x[o], ov = wp.own_v[o];
-            wp.res[lane] = pair_term_body(__ldg(&rx[j]), __ldg(&rv[j]), wp.d[q][o], xyz(ox), xyz(ov), ox.w, ov.w,
-                                          sp.k_mu, sp.dt);
+            wp.res[lane] = pair_term_body(__ldg(&rx[j]), __ldg(&rv[j]), wp.sq[q][o], xyz(ox), xyz(ov), ox.w, ov.w,
+                                          sp.k_mu, sp.k_coh, sp.dt);
         }
         __syncwarp();
         const uint32_t lo = max(my_off, c), hi = min(my_off + (uint32_t)np, c + 32u);
