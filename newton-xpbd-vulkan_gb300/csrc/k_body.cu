@@ -1041,50 +1041,25 @@ __global__ void __launch_bounds__(128) k_body_rigid(BodyArrays ba, RigidTables r
             }
             warp_ordered_add(ok, la, aa, lin, ang, cnt);
         }
-        // the partners' vertices, 32 slots per unit, units in (partner, vertex) order; the
-        // slots of kRigidUnits units are looked up together (most belong to other bodies), so
-        // a body with many partners does not wait on one unit's loads at a time
-        constexpr int kRigidUnits = 8;
         const int pc = rt.partner_count[ib];
-        int pi = 0;
-        uint32_t c0 = 0;
-        while (pi < pc) {
-            int ua[kRigidUnits];
-            uint32_t ud[kRigidUnits];
-            bool hit[kRigidUnits];
-            int nu = 0;
-            while (nu < kRigidUnits && pi < pc) {
-                const int a = rt.partners[ib * kPartnerCap + pi];
-                const uint32_t w0 = rt.dv_start[a], na = (rt.dv_start[a + 1] - w0) * kRigidSlots;
-                if (c0 < na) {
-                    const uint32_t idx = c0 + lane;
-                    ua[nu] = a;
-                    ud[nu] = idx < na ? w0 * kRigidSlots + idx : 0xffffffffu;  // slot index
-                    nu++;
-                    c0 += 32;
-                }
-                if (c0 >= na) {
-                    pi++;
-                    c0 = 0;
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kRigidUnits; u++) {
-                hit[u] = false;
-                if (u < nu && ud[u] != 0xffffffffu) {
-                    const uint32_t d = ud[u] / kRigidSlots;
-                    const int j = (int)(ud[u] % kRigidSlots);
-                    hit[u] = j < rt.rc_count[d] && __float_as_int(rt.rc[(size_t)ud[u] * 5].w) == b + 1;
-                }
-            }
-            for (int u = 0; u < nu; u++) {
-                const bool any = __any_sync(0xffffffffu, hit[u]);
-                if (!any) continue;
+        for (int pi = 0; pi < pc; pi++) {
+            const int a = rt.partners[ib * kPartnerCap + pi];
+            const uint32_t w0 = rt.dv_start[a], w1 = rt.dv_start[a + 1];
+            const uint32_t na = (w1 - w0) * kRigidSlots;
+            for (uint32_t c0 = 0; c0 < na; c0 += 32) {
+                const uint32_t idx = c0 + lane;
                 bool ok = false;
                 v3 la, aa, lb = mk3(0.0f, 0.0f, 0.0f), ab = lb;
-                if (hit[u]) {
-                    const RigidContact c = load_rc(rt.rc + (size_t)ud[u] * 5);
-                    ok = body_contact(ba, q_in, qd_in, ua[u] + 1, c, rp, la, aa, lb, ab);
+                if (idx < na) {
+                    const uint32_t d = w0 + idx / kRigidSlots;
+                    const int j = (int)(idx % kRigidSlots);
+                    if (j < rt.rc_count[d]) {
+                        const float4* sp = rt.rc + ((size_t)d * kRigidSlots + j) * 5;
+                        if (__float_as_int(sp[0].w) == b + 1) {
+                            const RigidContact c = load_rc(sp);
+                            ok = body_contact(ba, q_in, qd_in, a + 1, c, rp, la, aa, lb, ab);
+                        }
+                    }
                 }
                 warp_ordered_add(ok, lb, ab, lin, ang, cnt);
             }
