@@ -59,12 +59,12 @@ ALG_BYTES = {
     "1d. Contacts on Moving Meshes": 24,       # x, r, flags in; contact header out
     "1b. Contact Ranks (cap)": 12,             # header in; rank out
     "1f. Body Delta Entries (scan, sort)": 4,  # header in
-    "2b. Integrate + Cell Keys": 40,           # x, v, w, flags, r in; key, header out
+    "2b. Integrate + Cell Keys": 44,           # x, v, w, flags in; key out (+ r in, header out: plane only)
     "2e. Onesweep Pass 0": 12,                 # key in; key, id out
     "2e. Onesweep Pass 1": 16,                 # key, id in and out
     "2e. Onesweep Pass 2": 16,
     "2e. Onesweep Pass 3": 16,
-    "2g. Cell Table + Gather": 76,             # sorted key, id, x, v, w, r, flags in; records out
+    "2g. Cell Table + Gather": 88,             # sorted key, id, x, v, w, r, flags in; 36 B of records out
     "3. Solve+Apply(+Restitution)": 96,        # records, id, x0, v0, header in; x, v out
     "3c. Restitution (bodies)": 52,            # header, x0, v0, v in; v out
 }

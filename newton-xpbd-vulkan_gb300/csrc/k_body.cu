@@ -231,14 +231,14 @@ __device__ __forceinline__ uint32_t box_cell_hash(int ix, int iy, int iz, int sc
 __device__ __forceinline__ int cell_of(float v, float cs) { return f2i(floorf(v / cs)); }
 
 // cell (x, y, z) of the widened world box of dynamic body i that thread slot c (0 ..
-// kBoxCells - 1, 4 x 4 x 4 cells from the box's lowest cell) stands for; false past
-// the box's own cell range
+// kBoxCells - 1, kBoxAxis cells per axis from the box's lowest cell) stands for; false
+// past the box's own cell range
 __device__ __forceinline__ bool box_cell(const RigidTables& rt, int i, int c, int& x, int& y, int& z) {
     const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
     const float e = rt.grid_reach + l.w;
-    x = cell_of(l.x - e, rt.grid_cs) + (c & 3);
-    y = cell_of(l.y - e, rt.grid_cs) + ((c >> 2) & 3);
-    z = cell_of(l.z - e, rt.grid_cs) + (c >> 4);
+    x = cell_of(l.x - e, rt.grid_cs) + c % kBoxAxis;
+    y = cell_of(l.y - e, rt.grid_cs) + (c / kBoxAxis) % kBoxAxis;
+    z = cell_of(l.z - e, rt.grid_cs) + c / (kBoxAxis * kBoxAxis);
     return x <= cell_of(h.x + e, rt.grid_cs) && y <= cell_of(h.y + e, rt.grid_cs) && z <= cell_of(h.z + e, rt.grid_cs);
 }
 
@@ -251,12 +251,12 @@ __global__ void k_boxgrid_count(RigidTables rt, DeviceStatus* st) {
     int x, y, z;
     if (box_cell(rt, i, c, x, y, z))
         atomicAdd(&rt.grid_count[box_cell_hash(x, y, z, rt.dyn_scene[i], rt.grid_size)], 1u);
-    if (c == kBoxCells - 1) {  // a box wider than 4 cells per axis would lose cells: report it
+    if (c == kBoxCells - 1) {  // a box wider than kBoxAxis cells per axis would lose cells: report it
         const float4 l = rt.wbox[i * 2], h = rt.wbox[i * 2 + 1];
         const float e = rt.grid_reach + l.w;
-        if (cell_of(h.x + e, rt.grid_cs) - cell_of(l.x - e, rt.grid_cs) > 3 ||
-            cell_of(h.y + e, rt.grid_cs) - cell_of(l.y - e, rt.grid_cs) > 3 ||
-            cell_of(h.z + e, rt.grid_cs) - cell_of(l.z - e, rt.grid_cs) > 3)
+        if (cell_of(h.x + e, rt.grid_cs) - cell_of(l.x - e, rt.grid_cs) > kBoxAxis - 1 ||
+            cell_of(h.y + e, rt.grid_cs) - cell_of(l.y - e, rt.grid_cs) > kBoxAxis - 1 ||
+            cell_of(h.z + e, rt.grid_cs) - cell_of(l.z - e, rt.grid_cs) > kBoxAxis - 1)
             atomicOr(&st->error_bits, kErrBodyOverflow);
     }
 }
@@ -498,44 +498,51 @@ __device__ __forceinline__ void posed_candidates(const MeshTables& mt, const Rig
     }
 }
 
+constexpr int kPosedCand = 3;
+constexpr int kPosedWarps = 4;
+constexpr uint32_t kPosedMore = 0x80000000u;  // list entry: the particle has more than kPosedCand candidates
+
 // Triage (one thread per particle, in the previous substep's grid order): particles with
-// at least one candidate moving mesh go to the posed list, in grid order within a warp.
+// at least one candidate moving mesh go to the posed list, in grid order within a warp,
+// each with its first kPosedCand candidate meshes (-1 past its count).
 __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t* __restrict__ order,
                                                       const float4* __restrict__ x, const float* __restrict__ r,
                                                       const int* __restrict__ flags, MeshTables mt, RigidTables rt,
                                                       uint32_t* counter, uint32_t* list) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    bool any = false;
+    int c[kPosedCand] = {-1, -1, -1};
+    int nc = 0;
     int64_t i = -1;
     if (t < n) {
         i = order ? (int64_t)order[t] : t;
         if (flags[i] & 1)
-            posed_candidates(mt, rt, xyz(x[i]), r[i], rt.pscene ? (int)rt.pscene[i] : 0, [&](int, v3, q4) {
-                any = true;
-                return false;
+            posed_candidates(mt, rt, xyz(x[i]), r[i], rt.pscene ? (int)rt.pscene[i] : 0, [&](int mesh, v3, q4) {
+                if (nc < kPosedCand) c[nc] = mesh;
+                return ++nc <= kPosedCand;
             });
     }
+    const bool any = nc > 0;
     const uint32_t m = __ballot_sync(0xffffffffu, any);
     if (m) {
         const int leader = __ffs(m) - 1;
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (any) list[base + __popc(m & lanemask_lt())] = (uint32_t)i;
+        if (any)
+            reinterpret_cast<uint4*>(list)[base + __popc(m & lanemask_lt())] =
+                make_uint4((uint32_t)i | (nc > kPosedCand ? kPosedMore : 0u), (uint32_t)c[0], (uint32_t)c[1],
+                           (uint32_t)c[2]);
     }
 }
 
 // Particles against the moving meshes (generate_mesh_contacts.comp:197-411 in each body's
-// frame) for the posed list, one warp per 32 listed particles. Each lane lists its
-// particle's first kPosedCand candidate meshes in shared memory; the warp then runs all
-// (particle, mesh) queries of those lists one per lane, so lanes with one candidate do not
-// wait for lanes with three; finally each lane inserts its particle's contacts into its
-// slots in mesh order (the shader's mesh loop order; candidates past kPosedCand are
-// queried by their own lane afterwards, in candidate order).
-constexpr int kPosedCand = 3;
-constexpr int kPosedWarps = 4;
-
+// frame) for the posed list, one warp per 32 listed particles. Each lane copies its
+// particle's first kPosedCand candidate meshes, listed by the triage, to shared memory; the
+// warp then runs all (particle, mesh) queries of those lists one per lane, so lanes with one
+// candidate do not wait for lanes with three; finally each lane inserts its particle's
+// contacts into its slots in mesh order (the shader's mesh loop order; candidates past
+// kPosedCand are listed again and queried by their own lane afterwards, in candidate order).
 struct PosedHit {
     float4 a, b, c;  // (body_pos, found), (normal, 0), (body_vel, 0)
 };
@@ -563,7 +570,6 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ counter, const float4* __restrict__ x,
     const float* __restrict__ r, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* __restrict__ cinfo,
     float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
-    __shared__ uint32_t s_warp[kPosedWarps];
     __shared__ int s_cand[kPosedWarps][32][kPosedCand];
     __shared__ float4 s_pos[kPosedWarps][32];
     __shared__ uint32_t s_off[kPosedWarps][33];
@@ -571,22 +577,24 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < (int64_t)*counter;
+    const int64_t listed = (int64_t)*counter;
+    if (t - lane >= listed) return;  // the whole warp is past the list
+    const bool valid = t < listed;
     int64_t i = -1;
     v3 p = mk3(0.0f, 0.0f, 0.0f);
     float radius = 0.0f;
-    int ncand = 0;  // all candidates of this lane's particle
+    int ncand = 0;  // candidates listed by the triage (kPosedCand + 1: more follow)
     int scene = 0;
     if (valid) {
-        i = (int64_t)list[t];
+        const uint4 e = reinterpret_cast<const uint4*>(list)[t];
+        i = (int64_t)(e.x & ~kPosedMore);
         p = xyz(x[i]);
         radius = r[i];
         scene = rt.pscene ? (int)rt.pscene[i] : 0;
-        posed_candidates(mt, rt, p, radius, scene, [&](int mesh, v3, q4) {
-            if (ncand < kPosedCand) s_cand[warp][lane][ncand] = mesh;
-            ncand++;
-            return true;
-        });
+        s_cand[warp][lane][0] = (int)e.y;
+        s_cand[warp][lane][1] = (int)e.z;
+        s_cand[warp][lane][2] = (int)e.w;
+        ncand = (e.x & kPosedMore) ? kPosedCand + 1 : (e.w != 0xffffffffu ? 3 : e.z != 0xffffffffu ? 2 : 1);
     }
     s_pos[warp][lane] = make_float4(p.x, p.y, p.z, radius);
     const uint32_t own = (uint32_t)min(ncand, kPosedCand);
@@ -655,8 +663,10 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
         atomicOr(&st->error_bits, kErrStackOverflow);
         atomicAdd(&st->stack_overflows, 1u);
     }
-    const uint32_t tot = block_sum((uint32_t)(used - used0), s_warp);
-    if (threadIdx.x == 0 && tot) atomicAdd(ccount, tot);
+    // per-warp count (no block barrier: a warp that finishes early leaves at once)
+    uint32_t tot = (uint32_t)(used - used0);
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    if (lane == 0 && tot) atomicAdd(ccount, tot);
 }
 
 void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,

@@ -299,8 +299,8 @@ struct RigidTables {
     const int* dyn_scene;
     const uint32_t* pscene;
     // hashed grid of the dynamic bodies' world boxes (widened by grid_reach) for the particle
-    // queries: cell size grid_cs >= a third of any widened box, so a box covers at most
-    // kBoxCells cells; bucket h lists (dyn index, cell x, y, z) entries, any order, in
+    // queries: cell size grid_cs >= 1 / (kBoxAxis - 1) of any widened box, so a box covers
+    // at most kBoxAxis cells per axis, kBoxCells in all; bucket h lists (dyn index, cell x, y, z) entries, any order, in
     // grid_list[grid_start[h] ..); a particle takes only the entries of its own cell
     // (hash collisions never list a body twice for one cell)
     int grid_size;                // buckets (power of two)
@@ -309,7 +309,8 @@ struct RigidTables {
     uint32_t* grid_start;         // [grid_size + 1]
     int4* grid_list;              // [kBoxCells * n_dyn]
 };
-constexpr int kBoxCells = 64;
+constexpr int kBoxAxis = 4;
+constexpr int kBoxCells = kBoxAxis * kBoxAxis * kBoxAxis;
 // integrate_bodies.comp for every body; saves the pre-integration state to q_prev
 void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp);
 // world boxes of the dynamic bodies and their overlapping pairs

@@ -634,11 +634,13 @@ RigidTables Solver::rigid_tables() const {
     t.dyn_scene = dyn_scene_.p;
     t.pscene = pscene_.p;
     // box grid: a particle's side of the widening (soft margin + radius + pad, radii bounded
-    // by the larger of particle_max_radius and the largest finite radius set); cells a
-    // third of the largest widened box, so a box covers at most 4 cells per axis
+    // by the larger of particle_max_radius and the largest finite radius set); cells
+    // 1 / (kBoxAxis - 1) of the largest widened box, so a box covers at most kBoxAxis cells
+    // per axis
     t.grid_size = grid_size_;
     t.grid_reach = cfg_.soft_contact_margin + std::max(cfg_.particle_max_radius, r_max_) + 2.0f * t.pad;
-    t.grid_cs = (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f / 3.0f + 1e-4f;
+    t.grid_cs =
+        (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f / (float)(kBoxAxis - 1) + 1e-4f;
     t.grid_count = grid_count_.p;
     t.grid_start = grid_start_.p;
     t.grid_list = grid_list_.p;
@@ -786,11 +788,11 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
         dyn_max_margin_ = std::max(dyn_max_margin_, meshes_[b].shape_margin);
     }
     grid_size_ = 64;
-    while ((size_t)grid_size_ < 16 * dyn_list_.size()) grid_size_ *= 2;
+    while ((size_t)grid_size_ < (size_t)kBoxCells / 4 * dyn_list_.size()) grid_size_ *= 2;
     grid_count_.alloc((size_t)grid_size_, true);
     grid_start_.alloc((size_t)grid_size_ + 1, true);
     grid_list_.alloc(std::max<size_t>(dyn_list_.size() * kBoxCells, 1), true);
-    posed_list_.alloc(std::max<size_t>(n_, 1), false);
+    posed_list_.alloc(std::max<size_t>(n_, 1) * 4, false);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);
     upload_dyn_scenes();

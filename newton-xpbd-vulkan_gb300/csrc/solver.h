@@ -320,7 +320,7 @@ class Solver {
     float dyn_half_diag_ = 0.0f, dyn_max_margin_ = 0.0f;
     DevBuf<uint32_t> grid_count_, grid_start_;
     DevBuf<int4> grid_list_;
-    DevBuf<uint32_t> posed_list_;  // particles with candidate moving meshes, per substep
+    DevBuf<uint32_t> posed_list_;  // per substep: (particle, its first three candidate moving meshes) entries
     std::vector<int32_t> body_scene_;  // batched: scene of each body (-1: every scene)
     DevBuf<int> dyn_scene_;            // scene of each dynamic body (dyn index)
     DevBuf<uint32_t> dv_start_;
