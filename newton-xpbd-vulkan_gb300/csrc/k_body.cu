@@ -261,47 +261,87 @@ __global__ void k_boxgrid_count(RigidTables rt, DeviceStatus* st) {
     }
 }
 
-// exclusive scan of the bucket counts (one block, tiles of 4 counts per thread read
-// as one coalesced uint4); the counts become fill cursors
-__global__ void __launch_bounds__(1024) k_boxgrid_scan(RigidTables rt) {
-    __shared__ uint32_t s_warp[32];
-    __shared__ uint32_t s_carry;
+// Exclusive scan of the bucket counts in three launches (the bucket count grows with the
+// number of dynamic bodies): the sum of every tile of kBoxScanTile counts, one block's scan
+// of the tile sums, then every tile's own scan from its offset. Each thread reads its 4
+// counts as one uint4; the counts become fill cursors (zeroed).
+constexpr int kBoxScanThreads = 256;
+constexpr int kBoxScanTile = 4 * kBoxScanThreads;
+
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t own, uint32_t* s_warp, uint32_t& total) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_carry = 0;
-    __syncthreads();
-    for (int base = 0; base < rt.grid_size; base += 4096) {  // grid_size is a power of two >= 64
-        const int b = base + tid * 4;
-        uint4 c = make_uint4(0u, 0u, 0u, 0u);
-        if (b < rt.grid_size) c = *reinterpret_cast<const uint4*>(rt.grid_count + b);
-        const uint32_t own = c.x + c.y + c.z + c.w;
-        uint32_t incl = own;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) s_warp[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t w = s_warp[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            s_warp[lane] = w;  // inclusive over warps
-        }
-        __syncthreads();
-        const uint32_t carry = s_carry;
-        const uint32_t start = carry + (warp ? s_warp[warp - 1] : 0u) + incl - own;
-        if (b < rt.grid_size) {
-            *reinterpret_cast<uint4*>(rt.grid_start + b) =
-                make_uint4(start, start + c.x, start + c.x + c.y, start + c.x + c.y + c.z);
-            *reinterpret_cast<uint4*>(rt.grid_count + b) = make_uint4(0u, 0u, 0u, 0u);
-        }
-        __syncthreads();
-        if (tid == 0) s_carry = carry + s_warp[31];
-        __syncthreads();
+    uint32_t incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
     }
-    if (tid == 0) rt.grid_start[rt.grid_size] = s_carry;
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    total = 0;
+    for (int w = 0; w < kBoxScanThreads / 32; w++) {
+        const uint32_t v = s_warp[w];
+        if (w < warp) before += v;
+        total += v;
+    }
+    return before + incl - own;
+}
+
+__global__ void __launch_bounds__(kBoxScanThreads) k_boxgrid_tile_sums(RigidTables rt, uint32_t* tile_sum) {
+    __shared__ uint32_t s_warp[kBoxScanThreads / 32];
+    const int b = blockIdx.x * kBoxScanTile + threadIdx.x * 4;
+    uint4 c = make_uint4(0u, 0u, 0u, 0u);
+    if (b < rt.grid_size) c = *reinterpret_cast<const uint4*>(rt.grid_count + b);
+    uint32_t total;
+    block_excl_scan256(c.x + c.y + c.z + c.w, s_warp, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the tile sums in place (tiles <= 4 x 1024), the grand total
+// into grid_start[grid_size]
+__global__ void __launch_bounds__(1024) k_boxgrid_scan(RigidTables rt, uint32_t* tile_sum, int tiles) {
+    __shared__ uint32_t s_warp[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t v[4] = {0u, 0u, 0u, 0u};
+    for (int j = 0; j < 4; j++)
+        if (tid * 4 + j < tiles) v[j] = tile_sum[tid * 4 + j];
+    const uint32_t own = v[0] + v[1] + v[2] + v[3];
+    uint32_t incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = s_warp[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        s_warp[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = (warp ? s_warp[warp - 1] : 0u) + incl - own;
+    for (int j = 0; j < 4; j++) {
+        if (tid * 4 + j < tiles) tile_sum[tid * 4 + j] = run;
+        run += v[j];
+    }
+    if (tid == 0) rt.grid_start[rt.grid_size] = s_warp[31];
+}
+
+__global__ void __launch_bounds__(kBoxScanThreads) k_boxgrid_tile_scan(RigidTables rt, const uint32_t* tile_sum) {
+    __shared__ uint32_t s_warp[kBoxScanThreads / 32];
+    const int b = blockIdx.x * kBoxScanTile + threadIdx.x * 4;
+    uint4 c = make_uint4(0u, 0u, 0u, 0u);
+    if (b < rt.grid_size) c = *reinterpret_cast<const uint4*>(rt.grid_count + b);
+    uint32_t total;
+    const uint32_t start = tile_sum[blockIdx.x] + block_excl_scan256(c.x + c.y + c.z + c.w, s_warp, total);
+    if (b < rt.grid_size) {
+        *reinterpret_cast<uint4*>(rt.grid_start + b) =
+            make_uint4(start, start + c.x, start + c.x + c.y, start + c.x + c.y + c.z);
+        *reinterpret_cast<uint4*>(rt.grid_count + b) = make_uint4(0u, 0u, 0u, 0u);
+    }
 }
 
 __global__ void k_boxgrid_fill(RigidTables rt) {
@@ -322,7 +362,10 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
     cudaMemsetAsync(rt.grid_count, 0, sizeof(uint32_t) * (size_t)rt.grid_size, s);
     const int cells = (rt.n_dyn * kBoxCells + 127) / 128;
     k_boxgrid_count<<<cells, 128, 0, s>>>(rt, st);
-    k_boxgrid_scan<<<1, 1024, 0, s>>>(rt);
+    const int tiles = (rt.grid_size + kBoxScanTile - 1) / kBoxScanTile;
+    k_boxgrid_tile_sums<<<tiles, kBoxScanThreads, 0, s>>>(rt, rt.grid_tiles);
+    k_boxgrid_scan<<<1, 1024, 0, s>>>(rt, rt.grid_tiles, tiles);
+    k_boxgrid_tile_scan<<<tiles, kBoxScanThreads, 0, s>>>(rt, rt.grid_tiles);
     k_boxgrid_fill<<<cells, 128, 0, s>>>(rt);
 }
 
@@ -540,12 +583,13 @@ __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t*
 // frame) for the posed list, one warp per 32 listed particles. Each lane copies its
 // particle's first kPosedCand candidate meshes, listed by the triage, to shared memory; the
 // warp then runs all (particle, mesh) queries of those lists one per lane, so lanes with one
-// candidate do not wait for lanes with three; finally each lane inserts its particle's
-// contacts into its slots in mesh order (the shader's mesh loop order; candidates past
-// kPosedCand are listed again and queried by their own lane afterwards, in candidate order).
+// candidate do not wait for lanes with three. Each result goes to the hit buffer at (list
+// entry, candidate): the slots are not touched here, so this kernel can run beside the
+// static-mesh traversal, and k_posed_merge inserts the hits afterwards.
 struct PosedHit {
     float4 a, b, c;  // (body_pos, found), (normal, 0), (body_vel, 0)
 };
+static_assert(kPosedHitWords == kPosedCand * 3, "hit buffer layout: kPosedCand hits of 3 float4 per list entry");
 
 __device__ __forceinline__ void posed_insert(float4* base, int& used, int slot_cap, bool& slot_ovf, int mesh,
                                              v3 bp, v3 nw, v3 bv) {
@@ -566,84 +610,114 @@ __device__ __forceinline__ void posed_insert(float4* base, int& used, int slot_c
     used++;
 }
 
+// the number of candidates a list entry holds (kPosedCand + 1: more follow)
+__device__ __forceinline__ int posed_listed(const uint4& e) {
+    return (e.x & kPosedMore) ? kPosedCand + 1 : (e.w != 0xffffffffu ? 3 : e.z != 0xffffffffu ? 2 : 1);
+}
+
 __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ counter, const float4* __restrict__ x,
-    const float* __restrict__ r, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* __restrict__ cinfo,
-    float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+    const float* __restrict__ r, MeshTables mt, PosedHit* __restrict__ hits, DeviceStatus* st) {
     __shared__ int s_cand[kPosedWarps][32][kPosedCand];
     __shared__ float4 s_pos[kPosedWarps][32];
     __shared__ uint32_t s_off[kPosedWarps][33];
-    __shared__ PosedHit s_res[kPosedWarps][32 * kPosedCand];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t listed = (int64_t)*counter;
-    if (t - lane >= listed) return;  // the whole warp is past the list
-    const bool valid = t < listed;
-    int64_t i = -1;
-    v3 p = mk3(0.0f, 0.0f, 0.0f);
-    float radius = 0.0f;
-    int ncand = 0;  // candidates listed by the triage (kPosedCand + 1: more follow)
-    int scene = 0;
-    if (valid) {
-        const uint4 e = reinterpret_cast<const uint4*>(list)[t];
-        i = (int64_t)(e.x & ~kPosedMore);
-        p = xyz(x[i]);
-        radius = r[i];
-        scene = rt.pscene ? (int)rt.pscene[i] : 0;
-        s_cand[warp][lane][0] = (int)e.y;
-        s_cand[warp][lane][1] = (int)e.z;
-        s_cand[warp][lane][2] = (int)e.w;
-        ncand = (e.x & kPosedMore) ? kPosedCand + 1 : (e.w != 0xffffffffu ? 3 : e.z != 0xffffffffu ? 2 : 1);
-    }
-    s_pos[warp][lane] = make_float4(p.x, p.y, p.z, radius);
-    const uint32_t own = (uint32_t)min(ncand, kPosedCand);
-    uint32_t incl = own;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += y;
-    }
-    s_off[warp][lane] = incl - own;
-    if (lane == 31) s_off[warp][32] = incl;
-    __syncwarp();
-    const uint32_t total = s_off[warp][32];
-    bool stack_ovf = false, slot_ovf = false;
-    // the warp's (particle, mesh) queries, one per lane
-    for (uint32_t pr = (uint32_t)lane; pr < total; pr += 32) {
-        int o = 0;
-        while (o < 31 && s_off[warp][o + 1] <= pr) o++;
-        const int mesh = s_cand[warp][o][pr - s_off[warp][o]];
-        const float4 po = s_pos[warp][o];
-        const v3 pos_m = xyz(mt.pose[mesh * 2]);
-        const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
-        const v3 q = quat_rotate_inv(rot_m, vsub(xyz(po), pos_m));  // as posed_candidates computes it
-        v3 bp, bv, nn;
-        PosedHit h;
-        if (mesh_query(mt, mesh, po.w, q, bp, bv, nn, stack_ovf)) {
-            const v3 nw = quat_rotate(rot_m, nn);
-            h.a = make_float4(bp.x, bp.y, bp.z, 1.0f);
-            h.b = make_float4(nw.x, nw.y, nw.z, 0.0f);
-            h.c = make_float4(bv.x, bv.y, bv.z, 0.0f);
-        } else {
-            h.a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int64_t stride = (int64_t)gridDim.x * kPosedWarps * 32;
+    bool stack_ovf = false;
+    // chunks of 32 list entries per warp, grid-stride over the list
+    for (int64_t t0 = ((int64_t)blockIdx.x * kPosedWarps + warp) * 32; t0 < listed; t0 += stride) {
+        const int64_t t = t0 + lane;
+        uint32_t own = 0;
+        float4 po = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (t < listed) {
+            const uint4 e = reinterpret_cast<const uint4*>(list)[t];
+            const int64_t i = (int64_t)(e.x & ~kPosedMore);
+            const float4 xi = x[i];
+            po = make_float4(xi.x, xi.y, xi.z, r[i]);
+            s_cand[warp][lane][0] = (int)e.y;
+            s_cand[warp][lane][1] = (int)e.z;
+            s_cand[warp][lane][2] = (int)e.w;
+            own = (uint32_t)min(posed_listed(e), kPosedCand);
         }
-        s_res[warp][pr] = h;
+        s_pos[warp][lane] = po;
+        uint32_t incl = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        s_off[warp][lane] = incl - own;
+        if (lane == 31) s_off[warp][32] = incl;
+        __syncwarp();
+        const uint32_t total = s_off[warp][32];
+        // the warp's (particle, mesh) queries, one per lane
+        for (uint32_t pr = (uint32_t)lane; pr < total; pr += 32) {
+            int o = 0;
+            while (o < 31 && s_off[warp][o + 1] <= pr) o++;
+            const uint32_t kc = pr - s_off[warp][o];
+            const int mesh = s_cand[warp][o][kc];
+            const float4 pq = s_pos[warp][o];
+            const v3 pos_m = xyz(mt.pose[mesh * 2]);
+            const q4 rot_m = f4q(mt.pose[mesh * 2 + 1]);
+            const v3 q = quat_rotate_inv(rot_m, vsub(xyz(pq), pos_m));  // as posed_candidates computes it
+            v3 bp, bv, nn;
+            PosedHit h;
+            if (mesh_query(mt, mesh, pq.w, q, bp, bv, nn, stack_ovf)) {
+                const v3 nw = quat_rotate(rot_m, nn);
+                h.a = make_float4(bp.x, bp.y, bp.z, 1.0f);
+                h.b = make_float4(nw.x, nw.y, nw.z, 0.0f);
+                h.c = make_float4(bv.x, bv.y, bv.z, 0.0f);
+            } else {
+                h.a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                h.b = h.a;
+                h.c = h.a;
+            }
+            hits[(size_t)(t0 + o) * kPosedCand + kc] = h;
+        }
+        __syncwarp();  // the chunk's shared lists are read before the next chunk writes them
     }
-    __syncwarp();
-    int used0 = 0, used = 0;
-    if (valid) {
+    if (stack_ovf) {
+        atomicOr(&st->error_bits, kErrStackOverflow);
+        atomicAdd(&st->stack_overflows, 1u);
+    }
+}
+
+// The hits of every list entry inserted into its particle's slots after the static-mesh
+// contacts, in the shader's mesh loop order (posed_insert places each by its mesh index);
+// candidates past kPosedCand are listed again and queried here, in candidate order. One
+// thread per list entry, grid-stride over the list (its length is on the device).
+__global__ void __launch_bounds__(128) k_posed_merge(const uint32_t* __restrict__ list,
+                                                     const uint32_t* __restrict__ counter,
+                                                     const float4* __restrict__ x, const float* __restrict__ r,
+                                                     MeshTables mt, RigidTables rt, const PosedHit* __restrict__ hits,
+                                                     int slot_cap, uint32_t* __restrict__ cinfo,
+                                                     float4* __restrict__ cslot, uint32_t* ccount, DeviceStatus* st) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t listed = (int64_t)*counter;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31) >= listed) return;  // the whole warp is idle
+    bool stack_ovf = false, slot_ovf = false;
+    uint32_t added = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < listed; t += stride) {
+        int used0 = 0, used = 0;
+        const uint4 e = reinterpret_cast<const uint4*>(list)[t];
+        const int64_t i = (int64_t)(e.x & ~kPosedMore);
+        const int ncand = posed_listed(e);
+        const int cand[kPosedCand] = {(int)e.y, (int)e.z, (int)e.w};
         const uint32_t info = cinfo[i];
         used0 = used = info_slots(info);
         float4* base = cslot + (size_t)i * slot_cap * 3;
-        const uint32_t off = s_off[warp][lane];
-        for (uint32_t k = 0; k < own; k++) {
-            const PosedHit h = s_res[warp][off + k];
-            if (h.a.w != 0.0f)
-                posed_insert(base, used, slot_cap, slot_ovf, s_cand[warp][lane][k], xyz(h.a), xyz(h.b), xyz(h.c));
+        for (int k = 0; k < min(ncand, kPosedCand); k++) {
+            const PosedHit h = hits[(size_t)t * kPosedCand + k];
+            if (h.a.w != 0.0f) posed_insert(base, used, slot_cap, slot_ovf, cand[k], xyz(h.a), xyz(h.b), xyz(h.c));
         }
-        if (ncand > kPosedCand) {  // the rest, by this lane, in candidate order
+        if (ncand > kPosedCand) {  // the rest, in candidate order
+            const v3 p = xyz(x[i]);
+            const float radius = r[i];
             int k = 0;
-            posed_candidates(mt, rt, p, radius, scene, [&](int mesh, v3 q, q4 rot_m) {
+            posed_candidates(mt, rt, p, radius, rt.pscene ? (int)rt.pscene[i] : 0, [&](int mesh, v3 q, q4 rot_m) {
                 if (k++ < kPosedCand) return true;
                 v3 bp, bv, nn;
                 if (mesh_query(mt, mesh, radius, q, bp, bv, nn, stack_ovf))
@@ -654,6 +728,7 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
         // every slot added here belongs to a dynamic body
         if (used != used0)
             cinfo[i] = (info & kPlaneBit) | ((uint32_t)used << 1) | ((uint32_t)(used - used0) << 16);
+        added += (uint32_t)(used - used0);
     }
     if (slot_ovf) {
         atomicOr(&st->error_bits, kErrSlotOverflow);
@@ -663,8 +738,7 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
         atomicOr(&st->error_bits, kErrStackOverflow);
         atomicAdd(&st->stack_overflows, 1u);
     }
-    // per-warp count (no block barrier: a warp that finishes early leaves at once)
-    uint32_t tot = (uint32_t)(used - used0);
+    uint32_t tot = added;
     for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
     if (lane == 0 && tot) atomicAdd(ccount, tot);
 }
@@ -676,18 +750,24 @@ void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const
 }
 
 void launch_posed_queries(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
-                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* counter,
-                          uint32_t* list, DeviceStatus* st) {
+                          const uint32_t* counter, const uint32_t* list, float4* hits, DeviceStatus* st) {
     if (n <= 0 || rt.n_dyn <= 0) return;
-    k_collide_posed<<<(int)((n + 32 * kPosedWarps - 1) / (32 * kPosedWarps)), 32 * kPosedWarps, 0, s>>>(
-        list, counter, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, st);
+    // grid-stride over the listed entries (their count is on the device): about four rounds
+    // of resident blocks, so a slow chunk does not hold up the end of the launch
+    const int blocks = (int)std::min<int64_t>((n + 32 * kPosedWarps - 1) / (32 * kPosedWarps),
+                                              (int64_t)device_sm_count() * 6 * 4);
+    k_collide_posed<<<blocks, 32 * kPosedWarps, 0, s>>>(list, counter, x, r, mt, reinterpret_cast<PosedHit*>(hits),
+                                                       st);
 }
 
-void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
-                          const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
-                          float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st) {
-    launch_posed_triage(s, n, order, x, r, flags, mt, rt, counter, list);
-    launch_posed_queries(s, n, x, r, mt, rt, slot_cap, cinfo, cslot, ccount, counter, list, st);
+void launch_posed_merge(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
+                        int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, const uint32_t* counter,
+                        const uint32_t* list, const float4* hits, DeviceStatus* st) {
+    if (n <= 0 || rt.n_dyn <= 0) return;
+    const int blocks = (int)std::min<int64_t>((n + 127) / 128, (int64_t)device_sm_count() * 16);
+    k_posed_merge<<<blocks, 128, 0, s>>>(list, counter, x, r, mt, rt,
+                                                          reinterpret_cast<const PosedHit*>(hits), slot_cap, cinfo,
+                                                          cslot, ccount, st);
 }
 
 // ---------------------------------------------------------------- body-delta entries ----

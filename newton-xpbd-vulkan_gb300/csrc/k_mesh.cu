@@ -227,10 +227,11 @@ void launch_collide_triage(cudaStream_t s, int64_t n, const uint32_t* order, con
 // (bench frame 2.89 -> 2.80 ms; the traversal itself is as fast either way).
 void launch_collide_walk(cudaStream_t s, int64_t n, const float4* x, const float* r, PlaneParams pl, MeshTables mt,
                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* queue,
-                         const uint32_t* near, DeviceStatus* st) {
+                         const uint32_t* near, DeviceStatus* st, int blocks_per_sm) {
     if (n <= 0) return;
     const int threads = kCollideThreads;
-    const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads, (int64_t)device_sm_count() * 32);
+    const int blocks = (int)std::min<int64_t>((n * 32 + threads - 1) / threads,
+                                              (int64_t)device_sm_count() * std::max(1, std::min(blocks_per_sm, 32)));
     k_collide<<<blocks, threads, 0, s>>>(n, x, r, pl, mt, slot_cap, cinfo, cslot, ccount, queue, near, st);
 }
 

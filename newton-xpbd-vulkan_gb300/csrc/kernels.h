@@ -199,9 +199,10 @@ void launch_collide(cudaStream_t s, int64_t n, const uint32_t* order, const floa
 void launch_collide_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                            const int* flags, PlaneParams pl, MeshTables mt, uint32_t* cinfo, uint32_t* ccount,
                            uint32_t* queue, uint32_t* near);
+// (at most blocks_per_sm one-warp blocks per SM: fewer leave room for a kernel beside it)
 void launch_collide_walk(cudaStream_t s, int64_t n, const float4* x, const float* r, PlaneParams pl, MeshTables mt,
                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* queue,
-                         const uint32_t* near, DeviceStatus* st);
+                         const uint32_t* near, DeviceStatus* st, int blocks_per_sm = 32);
 // per-leaf-slot triangle cache for the slots [first, first + count)
 void launch_tri_cache(cudaStream_t s, int64_t first, int64_t count, const uint32_t* prim, const uint32_t* tris,
                       const float* verts, float4* cache);
@@ -307,10 +308,12 @@ struct RigidTables {
     float grid_cs, grid_reach;
     uint32_t* grid_count;         // [grid_size]
     uint32_t* grid_start;         // [grid_size + 1]
+    uint32_t* grid_tiles;         // scan scratch: [grid_size / 1024], at most 4,096 tiles
     int4* grid_list;              // [kBoxCells * n_dyn]
 };
-constexpr int kBoxAxis = 4;
+constexpr int kBoxAxis = 6;
 constexpr int kBoxCells = kBoxAxis * kBoxAxis * kBoxAxis;
+constexpr int kBoxBuckets = 64;  // buckets per dynamic body (rounded up to a power of two in all)
 // integrate_bodies.comp for every body; saves the pre-integration state to q_prev
 void launch_body_integrate(cudaStream_t s, BodyArrays ba, float4* q_prev, float4* qd_prev, RigidParams rp);
 // world boxes of the dynamic bodies and their overlapping pairs
@@ -318,18 +321,20 @@ void launch_body_pairs(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables
 // rigid contacts of every dynamic-body vertex against the plane and the other meshes
 void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTables mt, RigidParams rp,
                            DeviceStatus* st);
-// particle contacts against the meshes of dynamic bodies, merged into the slots in mesh order;
-// counter: one zeroed word, list: n words of scratch
-void launch_collide_posed(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
-                          const int* flags, MeshTables mt, RigidTables rt, int slot_cap, uint32_t* cinfo,
-                          float4* cslot, uint32_t* ccount, uint32_t* counter, uint32_t* list, DeviceStatus* st);
-// its two halves: the triage (reads `order`, lists the particles near a moving mesh) and
-// the queries of the listed particles
+// particle contacts against the meshes of dynamic bodies in three launches: the triage
+// (reads `order`; lists the particles near a moving mesh with their first candidates:
+// counter = one zeroed word, list = 4 words per particle), the queries of the listed
+// candidates (results to `hits`, kPosedHitWords float4 per particle; no slot is touched,
+// so they may run beside the static-mesh traversal), and the merge of the hits
+// into the slots in mesh order after that traversal
+constexpr int kPosedHitWords = 9;  // float4 per list entry in `hits`
 void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                          const int* flags, MeshTables mt, RigidTables rt, uint32_t* counter, uint32_t* list);
 void launch_posed_queries(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
-                          int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, uint32_t* counter,
-                          uint32_t* list, DeviceStatus* st);
+                          const uint32_t* counter, const uint32_t* list, float4* hits, DeviceStatus* st);
+void launch_posed_merge(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,
+                        int slot_cap, uint32_t* cinfo, float4* cslot, uint32_t* ccount, const uint32_t* counter,
+                        const uint32_t* list, const float4* hits, DeviceStatus* st);
 // body-delta entries: key = body of each dynamic slot at position rank[i].x + j, digit histograms
 void launch_dyn_emit(cudaStream_t s, int64_t n, const uint32_t* cinfo, DynSlots ds, const uint2* rank,
                      uint32_t cap, const SortPlan& sp, uint32_t* keys, uint32_t* hist, DeviceStatus* st);

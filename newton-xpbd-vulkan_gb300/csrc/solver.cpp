@@ -71,6 +71,8 @@ Solver::~Solver() {
     if (aux_) cudaStreamDestroy(aux_);
     if (fork_) cudaEventDestroy(fork_);
     if (join_) cudaEventDestroy(join_);
+    if (triaged_) cudaEventDestroy(triaged_);
+    if (walked_) cudaEventDestroy(walked_);
     for (auto& e : split_ev_)
         for (auto& x : e)
             if (x) cudaEventDestroy(x);
@@ -124,6 +126,8 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     XPBD_CUDA(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
     XPBD_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     XPBD_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
+    XPBD_CUDA(cudaEventCreateWithFlags(&triaged_, cudaEventDisableTiming));
+    XPBD_CUDA(cudaEventCreateWithFlags(&walked_, cudaEventDisableTiming));
 
     for (int p = 0; p < 2; p++) {
         x_[p].alloc(n_);
@@ -643,6 +647,7 @@ RigidTables Solver::rigid_tables() const {
         (2.0f * dyn_half_diag_ + 2.0f * (t.grid_reach + dyn_max_margin_)) * 1.01f / (float)(kBoxAxis - 1) + 1e-4f;
     t.grid_count = grid_count_.p;
     t.grid_start = grid_start_.p;
+    t.grid_tiles = grid_tiles_.p;
     t.grid_list = grid_list_.p;
     return t;
 }
@@ -788,11 +793,14 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
         dyn_max_margin_ = std::max(dyn_max_margin_, meshes_[b].shape_margin);
     }
     grid_size_ = 64;
-    while ((size_t)grid_size_ < (size_t)kBoxCells / 4 * dyn_list_.size()) grid_size_ *= 2;
+    while ((size_t)grid_size_ < (size_t)kBoxBuckets * dyn_list_.size()) grid_size_ *= 2;
     grid_count_.alloc((size_t)grid_size_, true);
     grid_start_.alloc((size_t)grid_size_ + 1, true);
+    grid_tiles_.alloc((size_t)grid_size_ / 1024 + 1, true);
+    if (grid_size_ > 4096 * 1024) throw std::runtime_error("too many dynamic bodies for the box grid");
     grid_list_.alloc(std::max<size_t>(dyn_list_.size() * kBoxCells, 1), true);
     posed_list_.alloc(std::max<size_t>(n_, 1) * 4, false);
+    posed_hits_.alloc(std::max<size_t>(n_, 1) * kPosedHitWords, false);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);
     upload_dyn_scenes();
@@ -1023,61 +1031,47 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     prof_mark(P_CLEAR);
     if (bodies) {
         launch_body_pairs(stream_, ba, rt, mesh_tables(), rp, st);
-        count_kernel(2);
+        count_kernel(7);  // bounds, pairs, box grid count, three scan kernels, fill
+        count_memset();
         prof_mark(P_BODY_CONTACT);
     }
-    // Contact generation forks onto the second stream once the triages have read the
-    // previous order (which the sort below overwrites): the static-mesh traversal, then the
-    // moving-mesh queries, rigid contacts and body-delta entries. The integrate / sort /
-    // gather chain reads none of their outputs (nor the body poses they read before the
-    // bodies integrate), and the join comes before the body integration and the first
-    // reader of contacts. Profiling keeps one stream in the original order so that each
-    // stage's events bracket its own kernels.
+    // Contact generation forks onto the second stream after the static-mesh triage (which
+    // reads the previous order that the sort below overwrites). With dynamic bodies the
+    // second stream runs the moving-mesh triage, its queries (results to the hit buffer) and
+    // the rigid contacts while the main stream runs the static-mesh traversal; then the
+    // second stream merges the hits into the slots behind the static contacts and builds the
+    // body-delta entries, while the main stream runs the integrate / sort / gather chain
+    // (the sort waits for the moving-mesh triage), which reads none of their outputs. The
+    // join comes before the bodies integrate and before the first reader of contacts.
+    // Without bodies the static-mesh traversal itself runs on the second stream beside the
+    // sort chain. Profiling keeps one stream in stage order so that each stage's events
+    // bracket its own kernels.
     const bool fork = mesh_pass && !profiling_;
     const MeshTables mt = mesh_tables();
     const uint32_t* prev_order = pair_v_[(plan_.passes - 1) & 1].p;
     uint32_t* posed_counter = sort_scratch_.p + cq_off_ + 2;
-    cudaStream_t cs = stream_;
-    if (fork) {
-        launch_collide_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, pl, mt, cinfo_.p, ccount,
-                              sort_scratch_.p + cq_off_, near_.p);
-        if (bodies)
-            launch_posed_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, mt, rt, posed_counter,
-                                posed_list_.p);
-        XPBD_CUDA(cudaEventRecord(fork_, stream_));
-        XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
-        cs = aux_;
-    }
-    if (mesh_pass) {
-        if (!fork)
-            launch_collide_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, pl, mt, cinfo_.p, ccount,
-                                  sort_scratch_.p + cq_off_, near_.p);
-        launch_collide_walk(cs, n, x_[src].p, r_.p, pl, mt, slot_cap_, cinfo_.p, cslot_.p, ccount,
-                            sort_scratch_.p + cq_off_, near_.p, st);
-        count_kernel(2);  // triage + traversal
-        prof_mark(P_CONTACT);
-    }
-    if (bodies) {
-        if (!fork)
-            launch_posed_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, mt, rt, posed_counter,
-                                posed_list_.p);
-        launch_posed_queries(cs, n, x_[src].p, r_.p, mt, rt, slot_cap_, cinfo_.p, cslot_.p, ccount, posed_counter,
-                             posed_list_.p, st);
+    const auto posed_queries = [&](cudaStream_t s) {
+        launch_posed_triage(s, n, prev_order, x_[src].p, r_.p, flags_.p, mt, rt, posed_counter, posed_list_.p);
+        if (fork) XPBD_CUDA(cudaEventRecord(triaged_, s));
+        launch_posed_queries(s, n, x_[src].p, r_.p, mt, rt, posed_counter, posed_list_.p, posed_hits_.p, st);
         count_kernel(2);  // triage + queries
-        prof_mark(P_POSED);
-        launch_rigid_contacts(cs, ba, rt, mt, rp, st);
+    };
+    const auto posed_merge = [&](cudaStream_t s) {
+        launch_posed_merge(s, n, x_[src].p, r_.p, mt, rt, slot_cap_, cinfo_.p, cslot_.p, ccount, posed_counter,
+                           posed_list_.p, posed_hits_.p, st);
         count_kernel();
-        prof_mark(P_RIGID);
+    };
+    const auto body_entries = [&](cudaStream_t s) {
         // body-delta entries: dynamic slots in contact order, grouped by body (stable sort)
-        launch_dyn_scan(cs, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
-        launch_dyn_emit(cs, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
+        launch_dyn_scan(s, n, cinfo_.p, ds, dyn_rank_.p, dyn_totals_.p, dyn_ws_.p);
+        launch_dyn_emit(s, n, cinfo_.p, ds, dyn_rank_.p, entry_cap_, eplan_, ekeys_.p,
                         esort_scratch_.p + ehist_off_, st);
         count_kernel(4);
         const uint32_t* ek = ekeys_.p;
         const uint32_t* ev = nullptr;
         const size_t elbw = sort_lookback_words(eplan_);
         for (int p = 0; p < eplan_.passes; p++) {
-            launch_onesweep_pass(cs, (int64_t)entry_cap_, eplan_, p, ek, ev, epk_[p & 1].p, epv_[p & 1].p,
+            launch_onesweep_pass(s, (int64_t)entry_cap_, eplan_, p, ek, ev, epk_[p & 1].p, epv_[p & 1].p,
                                  esort_scratch_.p + ehist_off_ + ((size_t)p << eplan_.bits),
                                  esort_scratch_.p + elb_off_ + (size_t)p * elbw, esort_scratch_.p + etc_off_ + p, st,
                                  dyn_totals_.p);
@@ -1085,12 +1079,48 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
             ek = epk_[p & 1].p;
             ev = epv_[p & 1].p;
         }
-        launch_body_segments(cs, entry_cap_, dyn_totals_.p, ek, seg_.p);
+        launch_body_segments(s, entry_cap_, dyn_totals_.p, ek, seg_.p);
         count_kernel();
         sorted_entries_ = ev;
-        prof_mark(P_BODY_ENTRIES);
+    };
+    if (mesh_pass)
+        launch_collide_triage(stream_, n, prev_order, x_[src].p, r_.p, flags_.p, pl, mt, cinfo_.p, ccount,
+                              sort_scratch_.p + cq_off_, near_.p);
+    cudaStream_t walk_s = stream_;  // the static-mesh traversal's stream
+    if (fork) {
+        XPBD_CUDA(cudaEventRecord(fork_, stream_));
+        XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
+        if (bodies) {
+            posed_queries(aux_);
+            launch_rigid_contacts(aux_, ba, rt, mt, rp, st);  // reads only the substep-start poses
+            count_kernel();
+        } else {
+            walk_s = aux_;
+        }
+    }
+    if (mesh_pass) {
+        launch_collide_walk(walk_s, n, x_[src].p, r_.p, pl, mt, slot_cap_, cinfo_.p, cslot_.p, ccount,
+                            sort_scratch_.p + cq_off_, near_.p, st, fork && bodies ? kWalkBlocksBeside : 32);
+        count_kernel(2);  // triage + traversal
+        prof_mark(P_CONTACT);
+    }
+    if (fork && bodies) {  // the hits join the slots once the static contacts are in place
+        XPBD_CUDA(cudaEventRecord(walked_, stream_));
+        XPBD_CUDA(cudaStreamWaitEvent(aux_, walked_, 0));
+        posed_merge(aux_);
+        body_entries(aux_);
     }
     if (fork) XPBD_CUDA(cudaEventRecord(join_, aux_));
+    if (bodies && !fork) {
+        posed_queries(stream_);
+        posed_merge(stream_);
+        prof_mark(P_POSED);
+        launch_rigid_contacts(stream_, ba, rt, mt, rp, st);
+        count_kernel();
+        prof_mark(P_RIGID);
+        body_entries(stream_);
+        prof_mark(P_BODY_ENTRIES);
+    }
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pscene_.p, pp, pl, keys_.p, plan_,
@@ -1100,6 +1130,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const uint32_t* kin = keys_.p;
     const uint32_t* vin = nullptr;
     const size_t lbw = sort_lookback_words(plan_);
+    if (fork && bodies) XPBD_CUDA(cudaStreamWaitEvent(stream_, triaged_, 0));  // it has read the previous order
     for (int p = 0; p < plan_.passes; p++) {
         uint32_t* ko = pair_k_[p & 1].p;
         uint32_t* vo = pair_v_[p & 1].p;

@@ -212,6 +212,9 @@ class Solver {
     void prof_mark(int slot);
     void apply_sort_plan(int bits, int items);
     bool sort_tuned_ = false;
+    // one-warp blocks per SM of the static-mesh traversal while the moving-mesh queries run
+    // beside it on the second stream (32, the SM's block limit, when it runs alone)
+    static constexpr int kWalkBlocksBeside = 16;
     // Solve-kernel form: timed on the scene's own last substep (its last iteration launched
     // again with its outputs in scratch buffers) after the first frame and again every
     // kSolveRetime frames, as the scene evolves (in the mixed workload the warp form turns
@@ -239,7 +242,7 @@ class Solver {
     // second stream of the frame graph: the mesh traversal runs on it beside the
     // integrate / sort / gather chain, which does not read contacts
     cudaStream_t aux_ = nullptr;
-    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr, triaged_ = nullptr, walked_ = nullptr;
     // Whether the first iteration's particle-particle part runs before the join, beside the
     // contact generation (split) or after it, fused with the rest (the faster depends on how
     // long the contact chain is next to the sort and the solve): -1 undecided, in which case
@@ -318,9 +321,10 @@ class Solver {
     DevBuf<int> dyn_, dyn_index_, posed_, walk_list_, partners_, partner_count_, rc_count_;
     int walk_count_ = 0, n_dyn_verts_ = 0, grid_size_ = 0;
     float dyn_half_diag_ = 0.0f, dyn_max_margin_ = 0.0f;
-    DevBuf<uint32_t> grid_count_, grid_start_;
+    DevBuf<uint32_t> grid_count_, grid_start_, grid_tiles_;
     DevBuf<int4> grid_list_;
     DevBuf<uint32_t> posed_list_;  // per substep: (particle, its first three candidate moving meshes) entries
+    DevBuf<float4> posed_hits_;    // per list entry: the query results of its listed candidates
     std::vector<int32_t> body_scene_;  // batched: scene of each body (-1: every scene)
     DevBuf<int> dyn_scene_;            // scene of each dynamic body (dyn index)
     DevBuf<uint32_t> dv_start_;
