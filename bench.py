@@ -339,6 +339,13 @@ def headline(result):
         head["diff_grad_mu_60_substeps"] = diff["grad_checked"]["soft_contact_mu"]
     if "cpu_baseline" in result:
         head["cpu_baseline"] = result["cpu_baseline"]["value"]
+    small = result.get("pile_4k", {})
+    if "value" in small:
+        head["pile_4k"] = small["value"]
+    for name in ("pile_4k", "particles_on_mesh", "batched"):
+        cpu = (result.get(name) or {}).get("cpu_baseline")
+        if cpu:
+            head[name + "_cpu"] = cpu["value"]
     return head
 
 
@@ -352,7 +359,8 @@ def run_gpu(args):
         dev = torch.device("cuda", local)
         parts = {}
         for key, name, fn in (("mesh", "particles_on_mesh", measure_mesh), ("batched", "batched", measure_batched),
-                              ("diff", "diff", measure_diff), ("pile", "pile_1m", measure_pile)):
+                              ("diff", "diff", measure_diff), ("pile", "pile_1m", measure_pile),
+                              ("pile4k", "pile_4k", measure_small_pile)):
             if key in args.only.split(","):
                 parts[name] = fn(args, dev)
         print(json.dumps(parts), flush=True)
@@ -432,7 +440,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_sample(sc, x_snap, v_snap, q_snap, qd_snap, budget_s=args.cpu_budget)
     del solver
-    for name, on, fn in (("particles_on_mesh", args.mesh_frames > 0, lambda: measure_mesh(args, dev)),
+    for name, on, fn in (("pile_4k", args.small_pile, lambda: measure_small_pile(args, dev)),
+                         ("particles_on_mesh", args.mesh_frames > 0, lambda: measure_mesh(args, dev)),
                          ("pile_1m", args.pile_frames > 0, lambda: measure_pile(args, dev)),
                          ("batched", args.batched_scenes > 0, lambda: measure_batched(args, dev)),
                          ("diff", args.diff_frames > 0, lambda: measure_diff(args, dev))):
@@ -496,6 +505,46 @@ def measure_mesh(args, dev):
                    "d2h_bytes_per_step": int(d2h)}}
     if args.cache_frames > 0:
         out["frame_cache"] = measure_cache(args, s, sc)
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_sample(sc, x_snap, v_snap, budget_s=args.cpu_budget / 3)
+    return out
+
+
+def measure_small_pile(args, dev):
+    """The reference's own CPU-runnable case: the 4,096-particle pile (16^3 lattice, r 0.01 m,
+    spacing 0.02 m, jitter +/-0.002 m, seed 42, plane + particle contacts), 120 frames of 10
+    substeps from the initial state, on the GPU (device-timed, one graph per frame; at this
+    size the step is launch-bound) and on the oracle (all host threads)."""
+    import torch
+
+    import oracle as O
+    import scenes
+    from helpers import config_for, make_pair
+
+    sc = scenes.pile()
+    frames = 120
+    s, _ = make_solver(sc, device_index=dev.index)
+    for _ in range(args.warmup):  # graph capture and sort tuning, then back to the initial state
+        s.step(DT, SUBSTEPS, ITERATIONS)
+    s.set_particles(sc.positions, sc.velocities)
+    stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
+    torch.cuda.synchronize(dev)
+    dev_s = timed_frames(s, stream, frames) * 1e-3
+    work = sc.n * SUBSTEPS * frames
+    out = {"workload": "pile_4k", "particles": sc.n, "frames": frames, "value": work / dev_s, "unit": UNIT,
+           "ms_per_frame": dev_s / frames * 1e3}
+    if not args.no_cpu_baseline:
+        O.load("f32").or_set_threads(os.cpu_count() or 1)
+        _, orc = make_pair(sc, config_for(sc, gpu=False), gpu=False)
+        t0 = time.perf_counter()
+        done = 0
+        while done < frames and time.perf_counter() - t0 < args.cpu_budget / 3:
+            orc.step(DT, SUBSTEPS, ITERATIONS)
+            done += 1
+        t = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sc.n * SUBSTEPS * done / t, "unit": UNIT,
+                               "cores": int(O.load("f32").or_get_threads()), "kind": "port",
+                               "sample": f"{done} frames of 10 substeps from the initial state ({t:.1f} s)"}
     return out
 
 
@@ -576,6 +625,22 @@ def measure_batched(args, dev):
     wall_p = time.perf_counter() - t0
     launches_p = sum(s.get_frame_stats()["kernels_per_frame"] for s in plain)
     del plain
+    cpu = None
+    if not args.no_cpu_baseline:  # the oracle stepping every 32nd scene in turn, one frame each
+        import oracle as O
+        from helpers import config_for, make_pair
+
+        O.load("f32").or_set_threads(os.cpu_count() or 1)
+        sample = batch.scenes[::32]
+        orcs = [make_pair(sc, config_for(sc, gpu=False), gpu=False)[1] for sc in sample]
+        t0 = time.perf_counter()
+        for orc in orcs:
+            orc.step(DT, SUBSTEPS, ITERATIONS)
+        t = time.perf_counter() - t0
+        n_s = sum(sc.n for sc in sample)
+        cpu = {"value": n_s * SUBSTEPS / t, "unit": UNIT, "cores": int(O.load("f32").or_get_threads()),
+               "kind": "port", "sample": f"one frame of every 32nd scene ({len(sample)} scenes, {n_s} particles, "
+                                         f"their boxes) stepped one scene after another ({t:.1f} s)"}
     return {"workload": "batched_piles", "scenes": len(batch.scenes), "particles": batch.n, "boxes": n_boxes,
             "counts": "log-uniform 1024-65536, seed 46", "frames": frames, "warmup": args.warmup,
             "batched_value": work / dev_b, "batched_wall_value": work / wall_b, "plain_value": work / wall_p,
@@ -585,6 +650,7 @@ def measure_batched(args, dev):
                               "peak": peak, "unit": "GB/s", "frac": round(step_gbs / peak, 4),
                               "peak_source": peak_kind},
             "stages": stage_table(stage_ms, prof_substeps, batch.n, peak),
+            "cpu_baseline": cpu,
             "note": "batched_value device-timed (CUDA events); *_wall_value and plain_value host wall clock "
                     "around stepping; batched_over_pile_1m = batched_value / the pile_1m value"}
 
@@ -601,6 +667,8 @@ def measure_pile(args, dev):
 
     sc = scenes.pile(dims=(128, 128, 64), name="pile_1m")
     s, _ = make_solver(sc, device_index=dev.index)
+    if args.pile_solve_form >= 0:  # a fixed solve-kernel form instead of the solver's timed choice
+        s.set_solve_form(args.pile_solve_form)
     for _ in range(args.pile_preroll + args.warmup):
         s.step(DT, SUBSTEPS, ITERATIONS)
     stream = torch.cuda.ExternalStream(s.cuda_stream, device=dev)
@@ -774,8 +842,11 @@ def main():
     ap.add_argument("--cache-frames", type=int, default=50, help="0 skips the frame-cache measurement")
     ap.add_argument("--diff-reps", type=int, default=3)
     ap.add_argument("--pile-frames", type=int, default=10, help="0 skips the 1M-particle plain pile measurement")
+    ap.add_argument("--no-small-pile", dest="small_pile", action="store_false",
+                    help="skip the 4,096-particle pile (the reference's CPU-runnable case)")
     ap.add_argument("--pile-preroll", type=int, default=20)
-    ap.add_argument("--only", default="", help="comma list of parts to run alone: mesh,batched,diff,pile")
+    ap.add_argument("--pile-solve-form", type=int, default=-1, help="fix the 1M pile's solve form (-1: timed choice)")
+    ap.add_argument("--only", default="", help="comma list of parts to run alone: mesh,batched,diff,pile,pile4k")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -541,20 +541,45 @@ __device__ __forceinline__ void posed_candidates(const MeshTables& mt, const Rig
     }
 }
 
-constexpr int kPosedCand = 3;
+constexpr int kPosedCand = kPosedListWords - 1;  // candidates a list entry carries
 constexpr int kPosedWarps = 4;
-constexpr uint32_t kPosedMore = 0x80000000u;  // list entry: the particle has more than kPosedCand candidates
+// list entry: word 0 = particle | (listed candidates << 28) | kPosedMore, words 1.. = the
+// candidate meshes in candidate order (-1 past the count)
+constexpr uint32_t kPosedMore = 0x80000000u;  // the particle has more than kPosedCand candidates
+constexpr uint32_t kPosedIndex = 0x0fffffffu;
+struct PosedEntry {
+    uint32_t w[kPosedListWords];
+};
+__device__ __forceinline__ PosedEntry load_entry(const uint32_t* list, int64_t t) {
+    PosedEntry e;
+    const uint4* src = reinterpret_cast<const uint4*>(list + (size_t)t * kPosedListWords);
+#pragma unroll
+    for (int j = 0; j < kPosedListWords / 4; j++) {
+        const uint4 q = src[j];
+        e.w[4 * j] = q.x;
+        e.w[4 * j + 1] = q.y;
+        e.w[4 * j + 2] = q.z;
+        e.w[4 * j + 3] = q.w;
+    }
+    return e;
+}
+// the number of candidates a list entry holds (kPosedCand + 1: more follow)
+__device__ __forceinline__ int posed_listed(const PosedEntry& e) {
+    return (e.w[0] & kPosedMore) ? kPosedCand + 1 : (int)((e.w[0] >> 28) & 7u);
+}
 
 // Triage (one thread per particle, in the previous substep's grid order): particles with
 // at least one candidate moving mesh go to the posed list, in grid order within a warp,
-// each with its first kPosedCand candidate meshes (-1 past its count).
+// each with its first kPosedCand candidate meshes.
 __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t* __restrict__ order,
                                                       const float4* __restrict__ x, const float* __restrict__ r,
                                                       const int* __restrict__ flags, MeshTables mt, RigidTables rt,
                                                       uint32_t* counter, uint32_t* list) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    int c[kPosedCand] = {-1, -1, -1};
+    int c[kPosedCand];
+#pragma unroll
+    for (int j = 0; j < kPosedCand; j++) c[j] = -1;
     int nc = 0;
     int64_t i = -1;
     if (t < n) {
@@ -572,10 +597,15 @@ __global__ void __launch_bounds__(128) k_posed_triage(int64_t n, const uint32_t*
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (any)
-            reinterpret_cast<uint4*>(list)[base + __popc(m & lanemask_lt())] =
-                make_uint4((uint32_t)i | (nc > kPosedCand ? kPosedMore : 0u), (uint32_t)c[0], (uint32_t)c[1],
-                           (uint32_t)c[2]);
+        if (any) {
+            uint32_t w[kPosedListWords];
+            w[0] = (uint32_t)i | ((uint32_t)min(nc, kPosedCand) << 28) | (nc > kPosedCand ? kPosedMore : 0u);
+#pragma unroll
+            for (int j = 0; j < kPosedCand; j++) w[j + 1] = (uint32_t)c[j];
+            uint4* dst = reinterpret_cast<uint4*>(list + (size_t)(base + __popc(m & lanemask_lt())) * kPosedListWords);
+#pragma unroll
+            for (int j = 0; j < kPosedListWords / 4; j++) dst[j] = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+        }
     }
 }
 
@@ -610,10 +640,6 @@ __device__ __forceinline__ void posed_insert(float4* base, int& used, int slot_c
     used++;
 }
 
-// the number of candidates a list entry holds (kPosedCand + 1: more follow)
-__device__ __forceinline__ int posed_listed(const uint4& e) {
-    return (e.x & kPosedMore) ? kPosedCand + 1 : (e.w != 0xffffffffu ? 3 : e.z != 0xffffffffu ? 2 : 1);
-}
 
 __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ counter, const float4* __restrict__ x,
@@ -632,14 +658,12 @@ __global__ void __launch_bounds__(32 * kPosedWarps, 6) k_collide_posed(
         uint32_t own = 0;
         float4 po = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (t < listed) {
-            const uint4 e = reinterpret_cast<const uint4*>(list)[t];
-            const int64_t i = (int64_t)(e.x & ~kPosedMore);
+            const PosedEntry e = load_entry(list, t);
+            const int64_t i = (int64_t)(e.w[0] & kPosedIndex);
             const float4 xi = x[i];
             po = make_float4(xi.x, xi.y, xi.z, r[i]);
-            s_cand[warp][lane][0] = (int)e.y;
-            s_cand[warp][lane][1] = (int)e.z;
-            s_cand[warp][lane][2] = (int)e.w;
             own = (uint32_t)min(posed_listed(e), kPosedCand);
+            for (uint32_t j = 0; j < own; j++) s_cand[warp][lane][j] = (int)e.w[j + 1];
         }
         s_pos[warp][lane] = po;
         uint32_t incl = own;
@@ -702,16 +726,16 @@ __global__ void __launch_bounds__(128) k_posed_merge(const uint32_t* __restrict_
     uint32_t added = 0;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < listed; t += stride) {
         int used0 = 0, used = 0;
-        const uint4 e = reinterpret_cast<const uint4*>(list)[t];
-        const int64_t i = (int64_t)(e.x & ~kPosedMore);
+        const PosedEntry e = load_entry(list, t);
+        const int64_t i = (int64_t)(e.w[0] & kPosedIndex);
         const int ncand = posed_listed(e);
-        const int cand[kPosedCand] = {(int)e.y, (int)e.z, (int)e.w};
         const uint32_t info = cinfo[i];
         used0 = used = info_slots(info);
         float4* base = cslot + (size_t)i * slot_cap * 3;
         for (int k = 0; k < min(ncand, kPosedCand); k++) {
             const PosedHit h = hits[(size_t)t * kPosedCand + k];
-            if (h.a.w != 0.0f) posed_insert(base, used, slot_cap, slot_ovf, cand[k], xyz(h.a), xyz(h.b), xyz(h.c));
+            if (h.a.w != 0.0f)
+                posed_insert(base, used, slot_cap, slot_ovf, (int)e.w[k + 1], xyz(h.a), xyz(h.b), xyz(h.c));
         }
         if (ncand > kPosedCand) {  // the rest, in candidate order
             const v3 p = xyz(x[i]);

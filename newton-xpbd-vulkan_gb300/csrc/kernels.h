@@ -323,11 +323,12 @@ void launch_rigid_contacts(cudaStream_t s, BodyArrays ba, RigidTables rt, MeshTa
                            DeviceStatus* st);
 // particle contacts against the meshes of dynamic bodies in three launches: the triage
 // (reads `order`; lists the particles near a moving mesh with their first candidates:
-// counter = one zeroed word, list = 4 words per particle), the queries of the listed
-// candidates (results to `hits`, kPosedHitWords float4 per particle; no slot is touched,
-// so they may run beside the static-mesh traversal), and the merge of the hits
-// into the slots in mesh order after that traversal
-constexpr int kPosedHitWords = 9;  // float4 per list entry in `hits`
+// counter = one zeroed word, list = kPosedListWords words per particle), the queries of the
+// listed candidates (results to `hits`, kPosedHitWords float4 per particle; no slot is
+// touched, so they may run beside the static-mesh traversal), and the merge of the hits
+// into the slots in mesh order after that traversal. Particle indices below 2^28.
+constexpr int kPosedListWords = 8;                        // the particle and 7 candidates
+constexpr int kPosedHitWords = 3 * (kPosedListWords - 1);  // float4 per list entry in `hits`
 void launch_posed_triage(cudaStream_t s, int64_t n, const uint32_t* order, const float4* x, const float* r,
                          const int* flags, MeshTables mt, RigidTables rt, uint32_t* counter, uint32_t* list);
 void launch_posed_queries(cudaStream_t s, int64_t n, const float4* x, const float* r, MeshTables mt, RigidTables rt,

@@ -799,7 +799,8 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     grid_tiles_.alloc((size_t)grid_size_ / 1024 + 1, true);
     if (grid_size_ > 4096 * 1024) throw std::runtime_error("too many dynamic bodies for the box grid");
     grid_list_.alloc(std::max<size_t>(dyn_list_.size() * kBoxCells, 1), true);
-    posed_list_.alloc(std::max<size_t>(n_, 1) * 4, false);
+    if (n_ >= ((size_t)1 << 28)) throw std::runtime_error("dynamic bodies need fewer than 2^28 particles");
+    posed_list_.alloc(std::max<size_t>(n_, 1) * kPosedListWords, false);
     posed_hits_.alloc(std::max<size_t>(n_, 1) * kPosedHitWords, false);
     up(dyn_, dyn_list_);
     up(dyn_index_, dyn_index);

@@ -323,7 +323,7 @@ class Solver {
     float dyn_half_diag_ = 0.0f, dyn_max_margin_ = 0.0f;
     DevBuf<uint32_t> grid_count_, grid_start_, grid_tiles_;
     DevBuf<int4> grid_list_;
-    DevBuf<uint32_t> posed_list_;  // per substep: (particle, its first three candidate moving meshes) entries
+    DevBuf<uint32_t> posed_list_;  // per substep: (particle, its first candidate moving meshes) entries
     DevBuf<float4> posed_hits_;    // per list entry: the query results of its listed candidates
     std::vector<int32_t> body_scene_;  // batched: scene of each body (-1: every scene)
     DevBuf<int> dyn_scene_;            // scene of each dynamic body (dyn index)
