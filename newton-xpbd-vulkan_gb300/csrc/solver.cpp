@@ -361,6 +361,7 @@ void Solver::add_mesh(const float* verts, size_t num_verts, const uint32_t* tris
 void Solver::finalize_meshes() {
     if (!initialized_) throw std::runtime_error("XpbdSolver::init must be called before finalize_meshes");
     XPBD_CUDA(cudaSetDevice(device_));
+    dyn_tables_ready_ = false;
     const size_t nm = meshes_.size(), nshapes = 1 + nm;
     // shapes: 0 = plane (body -1), c+1 = mesh c (body c); all bodies static (scene.cpp:206-247)
     std::vector<int> sb(nshapes);
@@ -543,6 +544,7 @@ void Solver::update_mesh(size_t mi, const float* verts, size_t num_verts, const 
     else
         std::fill(all_vels_.begin() + vs * 3, all_vels_.begin() + (vs + num_verts) * 3, 0.0f);
     std::copy(verts, verts + num_verts * 3, m.vertices.begin());
+    dyn_tables_ready_ = false;  // a dynamic mesh's extent sizes the box grid: the next set_bodies rebuilds
     // upload this mesh's vertices, then refit its BVH on the GPU (topology unchanged,
     // scene.cpp:657-695 refits on the host and re-uploads every node)
     const size_t nb = node_offsets_[mi], pb = prim_offsets_[mi], nt = m.indices.size() / 3;
@@ -743,17 +745,22 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     XPBD_CUDA(cudaMemcpy(body_flags_.p, hfl.data(), nb * 4, cudaMemcpyHostToDevice));
 
     // dynamic bodies: inverse mass > 0; their meshes are in the body frame
-    dyn_list_.clear();
-    std::vector<int> dyn_index(nb, -1), posed(nb, 0), walk;
+    std::vector<int> dyn_list, dyn_index(nb, -1), posed(nb, 0), walk;
     for (size_t b = 0; b < nb; b++) {
         if (hinvm[b] > 0.0f) {
-            dyn_index[b] = (int)dyn_list_.size();
-            dyn_list_.push_back((int)b);
+            dyn_index[b] = (int)dyn_list.size();
+            dyn_list.push_back((int)b);
             posed[b] = 1;
         } else {
             walk.push_back((int)b);
         }
     }
+    // the same dynamic bodies as before over unchanged meshes (a new state of the same
+    // scene): the tables, their buffers and the captured graphs stay; only the body arrays
+    // above change, and the graphs read them from device memory
+    if (dyn_tables_ready_ && dyn_list == dyn_list_) return;
+    dyn_list_ = dyn_list;
+    dyn_tables_ready_ = false;
     dyn_any_ = !dyn_list_.empty();
     clear_graphs();
     if (!dyn_any_) return;
@@ -839,6 +846,7 @@ void Solver::set_bodies(const float* q, const float* qd, const float* com, const
     dyn_rank_.alloc(std::max<size_t>(n_, 1), false);
     dyn_totals_.alloc(2, true);
     dyn_ws_.alloc(contact_scan_words((int64_t)n_), true);
+    dyn_tables_ready_ = true;
 }
 
 void Solver::get_bodies(float* q, float* qd, size_t nb) {

@@ -315,6 +315,7 @@ class Solver {
     // dynamic bodies
     DevBuf<float> body_I_;
     bool dyn_any_ = false;
+    bool dyn_tables_ready_ = false;  // the dynamic-body tables match dyn_list_ and the meshes
     std::vector<int> dyn_list_;
     xpbd_body_params body_params_{0.0f, 0.01f, 0.8f, 1, 0.0f, 0.0f, 1};
     DevBuf<float4> body_q_mid_, body_qd_mid_, body_q_prev_, body_qd_prev_;

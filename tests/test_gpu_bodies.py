@@ -144,3 +144,39 @@ def test_dynamic_mesh_larger_than_a_box_bitexact():
     nbod.inv_mass[nb - 1] = 1.0 / m
     sc.bodies = nbod
     _run(sc, 25)
+
+
+def test_set_bodies_state_in_place_and_dynamic_set_change_bitexact():
+    """set_bodies with the same dynamic bodies (a new state of the same scene, as a driver
+    restoring a frame does every step) uploads the state in place and keeps the tables and
+    graphs; a change of which bodies are dynamic rebuilds them. Both stay bit-exact."""
+    sc = box_scene(n_side=6, boxes=((0.05, 0.04, 0.03), (0.04, 0.03, 0.03)),
+                   positions=((0.0, 0.0, 0.15), (0.12, 0.02, 0.2)))
+    cfg = config_for(sc)
+    g, orc = make_pair(sc, cfg)
+    dt = 1.0 / 60.0
+
+    def both(frames, what):
+        for f in range(frames):
+            g.step(dt, 10, 1)
+            orc.step(dt, 10, 1)
+            assert_bitexact(g.get_body_q(), orc.get_body_q(), f"{what} body q frame {f}")
+            assert_bitexact(g.get_positions(), orc.get_positions(), f"{what} positions frame {f}")
+
+    both(4, "start")
+    q, qd = orc.get_body_q(), orc.get_body_qd()
+    x, v = orc.get_positions(), orc.get_velocities()
+    for _ in range(3):  # restore the same state, step, restore: the in-place path every time
+        g.set_particles(x, v)
+        g.set_bodies(q, qd)
+        g.step(dt, 10, 1)
+    g.set_particles(x, v)
+    g.set_bodies(q, qd)
+    orc.set_particles(x, v)
+    orc.set_bodies(q, qd)
+    both(3, "restored")
+    inv_mass = np.array(sc.bodies.inv_mass, np.float32).copy()
+    inv_mass[-1] = 0.0  # the second box becomes static: the tables are rebuilt
+    g.set_bodies(inv_mass=inv_mass)
+    orc.set_bodies(inv_mass=inv_mass)
+    both(3, "one box static")
