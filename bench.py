@@ -396,6 +396,9 @@ def run_gpu(args):
     for _ in range(args.warmup):
         flush()
         solver.step(DT, SUBSTEPS, ITERATIONS)
+    # the timed frames start here; the end-to-end pass below steps the same frames again
+    x_t0, v_t0 = solver.get_positions(), solver.get_velocities()
+    q_t0, qd_t0 = solver.get_body_q(), solver.get_body_qd()
     clocks = ClockSampler(local)
     barrier(world)
     torch.cuda.synchronize(dev)
@@ -414,8 +417,9 @@ def run_gpu(args):
     roofline, roofline_step = roofline_of("mixed", stage_ms, prof_substeps, sc.n, dev_ms / args.steps, peak,
                                           peak_kind)
 
-    # end to end through the public API with host buffers: set_particles + set_bodies -> step -> readback
-    e2e_s, h2d, d2h = e2e_frames(solver, args.steps, x_snap, v_snap, q_snap, qd_snap, flush,
+    # end to end through the public API with host buffers: set_particles + set_bodies -> step -> readback,
+    # from the state the timed frames started from, so both cover the same frames
+    e2e_s, h2d, d2h = e2e_frames(solver, args.steps, x_t0, v_t0, q_t0, qd_t0, flush,
                                  lambda: torch.cuda.synchronize(dev))
     e2e_s = reduce_max(e2e_s, world)
     e2e = {"value": particle_substeps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -488,6 +492,7 @@ def measure_mesh(args, dev):
     for _ in range(args.warmup):
         flush()
         s.step(DT, SUBSTEPS, ITERATIONS)
+    x_t0, v_t0 = s.get_positions(), s.get_velocities()  # where the timed frames (and the e2e pass) start
     frames = args.mesh_frames
     torch.cuda.synchronize(dev)
     dev_ms = timed_frames(s, stream, frames, flush)
@@ -495,7 +500,7 @@ def measure_mesh(args, dev):
     peak, peak_kind = measured_peak_hbm()
     roofline, roofline_step = roofline_of("particles_on_mesh", stage_ms, prof_substeps, sc.n, dev_ms / frames,
                                           peak, peak_kind)
-    e2e_s, h2d, d2h = e2e_frames(s, frames, x_snap, v_snap, flush=flush, sync=lambda: torch.cuda.synchronize(dev))
+    e2e_s, h2d, d2h = e2e_frames(s, frames, x_t0, v_t0, flush=flush, sync=lambda: torch.cuda.synchronize(dev))
     work = sc.n * SUBSTEPS * frames
     out = {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
            "preroll_frames": args.mesh_preroll, "frames": frames, "value": work / (dev_ms * 1e-3), "unit": UNIT,
