@@ -244,11 +244,13 @@ int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread);
  * reports the form in use (-1 while timing). */
 int xpbd_set_solve_split(xpbd_solver* s, int mode);
 int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
-/* Form of the solve kernel (no counterpart in the reference; results are identical either
- * way): 0 = each thread computes the pair terms of its own particle's neighbours, 1 = the
+/* Form of the solve kernel (no counterpart in the reference; results are identical in every
+ * form): 0 = each thread computes the pair terms of its own particle's neighbours, 1 = the
  * lanes of a warp compute their neighbours' pair terms together (balanced when neighbour
- * counts differ), -1 (default) = a solver of 16,384 particles or more times both on its own
- * last substep after its first frame and again every 16 frames, and keeps the faster.
+ * counts differ), 2 = as 0 with each block's neighbourhood records staged in shared memory
+ * (one scene only; slower on the benchmark scenes, so never chosen by the timing), -1
+ * (default) = a solver of 16,384 particles or more times forms 0 and 1 on its own last
+ * substep after its first frame and again every 16 frames, and keeps the faster.
  * xpbd_get_solve_form reports the form in use. */
 int xpbd_set_solve_form(xpbd_solver* s, int form);
 int xpbd_get_solve_form(const xpbd_solver* s, int* form);

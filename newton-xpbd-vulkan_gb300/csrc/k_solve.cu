@@ -10,6 +10,7 @@
 // mesh slots, then the particle-particle total), which makes the step
 // deterministic and needs no delta buffer, no fill and no atomics.
 #include <stdexcept>
+#include <type_traits>
 
 #include "contact.cuh"
 #include "kernels.h"
@@ -23,7 +24,43 @@ constexpr int kCoopCap = 12;  // accepted neighbours buffered per lane for the w
 // How a solve kernel computes the particle-particle totals (the solver times both on its scene
 // and keeps the faster; the results are the same bits): each thread its own neighbours' pair
 // terms, or the warp's pair pass
-enum { kFormThread = 0, kFormWarp = 1 };
+enum { kFormThread = 0, kFormWarp = 1, kFormStaged = 2 };
+
+// Shared staging of a block's neighbourhood (the staged form): the sorted records of every
+// (y, z) row of cells the block's particles reach, copied once; the per-cell bounds of those
+// rows; and each row's first sorted slot and offset in the staged copy. A block stages when
+// its particles reach at most 3 x 3 rows, kStageX cells along x without a wrap of the
+// 128-cell grid (so each row's cells hold one run of the sorted order), and kStageCap
+// records in all; otherwise its threads read the records from global memory as in form 0.
+constexpr int kStageX = 40;
+constexpr int kStageRows = 9;
+constexpr int kStageCap = 512;
+struct SolveStage {
+    float4 rx[kStageCap];
+    int cs[kStageRows][kStageX];  // cell start in the sorted order, -1: no particle this substep
+    int ce[kStageRows][kStageX];  // cell end
+    int lo[kStageRows];           // the row's first sorted slot
+    int off[kStageRows];          // its first record in rx
+    int len[kStageRows];
+    int box[6];                   // block's cell range: x min, x max, y min, y max, z min, z max
+    int ok;
+};
+// the cells a particle at xp (radius) reaches (solve_particle_particle_contacts.comp:119-131)
+struct CellRange {
+    int32_t xs, xe, ys, ye, zs, ze;
+};
+__device__ __forceinline__ CellRange cell_range(v3 xp, float radius, const SolveParams& sp) {
+    const float R = radius + sp.max_radius + sp.k_coh;
+    const float inv = sp.inv;
+    CellRange c;
+    c.xs = f2i(floorf((xp.x - R) * inv));
+    c.ys = f2i(floorf((xp.y - R) * inv));
+    c.zs = f2i(floorf((xp.z - R) * inv));
+    c.xe = min(f2i(floorf((xp.x + R) * inv)), c.xs + kGridDim - 1);
+    c.ye = min(f2i(floorf((xp.y + R) * inv)), c.ys + kGridDim - 1);
+    c.ze = min(f2i(floorf((xp.z + R) * inv)), c.zs + kGridDim - 1);
+    return c;
+}
 
 // Pair term of solve_particle_particle_contacts.comp:153-177 for a candidate the filter kept
 // at squared distance sq (exact_length's sum): the refined distance, the neighbour test
@@ -127,15 +164,11 @@ template <bool ALL_ACTIVE, class F>
 __device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float radius, const float4* __restrict__ rx,
                                           const float4* __restrict__ rv, const int* __restrict__ rf,
                                           const int4* __restrict__ table, bool split, uint32_t stamp,
-                                          const SolveParams& sp, F&& accept) {
+                                          const SolveParams& sp, F&& accept, const SolveStage* st = nullptr) {
     const int is_proxy = pflag & 2;
     const float R = radius + sp.max_radius + sp.k_coh;
-    const float inv = sp.inv;
-    const int32_t xs = f2i(floorf((xp.x - R) * inv)), ys = f2i(floorf((xp.y - R) * inv)),
-                  zs = f2i(floorf((xp.z - R) * inv));
-    const int32_t xe = min(f2i(floorf((xp.x + R) * inv)), xs + kGridDim - 1);
-    const int32_t ye = min(f2i(floorf((xp.y + R) * inv)), ys + kGridDim - 1);
-    const int32_t ze = min(f2i(floorf((xp.z + R) * inv)), zs + kGridDim - 1);
+    const CellRange cr = cell_range(xp, radius, sp);
+    const int32_t xs = cr.xs, ys = cr.ys, zs = cr.zs, xe = cr.xe, ye = cr.ye, ze = cr.ze;
     // cells xs..xe of one (cy, cz) row have consecutive keys unless the row wraps at 128
     // or is clamped at 0 (then the alias bit of x is the same for the whole row); their
     // particles then form one run of the sorted order, in the reference's visit order (x
@@ -146,7 +179,23 @@ __device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float rad
         for (int32_t cy = ys; cy <= ye; cy++) {
             for (int32_t cx = xs; cx <= xe; cx++) {
                 int lo, hi;
-                if (row_run) {
+                const float4* src = rx;  // where candidate kk's record is read: rx[kk], or the stage
+                if (st) {
+                    // the block staged this row (its range covers every thread's rows and cells)
+                    const int ny = st->box[3] - st->box[2] + 1;
+                    const int r = (cz - st->box[4]) * ny + (cy - st->box[2]);
+                    lo = 0x7fffffff;
+                    hi = -1;
+                    for (int32_t x = xs; x <= xe; x++) {
+                        const int c0 = st->cs[r][x - st->box[0]];
+                        if (c0 >= 0) {
+                            lo = min(lo, c0);
+                            hi = max(hi, st->ce[r][x - st->box[0]]);
+                        }
+                    }
+                    src = st->rx + (st->off[r] - st->lo[r]);
+                    cx = xe;  // the run covers the whole row
+                } else if (row_run) {
                     const int c0 = cell_index(xs, cy, cz, split);
                     lo = 0x7fffffff;
                     hi = -1;
@@ -171,7 +220,8 @@ __device__ __forceinline__ void pp_filter(int64_t k, int pflag, v3 xp, float rad
                     float4 nxs[2];
 #pragma unroll
                     for (int u = 0; u < 2; u++)
-                        nxs[u] = kk0 + u < hi ? __ldg(&rx[kk0 + u]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        nxs[u] = kk0 + u < hi ? (st ? src[kk0 + u] : __ldg(&rx[kk0 + u]))
+                                              : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
                         const int kk = kk0 + u;
@@ -208,17 +258,21 @@ __device__ __forceinline__ v3 pp_total(int64_t k, int pflag, v3 xp, v3 vp, float
                                        const int* __restrict__ rf, const int4* __restrict__ table, bool split,
                                        uint32_t stamp,
                                        const uint32_t* __restrict__ sids, const SolveParams& sp, const SolveDiag& dg,
-                                       int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads]) {
+                                       int (*s_kk)[kSolveThreads], float (*s_d)[kSolveThreads],
+                                       const SolveStage* st = nullptr) {
     v3 acc = mk3(0.0f, 0.0f, 0.0f);
     int np = 0;
-    pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float sq) {
-        s_kk[np][threadIdx.x] = kk;
-        s_d[np][threadIdx.x] = sq;
-        if (++np == kPairCap) {
-            pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
-            np = 0;
-        }
-    });
+    pp_filter<ALL_ACTIVE>(
+        k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp,
+        [&](int kk, float sq) {
+            s_kk[np][threadIdx.x] = kk;
+            s_d[np][threadIdx.x] = sq;
+            if (++np == kPairCap) {
+                pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
+                np = 0;
+            }
+        },
+        st);
     pair_block<DIAG>(np, s_kk, s_d, rx, rv, sids, xp, vp, radius, w1, id, sp, dg, acc);
     const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
     return mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f), __fmaf_rn(dw.z, sp.relax, 0.0f));
@@ -310,6 +364,68 @@ __device__ __forceinline__ v3 pp_total_warp(bool active, int64_t k, int pflag, v
 // total to the shape deltas in the same order.
 enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
 
+// The staged form's block setup (every thread of the block calls it; `active` = this thread
+// filters neighbours): the block's cell range, then, when it qualifies, the cell bounds of its
+// rows and their sorted records in shared memory. Returns whether the block staged (the same
+// for all its threads).
+__device__ __forceinline__ bool stage_block(SolveStage& st, bool active, v3 xp, float radius, const SolveParams& sp,
+                                            const float4* __restrict__ rx, const int4* __restrict__ table, bool split,
+                                            uint32_t stamp) {
+    const int tid = threadIdx.x;
+    if (tid < 6) st.box[tid] = (tid & 1) ? (int)0x80000000 : 0x7fffffff;
+    __syncthreads();
+    if (active) {
+        const CellRange c = cell_range(xp, radius, sp);
+        atomicMin(&st.box[0], c.xs);
+        atomicMax(&st.box[1], c.xe);
+        atomicMin(&st.box[2], c.ys);
+        atomicMax(&st.box[3], c.ye);
+        atomicMin(&st.box[4], c.zs);
+        atomicMax(&st.box[5], c.ze);
+    }
+    __syncthreads();
+    const int x0 = st.box[0], x1 = st.box[1], y0 = st.box[2], y1 = st.box[3], z0 = st.box[4], z1 = st.box[5];
+    const int xo = x0 + kGridOrigin;
+    // no thread filters, more than 3 x 3 rows, rows too long or wrapping: no staging
+    if (x0 > x1 || y1 - y0 > 2 || z1 - z0 > 2 || x1 - x0 >= kStageX || xo < 0 || (xo % kGridDim) + (x1 - x0) >= kGridDim)
+        return false;
+    const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, rows = ny * (z1 - z0 + 1);
+    for (int c = tid; c < rows * nx; c += kSolveThreads) {
+        const int r = c / nx, x = c - r * nx;
+        const int4 e = __ldg(&table[cell_index(x0 + x, y0 + r % ny, z0 + r / ny, split)]);
+        const bool live = (uint32_t)e.z == stamp;
+        st.cs[r][x] = live ? e.x : -1;
+        st.ce[r][x] = live ? e.y : -1;
+    }
+    __syncthreads();
+    if (tid < rows) {
+        int lo = 0x7fffffff, hi = -1;
+        for (int x = 0; x < nx; x++) {
+            if (st.cs[tid][x] >= 0) {
+                lo = min(lo, st.cs[tid][x]);
+                hi = max(hi, st.ce[tid][x]);
+            }
+        }
+        st.lo[tid] = hi > lo ? lo : 0;
+        st.len[tid] = hi > lo ? hi - lo : 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int off = 0;
+        for (int r = 0; r < rows; r++) {
+            st.off[r] = off;
+            off += st.len[r];
+        }
+        st.ok = off <= kStageCap;
+    }
+    __syncthreads();
+    if (!st.ok) return false;
+    for (int r = 0; r < rows; r++)
+        for (int i = tid; i < st.len[r]; i += kSolveThreads) st.rx[st.off[r] + i] = __ldg(&rx[st.lo[r] + i]);
+    __syncthreads();
+    return true;
+}
+
 template <bool LAST, bool ALL_ACTIVE, bool DIAG, int PP, int FORM>
 __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     int64_t n, const uint32_t* __restrict__ sids, const uint32_t* __restrict__ skeys, const float4* __restrict__ rx,
@@ -322,12 +438,15 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     // the warp's pair pass (pp_total_warp) computes the particle-particle totals; the
     // diagnostic kernels keep the per-thread form, which records every pair as it is summed
     constexpr bool WARP = FORM == kFormWarp && !DIAG && PP != kPPApply;
+    // the staged form: the block's neighbourhood records in shared memory (SolveStage)
+    constexpr bool STAGED = FORM == kFormStaged && !DIAG && PP != kPPApply;
     __shared__ int s_kk[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
     __shared__ float s_d[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
     __shared__ WarpPairs s_wp[WARP ? kSolveThreads / 32 : 1];
+    __shared__ typename std::conditional<STAGED, SolveStage, char>::type s_stage;
     const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (!WARP && k0 >= n) return;
-    const bool valid = k0 < n;  // every lane of a warp reaches the warp's pair pass
+    if (!WARP && !STAGED && k0 >= n) return;
+    const bool valid = k0 < n;  // every lane of a warp reaches the warp's pair pass (every thread the staging)
     const int64_t k = valid ? k0 : n - 1;
     const uint32_t id = sids[k];
     const float4 ox = rx[k], ov = rv[k];
@@ -335,6 +454,14 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     const v3 xp = xyz(ox), vp = xyz(ov);
     const float radius = ox.w, w1 = ov.w;
     v3 total = mk3(0.0f, 0.0f, 0.0f);
+    const SolveStage* stage = nullptr;
+    if constexpr (STAGED) {
+        // one scene only (scene-major keys index per-scene tables)
+        if (!skeys && stage_block(s_stage, valid && (pflag & 1) != 0, xp, radius, sp, rx, table_all,
+                                  sp.split_keys != 0, *stamp_p))
+            stage = &s_stage;
+        if (!valid) return;
+    }
     if constexpr (WARP) {
         // this particle's scene table (scene-major keys); one scene: the whole table
         const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
@@ -347,7 +474,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
             if (pflag & 1) {
                 const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
                 total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table,
-                                                   sp.split_keys != 0, *stamp_p, sids, sp, dg, s_kk, s_d);
+                                                   sp.split_keys != 0, *stamp_p, sids, sp, dg, s_kk, s_d, stage);
             }
         }
         pp[k] = make_float4(total.x, total.y, total.z, 0.0f);
@@ -393,7 +520,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
             // this particle's scene table (scene-major keys); one scene: the whole table
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
             total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
-                                               *stamp_p, sids, sp, dg, s_kk, s_d);
+                                               *stamp_p, sids, sp, dg, s_kk, s_d, stage);
         }
         delta = vadd(delta, total);
         // apply_particle_deltas.comp:43-54
@@ -491,6 +618,10 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
     XPBD_SOLVE(true, false, false, kPPFused, kFormWarp)
     XPBD_SOLVE(false, true, false, kPPFused, kFormWarp)
     XPBD_SOLVE(false, false, false, kPPFused, kFormWarp)
+    XPBD_SOLVE(true, true, false, kPPFused, kFormStaged)
+    XPBD_SOLVE(true, false, false, kPPFused, kFormStaged)
+    XPBD_SOLVE(false, true, false, kPPFused, kFormStaged)
+    XPBD_SOLVE(false, false, false, kPPFused, kFormStaged)
     XPBD_SOLVE(true, true, true, kPPFused, kFormThread)
     XPBD_SOLVE(true, false, true, kPPFused, kFormThread)
     XPBD_SOLVE(false, true, true, kPPFused, kFormThread)
@@ -501,6 +632,8 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
     XPBD_SOLVE(false, false, false, kPPOnly, kFormThread)
     XPBD_SOLVE(false, true, false, kPPOnly, kFormWarp)
     XPBD_SOLVE(false, false, false, kPPOnly, kFormWarp)
+    XPBD_SOLVE(false, true, false, kPPOnly, kFormStaged)
+    XPBD_SOLVE(false, false, false, kPPOnly, kFormStaged)
     XPBD_SOLVE(true, true, false, kPPApply, kFormThread)
     XPBD_SOLVE(true, false, false, kPPApply, kFormThread)
     XPBD_SOLVE(false, true, false, kPPApply, kFormThread)

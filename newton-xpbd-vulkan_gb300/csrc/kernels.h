@@ -220,8 +220,12 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   BodyDeltaOut bo = BodyDeltaOut{nullptr, nullptr}, int pp_mode = 0, float4* pp = nullptr,
                   int form = 0);
 // forms of the solve kernel (launch_solve's `form`): 0 = each thread sums its own neighbours'
-// pair terms, 1 = the lanes of a warp compute their neighbours' pair terms together; same bits
-constexpr int kSolveForms = 2;
+// pair terms, 1 = the lanes of a warp compute their neighbours' pair terms together, 2 = as 0
+// with the block's neighbourhood records staged in shared memory; same bits
+constexpr int kSolveForms = 3;
+// the forms the solver times on its scene and chooses from (the staged form measured slower
+// on every benchmark scene: it stays selectable, and tested, but is not timed)
+constexpr int kSolveTimedForms = 2;
 // restitution (apply_particle_shape_restitution.comp) after the body passes of the last
 // iteration, in particle order on the final state the last iteration wrote (v_out)
 void launch_restitute(cudaStream_t s, int64_t n, const int* flags, const float* radii, const float4* x0,

@@ -261,7 +261,7 @@ void Solver::set_solve_split(int mode) {
 
 void Solver::set_solve_form(int form) {
     require_init();
-    if (form < -1 || form >= kSolveForms) throw std::runtime_error("set_solve_form: -1 (timed choice), 0 or 1");
+    if (form < -1 || form >= kSolveForms) throw std::runtime_error("set_solve_form: -1 (timed choice), 0, 1 or 2");
     sync();
     solve_form_forced_ = form;
     if (form >= 0) solve_form_ = form;
@@ -294,11 +294,11 @@ void Solver::autotune_solve() {
     // two timed rounds, forms in opposite orders (a drift cancels); the first timing of a
     // solver has a warm-up round before them (first launches load the kernels)
     constexpr int kReps = 2;
-    cudaEvent_t ev[2 * kSolveForms * kReps];
+    cudaEvent_t ev[2 * kSolveTimedForms * kReps];
     for (auto& e : ev) XPBD_CUDA(cudaEventCreate(&e));
     for (int rep = solve_form_timed_ ? 1 : 0; rep <= kReps; rep++) {
-        for (int k = 0; k < kSolveForms; k++) {
-            const int f = (rep & 1) ? k : kSolveForms - 1 - k;
+        for (int k = 0; k < kSolveTimedForms; k++) {
+            const int f = (rep & 1) ? k : kSolveTimedForms - 1 - k;
             cudaEvent_t* e = ev + 2 * (f * kReps + std::max(rep - 1, 0));
             if (rep) XPBD_CUDA(cudaEventRecord(e[0], stream_));
             launch_solve(stream_, (int64_t)n_, true, all_active_, sids, skeys, rx_[it & 1].p, rv_[it & 1].p, rf_.p,
@@ -309,8 +309,8 @@ void Solver::autotune_solve() {
     }
     XPBD_CUDA(cudaGetLastError());
     XPBD_CUDA(cudaStreamSynchronize(stream_));
-    double ms[kSolveForms] = {0.0};
-    for (int f = 0; f < kSolveForms; f++)
+    double ms[kSolveTimedForms] = {0.0};
+    for (int f = 0; f < kSolveTimedForms; f++)
         for (int r = 0; r < kReps; r++) {
             float t = 0.0f;
             XPBD_CUDA(cudaEventElapsedTime(&t, ev[2 * (f * kReps + r)], ev[2 * (f * kReps + r) + 1]));
@@ -318,7 +318,7 @@ void Solver::autotune_solve() {
         }
     for (auto& e : ev) cudaEventDestroy(e);
     int best = 0;
-    for (int f = 1; f < kSolveForms; f++)
+    for (int f = 1; f < kSolveTimedForms; f++)
         if (ms[f] < ms[best]) best = f;
     solve_form_ = best;
     solve_form_timed_ = true;

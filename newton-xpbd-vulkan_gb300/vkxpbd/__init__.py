@@ -233,8 +233,9 @@ class XpbdSolver:
         return int(v.value)
 
     def set_solve_form(self, form):
-        """Solve-kernel form: 0 per-thread pair terms, 1 warp pair pass, -1 (default) timed on
-        the scene's own substeps (xpbd_set_solve_form). Results are identical."""
+        """Solve-kernel form: 0 per-thread pair terms, 1 warp pair pass, 2 per-thread from a
+        block's neighbourhood staged in shared memory, -1 (default) 0 or 1 timed on the scene's
+        own substeps (xpbd_set_solve_form). Results are identical."""
         _check(_lib.xpbd_set_solve_form(self._h, int(form)))
 
     @property

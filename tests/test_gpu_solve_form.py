@@ -1,12 +1,14 @@
-"""The two forms of the solve kernel against each other and the oracle.
+"""The three forms of the solve kernel against each other and the oracle.
 
-The solve kernel computes each particle's particle-particle total either per thread (each
-thread the pair terms of its own neighbours) or per warp (the lanes filter their own
-candidates, then compute all buffered pair terms of the warp together and each lane adds its
-own in candidate order). Both sum the same terms in the same order, so solvers forced to
-either form, and one choosing by timing, must agree bit for bit with the oracle: inactive,
-proxy and kinematic particles with cohesion and adhesion over two iterations, a heightfield
-with the split first iteration, dynamic boxes, and batched scenes.
+The solve kernel computes each particle's particle-particle total per thread (each thread the
+pair terms of its own neighbours), per warp (the lanes filter their own candidates, then
+compute all buffered pair terms of the warp together and each lane adds its own in candidate
+order), or per thread from a block's neighbourhood records staged in shared memory. All sum
+the same terms in the same order, so solvers forced to any form, and one choosing by timing,
+must agree bit for bit with the oracle: inactive, proxy and kinematic particles with cohesion
+and adhesion over two iterations, a heightfield with the split first iteration, dynamic
+boxes, batched scenes (which the staged form leaves to the global path), and a pile large
+enough for split grid keys.
 """
 import numpy as np
 import pytest
@@ -17,12 +19,13 @@ from helpers import assert_bitexact, box_scene, config_for, make_pair, mesh_pile
 pytestmark = pytest.mark.gpu
 
 DT = 1.0 / 60.0
+FORMS = (0, 1, 2)
 
 
 def _run(sc, cfg, frames, substeps, iterations, what, split=None, body_params=None):
     gpus = []
     orc = None
-    for form in (0, 1):
+    for form in FORMS:
         g, o = make_pair(sc, cfg, body_params=body_params)
         g.set_solve_form(form)
         if split is not None:
@@ -75,7 +78,7 @@ def test_forms_batched_scenes():
 
     oracles = [make_pair(sc, cfg, gpu=False)[1] for sc in batch.scenes]
     gs = []
-    for form in (0, 1):
+    for form in FORMS:
         g = vkxpbd.XpbdSolver()
         g.init_batched(cfg, batch.counts)
         g.finalize_meshes()
@@ -105,6 +108,13 @@ def test_timed_form_choice_is_exact():
         orc.step(DT, 10, 1)
         assert_bitexact(g.get_positions(), orc.get_positions(), f"timed form frame {f}")
         assert_bitexact(g.get_velocities(), orc.get_velocities(), f"timed form frame {f}")
-    assert g.solve_form in (0, 1)
+    assert g.solve_form in FORMS
     with pytest.raises(RuntimeError, match="set_solve_form"):
-        g.set_solve_form(2)
+        g.set_solve_form(3)
+
+
+def test_forms_split_keys_pile():
+    """40,000 particles (split grid keys): most blocks stage their rows in the staged form."""
+    sc = scenes.pile_of(40_000)
+    cfg = config_for(sc)
+    _run(sc, cfg, 4, 10, 1, "split-key pile")
