@@ -250,9 +250,9 @@ class Solver {
     // Results are the same either way.
     // The choice is timed again every kSplitRetime frames (both graphs exist by then, so
     // two frames each way): a scene's balance moves as it evolves (bodies settling into a
-    // pile multiply the moving-mesh queries).
+    // pile multiply the moving-mesh queries). Within 1% the split is kept.
     static constexpr int kSplitTrials = 6;
-    static constexpr int kSplitRetime = 16;
+    static constexpr int kSplitRetime = 8;
     int split_choice_ = -1;
     int split_frames_ = 0;  // frames since the last choice
     int split_forced_ = -1;  // set_solve_split: kept across graph rebuilds
