@@ -69,6 +69,7 @@ Solver::~Solver() {
     if (pinned_) cudaFreeHost(pinned_);
     if (stream_) cudaStreamDestroy(stream_);
     if (aux_) cudaStreamDestroy(aux_);
+    if (walk_stream_) cudaStreamDestroy(walk_stream_);
     if (fork_) cudaEventDestroy(fork_);
     if (join_) cudaEventDestroy(join_);
     if (triaged_) cudaEventDestroy(triaged_);
@@ -124,6 +125,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     XPBD_CUDA(cudaSetDevice(device_));
     XPBD_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     XPBD_CUDA(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+    XPBD_CUDA(cudaStreamCreateWithFlags(&walk_stream_, cudaStreamNonBlocking));
     XPBD_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
     XPBD_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     XPBD_CUDA(cudaEventCreateWithFlags(&triaged_, cudaEventDisableTiming));
@@ -1044,17 +1046,17 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         count_memset();
         prof_mark(P_BODY_CONTACT);
     }
-    // Contact generation forks onto the second stream after the static-mesh triage (which
-    // reads the previous order that the sort below overwrites). With dynamic bodies the
-    // second stream runs the moving-mesh triage, its queries (results to the hit buffer) and
-    // the rigid contacts while the main stream runs the static-mesh traversal; then the
-    // second stream merges the hits into the slots behind the static contacts and builds the
-    // body-delta entries, while the main stream runs the integrate / sort / gather chain
-    // (the sort waits for the moving-mesh triage), which reads none of their outputs. The
-    // join comes before the bodies integrate and before the first reader of contacts.
-    // Without bodies the static-mesh traversal itself runs on the second stream beside the
-    // sort chain. Profiling keeps one stream in stage order so that each stage's events
-    // bracket its own kernels.
+    // Contact generation forks after the static-mesh triage (which reads the previous order
+    // that the sort below overwrites). With dynamic bodies the second stream runs the
+    // moving-mesh triage, its queries (results to the hit buffer) and the rigid contacts, a
+    // third stream the static-mesh traversal, and the main stream the integrate / sort /
+    // gather chain (the sort waits for the moving-mesh triage) and the first iteration's
+    // particle-particle part when split, none of which reads their outputs; once the
+    // traversal is done the second stream merges the hits into the slots behind the static
+    // contacts and builds the body-delta entries. The join comes before the bodies integrate
+    // and before the first reader of contacts. Without bodies the static-mesh traversal runs
+    // on the second stream beside the sort chain. Profiling keeps one stream in stage order
+    // so that each stage's events bracket its own kernels.
     const bool fork = mesh_pass && !profiling_;
     const MeshTables mt = mesh_tables();
     const uint32_t* prev_order = pair_v_[(plan_.passes - 1) & 1].p;
@@ -1100,6 +1102,10 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         XPBD_CUDA(cudaEventRecord(fork_, stream_));
         XPBD_CUDA(cudaStreamWaitEvent(aux_, fork_, 0));
         if (bodies) {
+            // a third stream for the static traversal: beside the moving-mesh chain and the
+            // main stream's sort chain and first particle-particle pass
+            XPBD_CUDA(cudaStreamWaitEvent(walk_stream_, fork_, 0));
+            walk_s = walk_stream_;
             posed_queries(aux_);
             launch_rigid_contacts(aux_, ba, rt, mt, rp, st);  // reads only the substep-start poses
             count_kernel();
@@ -1114,7 +1120,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
         prof_mark(P_CONTACT);
     }
     if (fork && bodies) {  // the hits join the slots once the static contacts are in place
-        XPBD_CUDA(cudaEventRecord(walked_, stream_));
+        XPBD_CUDA(cudaEventRecord(walked_, walk_s));
         XPBD_CUDA(cudaStreamWaitEvent(aux_, walked_, 0));
         posed_merge(aux_);
         body_entries(aux_);

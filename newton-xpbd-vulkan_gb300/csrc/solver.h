@@ -242,6 +242,7 @@ class Solver {
     // second stream of the frame graph: the mesh traversal runs on it beside the
     // integrate / sort / gather chain, which does not read contacts
     cudaStream_t aux_ = nullptr;
+    cudaStream_t walk_stream_ = nullptr;  // the static-mesh traversal beside the moving-mesh chain
     cudaEvent_t fork_ = nullptr, join_ = nullptr, triaged_ = nullptr, walked_ = nullptr;
     // Whether the first iteration's particle-particle part runs before the join, beside the
     // contact generation (split) or after it, fused with the rest (the faster depends on how
