@@ -93,9 +93,10 @@ __device__ __forceinline__ bool shape_delta(const Contact& ct, int pflag, v3 px,
     }
     const float denom = w1 + w2;
     if (denom == 0.0f) return false;
-    const float vt_len = exact_length(vt);
+    float inv_vt;
+    const float vt_len = exact_length_rcp(vt, inv_vt);
     const float lambda_f = gmax(mu * lambda_n, -vt_len * sp.dt);
-    const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+    const v3 vt_dir = vt_len > 0.0f ? exact_div_rcp(vt, vt_len, inv_vt) : mk3(0.0f, 0.0f, 0.0f);
     const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -delta_n.x), __fmaf_rn(vt_dir.y, lambda_f, -delta_n.y),
                         __fmaf_rn(vt_dir.z, lambda_f, -delta_n.z));
     const v3 delta_total = vmuls(exact_div(diff, denom), sp.relax);

@@ -69,19 +69,20 @@ __device__ __forceinline__ CellRange cell_range(v3 xp, float radius, const Solve
 // inverse mass, :166).
 __device__ __forceinline__ float4 pair_term_body(float4 nx, float4 nv, float sq, v3 xp, v3 vp, float radius,
                                                  float w1, float k_mu, float k_coh, float dt) {
-    const float d = exact_sqrt(sq);
+    float inv_d, inv_vt;
+    const float d = exact_sqrt_rcp(sq, inv_d);
     const float err = d - radius - nx.w;
     if (err > k_coh || d <= 0.0f) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const v3 raw = vsub(xp, xyz(nx));
     const float denom = w1 + nv.w;
     if (denom <= 0.0f) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const v3 nn = exact_div(raw, d);
+    const v3 nn = exact_div_rcp(raw, d, inv_d);
     const v3 vrel = vsub(vp, xyz(nv));
     const float vn = exact_dot(nn, vrel);
     const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y), __fmaf_rn(vn, -nn.z, vrel.z));
-    const float vt_len = exact_length(vt);
+    const float vt_len = exact_length_rcp(vt, inv_vt);
     const float lambda_f = gmax(k_mu * err, -vt_len * dt);
-    const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+    const v3 vt_dir = vt_len > 0.0f ? exact_div_rcp(vt, vt_len, inv_vt) : mk3(0.0f, 0.0f, 0.0f);
     const v3 p2 = vmuls(nn, err);
     const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
                         __fmaf_rn(vt_dir.z, lambda_f, -p2.z));
@@ -105,19 +106,20 @@ __device__ __forceinline__ void pair_block(int np, const int (*s_kk)[kSolveThrea
         const int kk = s_kk[q][threadIdx.x];
         const float4 nx = __ldg(&rx[kk]);
         const float4 nv = __ldg(&rv[kk]);
-        const float d = exact_sqrt(s_d[q][threadIdx.x]);  // the buffer holds squared distances
+        float inv_d, inv_vt;
+        const float d = exact_sqrt_rcp(s_d[q][threadIdx.x], inv_d);  // the buffer holds squared distances
         const float err = d - radius - nx.w;
         if (err > sp.k_coh || d <= 0.0f) continue;  // :157
         const v3 raw = vsub(xp, xyz(nx));
         const float denom = w1 + nv.w;
         if (denom <= 0.0f) continue;
-        const v3 nn = exact_div(raw, d);
+        const v3 nn = exact_div_rcp(raw, d, inv_d);
         const v3 vrel = vsub(vp, xyz(nv));
         const float vn = exact_dot(nn, vrel);
         const v3 vt = mk3(__fmaf_rn(vn, -nn.x, vrel.x), __fmaf_rn(vn, -nn.y, vrel.y), __fmaf_rn(vn, -nn.z, vrel.z));
-        const float vt_len = exact_length(vt);
+        const float vt_len = exact_length_rcp(vt, inv_vt);
         const float lambda_f = gmax(sp.k_mu * err, -vt_len * sp.dt);
-        const v3 vt_dir = vt_len > 0.0f ? exact_div(vt, vt_len) : mk3(0.0f, 0.0f, 0.0f);
+        const v3 vt_dir = vt_len > 0.0f ? exact_div_rcp(vt, vt_len, inv_vt) : mk3(0.0f, 0.0f, 0.0f);
         const v3 p2 = vmuls(nn, err);
         const v3 diff = mk3(__fmaf_rn(vt_dir.x, lambda_f, -p2.x), __fmaf_rn(vt_dir.y, lambda_f, -p2.y),
                             __fmaf_rn(vt_dir.z, lambda_f, -p2.z));

@@ -401,8 +401,9 @@ __device__ __forceinline__ bool walk_finish(W& w, const MeshTables& mt, int ci, 
         sign = vdot(w.acc, vsub(p, shape_p)) > 0.0f ? 1.0f : -1.0f;
     }
     const v3 delta = vsub(p, shape_p);
-    const float delta_len = exact_length(delta);
-    nrm = delta_len > 0.0f ? vmuls(exact_div(delta, delta_len), sign) : mk3(0.0f, 0.0f, 1.0f);
+    float inv_len;
+    const float delta_len = exact_length_rcp(delta, inv_len);
+    nrm = delta_len > 0.0f ? vmuls(exact_div_rcp(delta, delta_len, inv_len), sign) : mk3(0.0f, 0.0f, 1.0f);
     const float d = delta_len * sign;
     body_pos = vfma_vs(vneg(nrm), d, p);
     return true;

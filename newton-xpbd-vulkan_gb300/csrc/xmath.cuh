@@ -75,6 +75,36 @@ __device__ __forceinline__ v3 exact_div(v3 v, float d) {
     v3 rem = mk3(__fmaf_rn(-d, q.x, v.x), __fmaf_rn(-d, q.y, v.y), __fmaf_rn(-d, q.z, v.z));
     return mk3(__fmaf_rn(rem.x, inv_d, q.x), __fmaf_rn(rem.y, inv_d, q.y), __fmaf_rn(rem.z, inv_d, q.z));
 }
+// exact_sqrt(a) and its IEEE reciprocal RN(1/exact_sqrt(a)) with one reciprocal where the
+// shader's arithmetic has a division and a reciprocal: the refinement's RN(0.5/d0) is
+// 0.5 * RN(1/d0) exactly (a power-of-two scaling commutes with rounding, and 1/d0 of a
+// float's square root is always a normal number), and the refined root equals d0 in all but
+// rare cases, where the reciprocal is taken again. a == 0 gives (0, +inf), as
+// exact_sqrt(0) = 0 and RN(1/0).
+__device__ __forceinline__ float exact_sqrt_rcp(float a, float& inv) {
+    if (a == 0.0f) {
+        inv = __frcp_rn(a);
+        return a;
+    }
+    const float d0 = __fsqrt_rn(a);
+    const float r0 = __frcp_rn(d0);
+    const float r = __fmaf_rn(-d0, d0, a);
+    const float d = __fmaf_rn(r, 0.5f * r0, d0);
+    inv = d == d0 ? r0 : __frcp_rn(d);
+    return d;
+}
+__device__ __forceinline__ float exact_length_rcp(v3 a, float& inv) {
+    float yy = a.y * a.y;
+    float xx_yy = __fmaf_rn(a.x, a.x, yy);
+    float sq = __fmaf_rn(a.z, a.z, xx_yy);
+    return exact_sqrt_rcp(sq, inv);
+}
+// exact_div with the divisor's IEEE reciprocal inv_d = RN(1/d) supplied
+__device__ __forceinline__ v3 exact_div_rcp(v3 v, float d, float inv_d) {
+    v3 q = vmuls(v, inv_d);
+    v3 rem = mk3(__fmaf_rn(-d, q.x, v.x), __fmaf_rn(-d, q.y, v.y), __fmaf_rn(-d, q.z, v.z));
+    return mk3(__fmaf_rn(rem.x, inv_d, q.x), __fmaf_rn(rem.y, inv_d, q.y), __fmaf_rn(rem.z, inv_d, q.z));
+}
 __device__ __forceinline__ float exact_div1(float v, float d) {  // generate_mesh_contacts.comp:57-62
     float inv_d = __frcp_rn(d);
     float q = v * inv_d;
