@@ -295,12 +295,19 @@ int xpbd_batch_scene_offsets(xpbd_solver* s, size_t* offsets, size_t cap);
  * not overlap d_sorted_keys or d_sorted_ids (rejected). The call returns once
  * the sort has finished on `stream`: it reads back an 8-byte status word and
  * fails ("device wait timed out") when a bounded wait inside the sort ran out,
- * in which case the output is invalid. The array's device address is resolved
- * once per device ordinal for the life of the process, so a cudaDeviceReset in
- * between is not supported. */
+ * in which case the output is invalid. Called while `stream` is being captured
+ * into a CUDA graph (where no synchronisation is allowed) it only records the
+ * sort and returns 0; after a replay of that graph has finished,
+ * xpbd_sort_keys_noalloc_status reads the replay's status word. The array's
+ * device address is resolved once per device ordinal for the life of the
+ * process, so a cudaDeviceReset in between is not supported. */
 #define XPBD_NOALLOC_MAX_KEYS (1 << 20)
 int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint32_t* d_sorted_ids, size_t n,
                            int key_bits, void* stream);
+/* The status of the last allocation-free sort on the current device (or of the
+ * last replay of a graph that recorded one), read after its stream finished:
+ * 0, or -1 with "device wait timed out" (output invalid). */
+int xpbd_sort_keys_noalloc_status(void);
 
 #ifdef __cplusplus
 }

@@ -414,4 +414,8 @@ int xpbd_sort_keys_noalloc(const uint32_t* d_keys, uint32_t* d_sorted_keys, uint
     });
 }
 
+int xpbd_sort_keys_noalloc_status(void) {
+    return guarded([&] { xpbd::sort_keys_noalloc_status(); });
+}
+
 }  // extern "C"

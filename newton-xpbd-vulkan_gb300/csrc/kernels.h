@@ -260,6 +260,9 @@ void launch_cell_bounds(cudaStream_t s, int64_t n, const uint32_t* skeys, int32_
 // stable sort of n keys (values = input index) using only the static scratch array of noalloc.cu
 void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* sorted_ids, int64_t n, int key_bits,
                        cudaStream_t s);
+// the status of the last sort (or graph replay of one) on the current device: throws when a
+// bounded wait inside it ran out; call after the stream has finished
+void sort_keys_noalloc_status();
 // ---------------------------------------------------------------- bodies ----
 // Body b belongs to mesh b. Dynamic bodies (inv_m > 0) are listed in `dyn` (ascending);
 // their mesh vertices are dv_local[dv_start[b] .. dv_start[b + 1]) (body frame).

@@ -17,7 +17,9 @@
 // every call. The input must not overlap either output (a pass may write the
 // output while an earlier one still reads the input). A call returns once the
 // sort has finished on its stream: it reads back the status block, and a
-// look-back wait that ran out (the output is then wrong) makes the call fail.
+// look-back wait that ran out (the output is then wrong) makes the call fail. A call
+// recorded into a stream capture only records the sort; the status block then holds
+// each replay's outcome (sort_keys_noalloc_status reads it).
 #include <cstdint>
 #include <mutex>
 #include <stdexcept>
@@ -129,11 +131,25 @@ void sort_keys_noalloc(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* so
         kin = ko;
         vin = vo;
     }
+    // recorded into a graph (a stream capture allows no synchronisation): the status block
+    // holds each replay's outcome, read with sort_keys_noalloc_status after the replay
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    XPBD_CUDA_NOALLOC(cudaStreamIsCapturing(s, &capturing));
+    if (capturing != cudaStreamCaptureStatusNone) return;
     // the status block of this call (a bounded look-back wait sets a bit instead of hanging)
     DeviceStatus host{};
     XPBD_CUDA_NOALLOC(
         cudaMemcpyAsync(&host, base + kNaStatus, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
     XPBD_CUDA_NOALLOC(cudaStreamSynchronize(s));
+    if (host.error_bits & kErrLookbackTimeout)
+        throw std::runtime_error("xpbd_sort_keys_noalloc: device wait timed out in the onesweep look-back "
+                                 "(output invalid)");
+}
+
+void sort_keys_noalloc_status() {
+    uint32_t* base = scratch_for_current_device();
+    DeviceStatus host{};
+    XPBD_CUDA_NOALLOC(cudaMemcpy(&host, base + kNaStatus, sizeof(DeviceStatus), cudaMemcpyDeviceToHost));
     if (host.error_bits & kErrLookbackTimeout)
         throw std::runtime_error("xpbd_sort_keys_noalloc: device wait timed out in the onesweep look-back "
                                  "(output invalid)");

@@ -104,6 +104,7 @@ SIGNATURES = {
     "xpbd_stage_name": (C.c_char_p, [C.c_int]),
     "xpbd_get_frame_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "xpbd_sort_keys_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _Z, C.c_int, C.c_void_p]),
+    "xpbd_sort_keys_noalloc_status": (C.c_int, []),
     "xpbd_body_params_default": (None, [C.POINTER(BodyParams)]),
     "xpbd_set_body_params": (C.c_int, [_P, C.POINTER(BodyParams)]),
     "xpbd_set_bodies": (C.c_int, [_P, _F, _F, _F, _F, _F, _F, _I, _Z]),

@@ -121,6 +121,47 @@ def test_noalloc_sort_reports_a_timed_out_wait():
     assert_bitexact(out_k, keys[order], "keys after the timed-out call")
 
 
+def test_noalloc_sort_inside_a_cuda_graph_capture():
+    """The call recorded into another framework's CUDA graph (torch.cuda.graph): no allocation
+    while capturing or replaying, each replay sorts the keys then in the input buffer, and the
+    replay's status is read afterwards with xpbd_sort_keys_noalloc_status."""
+    import torch
+
+    from helpers import assert_bitexact
+    from vkxpbd import _abi
+
+    lib = _abi.load()
+    dev = torch.device("cuda", 0)
+    n = 50_000
+    rng = np.random.default_rng(11)
+    d_keys = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_out_k = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_out_v = torch.zeros(n, dtype=torch.int32, device=dev)
+
+    def call():
+        return lib.xpbd_sort_keys_noalloc(C.c_void_p(d_keys.data_ptr()), C.c_void_p(d_out_k.data_ptr()),
+                                          C.c_void_p(d_out_v.data_ptr()), n, 21,
+                                          C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+
+    assert call() == 0, lib.xpbd_last_error().decode()  # first call on the device: outside the capture
+    torch.cuda.synchronize(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rc = call()
+    assert rc == 0, lib.xpbd_last_error().decode()
+    allocated = torch.cuda.memory_allocated(dev)
+    for rep in range(3):
+        keys = rng.integers(0, 1 << 21, size=n, dtype=np.uint32)
+        d_keys.copy_(torch.from_numpy(keys.view(np.int32)))
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        assert lib.xpbd_sort_keys_noalloc_status() == 0, lib.xpbd_last_error().decode()
+        order = np.argsort(keys, kind="stable").astype(np.uint32)
+        assert_bitexact(d_out_v.cpu().numpy().view(np.uint32), order, f"replay {rep}: ids")
+        assert_bitexact(d_out_k.cpu().numpy().view(np.uint32), keys[order], f"replay {rep}: keys")
+    assert torch.cuda.memory_allocated(dev) == allocated
+
+
 def test_noalloc_sort_rejects_too_many_keys():
     from vkxpbd import _abi
 
