@@ -884,8 +884,9 @@ __global__ void __launch_bounds__(128) k_body_particles(BodyArrays ba, const uin
     const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (b >= ba.nb) return;
-    v3 lin = mk3(0.0f, 0.0f, 0.0f), ang = lin;
-    float cnt = 0.0f;
+    // lanes 0-6 each sum one component of the entries in entry order: linear x, y, z, the
+    // count (w: 1 for a contact with a delta, 0 without), angular x, y, z
+    float part = 0.0f;
     if (ba.invm[b] > 0.0f) {
         const uint2 sg = seg[b];
         uint32_t idx[PER_LANE];  // entry ids of the next chunk to copy
@@ -914,25 +915,27 @@ __global__ void __launch_bounds__(128) k_body_particles(BodyArrays ba, const uin
             load_ids(base + 2 * kBodyChunk);      // the chunk after it
             cp_async_wait_prev();                 // this chunk has arrived
             __syncwarp();
-            if (lane == 0) {
-                // entries of contacts that produced no delta (w = 0) add +0: a sum that starts
-                // at +0 is never -0, so adding +0 leaves it unchanged and the loop needs no branch
+            if (lane < 7) {
+                // an entry of a contact that produced no delta is all zeros (k_solve writes it
+                // so): a sum that starts at +0 is never -0, so adding +0 leaves it unchanged
+                // and the loop needs no test
+                const float* src = lane < 4 ? reinterpret_cast<const float*>(&s_a[w][buf][0]) + lane
+                                            : reinterpret_cast<const float*>(&s_c[w][buf][0]) + (lane - 4);
                 const int m = (int)min((uint32_t)kBodyChunk, sg.y - base);
 #pragma unroll 8
-                for (int l = 0; l < m; l++) {
-                    const float4 al = s_a[w][buf][l], cl = s_c[w][buf][l];
-                    const bool on = al.w != 0.0f;
-                    lin = vadd(lin, on ? xyz(al) : mk3(0.0f, 0.0f, 0.0f));
-                    ang = vadd(ang, on ? xyz(cl) : mk3(0.0f, 0.0f, 0.0f));
-                    cnt += on ? 1.0f : 0.0f;
-                }
+                for (int l = 0; l < m; l++) part += src[l * 4];
             }
             __syncwarp();  // the buffer is refilled by the next round's copies
             buf ^= 1;
         }
         cp_async_wait_all();
     }
-    if (lane == 0) apply_body_delta(ba, b, rp.dt, q_in, qd_in, lin, ang, cnt, rp.particle_weighting, q_out, qd_out);
+    float c[7];
+#pragma unroll
+    for (int j = 0; j < 7; j++) c[j] = __shfl_sync(0xffffffffu, part, j);
+    if (lane == 0)
+        apply_body_delta(ba, b, rp.dt, q_in, qd_in, mk3(c[0], c[1], c[2]), mk3(c[4], c[5], c[6]), c[3],
+                         rp.particle_weighting, q_out, qd_out);
 }
 
 void launch_body_particles(cudaStream_t s, BodyArrays ba, const uint2* seg, const uint32_t* sorted_entries,
