@@ -248,9 +248,11 @@ int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
  * form): 0 = each thread computes the pair terms of its own particle's neighbours, 1 = the
  * lanes of a warp compute their neighbours' pair terms together (balanced when neighbour
  * counts differ), 2 = as 0 with each block's neighbourhood records staged in shared memory
- * (one scene only; slower on the benchmark scenes, so never chosen by the timing), -1
- * (default) = a solver of 16,384 particles or more times forms 0 and 1 on its own last
- * substep after its first frame and again every 16 frames, and keeps the faster.
+ * (one scene only; slower on the benchmark scenes, so never chosen by the timing), 3 = one
+ * warp per particle (the lanes test its candidates and compute its pair terms together), -1
+ * (default) = form 3 for scenes of at most 8,192 particles, form 0 up to 16,383, and from
+ * 16,384 particles forms 0 and 1 timed on the solver's own last substep after its first
+ * frame and again every 16 frames, keeping the faster.
  * xpbd_get_solve_form reports the form in use. */
 int xpbd_set_solve_form(xpbd_solver* s, int form);
 int xpbd_get_solve_form(const xpbd_solver* s, int* form);

@@ -24,7 +24,7 @@ constexpr int kCoopCap = 12;  // accepted neighbours buffered per lane for the w
 // How a solve kernel computes the particle-particle totals (the solver times both on its scene
 // and keeps the faster; the results are the same bits): each thread its own neighbours' pair
 // terms, or the warp's pair pass
-enum { kFormThread = 0, kFormWarp = 1, kFormStaged = 2 };
+enum { kFormThread = 0, kFormWarp = 1, kFormStaged = 2, kFormParticleWarp = 3 };
 
 // Shared staging of a block's neighbourhood (the staged form): the sorted records of every
 // (y, z) row of cells the block's particles reach, copied once; the per-cell bounds of those
@@ -366,6 +366,89 @@ __device__ __forceinline__ v3 pp_total_warp(bool active, int64_t k, int pflag, v
 // total to the shape deltas in the same order.
 enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
 
+// The particle-particle total of one particle computed by a whole warp (the per-particle-warp
+// form; every lane calls it for the same particle and gets the same total). The lanes take
+// the particle's candidates 32 at a time in the filter's order (rows of cells z outer, y
+// inner, each row one run of the sorted order), each testing one candidate as pp_filter
+// does and computing its pair term; the accepted terms of a round are then added in lane
+// order, which is candidate order. A particle whose rows wrap the grid or number more than
+// 32 is done by lane 0 alone in the filter's order.
+template <bool ALL_ACTIVE>
+__device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1,
+                                             const float4* __restrict__ rx, const float4* __restrict__ rv,
+                                             const int* __restrict__ rf, const int4* __restrict__ table, bool split,
+                                             uint32_t stamp, const SolveParams& sp) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int is_proxy = pflag & 2;
+    const float R = radius + sp.max_radius + sp.k_coh;
+    const CellRange cr = cell_range(xp, radius, sp);
+    const int nyr = cr.ye - cr.ys + 1, rows = nyr * (cr.ze - cr.zs + 1);
+    const int32_t xo = cr.xs + kGridOrigin;
+    const bool row_run = xo >= 0 && (xo % kGridDim) + (cr.xe - cr.xs) < kGridDim;
+    v3 acc = mk3(0.0f, 0.0f, 0.0f);
+    if (!row_run || rows > 32) {
+        if (lane == 0)
+            pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float sq) {
+                const float4 t = pair_term(__ldg(&rx[kk]), __ldg(&rv[kk]), sq, xp, vp, radius, w1, sp.k_mu,
+                                           sp.k_coh, sp.dt);
+                if (t.w != 0.0f) acc = vadd(acc, xyz(t));
+            });
+        acc = mk3(__shfl_sync(FULL, acc.x, 0), __shfl_sync(FULL, acc.y, 0), __shfl_sync(FULL, acc.z, 0));
+    } else {
+        int lo = 0x7fffffff, hi = -1;  // lane r: the sorted range of row r
+        if (lane < rows) {
+            const int c0 = cell_index(cr.xs, cr.ys + lane % nyr, cr.zs + lane / nyr, split);
+            for (int j = 0; j <= cr.xe - cr.xs; j++) {
+                const int4 e = __ldg(&table[c0 + j]);
+                if ((uint32_t)e.z == stamp) {
+                    lo = min(lo, e.x);
+                    hi = max(hi, e.y);
+                }
+            }
+        }
+        const int len = hi > lo ? hi - lo : 0;
+        int incl = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int excl = incl - len;
+        const int total_c = __shfl_sync(FULL, incl, 31);
+        for (int base = 0; base < total_c; base += 32) {
+            const int c = base + lane;
+            int r = 0;  // the row of candidate c: the last row starting at or before it
+            for (int q = 1; q < rows; q++)
+                if (__shfl_sync(FULL, excl, q) <= c) r = q;
+            const int kk = __shfl_sync(FULL, lo, r) + (c - __shfl_sync(FULL, excl, r));
+            float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (c < total_c && kk != k) {
+                const int nflag = ALL_ACTIVE ? 1 : __ldg(&rf[kk]);
+                bool ok = (nflag & 1) != 0;
+                if (!ALL_ACTIVE && ok && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
+                    ok = false;
+                if (ok) {
+                    const float4 nx = __ldg(&rx[kk]);
+                    const v3 raw = vsub(xp, xyz(nx));
+                    if (!(fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R)) {
+                        const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
+                        const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
+                        if (!(sq > reach * reach))
+                            t = pair_term_body(nx, __ldg(&rv[kk]), sq, xp, vp, radius, w1, sp.k_mu, sp.k_coh, sp.dt);
+                    }
+                }
+            }
+            for (uint32_t m = __ballot_sync(FULL, t.w != 0.0f); m; m &= m - 1) {
+                const int src = __ffs(m) - 1;
+                acc = vadd(acc, mk3(__shfl_sync(FULL, t.x, src), __shfl_sync(FULL, t.y, src),
+                                    __shfl_sync(FULL, t.z, src)));
+            }
+        }
+    }
+    const v3 dw = mk3(__fmaf_rn(acc.x, w1, 0.0f), __fmaf_rn(acc.y, w1, 0.0f), __fmaf_rn(acc.z, w1, 0.0f));
+    return mk3(__fmaf_rn(dw.x, sp.relax, 0.0f), __fmaf_rn(dw.y, sp.relax, 0.0f), __fmaf_rn(dw.z, sp.relax, 0.0f));
+}
+
 // The staged form's block setup (every thread of the block calls it; `active` = this thread
 // filters neighbours): the block's cell range, then, when it qualifies, the cell bounds of its
 // rows and their sorted records in shared memory. Returns whether the block staged (the same
@@ -442,12 +525,15 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     constexpr bool WARP = FORM == kFormWarp && !DIAG && PP != kPPApply;
     // the staged form: the block's neighbourhood records in shared memory (SolveStage)
     constexpr bool STAGED = FORM == kFormStaged && !DIAG && PP != kPPApply;
+    // the per-particle-warp form: one particle per warp (pp_total_pwarp), lane 0 then goes on
+    constexpr bool PWARP = FORM == kFormParticleWarp && !DIAG && PP != kPPApply;
     __shared__ int s_kk[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
     __shared__ float s_d[(PP == kPPApply || WARP) ? 1 : kPairCap][kSolveThreads];
     __shared__ WarpPairs s_wp[WARP ? kSolveThreads / 32 : 1];
     __shared__ typename std::conditional<STAGED, SolveStage, char>::type s_stage;
-    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (!WARP && !STAGED && k0 >= n) return;
+    const int64_t k0 = PWARP ? (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)
+                             : (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (!WARP && !STAGED && k0 >= n) return;  // (whole warps in the per-particle-warp form)
     const bool valid = k0 < n;  // every lane of a warp reaches the warp's pair pass (every thread the staging)
     const int64_t k = valid ? k0 : n - 1;
     const uint32_t id = sids[k];
@@ -464,6 +550,14 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
             stage = &s_stage;
         if (!valid) return;
     }
+    if constexpr (PWARP) {
+        if (pflag & 1) {  // the same particle in every lane
+            const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
+            total = pp_total_pwarp<ALL_ACTIVE>(k, pflag, xp, vp, radius, w1, rx, rv, rf, table, sp.split_keys != 0,
+                                               *stamp_p, sp);
+        }
+        if ((threadIdx.x & 31) != 0) return;
+    }
     if constexpr (WARP) {
         // this particle's scene table (scene-major keys); one scene: the whole table
         const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
@@ -472,7 +566,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
         if (!valid) return;
     }
     if constexpr (PP == kPPOnly) {
-        if constexpr (!WARP) {
+        if constexpr (!WARP && !PWARP) {
             if (pflag & 1) {
                 const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
                 total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table,
@@ -518,7 +612,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
         }
         if constexpr (PP == kPPApply) {
             total = xyz(pp[k]);
-        } else if constexpr (!WARP) {
+        } else if constexpr (!WARP && !PWARP) {
             // this particle's scene table (scene-major keys); one scene: the whole table
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
             total = pp_total<ALL_ACTIVE, DIAG>(k, pflag, xp, vp, radius, w1, id, rx, rv, rf, table, sp.split_keys != 0,
@@ -601,10 +695,11 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   SolveDiag dg, BodyDeltaOut bo, int pp_mode, float4* pp, int form) {
     if (n <= 0) return;
     const int threads = kSolveThreads;
-    const int blocks = (int)((n + threads - 1) / threads);
     const bool diag = dg.pair_header != nullptr;
-    // the warp form applies where the particle-particle totals are computed without diagnostics
+    // the warp forms apply where the particle-particle totals are computed without diagnostics
     if (diag || pp_mode == kPPApply) form = kFormThread;
+    const int64_t per_block = form == kFormParticleWarp ? threads / 32 : threads;
+    const int blocks = (int)((n + per_block - 1) / per_block);
 #define XPBD_SOLVE(L, A, D, P, F)                                                                                  \
     if (last == L && all_active == A && diag == D && pp_mode == P && form == F) {                                 \
         k_solve<L, A, D, P, F><<<blocks, threads, 0, s>>>(n, sids, skeys, rx, rv, rf, table, stamp, x0, v0, cinfo, \
@@ -624,6 +719,10 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
     XPBD_SOLVE(true, false, false, kPPFused, kFormStaged)
     XPBD_SOLVE(false, true, false, kPPFused, kFormStaged)
     XPBD_SOLVE(false, false, false, kPPFused, kFormStaged)
+    XPBD_SOLVE(true, true, false, kPPFused, kFormParticleWarp)
+    XPBD_SOLVE(true, false, false, kPPFused, kFormParticleWarp)
+    XPBD_SOLVE(false, true, false, kPPFused, kFormParticleWarp)
+    XPBD_SOLVE(false, false, false, kPPFused, kFormParticleWarp)
     XPBD_SOLVE(true, true, true, kPPFused, kFormThread)
     XPBD_SOLVE(true, false, true, kPPFused, kFormThread)
     XPBD_SOLVE(false, true, true, kPPFused, kFormThread)
@@ -636,6 +735,8 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
     XPBD_SOLVE(false, false, false, kPPOnly, kFormWarp)
     XPBD_SOLVE(false, true, false, kPPOnly, kFormStaged)
     XPBD_SOLVE(false, false, false, kPPOnly, kFormStaged)
+    XPBD_SOLVE(false, true, false, kPPOnly, kFormParticleWarp)
+    XPBD_SOLVE(false, false, false, kPPOnly, kFormParticleWarp)
     XPBD_SOLVE(true, true, false, kPPApply, kFormThread)
     XPBD_SOLVE(true, false, false, kPPApply, kFormThread)
     XPBD_SOLVE(false, true, false, kPPApply, kFormThread)

@@ -221,8 +221,10 @@ void launch_solve(cudaStream_t s, int64_t n, bool last, bool all_active, const u
                   int form = 0);
 // forms of the solve kernel (launch_solve's `form`): 0 = each thread sums its own neighbours'
 // pair terms, 1 = the lanes of a warp compute their neighbours' pair terms together, 2 = as 0
-// with the block's neighbourhood records staged in shared memory; same bits
-constexpr int kSolveForms = 3;
+// with the block's neighbourhood records staged in shared memory, 3 = one warp per particle
+// (its lanes test the candidates and compute the pair terms 32 at a time: small scenes,
+// whose time is one particle's latency); same bits
+constexpr int kSolveForms = 4;
 // the forms the solver times on its scene and chooses from (the staged form measured slower
 // on every benchmark scene: it stays selectable, and tested, but is not timed)
 constexpr int kSolveTimedForms = 2;

@@ -112,6 +112,7 @@ void Solver::init_batched(const xpbd_config& cfg, const size_t* scene_counts, si
     for (size_t s = 0; s < n_scenes; s++) scene_off_[s + 1] = scene_off_[s] + scene_counts[s];
     const size_t num_particles = scene_off_[n_scenes];
     n_ = num_particles;
+    solve_form_ = default_solve_form();
     contact_max_ = (int64_t)(max_contacts ? max_contacts : num_particles * 2);  // scene.cpp:68
     key_bits_ = 21;
     while (n_scenes > 1 && (size_t(1) << (key_bits_ - 21)) < n_scenes) key_bits_++;
@@ -263,10 +264,10 @@ void Solver::set_solve_split(int mode) {
 
 void Solver::set_solve_form(int form) {
     require_init();
-    if (form < -1 || form >= kSolveForms) throw std::runtime_error("set_solve_form: -1 (timed choice), 0, 1 or 2");
+    if (form < -1 || form >= kSolveForms) throw std::runtime_error("set_solve_form: -1 (timed choice), 0, 1, 2 or 3");
     sync();
     solve_form_forced_ = form;
-    if (form >= 0) solve_form_ = form;
+    solve_form_ = form >= 0 ? form : default_solve_form();
     solve_form_timed_ = false;
 }
 

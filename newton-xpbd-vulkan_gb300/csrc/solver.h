@@ -220,7 +220,11 @@ class Solver {
     // kSolveRetime frames, as the scene evolves (in the mixed workload the warp form turns
     // faster once the boxes press into the pile); every form gives the same bits.
     static constexpr uint64_t kSolveRetime = 16;
-    static constexpr size_t kSolveTuneMinParticles = 16384;  // smaller scenes keep form 0
+    static constexpr size_t kSolveTuneMinParticles = 16384;  // smaller scenes keep the default
+    // the default form: one warp per particle for small scenes, whose solve time is one
+    // particle's latency (4,096 particles: 28.8 -> 20.8 us per substep; slower from 16,384)
+    static constexpr size_t kParticleWarpMaxParticles = 8192;
+    int default_solve_form() const { return n_ <= kParticleWarpMaxParticles ? 3 : 0; }
     int solve_form_ = 0, solve_form_forced_ = -1;
     uint64_t solve_form_frame_ = 0;
     bool solve_form_timed_ = false;

@@ -234,8 +234,9 @@ class XpbdSolver:
 
     def set_solve_form(self, form):
         """Solve-kernel form: 0 per-thread pair terms, 1 warp pair pass, 2 per-thread from a
-        block's neighbourhood staged in shared memory, -1 (default) 0 or 1 timed on the scene's
-        own substeps (xpbd_set_solve_form). Results are identical."""
+        block's neighbourhood staged in shared memory, 3 one warp per particle, -1 (default)
+        3 for small scenes, else 0 or 1 timed on the scene's own substeps
+        (xpbd_set_solve_form). Results are identical."""
         _check(_lib.xpbd_set_solve_form(self._h, int(form)))
 
     @property

@@ -19,7 +19,7 @@ from helpers import assert_bitexact, box_scene, config_for, make_pair, mesh_pile
 pytestmark = pytest.mark.gpu
 
 DT = 1.0 / 60.0
-FORMS = (0, 1, 2)
+FORMS = (0, 1, 2, 3)
 
 
 def _run(sc, cfg, frames, substeps, iterations, what, split=None, body_params=None):
@@ -110,7 +110,7 @@ def test_timed_form_choice_is_exact():
         assert_bitexact(g.get_velocities(), orc.get_velocities(), f"timed form frame {f}")
     assert g.solve_form in FORMS
     with pytest.raises(RuntimeError, match="set_solve_form"):
-        g.set_solve_form(3)
+        g.set_solve_form(4)
 
 
 def test_forms_split_keys_pile():
