@@ -416,6 +416,98 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
 }
 
 // ---------------------------------------------------------------------------
+// Small sorts: every pass of the stable LSD radix sort of at most kSmallSortKeys keys in one
+// block and one launch, the keys held in shared memory between passes (a small scene's sort
+// is three dependent launches of one tile otherwise). Each pass ranks the keys as a onesweep
+// tile does (warps in index order, __match_any_sync within a warp), so the permutation is
+// the same stable order.
+// ---------------------------------------------------------------------------
+constexpr int kSmallSortThreads = 256, kSmallSortItems = 16;
+constexpr int kSmallSortKeys = kSmallSortThreads * kSmallSortItems;
+
+__global__ void __launch_bounds__(kSmallSortThreads) k_sort_small(int n, int passes, const uint32_t* __restrict__ keys_in,
+                                                                  uint32_t* __restrict__ keys_out,
+                                                                  uint32_t* __restrict__ vals_out) {
+    constexpr int BITS = 8, BINS = 1 << BITS, THREADS = kSmallSortThreads, ITEMS = kSmallSortItems;
+    constexpr int WARPS = THREADS / 32, TILE = kSmallSortKeys;
+    static_assert(BINS == THREADS, "one digit per thread");
+    extern __shared__ uint32_t smem[];
+    uint32_t* s_k[2] = {smem, smem + TILE};
+    uint32_t* s_v[2] = {smem + 2 * TILE, smem + 3 * TILE};
+    uint32_t* s_whist = smem + 4 * TILE;  // WARPS * BINS
+    __shared__ uint32_t s_scan[WARPS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < n; i += THREADS) {
+        s_k[0][i] = keys_in[i];
+        s_v[0][i] = (uint32_t)i;
+    }
+    const uint32_t lt = lanemask_lt();
+    int cur = 0;
+    for (int p = 0; p < passes; p++) {
+        for (int i = tid; i < WARPS * BINS; i += THREADS) s_whist[i] = 0;
+        __syncthreads();
+        uint32_t kreg[ITEMS], vreg[ITEMS], rreg[ITEMS], dreg[ITEMS];
+#pragma unroll
+        for (int j = 0; j < ITEMS; j++) {
+            const int local = warp * 32 * ITEMS + j * 32 + lane;
+            const bool valid = local < n;
+            const uint32_t key = valid ? s_k[cur][local] : 0u;
+            const uint32_t d = valid ? ((key >> (p * BITS)) & (BINS - 1)) : (uint32_t)BINS;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            uint32_t old = 0;
+            if (valid) old = s_whist[warp * BINS + d];
+            __syncwarp();
+            if (valid && (peers & lt) == 0) s_whist[warp * BINS + d] = old + __popc(peers);
+            __syncwarp();
+            kreg[j] = key;
+            vreg[j] = valid ? s_v[cur][local] : 0u;
+            rreg[j] = old + __popc(peers & lt);
+            dreg[j] = d;
+        }
+        __syncthreads();
+        // thread `tid` owns digit `tid`: the warps' exclusive prefix in place, the digit's total
+        uint32_t tot = 0;
+        for (int wv = 0; wv < WARPS; wv++) {
+            const uint32_t c = s_whist[wv * BINS + tid];
+            s_whist[wv * BINS + tid] = tot;
+            tot += c;
+        }
+        uint32_t dummy;
+        const uint32_t digit_base = block_excl_scan<THREADS>(tot, s_scan, dummy);
+        // each (warp, digit) start = digit start + the warps before it
+        for (int wv = 0; wv < WARPS; wv++) s_whist[wv * BINS + tid] += digit_base;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < ITEMS; j++) {
+            if (dreg[j] < (uint32_t)BINS) {
+                const uint32_t dst = s_whist[warp * BINS + dreg[j]] + rreg[j];
+                s_k[cur ^ 1][dst] = kreg[j];
+                s_v[cur ^ 1][dst] = vreg[j];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (int i = tid; i < n; i += THREADS) {
+        keys_out[i] = s_k[cur][i];
+        vals_out[i] = s_v[cur][i];
+    }
+}
+
+bool launch_sort_small(cudaStream_t s, int64_t n, int key_bits, const uint32_t* keys_in, uint32_t* keys_out,
+                       uint32_t* vals_out) {
+    if (n <= 0 || n > kSmallSortKeys) return false;
+    const size_t smem = sizeof(uint32_t) * ((size_t)4 * kSmallSortKeys + (size_t)(kSmallSortThreads / 32) * 256);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    k_sort_small<<<1, kSmallSortThreads, smem, s>>>((int)n, (key_bits + 7) / 8, keys_in, keys_out, vals_out);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // Cell table (start, end, generation stamp) + sorted-order particle records
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_cells_gather(int64_t n, const uint32_t* __restrict__ skeys,

@@ -166,6 +166,10 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          const float* r, const int* flags, const uint32_t* pscene, PredictParams pp, PlaneParams pl,
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
                          uint32_t* ccount, uint32_t* stamp);
+// every pass of a stable LSD sort of at most 4,096 keys (key_bits wide, 8-bit digits) in one
+// launch of one block; values = input index. Returns false (nothing launched) for more keys.
+bool launch_sort_small(cudaStream_t s, int64_t n, int key_bits, const uint32_t* keys_in, uint32_t* keys_out,
+                       uint32_t* vals_out);
 // one onesweep pass; vals_in == nullptr means vals are the element index; n_dev (optional)
 // holds the element count on the device (at most n, the capacity the grid is sized for).
 // debug_hold: the pass honours the look-back test hook (set_lookback_debug)

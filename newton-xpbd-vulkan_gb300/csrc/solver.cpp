@@ -1147,17 +1147,26 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const uint32_t* vin = nullptr;
     const size_t lbw = sort_lookback_words(plan_);
     if (fork && bodies) XPBD_CUDA(cudaStreamWaitEvent(stream_, triaged_, 0));  // it has read the previous order
-    for (int p = 0; p < plan_.passes; p++) {
-        uint32_t* ko = pair_k_[p & 1].p;
-        uint32_t* vo = pair_v_[p & 1].p;
-        launch_onesweep_pass(stream_, n, plan_, p, kin, vin, ko, vo,
-                             sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
-                             sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st,
-                             nullptr, true);
+    const int last = (plan_.passes - 1) & 1;  // the buffers the last pass writes (read by the rest)
+    if (launch_sort_small(stream_, n, key_bits_, keys_.p, pair_k_[last].p, pair_v_[last].p)) {
+        // a scene of one tile: every pass in one launch (the same stable order)
         count_kernel();
-        prof_mark(P_SORT0 + std::min(p, 3));
-        kin = ko;
-        vin = vo;
+        prof_mark(P_SORT0);
+        kin = pair_k_[last].p;
+        vin = pair_v_[last].p;
+    } else {
+        for (int p = 0; p < plan_.passes; p++) {
+            uint32_t* ko = pair_k_[p & 1].p;
+            uint32_t* vo = pair_v_[p & 1].p;
+            launch_onesweep_pass(stream_, n, plan_, p, kin, vin, ko, vo,
+                                 sort_scratch_.p + hist_off_ + ((size_t)p << plan_.bits),
+                                 sort_scratch_.p + lb_off_ + (size_t)p * lbw, sort_scratch_.p + tc_off_ + p, st,
+                                 nullptr, true);
+            count_kernel();
+            prof_mark(P_SORT0 + std::min(p, 3));
+            kin = ko;
+            vin = vo;
+        }
     }
     const uint32_t* skeys = kin;
     const uint32_t* sids = vin;
