@@ -69,6 +69,14 @@ ALG_BYTES = {
     "3c. Restitution (bodies)": 52,            # header, x0, v0, v in; v out
 }
 STEP_ALG_BYTES = 76
+SLOT_BYTES = 48  # one contact slot (body point, normal, body velocity: 3 float4) read by the solve
+
+
+def alg_bytes(stage, n, contacts=0):
+    """Algorithmic bytes of one launch of a stage over n particles; the solve also reads the
+    substep's contact slots (contacts = the contact count of a substep)."""
+    extra = SLOT_BYTES * contacts if stage.startswith("3. Solve") else 0
+    return ALG_BYTES[stage] * n + extra
 
 
 def dist_env():
@@ -183,7 +191,7 @@ def launches_of(stage, prof_substeps):
     return prof_substeps * (ITERATIONS if per_iteration else 1)
 
 
-def stage_table(stage_ms, prof_substeps, n, peak):
+def stage_table(stage_ms, prof_substeps, n, peak, contacts=0):
     out = {}
     for k, v in stage_ms.items():
         if v <= 0:
@@ -191,7 +199,7 @@ def stage_table(stage_ms, prof_substeps, n, peak):
         us = v / launches_of(k, prof_substeps) * 1e3
         st = {"us_per_launch": round(us, 2)}
         if k in ALG_BYTES:
-            gbs = ALG_BYTES[k] * n / (us * 1e-6) / 1e9
+            gbs = alg_bytes(k, n, contacts) / (us * 1e-6) / 1e9
             st.update({"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)})
         out[k] = st
     return out
@@ -211,18 +219,19 @@ def profile_stages(solver, frames, flush=None):
     return stage_ms, prof_substeps
 
 
-def roofline_of(workload, stage_ms, prof_substeps, n, step_ms, peak, peak_kind):
+def roofline_of(workload, stage_ms, prof_substeps, n, step_ms, peak, peak_kind, contacts=0):
     """Dominant kernel (most device time among the kernels with algorithmic bytes) against
-    the measured HBM copy bandwidth, and the whole substep with 76 B per particle-substep."""
+    the measured HBM copy bandwidth, and the whole substep with 76 B per particle-substep.
+    contacts: a substep's contact count (the solve reads one 48-byte slot per contact)."""
     ranked = sorted(((v, k) for k, v in stage_ms.items() if k in ALG_BYTES and v > 0), reverse=True)
     if not ranked:
         raise RuntimeError(f"no per-kernel stage times were recorded: {stage_ms}")
     dom_ms, dom = ranked[0]
     avg_ms = dom_ms / launches_of(dom, prof_substeps)
-    achieved = ALG_BYTES[dom] * n / (avg_ms * 1e-3) / 1e9
+    achieved = alg_bytes(dom, n, contacts) / (avg_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "alg_bytes_per_launch": ALG_BYTES[dom] * n, "avg_launch_us": round(avg_ms * 1e3, 2),
+                "alg_bytes_per_launch": alg_bytes(dom, n, contacts), "avg_launch_us": round(avg_ms * 1e3, 2),
                 "traffic": dram_traffic(workload, dom),
                 "share_of_step": round(dom_ms / sum(v for v in stage_ms.values() if v > 0), 3)}
     step_gbs = STEP_ALG_BYTES * n * SUBSTEPS * ITERATIONS / (step_ms * 1e-3) / 1e9
@@ -414,8 +423,9 @@ def run_gpu(args):
 
     stage_ms, prof_substeps = profile_stages(solver, min(args.steps, 10), flush)
     peak, peak_kind = measured_peak_hbm()
+    contacts = int(solver.last_contact_count)  # the last profiled substep's
     roofline, roofline_step = roofline_of("mixed", stage_ms, prof_substeps, sc.n, dev_ms / args.steps, peak,
-                                          peak_kind)
+                                          peak_kind, contacts)
 
     # end to end through the public API with host buffers: set_particles + set_bodies -> step -> readback,
     # from the state the timed frames started from, so both cover the same frames
@@ -437,7 +447,8 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single"},
         "roofline": roofline,
         "roofline_step": roofline_step,
-        "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
+        "stages": stage_table(stage_ms, prof_substeps, sc.n, peak, contacts),
+        "contacts_last_substep": contacts,
         "boxes_finite": bool(np.isfinite(bq).all() and np.isfinite(bqd).all()),
         "e2e": e2e, "gpu_launches": int(kernels_timed), "clocks": clk,
     }
@@ -498,14 +509,15 @@ def measure_mesh(args, dev):
     dev_ms = timed_frames(s, stream, frames, flush)
     stage_ms, prof_substeps = profile_stages(s, min(frames, 30), flush)
     peak, peak_kind = measured_peak_hbm()
+    contacts = int(s.last_contact_count)
     roofline, roofline_step = roofline_of("particles_on_mesh", stage_ms, prof_substeps, sc.n, dev_ms / frames,
-                                          peak, peak_kind)
+                                          peak, peak_kind, contacts)
     e2e_s, h2d, d2h = e2e_frames(s, frames, x_t0, v_t0, flush=flush, sync=lambda: torch.cuda.synchronize(dev))
     work = sc.n * SUBSTEPS * frames
     out = {"workload": "particles_on_mesh", "particles": sc.n, "triangles": int(sc.meshes[0][1].shape[0]),
            "preroll_frames": args.mesh_preroll, "frames": frames, "value": work / (dev_ms * 1e-3), "unit": UNIT,
            "ms_per_frame": dev_ms / frames, "roofline": roofline, "roofline_step": roofline_step,
-           "stages": stage_table(stage_ms, prof_substeps, sc.n, peak),
+           "stages": stage_table(stage_ms, prof_substeps, sc.n, peak, contacts),
            "e2e": {"value": work / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)}}
     if args.cache_frames > 0:
@@ -684,13 +696,14 @@ def measure_pile(args, dev):
     stage_ms, prof_substeps = profile_stages(s, min(frames, 5))
     peak, peak_kind = measured_peak_hbm()
     work = sc.n * SUBSTEPS * frames
+    contacts = int(s.last_contact_count)
     roofline, roofline_step = roofline_of("pile_1m", stage_ms, prof_substeps, sc.n, dev_s * 1e3 / frames, peak,
-                                          peak_kind)
+                                          peak_kind, contacts)
     return {"workload": "pile_1m", "particles": sc.n, "preroll_frames": args.pile_preroll, "frames": frames,
             "value": work / dev_s, "unit": UNIT, "ms_per_frame": dev_s / frames * 1e3,
             "launches_per_frame": int(launches), "contacts_last_substep": int(s.last_contact_count),
             "roofline": roofline, "roofline_step": roofline_step,
-            "stages": stage_table(stage_ms, prof_substeps, sc.n, peak)}
+            "stages": stage_table(stage_ms, prof_substeps, sc.n, peak, contacts)}
 
 
 def measure_cache(args, solver, sc):
