@@ -252,7 +252,7 @@ int xpbd_get_solve_split(const xpbd_solver* s, int* mode);
  * warp per particle (the lanes test its candidates and compute its pair terms together), -1
  * (default) = form 3 for scenes of at most 8,192 particles, form 0 up to 16,383, and from
  * 16,384 particles forms 0 and 1 timed on the solver's own last substep after its first
- * frame and again every 16 frames, keeping the faster.
+ * frame and again every 64 frames, switching only to a form faster by more than 2%.
  * xpbd_get_solve_form reports the form in use. */
 int xpbd_set_solve_form(xpbd_solver* s, int form);
 int xpbd_get_solve_form(const xpbd_solver* s, int* form);

@@ -320,9 +320,9 @@ void Solver::autotune_solve() {
             ms[f] += t;
         }
     for (auto& e : ev) cudaEventDestroy(e);
-    int best = 0;
-    for (int f = 1; f < kSolveTimedForms; f++)
-        if (ms[f] < ms[best]) best = f;
+    int best = solve_form_timed_ && solve_form_ < kSolveTimedForms ? solve_form_ : 0;  // the form in use
+    for (int f = 0; f < kSolveTimedForms; f++)
+        if (f != best && ms[f] < ms[best] * 0.98) best = f;
     solve_form_ = best;
     solve_form_timed_ = true;
     solve_form_frame_ = frames_run_;

@@ -217,9 +217,10 @@ class Solver {
     static constexpr int kWalkBlocksBeside = 16;
     // Solve-kernel form: timed on the scene's own last substep (its last iteration launched
     // again with its outputs in scratch buffers) after the first frame and again every
-    // kSolveRetime frames, as the scene evolves (in the mixed workload the warp form turns
-    // faster once the boxes press into the pile); every form gives the same bits.
-    static constexpr uint64_t kSolveRetime = 16;
+    // kSolveRetime frames, as the scene evolves; every form gives the same bits. A retime
+    // launches the scene's last iteration eight more times, so it is rare, and the form in
+    // use is kept unless the other is faster by more than 2%.
+    static constexpr uint64_t kSolveRetime = 64;
     static constexpr size_t kSolveTuneMinParticles = 16384;  // smaller scenes keep the default
     // the default form: one warp per particle for small scenes, whose solve time is one
     // particle's latency (4,096 particles: 28.8 -> 20.8 us per substep; slower from 16,384)
