@@ -240,7 +240,7 @@ int xpbd_set_sort_variant(xpbd_solver* s, int bits, int keys_per_thread);
  * generation (no counterpart in the reference; results are identical either way):
  * 0 = fused after the contacts, 1 = its particle-particle part computed beside contact
  * generation and the rest after it, -1 (default) = each solver times both over its first
- * frames, keeps the faster (the split within 1%), and times both again every 8 frames. xpbd_get_solve_split
+ * frames, keeps the faster (the split within 1%), and times both again every 16 frames. xpbd_get_solve_split
  * reports the form in use (-1 while timing). */
 int xpbd_set_solve_split(xpbd_solver* s, int mode);
 int xpbd_get_solve_split(const xpbd_solver* s, int* mode);

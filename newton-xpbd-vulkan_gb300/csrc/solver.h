@@ -258,7 +258,7 @@ class Solver {
     // two frames each way): a scene's balance moves as it evolves (bodies settling into a
     // pile multiply the moving-mesh queries). Within 1% the split is kept.
     static constexpr int kSplitTrials = 6;
-    static constexpr int kSplitRetime = 8;
+    static constexpr int kSplitRetime = 16;
     int split_choice_ = -1;
     int split_frames_ = 0;  // frames since the last choice
     int split_forced_ = -1;  // set_solve_split: kept across graph rebuilds
