@@ -412,7 +412,12 @@ def run_gpu(args):
     barrier(world)
     torch.cuda.synchronize(dev)
     kernels_before = solver.kernels_launched
+    if args.profile_timed:  # a profiler started with collection off (ncu --profile-from-start off) sees these frames
+        torch.cuda.profiler.start()
     dev_ms = timed_frames(solver, stream, args.steps, flush)
+    if args.profile_timed:
+        torch.cuda.synchronize(dev)
+        torch.cuda.profiler.stop()
     kernels_timed = solver.kernels_launched - kernels_before
     torch.cuda.synchronize(dev)
     barrier(world)
@@ -864,6 +869,8 @@ def main():
                     help="skip the 4,096-particle pile (the reference's CPU-runnable case)")
     ap.add_argument("--pile-preroll", type=int, default=20)
     ap.add_argument("--pile-solve-form", type=int, default=-1, help="fix the 1M pile's solve form (-1: timed choice)")
+    ap.add_argument("--profile-timed", action="store_true",
+                    help="bracket the mixed workload's timed frames with cudaProfilerStart/Stop")
     ap.add_argument("--only", default="", help="comma list of parts to run alone: mesh,batched,diff,pile,pile4k")
     args = ap.parse_args()
     if args.warmup < 3:
