@@ -96,8 +96,9 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          uint32_t* stamp) {
     if (n <= 0) return;
     int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)device_sm_count() * 8);
-    size_t smem = sizeof(uint32_t) * (size_t)sp.passes << sp.bits;
-    k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pscene, pp, pl, keys, sp.bits, sp.passes, hist,
+    const int passes = hist ? sp.passes : 0;  // no histogram wanted: none built
+    size_t smem = sizeof(uint32_t) * (size_t)passes << sp.bits;
+    k_predict_keys<<<blocks, 256, smem, s>>>(n, x, v, w, r, flags, pscene, pp, pl, keys, sp.bits, passes, hist,
                                             cinfo, ccount, stamp);
 }
 
@@ -424,6 +425,7 @@ void launch_onesweep_pass(cudaStream_t s, int64_t n, const SortPlan& sp, int pas
 // ---------------------------------------------------------------------------
 constexpr int kSmallSortThreads = 256, kSmallSortItems = 16;
 constexpr int kSmallSortKeys = kSmallSortThreads * kSmallSortItems;
+static_assert(kSmallSortKeys == kSmallSortMaxKeys, "the one-block sort's capacity");
 
 __global__ void __launch_bounds__(kSmallSortThreads) k_sort_small(int n, int passes, const uint32_t* __restrict__ keys_in,
                                                                   uint32_t* __restrict__ keys_out,

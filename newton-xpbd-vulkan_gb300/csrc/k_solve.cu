@@ -399,7 +399,19 @@ __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp,
         int lo = 0x7fffffff, hi = -1;  // lane r: the sorted range of row r
         if (lane < rows) {
             const int c0 = cell_index(cr.xs, cr.ys + lane % nyr, cr.zs + lane / nyr, split);
-            for (int j = 0; j <= cr.xe - cr.xs; j++) {
+            const int ncell = cr.xe - cr.xs + 1;
+            // the first three cells' entries are loaded together (a row usually has three)
+            int4 e3[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) e3[j] = j < ncell ? __ldg(&table[c0 + j]) : make_int4(0, -1, 0, 0);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                if (j < ncell && (uint32_t)e3[j].z == stamp) {
+                    lo = min(lo, e3[j].x);
+                    hi = max(hi, e3[j].y);
+                }
+            }
+            for (int j = 3; j < ncell; j++) {
                 const int4 e = __ldg(&table[c0 + j]);
                 if ((uint32_t)e.z == stamp) {
                     lo = min(lo, e.x);
@@ -428,13 +440,15 @@ __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp,
                 if (!ALL_ACTIVE && ok && is_proxy != 0 && (((nflag & 2) != 0) || (__ldg(&rv[kk].w) <= 0.0f)))
                     ok = false;
                 if (ok) {
+                    // both records at once: the velocity is needed by every accepted candidate
                     const float4 nx = __ldg(&rx[kk]);
+                    const float4 nv = __ldg(&rv[kk]);
                     const v3 raw = vsub(xp, xyz(nx));
                     if (!(fabsf(raw.x) > R || fabsf(raw.y) > R || fabsf(raw.z) > R)) {
                         const float sq = __fmaf_rn(raw.z, raw.z, __fmaf_rn(raw.x, raw.x, raw.y * raw.y));
                         const float reach = ((radius + nx.w) + sp.k_coh) * 1.0000153f;
                         if (!(sq > reach * reach))
-                            t = pair_term_body(nx, __ldg(&rv[kk]), sq, xp, vp, radius, w1, sp.k_mu, sp.k_coh, sp.dt);
+                            t = pair_term_body(nx, nv, sq, xp, vp, radius, w1, sp.k_mu, sp.k_coh, sp.dt);
                     }
                 }
             }
@@ -550,6 +564,17 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
             stage = &s_stage;
         if (!valid) return;
     }
+    // the per-particle-warp form loads lane 0's shape-contact inputs before the pair pass, so
+    // their latency overlaps it instead of following it
+    uint32_t pre_info = 0u;
+    float4 pre_x0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), pre_v0 = pre_x0;
+    if constexpr (PWARP && PP != kPPOnly) {
+        if (pflag & 1) {
+            pre_info = cinfo ? cinfo[id] : 0u;
+            pre_x0 = x0a[id];
+            if (LAST && sp.enable_restitution) pre_v0 = v0a[id];
+        }
+    }
     if constexpr (PWARP) {
         if (pflag & 1) {  // the same particle in every lane
             const int4* __restrict__ table = skeys ? table_all + ((size_t)(skeys[k] >> 21) << 21) : table_all;
@@ -580,8 +605,8 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
     v3 delta = mk3(0.0f, 0.0f, 0.0f);
 
     if (pflag & 1) {
-        const uint32_t info = cinfo ? cinfo[id] : 0u;
-        const v3 x0 = xyz(x0a[id]);
+        const uint32_t info = PWARP ? pre_info : (cinfo ? cinfo[id] : 0u);
+        const v3 x0 = xyz(PWARP ? pre_x0 : x0a[id]);
         const int ncon = (int)(info & kPlaneBit) + info_slots(info);
         const float4* slots = cslot + (size_t)id * sp.slot_cap * 3;
         // shape contacts, canonical order (scene.cpp:946-947)
@@ -628,7 +653,7 @@ __global__ void __launch_bounds__(kSolveThreads, 16) k_solve(
             x_new = vadd(x0, vmuls(v_new, sp.dt));
         }
         if (LAST && sp.enable_restitution && ncon) {
-            const v3 v_old = xyz(v0a[id]);
+            const v3 v_old = xyz(PWARP ? pre_v0 : v0a[id]);
             const v3 v_snap = v_new;
             for (int c = 0; c < ncon; c++) {
                 if (!contact_kept(info, c, cr, id, sp.contact_max)) continue;

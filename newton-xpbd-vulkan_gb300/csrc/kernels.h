@@ -158,7 +158,7 @@ struct SortPlan {
 SortPlan make_sort_plan(int64_t n, int key_bits, int bits, int items);
 size_t sort_lookback_words(const SortPlan& p);  // per pass
 
-// keys[i] (+ optional plane contacts, + all-pass digit histograms)
+// keys[i] (+ optional plane contacts, + all-pass digit histograms into hist unless it is null)
 // Batched scenes: pscene[i] is particle i's scene and the key becomes (scene << 21) | cell,
 // which is also the entry of a scene-major table of 128^3 cells per scene (pscene == null:
 // one scene).
@@ -166,8 +166,10 @@ void launch_predict_keys(cudaStream_t s, int64_t n, const float4* x, const float
                          const float* r, const int* flags, const uint32_t* pscene, PredictParams pp, PlaneParams pl,
                          uint32_t* keys, const SortPlan& sp, uint32_t* hist, uint32_t* cinfo,
                          uint32_t* ccount, uint32_t* stamp);
-// every pass of a stable LSD sort of at most 4,096 keys (key_bits wide, 8-bit digits) in one
-// launch of one block; values = input index. Returns false (nothing launched) for more keys.
+// every pass of a stable LSD sort of at most kSmallSortMaxKeys keys (key_bits wide, 8-bit
+// digits) in one launch of one block; values = input index. Returns false (nothing launched)
+// for more keys.
+constexpr int64_t kSmallSortMaxKeys = 4096;
 bool launch_sort_small(cudaStream_t s, int64_t n, int key_bits, const uint32_t* keys_in, uint32_t* keys_out,
                        uint32_t* vals_out);
 // one onesweep pass; vals_in == nullptr means vals are the element index; n_dev (optional)

@@ -1031,9 +1031,14 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     const RigidTables rt = rigid_tables();
     const DynSlots ds{cslot_.p, slot_cap_, shape_body_.p, body_invm_.p};
 
+    // a scene of one sort tile sorts in one block (launch_sort_small) and reads no digit
+    // histogram; without a mesh pass and bodies nothing else uses the sort scratch either
+    const bool small_sort = n <= kSmallSortMaxKeys;
     prof_mark(-1);
-    XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
-    count_memset();
+    if (!small_sort || mesh_pass || bodies) {
+        XPBD_CUDA(cudaMemsetAsync(sort_scratch_.p, 0, sort_scratch_.bytes(), stream_));
+        count_memset();
+    }
     if (bodies) {
         XPBD_CUDA(cudaMemsetAsync(esort_scratch_.p, 0, esort_scratch_.bytes(), stream_));
         XPBD_CUDA(cudaMemsetAsync(seg_.p, 0, seg_.bytes(), stream_));
@@ -1140,7 +1145,7 @@ void Solver::record_substep(Mode mode, int sub, int iterations, float sdt, int s
     // plane contacts are fused into the key kernel when there is no mesh pass
     uint32_t* key_cinfo = (gen && !mesh_pass) ? cinfo_.p : nullptr;
     launch_predict_keys(stream_, n, x_[src].p, v_[src].p, w_.p, r_.p, flags_.p, pscene_.p, pp, pl, keys_.p, plan_,
-                        sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
+                        small_sort ? nullptr : sort_scratch_.p + hist_off_, key_cinfo, ccount, stamp_.p);
     count_kernel();
     prof_mark(P_INTEGRATE_KEYS);
     const uint32_t* kin = keys_.p;
