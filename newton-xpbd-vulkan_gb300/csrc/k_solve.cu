@@ -369,10 +369,14 @@ enum { kPPFused = 0, kPPOnly = 1, kPPApply = 2 };
 // The particle-particle total of one particle computed by a whole warp (the per-particle-warp
 // form; every lane calls it for the same particle and gets the same total). The lanes take
 // the particle's candidates 32 at a time in the filter's order (rows of cells z outer, y
-// inner, each row one run of the sorted order), each testing one candidate as pp_filter
-// does and computing its pair term; the accepted terms of a round are then added in lane
-// order, which is candidate order. A particle whose rows wrap the grid or number more than
-// 32 is done by lane 0 alone in the filter's order.
+// inner, x ascending within a row), each testing one candidate as pp_filter does and
+// computing its pair term; the accepted terms of a round are then added in lane order, which
+// is candidate order. A row's cells have consecutive keys up to the grid's wrap (every 128
+// cells, where the reference's key wraps and a split key's alias bit changes) and again
+// after it, so a row is one run of the sorted order, or two when it crosses the wrap: the
+// cells before it, then the cells after it, which is the row's x order. A particle with more
+// than 32 such runs, or with cells clamped at grid coordinate 0, is done by lane 0 alone in
+// the filter's order.
 template <bool ALL_ACTIVE>
 __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp, float radius, float w1,
                                              const float4* __restrict__ rx, const float4* __restrict__ rv,
@@ -385,9 +389,13 @@ __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp,
     const CellRange cr = cell_range(xp, radius, sp);
     const int nyr = cr.ye - cr.ys + 1, rows = nyr * (cr.ze - cr.zs + 1);
     const int32_t xo = cr.xs + kGridOrigin;
-    const bool row_run = xo >= 0 && (xo % kGridDim) + (cr.xe - cr.xs) < kGridDim;
+    const int ncx = cr.xe - cr.xs + 1;  // at most kGridDim (cell_range)
+    // cells of a row before the wrap; the rest (if any) follow it
+    const int first = xo >= 0 ? min(ncx, kGridDim - (xo % kGridDim)) : ncx;
+    const int nseg = first < ncx ? 2 : 1;
+    const int segs = rows * nseg;  // runs of the sorted order, in visit order
     v3 acc = mk3(0.0f, 0.0f, 0.0f);
-    if (!row_run || rows > 32) {
+    if (xo < 0 || segs > 32) {
         if (lane == 0)
             pp_filter<ALL_ACTIVE>(k, pflag, xp, radius, rx, rv, rf, table, split, stamp, sp, [&](int kk, float sq) {
                 const float4 t = pair_term(__ldg(&rx[kk]), __ldg(&rv[kk]), sq, xp, vp, radius, w1, sp.k_mu,
@@ -396,11 +404,12 @@ __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp,
             });
         acc = mk3(__shfl_sync(FULL, acc.x, 0), __shfl_sync(FULL, acc.y, 0), __shfl_sync(FULL, acc.z, 0));
     } else {
-        int lo = 0x7fffffff, hi = -1;  // lane r: the sorted range of row r
-        if (lane < rows) {
-            const int c0 = cell_index(cr.xs, cr.ys + lane % nyr, cr.zs + lane / nyr, split);
-            const int ncell = cr.xe - cr.xs + 1;
-            // the first three cells' entries are loaded together (a row usually has three)
+        int lo = 0x7fffffff, hi = -1;  // lane s: the sorted range of run s
+        if (lane < segs) {
+            const int row = lane / nseg, after = lane - row * nseg;  // after: the run past the wrap
+            const int c0 = cell_index(cr.xs + (after ? first : 0), cr.ys + row % nyr, cr.zs + row / nyr, split);
+            const int ncell = after ? ncx - first : first;
+            // the first three cells' entries are loaded together (a run rarely has more)
             int4 e3[3];
 #pragma unroll
             for (int j = 0; j < 3; j++) e3[j] = j < ncell ? __ldg(&table[c0 + j]) : make_int4(0, -1, 0, 0);
@@ -429,8 +438,8 @@ __device__ __forceinline__ v3 pp_total_pwarp(int64_t k, int pflag, v3 xp, v3 vp,
         const int total_c = __shfl_sync(FULL, incl, 31);
         for (int base = 0; base < total_c; base += 32) {
             const int c = base + lane;
-            int r = 0;  // the row of candidate c: the last row starting at or before it
-            for (int q = 1; q < rows; q++)
+            int r = 0;  // the run of candidate c: the last run starting at or before it
+            for (int q = 1; q < segs; q++)
                 if (__shfl_sync(FULL, excl, q) <= c) r = q;
             const int kk = __shfl_sync(FULL, lo, r) + (c - __shfl_sync(FULL, excl, r));
             float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
