@@ -246,6 +246,10 @@ def timed_frames(solver, stream, frames, flush=None):
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
     for k in range(frames):
+        # the previous frame is finished (its status read back) before this one is queued, so
+        # the launch below waits for nothing; the flush then runs on the device while the host
+        # launches the frame, and the host's turnaround stays outside the frame's events
+        solver.sync()
         if flush is not None:
             flush()
         ev[k][0].record(stream)
