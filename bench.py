@@ -240,11 +240,13 @@ def roofline_of(workload, stage_ms, prof_substeps, n, step_ms, peak, peak_kind, 
     return roofline, roofline_step
 
 
-def timed_frames(solver, stream, frames, flush=None):
-    """Device time (ms) of `frames` frames, CUDA events on the solver's stream."""
+def timed_frames(solver, stream, frames, flush=None, per_frame=False):
+    """Device time (ms) of `frames` frames, CUDA events on the solver's stream. per_frame:
+    also each frame's device time and kernel count (the kernels of the graph it replayed)."""
     import torch
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    kernels = []
     for k in range(frames):
         # the previous frame is finished (its status read back) before this one is queued, so
         # the launch below waits for nothing; the flush then runs on the device while the host
@@ -253,11 +255,15 @@ def timed_frames(solver, stream, frames, flush=None):
         if flush is not None:
             flush()
         ev[k][0].record(stream)
+        before = solver.kernels_launched if per_frame else 0
         solver.step_async(DT, SUBSTEPS, ITERATIONS)
         ev[k][1].record(stream)
+        if per_frame:
+            kernels.append(solver.kernels_launched - before)
     solver.sync()
     torch.cuda.synchronize()
-    return sum(a.elapsed_time(b) for a, b in ev)
+    times = [a.elapsed_time(b) for a, b in ev]
+    return (sum(times), times, kernels) if per_frame else sum(times)
 
 
 def e2e_frames(solver, frames, x, v, body_q=None, body_qd=None, flush=None, sync=None):
@@ -418,7 +424,8 @@ def run_gpu(args):
     kernels_before = solver.kernels_launched
     if args.profile_timed:  # a profiler started with collection off (ncu --profile-from-start off) sees these frames
         torch.cuda.profiler.start()
-    dev_ms = timed_frames(solver, stream, args.steps, flush)
+    dev_ms, frame_ms, frame_kernels = timed_frames(solver, stream, args.steps, flush, per_frame=True)
+    choices = {"solve_form": solver.solve_form, "solve_split": solver.solve_split}
     if args.profile_timed:
         torch.cuda.synchronize(dev)
         torch.cuda.profiler.stop()
@@ -460,6 +467,10 @@ def run_gpu(args):
         "contacts_last_substep": contacts,
         "boxes_finite": bool(np.isfinite(bq).all() and np.isfinite(bqd).all()),
         "e2e": e2e, "gpu_launches": int(kernels_timed), "clocks": clk,
+        # each timed frame's device time and kernel count (a frame whose first iteration is
+        # split launches one solve kernel more per substep), and the solver's choices after them
+        "frames": {"ms": [round(t, 3) for t in frame_ms], "kernels": [int(c) for c in frame_kernels],
+                   "choices_after": choices},
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_sample(sc, x_snap, v_snap, q_snap, qd_snap, budget_s=args.cpu_budget)

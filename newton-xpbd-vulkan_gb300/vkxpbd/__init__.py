@@ -241,7 +241,7 @@ class XpbdSolver:
 
     @property
     def solve_form(self):
-        """The solve-kernel form in use (0 or 1)."""
+        """The solve-kernel form in use (0-3; see set_solve_form)."""
         v = C.c_int(0)
         _check(_lib.xpbd_get_solve_form(self._h, C.byref(v)))
         return int(v.value)
